@@ -1,0 +1,284 @@
+/*
+ * gbqv.h — C ABI of the GB300 statevector / density-matrix engine (libgbqv.so).
+ *
+ * The engine replaces the `statevec_t` / `densmat_t` template argument that
+ * Qiskit Aer's State classes are instantiated with: the member surface of
+ * QV::QubitVector<T> (src/simulators/statevector/qubitvector.hpp:61-651),
+ * its GPU twin QubitVectorThrust (qubitvector_thrust.hpp:57-560) and
+ * QV::DensityMatrix<T> (src/simulators/density_matrix/densitymatrix.hpp:34-171).
+ * Each entry point below names the reference member it stands in for.
+ *
+ * Conventions (all follow the reference):
+ *   - A state of n qubits is 2^n amplitudes; amplitude index bit q is qubit q.
+ *   - Matrices are column-major, mat[row + DIM*col], and qubits[0] is the
+ *     least-significant bit of the matrix row/column index
+ *     (transformer.hpp:157-159, indexes.hpp:223-235).
+ *   - Multi-controlled gates take the target as the LAST qubit
+ *     (qubitvector.hpp:1446-1720).
+ *   - Pauli labels are read right to left: label[N-1-i] acts on qubits[i]
+ *     (qubitvector.hpp:2235-2272).
+ *   - A density matrix of n qubits is vec(rho) over 2n vector qubits,
+ *     column-stacked: rho[i,j] sits at index i + 2^n * j
+ *     (densitymatrix.hpp:265-323).
+ *
+ * Ownership and threading: a handle owns its device state and one CUDA
+ * stream.  Inputs (qubit lists, matrices, uniforms) are host pointers that
+ * are consumed before the call returns; outputs go to caller-owned host
+ * buffers.  A handle is used by one thread at a time; different handles may
+ * be used concurrently.  Calls that return a value synchronise the handle's
+ * stream; others are asynchronous until gbqv_synchronize().
+ *
+ * Errors: every function returns GBQV_OK (0) or a positive error code and
+ * never throws across the ABI (the reference throws std::runtime_error /
+ * std::invalid_argument, qubitvector.hpp:698-747, 2266-2268).  The message
+ * of the most recent failure on a handle is gbqv_last_error(handle); failures
+ * that have no handle are reported by gbqv_last_error(NULL) (thread-local).
+ */
+#ifndef GBQV_H_
+#define GBQV_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbqv_state *gbqv_handle;
+typedef struct gbqv_circuit *gbqv_circuit_t;
+
+/* Interleaved complex double, layout-compatible with std::complex<double>. */
+typedef struct {
+  double re, im;
+} gbqv_c128;
+
+enum gbqv_status {
+  GBQV_OK = 0,
+  GBQV_ERR_ARG = 1,      /* bad size, null pointer, bad label, bad axis      */
+  GBQV_ERR_QUBIT = 2,    /* qubit index out of range or repeated             */
+  GBQV_ERR_CUDA = 3,     /* CUDA launch / runtime failure                    */
+  GBQV_ERR_ALLOC = 4,    /* device memory could not be allocated             */
+  GBQV_ERR_KIND = 5,     /* operation not valid for this state kind          */
+  GBQV_ERR_TIMEOUT = 6   /* a bounded device-side wait gave up               */
+};
+
+enum gbqv_precision { GBQV_C64 = 0, GBQV_C128 = 1 };
+enum gbqv_kind { GBQV_STATEVECTOR = 0, GBQV_DENSITY_MATRIX = 1 };
+
+/* Rotation axes, QV::Rotation (qubitvector.hpp:50-59). */
+enum gbqv_rotation {
+  GBQV_ROT_X = 0, GBQV_ROT_Y = 1, GBQV_ROT_Z = 2,
+  GBQV_ROT_XX = 3, GBQV_ROT_YY = 4, GBQV_ROT_ZZ = 5, GBQV_ROT_ZX = 6
+};
+
+/* ------------------------------------------------------------------ */
+/* Library                                                              */
+/* ------------------------------------------------------------------ */
+
+/* ABI version of this header (major*10000 + minor*100 + patch). */
+int gbqv_version(void);
+/* Message of the last failure on h; h == NULL gives this thread's last
+ * handle-less failure.  The pointer stays valid until the next call on h. */
+const char *gbqv_last_error(gbqv_handle h);
+/* Number of CUDA devices visible (0 when no GPU); never fails. */
+int gbqv_device_count(void);
+
+/* ------------------------------------------------------------------ */
+/* State lifetime — QubitVector(num_qubits) / set_num_qubits           */
+/* (qubitvector.hpp:754-767, 913-967); QubitVectorThrust chunk_setup  */
+/* + DeviceChunkContainer::Allocate (device_chunk_container.hpp:319). */
+/* ------------------------------------------------------------------ */
+
+/* n = number of qubits (a density matrix of n qubits holds 4^n entries). */
+int gbqv_create(int num_qubits, int precision, int kind, gbqv_handle *out);
+int gbqv_destroy(gbqv_handle h);
+int gbqv_num_qubits(gbqv_handle h, int *out);
+/* Number of vector qubits: n for a statevector, 2n for a density matrix. */
+int gbqv_num_vector_qubits(gbqv_handle h, int *out);
+int gbqv_synchronize(gbqv_handle h);
+/* Device pointer of the amplitudes (complex<double> or complex<float>). */
+int gbqv_device_data(gbqv_handle h, void **out);
+
+/* QubitVector::zero (qubitvector.hpp:973-979). */
+int gbqv_zero(gbqv_handle h);
+/* QubitVector::initialize -> |0...0>; DensityMatrix::initialize -> |0><0|
+ * (qubitvector.hpp:1076-1080, densitymatrix.hpp:198-204). */
+int gbqv_initialize(gbqv_handle h);
+/* QubitVector::initialize_from_vector (qubitvector.hpp:1082-1110).  For a
+ * density matrix a length-2^n vector is taken as a pure state and
+ * vec(|psi><psi|) is stored (densitymatrix.hpp:206-226). */
+int gbqv_initialize_from_vector(gbqv_handle h, const gbqv_c128 *vec, uint64_t len);
+/* QubitVector::copy_to_vector / move_to_vector (qubitvector.hpp:1008-1050);
+ * len must equal the number of stored amplitudes. */
+int gbqv_copy_to_host(gbqv_handle h, gbqv_c128 *out, uint64_t len);
+/* QubitVector::checkpoint / revert / inner_product
+ * (qubitvector.hpp:994-1041): <state|checkpoint>. */
+int gbqv_checkpoint(gbqv_handle h);
+int gbqv_revert(gbqv_handle h, int keep);
+int gbqv_inner_product(gbqv_handle h, gbqv_c128 *out);
+
+/* ------------------------------------------------------------------ */
+/* Gate application on the (vector) qubits of the state                */
+/* ------------------------------------------------------------------ */
+
+/* QubitVector::apply_matrix (qubitvector.hpp:1298-1303, transformer.hpp:89-232):
+ * dense 2^k x 2^k column-major matrix, 1 <= k <= 10. */
+int gbqv_apply_matrix(gbqv_handle h, const uint64_t *qubits, int k, const gbqv_c128 *mat);
+/* QubitVector::apply_diagonal_matrix (qubitvector.hpp:1342-1347,
+ * transformer.hpp:234-372): diag has 2^k entries, 1 <= k <= 20. */
+int gbqv_apply_diagonal_matrix(gbqv_handle h, const uint64_t *qubits, int k, const gbqv_c128 *diag);
+/* QubitVector::apply_mcx / apply_mcy / apply_mcswap (qubitvector.hpp:1446-1573). */
+int gbqv_apply_mcx(gbqv_handle h, const uint64_t *qubits, int nq);
+int gbqv_apply_mcy(gbqv_handle h, const uint64_t *qubits, int nq);
+int gbqv_apply_mcswap(gbqv_handle h, const uint64_t *qubits, int nq);
+/* QubitVector::apply_mcphase (qubitvector.hpp:1575-1612). */
+int gbqv_apply_mcphase(gbqv_handle h, const uint64_t *qubits, int nq, gbqv_c128 phase);
+/* QubitVector::apply_mcu (qubitvector.hpp:1614-1720): mat is 2x2 column-major. */
+int gbqv_apply_mcu(gbqv_handle h, const uint64_t *qubits, int nq, const gbqv_c128 *mat);
+/* QubitVector::apply_rotation (qubitvector.hpp:1722-1750), axis = gbqv_rotation. */
+int gbqv_apply_rotation(gbqv_handle h, const uint64_t *qubits, int nq, int axis, double theta);
+/* QubitVector::apply_pauli (qubitvector.hpp:2392-2433). */
+int gbqv_apply_pauli(gbqv_handle h, const uint64_t *qubits, int nq, const char *label, gbqv_c128 coeff);
+/* QubitVector::apply_permutation_matrix (qubitvector.hpp:1349-1434):
+ * pairs = [a0, b0, a1, b1, ...] of local indices to swap, in order. */
+int gbqv_apply_permutation_matrix(gbqv_handle h, const uint64_t *qubits, int k,
+                                  const uint64_t *pairs, int npairs);
+/* QubitVector::apply_multiplexer (qubitvector.hpp:1305-1340): mat is the
+ * (2^nt * 2^nc) x 2^nt column-major stack of 2^nc blocks. */
+int gbqv_apply_multiplexer(gbqv_handle h, const uint64_t *controls, int nc,
+                           const uint64_t *targets, int nt, const gbqv_c128 *mat);
+/* QubitVector::apply_multi_swaps (qubitvector.hpp:1842-1871): swaps qubit
+ * pairs (q0,q1), (q2,q3), ... */
+int gbqv_apply_multi_swaps(gbqv_handle h, const uint64_t *qubits, int nq);
+
+/* ------------------------------------------------------------------ */
+/* Reductions (FP64 accumulation in every precision)                    */
+/* ------------------------------------------------------------------ */
+
+/* QubitVector::norm (qubitvector.hpp:1878-1886); for a density matrix this is
+ * the squared Frobenius norm of the stored vector, as in the reference. */
+int gbqv_norm(gbqv_handle h, double *out);
+/* QubitVector::norm(qubits, mat) (qubitvector.hpp:1888-2082): ||M psi||^2. */
+int gbqv_norm_matrix(gbqv_handle h, const uint64_t *qubits, int k, const gbqv_c128 *mat, double *out);
+/* QubitVector::probabilities() / probabilities(qubits)
+ * (qubitvector.hpp:2089-2143); DensityMatrix uses the diagonal
+ * (densitymatrix.hpp:516-520).  k == 0 means all qubits (out has 2^n). */
+int gbqv_probabilities(gbqv_handle h, const uint64_t *qubits, int k, double *out);
+/* QubitVector::sample_measure (qubitvector.hpp:2148-2228): for each uniform
+ * r in [0,1) the first basis index whose cumulative probability exceeds r. */
+int gbqv_sample_measure(gbqv_handle h, const double *rnds, uint64_t shots, uint64_t *out);
+/* QubitVector::expval_pauli (qubitvector.hpp:2299-2347) and
+ * DensityMatrix::expval_pauli (densitymatrix.hpp:445-496). */
+int gbqv_expval_pauli(gbqv_handle h, const uint64_t *qubits, int nq, const char *label,
+                      gbqv_c128 initial_phase, double *out);
+/* Many Pauli terms in one call: the loop of Base::apply_save_expval
+ * (src/simulators/state.hpp:416-447) without one host round trip per term.
+ * Term t acts on qubits[offsets[t] .. offsets[t+1]) with labels[t];
+ * out[t] = <P_t>.  Returns sum_t coeffs[t] * out[t] in *total when non-NULL. */
+int gbqv_expval_pauli_many(gbqv_handle h, int nterms, const uint64_t *qubits,
+                           const int *offsets, const char *const *labels,
+                           const double *coeffs, double *out, double *total);
+
+/* ------------------------------------------------------------------ */
+/* Density-matrix surface (GBQV_DENSITY_MATRIX handles only)            */
+/* ------------------------------------------------------------------ */
+
+/* DensityMatrix::apply_superop_matrix (densitymatrix.hpp:284-288): a
+ * 4^k x 4^k superoperator on qubits and qubits+n. */
+int gbqv_dm_apply_superop_matrix(gbqv_handle h, const uint64_t *qubits, int k, const gbqv_c128 *mat);
+/* DensityMatrix::apply_diagonal_superop_matrix (densitymatrix.hpp:290-295). */
+int gbqv_dm_apply_diagonal_superop_matrix(gbqv_handle h, const uint64_t *qubits, int k,
+                                          const gbqv_c128 *diag);
+/* DensityMatrix::apply_unitary_matrix (densitymatrix.hpp:297-317): one 2k-qubit
+ * superoperator for k <= 4, else U then conj(U) on the column qubits. */
+int gbqv_dm_apply_unitary_matrix(gbqv_handle h, const uint64_t *qubits, int k, const gbqv_c128 *mat);
+/* DensityMatrix::apply_diagonal_unitary_matrix (densitymatrix.hpp:319-325). */
+int gbqv_dm_apply_diagonal_unitary_matrix(gbqv_handle h, const uint64_t *qubits, int k,
+                                          const gbqv_c128 *diag);
+/* DensityMatrix::apply_cnot / apply_swap / apply_x / apply_y / apply_phase /
+ * apply_cphase / apply_toffoli (densitymatrix.hpp:331-440). */
+int gbqv_dm_apply_cnot(gbqv_handle h, uint64_t ctrl, uint64_t trgt);
+int gbqv_dm_apply_swap(gbqv_handle h, uint64_t q0, uint64_t q1);
+int gbqv_dm_apply_x(gbqv_handle h, uint64_t q);
+int gbqv_dm_apply_y(gbqv_handle h, uint64_t q);
+int gbqv_dm_apply_phase(gbqv_handle h, uint64_t q, gbqv_c128 phase);
+int gbqv_dm_apply_cphase(gbqv_handle h, uint64_t q0, uint64_t q1, gbqv_c128 phase);
+int gbqv_dm_apply_toffoli(gbqv_handle h, uint64_t c0, uint64_t c1, uint64_t t);
+/* DensityMatrix::apply_reset (densitymatrix.hpp:522-529). */
+int gbqv_dm_apply_reset(gbqv_handle h, const uint64_t *qubits, int k);
+/* Tr(rho), UnitaryMatrix::trace used by DensityMatrix (unitarymatrix.hpp). */
+int gbqv_dm_trace(gbqv_handle h, gbqv_c128 *out);
+
+/* ------------------------------------------------------------------ */
+/* Circuits: op list, Aer's Fusion pass, execution                      */
+/* ------------------------------------------------------------------ */
+/* A circuit is the host-side op list that Aer's Circuit/Op hold
+ * (src/framework/circuit.hpp, operations.hpp); the builder calls mirror
+ * aer_compiler.py:_assemble_op (qiskit_aer/backends/aer_compiler.py:875-1020). */
+
+int gbqv_circuit_create(int num_qubits, gbqv_circuit_t *out);
+int gbqv_circuit_destroy(gbqv_circuit_t c);
+/* A named gate of the statevector gate set (statevector_state.hpp:313-384),
+ * params are the gate's real parameters. */
+int gbqv_circuit_gate(gbqv_circuit_t c, const char *name, const uint64_t *qubits, int nq,
+                      const double *params, int nparams);
+/* "unitary" op (Operations::make_unitary) with a 2^k x 2^k column-major matrix. */
+int gbqv_circuit_unitary(gbqv_circuit_t c, const uint64_t *qubits, int k, const gbqv_c128 *mat);
+/* "diagonal" op (Operations::make_diagonal) with 2^k entries. */
+int gbqv_circuit_diagonal(gbqv_circuit_t c, const uint64_t *qubits, int k, const gbqv_c128 *diag);
+/* "superop" op (Operations::make_superop), 4^k x 4^k column-major. */
+int gbqv_circuit_superop(gbqv_circuit_t c, const uint64_t *qubits, int k, const gbqv_c128 *mat);
+/* "kraus" op: nk Kraus matrices of 2^k x 2^k, back to back. */
+int gbqv_circuit_kraus(gbqv_circuit_t c, const uint64_t *qubits, int k, int nk, const gbqv_c128 *mats);
+/* "reset" op. */
+int gbqv_circuit_reset(gbqv_circuit_t c, const uint64_t *qubits, int k);
+/* "barrier" op (ignored by fusion, Fusion::can_ignore fusion.hpp:120-129). */
+int gbqv_circuit_barrier(gbqv_circuit_t c, const uint64_t *qubits, int k);
+int gbqv_circuit_num_ops(gbqv_circuit_t c, int *out);
+/* Op i: type (see gbqv_op_type), number of qubits, and its qubits (up to
+ * max_qubits written); name is copied into name_buf (NUL-terminated). */
+enum gbqv_op_type { GBQV_OP_GATE = 0, GBQV_OP_MATRIX = 1, GBQV_OP_DIAGONAL = 2,
+                    GBQV_OP_SUPEROP = 3, GBQV_OP_KRAUS = 4, GBQV_OP_RESET = 5,
+                    GBQV_OP_BARRIER = 6 };
+int gbqv_circuit_op_info(gbqv_circuit_t c, int i, int *type, int *nq, uint64_t *qubits,
+                         int max_qubits, char *name_buf, int name_len);
+/* Matrix (MATRIX: 4^k entries; DIAGONAL: 2^k; SUPEROP: 16^k) of op i. */
+int gbqv_circuit_op_matrix(gbqv_circuit_t c, int i, gbqv_c128 *out, uint64_t len);
+
+/* Fusion configuration, Fusion::set_config (transpile/fusion.hpp:722-748)
+ * with the per-method defaults of Executor::transpile_fusion
+ * (simulators/circuit_executor.hpp:1228-1287). */
+typedef struct {
+  int enable;          /* fusion_enable (default 1)                           */
+  int max_qubit;       /* fusion_max_qubit (statevector 5, density matrix 2)  */
+  int threshold;       /* fusion_threshold (statevector 14, density matrix 7) */
+  double cost_factor;  /* fusion_cost_factor (1.8)                            */
+  int avx2_costs;      /* 1: CostBasedFusion AVX2 cost table (fusion.hpp:1119)*/
+  int allow_superop;   /* set when the op set holds superop/kraus/reset       */
+  int allow_kraus;
+} gbqv_fusion_config;
+
+/* Fills the defaults for method 0 = statevector, 1 = density_matrix. */
+int gbqv_fusion_default_config(int method, gbqv_fusion_config *cfg);
+/* Fusion::optimize_circuit (fusion.hpp:750-846) in place.  *applied gets the
+ * "applied" metadata flag, *method_name (may be NULL) "unitary"/"superop"/
+ * "kraus", written into a buffer of method_len bytes. */
+int gbqv_circuit_fuse(gbqv_circuit_t c, const gbqv_fusion_config *cfg, int *applied,
+                      char *method_name, int method_len);
+
+/* Apply every op of c to the state (State::apply_ops, state.hpp:295-340),
+ * dispatching gates as Statevector::State::apply_gate
+ * (statevector_state.hpp:733-865) or DensityMatrix::State::apply_gate
+ * (densitymatrix_state.hpp:641-850).  Runs of dense/diagonal ops are
+ * scheduled into cache-blocked passes over HBM. */
+int gbqv_execute(gbqv_handle h, gbqv_circuit_t c);
+
+/* Execution policy for gbqv_execute (no reference counterpart: Aer applies
+ * one op per pass).  blocking = 0 applies one kernel per op. */
+int gbqv_set_blocking(gbqv_handle h, int blocking);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBQV_H_ */
