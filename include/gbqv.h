@@ -82,6 +82,11 @@ int gbqv_version(void);
 const char *gbqv_last_error(gbqv_handle h);
 /* Number of CUDA devices visible (0 when no GPU); never fails. */
 int gbqv_device_count(void);
+/* The uniform stream of RngEngine::rand(0, 1) after set_seed(seed)
+ * (src/framework/rng.hpp:65-67, 96): std::uniform_real_distribution<double>
+ * over std::mt19937_64.  These are the draws State::sample_measure consumes
+ * (statevector_state.hpp:1016-1027); needs no GPU. */
+int gbqv_uniforms(uint64_t seed, uint64_t count, double *out);
 
 /* ------------------------------------------------------------------ */
 /* State lifetime — QubitVector(num_qubits) / set_num_qubits           */
@@ -249,6 +254,7 @@ int gbqv_circuit_op_matrix(gbqv_circuit_t c, int i, gbqv_c128 *out, uint64_t len
  * with the per-method defaults of Executor::transpile_fusion
  * (simulators/circuit_executor.hpp:1228-1287). */
 typedef struct {
+  int method;          /* 0 = statevector, 1 = density_matrix                 */
   int enable;          /* fusion_enable (default 1)                           */
   int max_qubit;       /* fusion_max_qubit (statevector 5, density matrix 2)  */
   int threshold;       /* fusion_threshold (statevector 14, density matrix 7) */
@@ -272,6 +278,20 @@ int gbqv_circuit_fuse(gbqv_circuit_t c, const gbqv_fusion_config *cfg, int *appl
  * (densitymatrix_state.hpp:641-850).  Runs of dense/diagonal ops are
  * scheduled into cache-blocked passes over HBM. */
 int gbqv_execute(gbqv_handle h, gbqv_circuit_t c);
+
+/* Adjoint-method gradient of E(theta) = <psi(theta)|H|psi(theta)>, psi =
+ * c applied to |0...0>.  No counterpart in the reference (Aer has no gradient
+ * code); it extends the statevector surface for the torch.autograd wrapper.
+ * param_of_op[i] is -1 for a fixed op, else the index of the parameter that
+ * replaces params[0] of gate i, which must be rx, ry, rz, rxx, ryy, rzz or
+ * rzx (U = exp(-i theta P / 2)).  H = sum_t coeffs[t] P_t with the Pauli
+ * terms laid out as in gbqv_expval_pauli_many.  Writes E to *energy and
+ * dE/dparams to grad[0..nparams).  Uses two state buffers (the handle's and
+ * one scratch buffer of the same size); on return the handle holds the
+ * state after the first op (the end point of the reverse sweep). */
+int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const int *param_of_op, const double *params,
+                             int nparams, int nterms, const uint64_t *qubits, const int *offsets,
+                             const char *const *labels, const double *coeffs, double *energy, double *grad);
 
 /* Execution policy for gbqv_execute (no reference counterpart: Aer applies
  * one op per pass).  blocking = 0 applies one kernel per op. */

@@ -1,0 +1,33 @@
+"""GB300-native statevector / density-matrix engine with Qiskit Aer's qreg
+surface.
+
+Package layout:
+  csrc/           CUDA kernels (sm_103a) + C++ host code behind the C ABI
+                  declared in include/gbqv.h (built into libgbqv.so)
+  _capi.py        ctypes binding of that ABI
+  qubitvector.py  QubitVector / DensityMatrix (the reference's qreg surface)
+  circuit.py      instruction list -> engine op list
+  noise.py        noise channels as superoperators
+  simulator.py    AerSimulator-shaped run() with fusion, sampling, saves
+  adjoint.py      adjoint-method gradients behind torch.autograd
+"""
+from ._capi import GBQVError, lib
+from .circuit import NativeCircuit, QuantumCircuit
+from .noise import (NoiseModel, QuantumError, amplitude_damping_error, depolarizing_error,
+                    phase_amplitude_damping_error)
+from .qubitvector import DensityMatrix, QubitVector
+from .simulator import AerSimulator, Result, uniforms
+from . import adjoint
+
+__all__ = [
+    "AerSimulator", "adjoint", "DensityMatrix", "GBQVError", "NativeCircuit", "NoiseModel", "QuantumCircuit",
+    "QuantumError", "QubitVector", "Result", "amplitude_damping_error", "depolarizing_error", "lib",
+    "phase_amplitude_damping_error", "uniforms",
+]
+
+
+def build(force: bool = False):
+    """Compile libgbqv.so in tree (nvcc, sm_103a)."""
+    from . import _build
+
+    return _build.build(force=force)

@@ -1,0 +1,220 @@
+"""A minimal circuit builder (qiskit is not a dependency) whose instructions
+assemble into the engine's op list the way ``aer_compiler._assemble_op``
+(qiskit_aer/backends/aer_compiler.py:875-1020) assembles qiskit instructions
+into AerCircuit ops: named gates, ``unitary``, ``diagonal``, ``superop``,
+``kraus``, ``reset``, ``barrier``, final ``measure`` and the save
+instructions ``save_statevector`` / ``save_density_matrix`` /
+``save_probabilities`` / ``save_expectation_value``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi as A
+
+
+@dataclass
+class Instruction:
+    kind: str                      # "gate" | "unitary" | "diagonal" | "superop" | "kraus" | "reset" | "barrier" | "measure" | "save"
+    name: str
+    qubits: list
+    params: list = field(default_factory=list)
+    data: object = None            # matrix / diagonal / kraus list / save payload
+    clbits: list = field(default_factory=list)
+
+
+class QuantumCircuit:
+    def __init__(self, num_qubits: int, num_clbits: int = 0, name: str = "circuit"):
+        self.num_qubits = int(num_qubits)
+        self.num_clbits = int(num_clbits)
+        self.name = name
+        self.data: list[Instruction] = []
+
+    # ---- generic ----
+    def append_gate(self, name: str, qubits, params=()):
+        self.data.append(Instruction("gate", name, [int(q) for q in qubits], [float(p) for p in params]))
+        return self
+
+    def unitary(self, mat, qubits, label="unitary"):
+        self.data.append(Instruction("unitary", label, [int(q) for q in qubits], data=np.asarray(mat, dtype=complex)))
+        return self
+
+    def diagonal(self, diag, qubits):
+        self.data.append(Instruction("diagonal", "diagonal", [int(q) for q in qubits], data=np.asarray(diag, dtype=complex)))
+        return self
+
+    def superop(self, mat, qubits):
+        self.data.append(Instruction("superop", "superop", [int(q) for q in qubits], data=np.asarray(mat, dtype=complex)))
+        return self
+
+    def kraus(self, mats, qubits):
+        self.data.append(Instruction("kraus", "kraus", [int(q) for q in qubits], data=[np.asarray(m, dtype=complex) for m in mats]))
+        return self
+
+    def reset(self, qubits):
+        qubits = [qubits] if np.isscalar(qubits) else qubits
+        self.data.append(Instruction("reset", "reset", [int(q) for q in qubits]))
+        return self
+
+    def barrier(self, *qubits):
+        self.data.append(Instruction("barrier", "barrier", [int(q) for q in qubits]))
+        return self
+
+    def measure(self, qubits, clbits):
+        qubits = [qubits] if np.isscalar(qubits) else qubits
+        clbits = [clbits] if np.isscalar(clbits) else clbits
+        self.num_clbits = max(self.num_clbits, max(clbits) + 1)
+        self.data.append(Instruction("measure", "measure", [int(q) for q in qubits], clbits=[int(c) for c in clbits]))
+        return self
+
+    def measure_all(self):
+        return self.measure(list(range(self.num_qubits)), list(range(self.num_qubits)))
+
+    def save_statevector(self, label="statevector"):
+        self.data.append(Instruction("save", "statevector", [], data=label))
+        return self
+
+    def save_density_matrix(self, label="density_matrix"):
+        self.data.append(Instruction("save", "density_matrix", [], data=label))
+        return self
+
+    def save_probabilities(self, qubits=None, label="probabilities"):
+        q = list(range(self.num_qubits)) if qubits is None else [int(x) for x in qubits]
+        self.data.append(Instruction("save", "probabilities", q, data=label))
+        return self
+
+    def save_expectation_value(self, terms, label="expectation_value"):
+        """terms: list of (coeff, label, qubits) — the (pauli, coeff) list
+        SaveExpectationValue builds (save_expectation_value.py:61-68)."""
+        self.data.append(Instruction("save", "expval", [], data=(label, list(terms))))
+        return self
+
+    # ---- standard gates (names of the reference gate sets) ----
+    def _g(name, nq, npar=0):
+        def f(self, *args):
+            params, qubits = args[:npar], args[npar:]
+            if len(qubits) == 1 and not np.isscalar(qubits[0]):
+                qubits = tuple(qubits[0])
+            return self.append_gate(name, qubits, params)
+        f.__name__ = name
+        return f
+
+    id = _g("id", 1); x = _g("x", 1); y = _g("y", 1); z = _g("z", 1); h = _g("h", 1)
+    s = _g("s", 1); sdg = _g("sdg", 1); t = _g("t", 1); tdg = _g("tdg", 1); sx = _g("sx", 1); sxdg = _g("sxdg", 1)
+    rx = _g("rx", 1, 1); ry = _g("ry", 1, 1); rz = _g("rz", 1, 1); p = _g("p", 1, 1); u1 = _g("u1", 1, 1)
+    u2 = _g("u2", 1, 2); u3 = _g("u3", 1, 3); u = _g("u", 1, 3); r = _g("r", 1, 2)
+    cx = _g("cx", 2); cy = _g("cy", 2); cz = _g("cz", 2); swap = _g("swap", 2); ecr = _g("ecr", 2)
+    cp = _g("cp", 2, 1); crx = _g("crx", 2, 1); cry = _g("cry", 2, 1); crz = _g("crz", 2, 1)
+    rxx = _g("rxx", 2, 1); ryy = _g("ryy", 2, 1); rzz = _g("rzz", 2, 1); rzx = _g("rzx", 2, 1)
+    ccx = _g("ccx", 3); cswap = _g("cswap", 3); ccz = _g("ccz", 3)
+    del _g
+
+    def mcx(self, controls, target):
+        return self.append_gate("mcx", list(controls) + [target])
+
+    def mcp(self, lam, controls, target):
+        return self.append_gate("mcp", list(controls) + [target], [lam])
+
+    # ---- assembly ----
+    def split_final(self):
+        """Ops before the first measurement / save, the trailing measures, and
+        the saves (a sampleable circuit: measures only at the end,
+        Executor::check_measure_sampling_opt)."""
+        body, meas, saves = [], [], []
+        for ins in self.data:
+            if ins.kind == "measure":
+                meas.append(ins)
+            elif ins.kind == "save":
+                saves.append((len(body), ins))
+            else:
+                if meas:
+                    raise ValueError("only final measurements are supported (no mid-circuit measure)")
+                body.append(ins)
+        return body, meas, saves
+
+
+class NativeCircuit:
+    """The engine's op list (gbqv_circuit_t) built from instructions."""
+
+    def __init__(self, num_qubits: int, instructions=()):
+        self._L = A.lib()
+        h = C.c_void_p()
+        A.check(self._L.gbqv_circuit_create(int(num_qubits), C.byref(h)))
+        self._h = h
+        self.num_qubits = num_qubits
+        for ins in instructions:
+            self.add(ins)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gbqv_circuit_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def add(self, ins: Instruction):
+        q, qp, k = A.qubits_arg(ins.qubits)
+        L = self._L
+        if ins.kind == "gate":
+            pa = np.ascontiguousarray(np.asarray(ins.params, dtype=np.float64))
+            A.check(L.gbqv_circuit_gate(self._h, ins.name.encode(), qp, k, pa.ctypes.data_as(A.dp), pa.size))
+        elif ins.kind == "unitary":
+            m, mp = A.cmat_arg(ins.data)
+            A.check(L.gbqv_circuit_unitary(self._h, qp, k, mp))
+        elif ins.kind == "diagonal":
+            m, mp = A.cmat_arg(np.asarray(ins.data).reshape(-1))
+            A.check(L.gbqv_circuit_diagonal(self._h, qp, k, mp))
+        elif ins.kind == "superop":
+            m, mp = A.cmat_arg(ins.data)
+            A.check(L.gbqv_circuit_superop(self._h, qp, k, mp))
+        elif ins.kind == "kraus":
+            flat = np.concatenate([np.asarray(x, dtype=complex).reshape(-1, order="F") for x in ins.data])
+            m, mp = A.cmat_arg(flat)
+            A.check(L.gbqv_circuit_kraus(self._h, qp, k, len(ins.data), mp))
+        elif ins.kind == "reset":
+            A.check(L.gbqv_circuit_reset(self._h, qp, k))
+        elif ins.kind == "barrier":
+            A.check(L.gbqv_circuit_barrier(self._h, qp, k))
+        else:
+            raise ValueError(f"cannot assemble {ins.kind}")
+
+    def num_ops(self) -> int:
+        n = C.c_int()
+        A.check(self._L.gbqv_circuit_num_ops(self._h, C.byref(n)))
+        return n.value
+
+    def ops(self):
+        """[(type, name, qubits)] of the current op list."""
+        out = []
+        for i in range(self.num_ops()):
+            t, nq = C.c_int(), C.c_int()
+            qb = (C.c_uint64 * 64)()
+            name = C.create_string_buffer(64)
+            A.check(self._L.gbqv_circuit_op_info(self._h, i, C.byref(t), C.byref(nq), qb, 64, name, 64))
+            out.append((t.value, name.value.decode(), [int(qb[j]) for j in range(nq.value)]))
+        return out
+
+    def op_matrix(self, i: int) -> np.ndarray:
+        t, name, q = self.ops()[i]
+        k = len(q)
+        size = {1: 1 << (2 * k), 2: 1 << k, 3: 1 << (4 * k)}.get(t, 1 << (2 * k))
+        out = np.empty(size, dtype=np.complex128)
+        A.check(self._L.gbqv_circuit_op_matrix(self._h, i, out.ctypes.data_as(A.vp), size))
+        return out
+
+    def fuse(self, config: "A.FusionConfig"):
+        applied = C.c_int()
+        name = C.create_string_buffer(16)
+        A.check(self._L.gbqv_circuit_fuse(self._h, C.byref(config), C.byref(applied), name, 16))
+        return bool(applied.value), name.value.decode()

@@ -1,0 +1,125 @@
+// gbqv_internal.h — declarations shared by the host side of libgbqv
+// (gbqv_capi.cpp, gbqv_circuit.cpp) and the CUDA kernels (gbqv_kernels.cu).
+// Nothing here crosses the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+struct gbqv_state;
+
+namespace gbqv {
+
+using cd = std::complex<double>;
+using reg_t = std::vector<uint64_t>;
+
+// Thrown inside the library, turned into a status code at the C ABI.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char *what);
+
+// Limits of the kernels.
+constexpr int kMaxQubits = 40;         // 2^40 c64 = 8 TB: capped by memory anyway
+constexpr int kMaxDenseParamK = 5;     // dense k <= 5: matrix passed as kernel parameter
+constexpr int kMaxDenseK = 10;         // dense k <= 10: matrix in device memory
+constexpr int kMaxDiagK = 10;          // diagonal entries passed as kernel parameter
+constexpr int kMaxPermPairs = 1024;
+constexpr int kReduceBlocks = 152 * 4; // 4 CTAs per SM on a GB300
+constexpr int kReduceThreads = 256;
+constexpr int kSampleBlockBits = 10;   // sub-block of the sampling prefix sums
+constexpr int kMaxTerms = 4096;        // Pauli terms per reduction launch
+
+// Per-handle device state.  Scratch buffers grow on demand and live until
+// the handle is destroyed.
+struct Device {
+  int n = 0;            // vector qubits (2 * logical for a density matrix)
+  int nq = 0;           // logical qubits
+  bool dbl = true;      // complex128 (true) or complex64 (false)
+  bool density = false;
+  int blocking = 1;
+  void *state = nullptr;
+  void *ckpt = nullptr;
+  cudaStream_t stream = nullptr;
+  // scratch
+  double *partials = nullptr; size_t partials_cap = 0;   // reduction partials
+  double *results = nullptr;  size_t results_cap = 0;    // reduction outputs (device)
+  double *h_results = nullptr; size_t h_results_cap = 0; // pinned host mirror
+  void *mat = nullptr; size_t mat_cap = 0;               // large matrices
+  void *aux = nullptr; size_t aux_cap = 0;               // sampling / probabilities
+  void *aux2 = nullptr; size_t aux2_cap = 0;
+  uint64_t amps() const { return 1ULL << n; }
+  size_t amp_bytes() const { return dbl ? 16 : 8; }
+};
+
+void *grow(void *&buf, size_t &cap, size_t bytes);
+Device &device_of(gbqv_state *h);
+// Records the message for gbqv_last_error(h) (h == nullptr: thread-local).
+void set_last_error(gbqv_state *h, const std::string &msg);
+
+// ---- launchers (gbqv_kernels.cu); all are asynchronous on dev.stream ----
+void launch_dense(Device &dev, const reg_t &qubits, const cd *mat);
+void launch_diagonal(Device &dev, const reg_t &qubits, const cd *diag);
+// mc kinds: 0 = X, 1 = Y, 2 = phase (mat[0] = phase), 3 = U (mat = 2x2),
+// 4 = diagonal U (mat[0], mat[1]), 5 = SWAP of the last two qubits
+void launch_mc(Device &dev, const reg_t &qubits, int kind, const cd *mat);
+void launch_swaps(Device &dev, const reg_t &qubits, const std::vector<std::pair<uint32_t, uint32_t>> &pairs);
+void launch_pauli(Device &dev, uint64_t x_mask, uint64_t z_mask, uint64_t x_max, cd phase);
+void launch_dm_y(Device &dev, uint64_t q);
+void launch_scale(Device &dev, cd s);
+void launch_set_basis(Device &dev, uint64_t index, cd value); // zero + one entry
+
+// Reductions: write results into dev.results[0..count) (device), async.
+void reduce_norm(Device &dev);                                   // 1 value
+void reduce_norm_matrix(Device &dev, const reg_t &qubits, const cd *mat); // 1 value
+struct PauliTerm { uint64_t x_mask, z_mask, x_max; double ph_re, ph_im; int diag_only; };
+void reduce_expval(Device &dev, const std::vector<PauliTerm> &terms); // terms.size() values
+void reduce_dm_expval(Device &dev, const std::vector<PauliTerm> &terms);
+void reduce_inner_product(Device &dev);                          // 2 values (re, im)
+void reduce_probabilities(Device &dev, const reg_t &qubits);     // 2^k values
+void reduce_dm_trace(Device &dev);                               // 2 values
+// Probabilities of every basis state into a device buffer of 2^nq doubles.
+void probabilities_all(Device &dev, double *d_out);
+// Sampling: rnds/out are device buffers of `shots` entries.
+void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out);
+
+// Adjoint gradients: out = sum_t c_t P_t src (one pass), and
+// <lam|P|psi> into dev.results[2*slot .. 2*slot+1] (re, im).
+struct HamTerm { uint64_t x_mask, z_mask; double re, im; };
+void ham_apply(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms);
+void reduce_pauli_inner(Device &dev, const void *lam, const void *psi, uint64_t x_mask, uint64_t z_mask, cd phase,
+                        int slot);
+
+// Fused-run (cache-blocked) execution: a run of dense/diagonal ops whose
+// qubits all lie inside one tile of `tile_bits` vector qubits.
+struct RunOp {
+  int kind;       // 0 dense, 1 diagonal
+  reg_t qubits;
+  std::vector<cd> mat;
+};
+// Dispatch rules of the reference members, shared by the C ABI and the
+// circuit executor (gbqv_capi.cpp).
+void apply_matrix_impl(Device &dev, const reg_t &q, const cd *mat);
+void apply_diag_impl(Device &dev, const reg_t &q, const cd *diag);
+void apply_mcu_impl(Device &dev, const reg_t &q, const cd *mat);
+reg_t superop_qubits(const Device &d, const reg_t &q);
+void dm_unitary(Device &d, const reg_t &q, const cd *mat);
+void dm_diag_unitary(Device &d, const reg_t &q, const cd *diag);
+
+// Tile geometry of the run kernel for this state: tile qubits (m), the low
+// qubits every tile contains (c), the matrix pool size in complex128 units,
+// and the longest run.
+int run_tile_qubits(const Device &dev);
+int run_low_qubits(const Device &dev);
+size_t run_pool_bytes(const Device &dev);
+int run_max_ops();
+void launch_run(Device &dev, const std::vector<const RunOp *> &ops);
+
+}  // namespace gbqv

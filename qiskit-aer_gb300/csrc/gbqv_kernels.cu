@@ -1,0 +1,1300 @@
+// gbqv_kernels.cu — sm_103a kernels of the GB300 statevector / density-matrix
+// engine and their launchers.
+//
+// Layout in HBM: one contiguous array of 2^n interleaved complex amplitudes
+// (complex<double>: 16 B, complex<float>: 8 B), amplitude index bit q = qubit
+// q, 256-byte aligned (cudaMalloc).  A density matrix is vec(rho) over 2n
+// vector qubits, column-stacked (rho[i,j] at i + 2^n j), as the reference
+// stores it (src/simulators/density_matrix/densitymatrix.hpp:265-323).
+//
+// Every kernel is a grid-stride loop sized to a multiple of the 152 SMs.
+// A thread owns one "group": the 2^k amplitudes that a k-qubit op mixes,
+// found by inserting zero bits at the sorted target positions of the group
+// number (src/simulators/statevector/indexes.hpp:212-258).  Consecutive
+// threads own consecutive groups, so every load of a group member is
+// coalesced across the warp whenever the targets sit above the 16-byte
+// word; low targets are served from L1 (the partner amplitude is in the
+// same 128-byte line).
+//
+// Reductions accumulate in FP64 in every precision, reduce each CTA with
+// warp shuffles, and combine the CTA partials in a fixed order in a second
+// launch, so results are deterministic run to run.
+#include "gbqv_internal.h"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+
+namespace gbqv {
+
+namespace {
+
+template <typename R> struct V2;
+template <> struct V2<double> { using t = double2; };
+template <> struct V2<float> { using t = float2; };
+
+template <typename T>
+__device__ __forceinline__ T cmul(T a, T b) {
+  T r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+
+// acc += a * b (four FMAs)
+template <typename T>
+__device__ __forceinline__ void cfma(T &acc, T a, T b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+
+template <typename T>
+__device__ __forceinline__ bool is_one(T a) { return a.x == 1 && a.y == 0; }
+
+__device__ __forceinline__ uint64_t insert_zeros(uint64_t i, const uint64_t *lowmask, int k) {
+  for (int j = 0; j < k; ++j) {
+    const uint64_t m = lowmask[j];
+    i = ((i & ~m) << 1) | (i & m);
+  }
+  return i;
+}
+
+template <int K>
+__device__ __forceinline__ uint64_t insert_zeros_k(uint64_t i, const uint64_t *lowmask) {
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    const uint64_t m = lowmask[j];
+    i = ((i & ~m) << 1) | (i & m);
+  }
+  return i;
+}
+
+inline int grid_for(uint64_t work, int threads, int per_sm = 8) {
+  uint64_t blocks = (work + threads - 1) / threads;
+  uint64_t cap = 152ULL * per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+void sorted_masks(const reg_t &qubits, uint64_t *lowmask) {
+  reg_t s = qubits;
+  std::sort(s.begin(), s.end());
+  for (size_t j = 0; j < s.size(); ++j) lowmask[j] = (1ULL << s[j]) - 1;
+}
+
+void local_offsets(const reg_t &qubits, uint64_t *offs) {
+  const int k = (int)qubits.size();
+  offs[0] = 0;
+  for (int j = 0; j < k; ++j) {
+    const uint64_t n = 1ULL << j, bit = 1ULL << qubits[j];
+    for (uint64_t m = 0; m < n; ++m) offs[n + m] = offs[m] | bit;
+  }
+}
+
+template <typename T> T to_dev(const cd &z);
+template <> double2 to_dev<double2>(const cd &z) { return make_double2(z.real(), z.imag()); }
+template <> float2 to_dev<float2>(const cd &z) { return make_float2((float)z.real(), (float)z.imag()); }
+
+void check_launch(const char *what) { cuda_check(cudaGetLastError(), what); }
+
+// -------------------------------------------------------------------------
+// Dense k-qubit matrix, k <= 5: the matrix rides in the kernel parameters
+// (constant bank, broadcast to the warp), the group in registers.
+// Transformer::apply_matrix_n (transformer.hpp:151-171).
+// -------------------------------------------------------------------------
+template <typename T, int K>
+struct DenseParams {
+  T mat[1 << (2 * K)];
+  uint64_t offs[1 << K];
+  uint64_t lowmask[K];
+  uint64_t ngroups;
+};
+
+template <typename T, int K, bool NORM>
+__global__ void __launch_bounds__(256) k_dense(T *__restrict__ psi, const __grid_constant__ DenseParams<T, K> p,
+                                               double *__restrict__ partials) {
+  constexpr int D = 1 << K;
+  double nacc = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < p.ngroups; g += stride) {
+    const uint64_t base = insert_zeros_k<K>(g, p.lowmask);
+    T v[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) v[a] = psi[base + p.offs[a]];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      T acc;
+      acc.x = 0;
+      acc.y = 0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) cfma(acc, p.mat[r + D * c], v[c]);
+      if (NORM)
+        nacc += (double)(acc.x * acc.x + acc.y * acc.y);
+      else
+        psi[base + p.offs[r]] = acc;
+    }
+  }
+  if (NORM) {
+    for (int o = 16; o > 0; o >>= 1) nacc += __shfl_xor_sync(0xffffffffu, nacc, o);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nacc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    }
+  }
+}
+
+// Dense k-qubit matrix, 6 <= k <= 10: one CTA per group, the group staged in
+// shared memory, the matrix read from device memory (L2 resident); thread r
+// computes output row r.  MatrixMultNxN (chunk/thrust_kernels.hpp:900-933).
+template <typename T>
+__global__ void k_dense_big(T *__restrict__ psi, const T *__restrict__ mat, int k, uint64_t ngroups,
+                            const uint64_t *__restrict__ meta) {
+  extern __shared__ unsigned char smem_raw[];
+  T *cache = reinterpret_cast<T *>(smem_raw);
+  const int D = 1 << k;
+  const uint64_t *offs = meta;
+  const uint64_t *lowmask = meta + D;
+  for (uint64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const uint64_t base = insert_zeros(g, lowmask, k);
+    for (int a = threadIdx.x; a < D; a += blockDim.x) cache[a] = psi[base + offs[a]];
+    __syncthreads();
+    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+      T acc;
+      acc.x = 0;
+      acc.y = 0;
+      for (int c = 0; c < D; ++c) cfma(acc, mat[r + (uint64_t)D * c], cache[c]);
+      psi[base + offs[r]] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int K>
+void dense_small(Device &dev, const reg_t &qubits, const cd *mat, bool norm) {
+  DenseParams<T, K> p;
+  constexpr int D = 1 << K;
+  for (int i = 0; i < D * D; ++i) p.mat[i] = to_dev<T>(mat[i]);
+  local_offsets(qubits, p.offs);
+  sorted_masks(qubits, p.lowmask);
+  p.ngroups = dev.amps() >> K;
+  const int threads = 256;
+  if (norm) {
+    const int grid = kReduceBlocks;
+    k_dense<T, K, true><<<grid, threads, 0, dev.stream>>>(reinterpret_cast<T *>(dev.state), p, dev.partials);
+  } else {
+    const int grid = grid_for(p.ngroups, threads);
+    k_dense<T, K, false><<<grid, threads, 0, dev.stream>>>(reinterpret_cast<T *>(dev.state), p, nullptr);
+  }
+  check_launch("dense matrix kernel");
+}
+
+template <typename T>
+void dense_any(Device &dev, const reg_t &qubits, const cd *mat, bool norm) {
+  const int k = (int)qubits.size();
+  switch (k) {
+    case 1: return dense_small<T, 1>(dev, qubits, mat, norm);
+    case 2: return dense_small<T, 2>(dev, qubits, mat, norm);
+    case 3: return dense_small<T, 3>(dev, qubits, mat, norm);
+    case 4: return dense_small<T, 4>(dev, qubits, mat, norm);
+    case 5: return dense_small<T, 5>(dev, qubits, mat, norm);
+    default: break;
+  }
+  if (norm) throw Error(1, "norm(qubits, mat) supports at most 5 qubits");
+  const int D = 1 << k;
+  // matrix + offsets + masks in one device buffer
+  const size_t mat_bytes = sizeof(T) * (size_t)D * D;
+  const size_t meta_bytes = sizeof(uint64_t) * (D + k);
+  grow(dev.mat, dev.mat_cap, mat_bytes + meta_bytes);
+  std::vector<T> hm((size_t)D * D);
+  for (size_t i = 0; i < hm.size(); ++i) hm[i] = to_dev<T>(mat[i]);
+  std::vector<uint64_t> meta(D + k);
+  local_offsets(qubits, meta.data());
+  sorted_masks(qubits, meta.data() + D);
+  cuda_check(cudaMemcpyAsync(dev.mat, hm.data(), mat_bytes, cudaMemcpyHostToDevice, dev.stream), "matrix upload");
+  uint64_t *d_meta = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(dev.mat) + mat_bytes);
+  cuda_check(cudaMemcpyAsync(d_meta, meta.data(), meta_bytes, cudaMemcpyHostToDevice, dev.stream), "matrix upload");
+  // the host copies above are from pageable memory: cudaMemcpyAsync returns
+  // only once the source has been consumed, so hm/meta may go out of scope.
+  const uint64_t ngroups = dev.amps() >> k;
+  const int threads = std::min(D, 1024);
+  const int grid = (int)std::min<uint64_t>(ngroups, 152ULL * 16);
+  k_dense_big<T><<<grid, threads, sizeof(T) * D, dev.stream>>>(reinterpret_cast<T *>(dev.state),
+                                                                 reinterpret_cast<const T *>(dev.mat), k, ngroups,
+                                                                 d_meta);
+  check_launch("dense matrix kernel (k > 5)");
+}
+
+// -------------------------------------------------------------------------
+// Diagonal matrix: Transformer::apply_diagonal_matrix (transformer.hpp:234-258)
+// -------------------------------------------------------------------------
+template <typename T>
+struct DiagParams {
+  T diag[1 << kMaxDiagK];
+  uint64_t qbit[kMaxDiagK];
+  int k;
+  uint64_t n_amps;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_diag(T *__restrict__ psi, const __grid_constant__ DiagParams<T> p) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_amps; i += stride) {
+    uint32_t iv = 0;
+    for (int j = 0; j < p.k; ++j) iv |= ((i & p.qbit[j]) != 0) << j;
+    const T d = p.diag[iv];
+    if (!is_one(d)) psi[i] = cmul(psi[i], d);
+  }
+}
+
+template <typename T>
+void diag_any(Device &dev, const reg_t &qubits, const cd *diag) {
+  const int k = (int)qubits.size();
+  if (k > kMaxDiagK) throw Error(1, "diagonal matrix supports at most 10 qubits per call");
+  DiagParams<T> p;
+  for (int i = 0; i < (1 << k); ++i) p.diag[i] = to_dev<T>(diag[i]);
+  for (int j = 0; j < k; ++j) p.qbit[j] = 1ULL << qubits[j];
+  p.k = k;
+  p.n_amps = dev.amps();
+  k_diag<T><<<grid_for(p.n_amps, 256), 256, 0, dev.stream>>>(reinterpret_cast<T *>(dev.state), p);
+  check_launch("diagonal kernel");
+}
+
+// -------------------------------------------------------------------------
+// Multi-controlled gates (qubitvector.hpp:1446-1720)
+// -------------------------------------------------------------------------
+template <typename T>
+struct McParams {
+  uint64_t lowmask[kMaxQubits];
+  int nq;
+  int kind;
+  uint64_t p0, p1;
+  uint64_t ngroups;
+  T m[4];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mc(T *__restrict__ psi, const __grid_constant__ McParams<T> p) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < p.ngroups; g += stride) {
+    const uint64_t b = insert_zeros(g, p.lowmask, p.nq);
+    const uint64_t i0 = b | p.p0, i1 = b | p.p1;
+    switch (p.kind) {
+      case 0:
+      case 5: {  // X / SWAP: exchange
+        const T a = psi[i0];
+        psi[i0] = psi[i1];
+        psi[i1] = a;
+        break;
+      }
+      case 1: {  // Y: (i0, i1) <- (-i a1, i a0)
+        const T a0 = psi[i0], a1 = psi[i1];
+        T r0, r1;
+        r0.x = a1.y;
+        r0.y = -a1.x;
+        r1.x = -a0.y;
+        r1.y = a0.x;
+        psi[i0] = r0;
+        psi[i1] = r1;
+        break;
+      }
+      case 2:  // phase on the all-ones entry
+        psi[i1] = cmul(psi[i1], p.m[0]);
+        break;
+      case 3: {  // 2x2 column-major
+        const T a0 = psi[i0], a1 = psi[i1];
+        T r0 = cmul(p.m[0], a0), r1 = cmul(p.m[1], a0);
+        cfma(r0, p.m[2], a1);
+        cfma(r1, p.m[3], a1);
+        psi[i0] = r0;
+        psi[i1] = r1;
+        break;
+      }
+      case 4:  // diagonal 2x2
+        psi[i0] = cmul(p.m[0], psi[i0]);
+        psi[i1] = cmul(p.m[1], psi[i1]);
+        break;
+    }
+  }
+}
+
+template <typename T>
+void mc_any(Device &dev, const reg_t &qubits, int kind, const cd *mat) {
+  McParams<T> p;
+  const int N = (int)qubits.size();
+  sorted_masks(qubits, p.lowmask);
+  p.nq = N;
+  p.kind = kind;
+  uint64_t ctrl = 0;
+  if (kind == 5) {
+    for (int j = 0; j < N - 2; ++j) ctrl |= 1ULL << qubits[j];
+    p.p0 = ctrl | (1ULL << qubits[N - 2]);
+    p.p1 = ctrl | (1ULL << qubits[N - 1]);
+  } else {
+    for (int j = 0; j < N - 1; ++j) ctrl |= 1ULL << qubits[j];
+    p.p0 = ctrl;
+    p.p1 = ctrl | (1ULL << qubits[N - 1]);
+  }
+  p.ngroups = dev.amps() >> N;
+  const int nm = kind == 2 ? 1 : kind == 3 ? 4 : kind == 4 ? 2 : 0;
+  for (int i = 0; i < 4; ++i) p.m[i] = to_dev<T>(i < nm ? mat[i] : cd(0, 0));
+  k_mc<T><<<grid_for(p.ngroups, 256), 256, 0, dev.stream>>>(reinterpret_cast<T *>(dev.state), p);
+  check_launch("multi-controlled gate kernel");
+}
+
+// -------------------------------------------------------------------------
+// Ordered pair swaps inside each group: apply_permutation_matrix
+// (qubitvector.hpp:1349-1434); the density-matrix cnot / swap / toffoli / x
+// are such permutations on (q, q+n) (densitymatrix.hpp:331-440).
+// -------------------------------------------------------------------------
+struct SwapParams {
+  uint64_t offs[1 << 10];
+  uint64_t lowmask[10];
+  uint32_t pairs[2 * kMaxPermPairs];
+  int k, npairs;
+  uint64_t ngroups;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_swaps(T *__restrict__ psi, const SwapParams *__restrict__ p) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < p->ngroups; g += stride) {
+    const uint64_t b = insert_zeros(g, p->lowmask, p->k);
+    for (int j = 0; j < p->npairs; ++j) {
+      const uint64_t i0 = b + p->offs[p->pairs[2 * j]], i1 = b + p->offs[p->pairs[2 * j + 1]];
+      const T a = psi[i0];
+      psi[i0] = psi[i1];
+      psi[i1] = a;
+    }
+  }
+}
+
+template <typename T>
+void swaps_any(Device &dev, const reg_t &qubits, const std::vector<std::pair<uint32_t, uint32_t>> &pairs) {
+  const int k = (int)qubits.size();
+  if (k > 10) throw Error(1, "permutation matrix supports at most 10 qubits");
+  if (pairs.size() > (size_t)kMaxPermPairs) throw Error(1, "too many permutation pairs");
+  auto p = std::make_unique<SwapParams>();
+  local_offsets(qubits, p->offs);
+  sorted_masks(qubits, p->lowmask);
+  for (size_t j = 0; j < pairs.size(); ++j) {
+    p->pairs[2 * j] = pairs[j].first;
+    p->pairs[2 * j + 1] = pairs[j].second;
+  }
+  p->k = k;
+  p->npairs = (int)pairs.size();
+  p->ngroups = dev.amps() >> k;
+  grow(dev.mat, dev.mat_cap, sizeof(SwapParams));
+  cuda_check(cudaMemcpyAsync(dev.mat, p.get(), sizeof(SwapParams), cudaMemcpyHostToDevice, dev.stream),
+             "permutation upload");
+  k_swaps<T><<<grid_for(p->ngroups, 256), 256, 0, dev.stream>>>(reinterpret_cast<T *>(dev.state),
+                                                                   reinterpret_cast<const SwapParams *>(dev.mat));
+  check_launch("permutation kernel");
+}
+
+// -------------------------------------------------------------------------
+// Pauli string: QubitVector::apply_pauli (qubitvector.hpp:2392-2433)
+// -------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_pauli(T *__restrict__ psi, uint64_t x_mask, uint64_t z_mask, uint64_t x_max,
+                                               T phase, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t mask_l = (1ULL << x_max) - 1;
+  const uint64_t mask_u = ~((1ULL << (x_max + 1)) - 1);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    if (!x_mask) {
+      T a = psi[i];
+      if (z_mask && (__popcll(i & z_mask) & 1)) {
+        a.x = -a.x;
+        a.y = -a.y;
+      }
+      psi[i] = cmul(a, phase);
+    } else {
+      const uint64_t i0 = ((i << 1) & mask_u) | (i & mask_l);
+      const uint64_t i1 = i0 ^ x_mask;
+      T a0 = psi[i1], a1 = psi[i0];  // swapped
+      if (z_mask && (__popcll(i0 & z_mask) & 1)) {
+        a0.x = -a0.x;
+        a0.y = -a0.y;
+      }
+      if (z_mask && (__popcll(i1 & z_mask) & 1)) {
+        a1.x = -a1.x;
+        a1.y = -a1.y;
+      }
+      psi[i0] = cmul(a0, phase);
+      psi[i1] = cmul(a1, phase);
+    }
+  }
+}
+
+// DensityMatrix Y superoperator (densitymatrix.hpp:415-428) on (q, q+n):
+// swap(0,3); (1,2) <- (-a2, -a1).
+template <typename T>
+__global__ void k_dm_y(T *__restrict__ psi, uint64_t m0, uint64_t m1, uint64_t b0, uint64_t b1, uint64_t ngroups) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += stride) {
+    uint64_t b = ((g & ~m0) << 1) | (g & m0);
+    b = ((b & ~m1) << 1) | (b & m1);
+    const T a0 = psi[b], a1 = psi[b | b0], a2 = psi[b | b1], a3 = psi[b | b0 | b1];
+    T n1, n2;
+    n1.x = -a2.x;
+    n1.y = -a2.y;
+    n2.x = -a1.x;
+    n2.y = -a1.y;
+    psi[b] = a3;
+    psi[b | b0 | b1] = a0;
+    psi[b | b0] = n1;
+    psi[b | b1] = n2;
+  }
+}
+
+template <typename T>
+__global__ void k_scale(T *__restrict__ psi, T s, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) psi[i] = cmul(psi[i], s);
+}
+
+template <typename T>
+__global__ void k_set_basis(T *__restrict__ psi, uint64_t index, T value, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    T z;
+    z.x = 0;
+    z.y = 0;
+    psi[i] = i == index ? value : z;
+  }
+}
+
+// -------------------------------------------------------------------------
+// Reductions
+// -------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  }
+  return s;  // valid in thread 0
+}
+
+// partials laid out [value][block]; out[v] = sum over blocks in order.
+__global__ void k_finish(const double *__restrict__ partials, int nblocks, int nvalues, double *__restrict__ out) {
+  for (int v = blockIdx.x; v < nvalues; v += gridDim.x) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(size_t)v * nblocks + b];
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[v] = s;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_norm(const T *__restrict__ psi, uint64_t count, double *__restrict__ partials) {
+  double acc = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const T a = psi[i];
+    acc += (double)(a.x * a.x + a.y * a.y);
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+// Expectation values of many Pauli strings, term = blockIdx.y
+// (QubitVector::expval_pauli, qubitvector.hpp:2299-2347).
+struct TermDev {
+  uint64_t x_mask, z_mask, x_max;
+  double ph_re, ph_im;
+  int diag_only;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n, const TermDev *__restrict__ terms,
+                                                double *__restrict__ partials) {
+  const TermDev t = terms[blockIdx.y];
+  using R = decltype(T::x);
+  const R pr = (R)t.ph_re, pi = (R)t.ph_im;
+  double acc = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if (!t.x_mask) {
+    const uint64_t count = 1ULL << n;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+      const T a = psi[i];
+      // real(phase * a * conj(a)) = Re(phase) * |a|^2 in the data precision
+      R v = pr * (a.x * a.x + a.y * a.y);
+      if (t.z_mask && (__popcll(i & t.z_mask) & 1)) v = -v;
+      acc += (double)v;
+    }
+  } else {
+    const uint64_t count = 1ULL << (n - 1);
+    const uint64_t mask_l = (1ULL << t.x_max) - 1;
+    const uint64_t mask_u = ~((1ULL << (t.x_max + 1)) - 1);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+      const uint64_t i0 = ((i << 1) & mask_u) | (i & mask_l);
+      const uint64_t i1 = i0 ^ t.x_mask;
+      const T a0 = psi[i0], a1 = psi[i1];
+      // z = a1 * conj(a0); v0 = Re(phase * z), v1 = Re(phase * conj(z))
+      const R zr = a1.x * a0.x + a1.y * a0.y;
+      const R zi = a1.y * a0.x - a1.x * a0.y;
+      R v0 = pr * zr - pi * zi;
+      R v1 = pr * zr + pi * zi;
+      if (t.z_mask && (__popcll(i0 & t.z_mask) & 1)) v0 = -v0;
+      if (t.z_mask && (__popcll(i1 & t.z_mask) & 1)) v1 = -v1;
+      acc += (double)v0;
+      acc += (double)v1;
+    }
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = acc;
+}
+
+// DensityMatrix::expval_pauli (densitymatrix.hpp:445-496): rho is 2^nq x 2^nq.
+template <typename T>
+__global__ void __launch_bounds__(256) k_dm_expval(const T *__restrict__ rho, int nq, const TermDev *__restrict__ terms,
+                                                   double *__restrict__ partials) {
+  const TermDev t = terms[blockIdx.y];
+  using R = decltype(T::x);
+  const uint64_t nrows = 1ULL << nq;
+  double acc = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if (!t.x_mask) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+      R v = rho[i * (nrows + 1)].x;
+      if (t.z_mask && (__popcll(i & t.z_mask) & 1)) v = -v;
+      acc += (double)v;
+    }
+  } else {
+    const R pr = (R)t.ph_re, pi = (R)t.ph_im;
+    const uint64_t mask_l = (1ULL << t.x_max) - 1;
+    const uint64_t mask_u = ~((1ULL << (t.x_max + 1)) - 1);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (nrows >> 1); i += stride) {
+      const uint64_t iv = ((i << 1) & mask_u) | (i & mask_l);
+      const T a = rho[(iv ^ t.x_mask) + nrows * iv];
+      R v = 2 * (pr * a.x - pi * a.y);
+      if (t.z_mask && (__popcll(iv & t.z_mask) & 1)) v = -v;
+      acc += (double)v;
+    }
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_inner(const T *__restrict__ psi, const T *__restrict__ ck, uint64_t count,
+                                               double *__restrict__ partials) {
+  double re = 0.0, im = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const T a = psi[i], b = ck[i];
+    // a * conj(b)
+    re += (double)(a.x * b.x + a.y * b.y);
+    im += (double)(a.y * b.x - a.x * b.y);
+  }
+  re = block_sum(re);
+  if (threadIdx.x == 0) partials[blockIdx.x] = re;
+  im = block_sum(im);
+  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = im;
+}
+
+template <typename T>
+__global__ void k_dm_trace(const T *__restrict__ rho, uint64_t nrows, double *__restrict__ partials) {
+  double re = 0.0, im = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+    const T a = rho[i * (nrows + 1)];
+    re += (double)a.x;
+    im += (double)a.y;
+  }
+  re = block_sum(re);
+  if (threadIdx.x == 0) partials[blockIdx.x] = re;
+  im = block_sum(im);
+  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = im;
+}
+
+// Marginal probabilities over k <= 10 qubits (QubitVector::probabilities,
+// qubitvector.hpp:2096-2143).  Bins [32*blockIdx.y, +32) per launch row;
+// each thread accumulates its 32 bins in registers.
+struct ProbParams {
+  uint64_t offs[1 << 10];
+  uint64_t lowmask[10];
+  int k;
+  uint64_t ngroups;
+  uint64_t diag_stride;  // 0: statevector |a|^2; else density-matrix diagonal stride (nrows+1)
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_probs(const T *__restrict__ psi, const ProbParams *__restrict__ p,
+                                               double *__restrict__ partials) {
+  const int D = 1 << p->k;
+  const int bin0 = blockIdx.y * 32;
+  const int nb = min(32, D - bin0);
+  double acc[32];
+#pragma unroll
+  for (int b = 0; b < 32; ++b) acc[b] = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < p->ngroups; g += stride) {
+    const uint64_t base = insert_zeros(g, p->lowmask, p->k);
+#pragma unroll
+    for (int b = 0; b < 32; ++b) {
+      if (b < nb) {
+        const uint64_t idx = base + p->offs[bin0 + b];
+        if (p->diag_stride) {
+          acc[b] += (double)psi[idx * p->diag_stride].x;
+        } else {
+          const T a = psi[idx];
+          acc[b] += (double)(a.x * a.x + a.y * a.y);
+        }
+      }
+    }
+  }
+  for (int b = 0; b < nb; ++b) {
+    const double s = block_sum(acc[b]);
+    if (threadIdx.x == 0) partials[(size_t)(bin0 + b) * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+template <typename T>
+__global__ void k_probs_all(const T *__restrict__ psi, uint64_t count, uint64_t diag_stride, double *__restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    if (diag_stride) {
+      out[i] = (double)psi[i * diag_stride].x;
+    } else {
+      const T a = psi[i];
+      out[i] = (double)(a.x * a.x + a.y * a.y);
+    }
+  }
+}
+
+// -------------------------------------------------------------------------
+// Sampling (QubitVector::sample_measure, qubitvector.hpp:2148-2228):
+// FP64 sums of 2^10-amplitude sub-blocks, an exclusive prefix over them, then
+// one warp per shot: binary search over the sub-block prefix, and an in-warp
+// scan of the sub-block's probabilities to the first index whose cumulative
+// probability exceeds the uniform.
+// -------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ double prob_at(const T *psi, uint64_t i, uint64_t diag_stride) {
+  if (diag_stride) return (double)psi[i * diag_stride].x;
+  const T a = psi[i];
+  return (double)(a.x * a.x + a.y * a.y);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_block_sums(const T *__restrict__ psi, uint64_t nblocks, int block_bits,
+                                                    uint64_t diag_stride, double *__restrict__ sums) {
+  // one warp per sub-block
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t bsz = 1ULL << block_bits;
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nblocks; w += warps) {
+    double s = 0.0;
+    for (uint64_t j = lane; j < bsz; j += 32) s += prob_at(psi, w * bsz + j, diag_stride);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sums[w] = s;
+  }
+}
+
+// In-place inclusive scan of each chunk of 1024 values; chunk totals to tot.
+__global__ void k_scan_chunks(double *__restrict__ v, uint64_t count, double *__restrict__ tot) {
+  __shared__ double s[1024];
+  const uint64_t base = (uint64_t)blockIdx.x * 1024;
+  const int t = threadIdx.x;
+  s[t] = base + t < count ? v[base + t] : 0.0;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const double add = t >= off ? s[t - off] : 0.0;
+    __syncthreads();
+    s[t] += add;
+    __syncthreads();
+  }
+  if (base + t < count) v[base + t] = s[t];
+  if (t == 1023) tot[blockIdx.x] = s[1023];
+}
+
+// Sequential exclusive scan of the (few) chunk totals, then add to chunks.
+__global__ void k_scan_totals(double *__restrict__ tot, uint64_t nchunks) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double run = 0.0;
+    for (uint64_t c = 0; c < nchunks; ++c) {
+      const double t = tot[c];
+      tot[c] = run;
+      run += t;
+    }
+  }
+}
+
+__global__ void k_add_offsets(double *__restrict__ v, uint64_t count, const double *__restrict__ tot) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) v[i] += tot[i >> 10];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_sample(const T *__restrict__ psi, int n, const double *__restrict__ cdf,
+                                                uint64_t nblocks, int block_bits, uint64_t diag_stride,
+                                                const double *__restrict__ rnds, uint64_t shots,
+                                                uint64_t *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t END = 1ULL << n;
+  for (uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < shots; s += warps) {
+    const double r = rnds[s];
+    // first sub-block whose inclusive prefix exceeds r
+    uint64_t lo = 0, hi = nblocks;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (r < cdf[mid]) hi = mid; else lo = mid + 1;
+    }
+    uint64_t result = END - 1;
+    if (lo < nblocks) {
+      const uint64_t blk = lo;
+      double p = blk ? cdf[blk - 1] : 0.0;
+      const uint64_t bsz = 1ULL << block_bits, b0 = blk * bsz;
+      bool found = false;
+      for (uint64_t j0 = 0; j0 < bsz && !found; j0 += 32) {
+        const uint64_t idx = b0 + j0 + lane;
+        double v = (j0 + lane < bsz) ? prob_at(psi, idx, diag_stride) : 0.0;
+        // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+          const double u = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += u;
+        }
+        const bool hit = (j0 + lane < bsz) && (r < p + v);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (m) {
+          result = b0 + j0 + (__ffs(m) - 1);
+          found = true;
+        }
+        p += __shfl_sync(0xffffffffu, v, 31);
+      }
+      if (!found) result = b0 + bsz - 1;  // rounding between block sum and walk
+      if (result > END - 1) result = END - 1;
+    }
+    if (lane == 0) out[s] = result;
+  }
+}
+
+template <typename T>
+T *st(Device &dev) { return reinterpret_cast<T *>(dev.state); }
+
+void ensure_partials(Device &dev, size_t values) {
+  grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * kReduceBlocks * values);
+  grow(reinterpret_cast<void *&>(dev.results), dev.results_cap, sizeof(double) * values);
+}
+
+void finish(Device &dev, int nvalues, int nblocks = kReduceBlocks) {
+  k_finish<<<std::min(nvalues, 1024), 256, 0, dev.stream>>>(dev.partials, nblocks, nvalues, dev.results);
+  check_launch("reduction finish");
+}
+
+uint64_t diag_stride(const Device &dev) { return dev.density ? (1ULL << dev.nq) + 1 : 0; }
+int sample_bits(const Device &dev) { return dev.density ? dev.nq : dev.n; }
+
+}  // namespace
+
+// ============================== launchers ==============================
+
+#define DISPATCH(dev, F, ...) ((dev).dbl ? F<double2>(__VA_ARGS__) : F<float2>(__VA_ARGS__))
+
+void launch_dense(Device &dev, const reg_t &qubits, const cd *mat) { DISPATCH(dev, dense_any, dev, qubits, mat, false); }
+
+void launch_diagonal(Device &dev, const reg_t &qubits, const cd *diag) { DISPATCH(dev, diag_any, dev, qubits, diag); }
+
+void launch_mc(Device &dev, const reg_t &qubits, int kind, const cd *mat) { DISPATCH(dev, mc_any, dev, qubits, kind, mat); }
+
+void launch_swaps(Device &dev, const reg_t &qubits, const std::vector<std::pair<uint32_t, uint32_t>> &pairs) {
+  DISPATCH(dev, swaps_any, dev, qubits, pairs);
+}
+
+void launch_pauli(Device &dev, uint64_t x_mask, uint64_t z_mask, uint64_t x_max, cd phase) {
+  const uint64_t count = x_mask ? dev.amps() >> 1 : dev.amps();
+  const int grid = grid_for(count, 256);
+  if (dev.dbl)
+    k_pauli<double2><<<grid, 256, 0, dev.stream>>>(st<double2>(dev), x_mask, z_mask, x_max, to_dev<double2>(phase), count);
+  else
+    k_pauli<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), x_mask, z_mask, x_max, to_dev<float2>(phase), count);
+  check_launch("pauli kernel");
+}
+
+void launch_dm_y(Device &dev, uint64_t q) {
+  const uint64_t qa = q, qb = q + dev.nq;
+  const uint64_t m0 = (1ULL << qa) - 1, m1 = (1ULL << qb) - 1;
+  const uint64_t ngroups = dev.amps() >> 2;
+  const int grid = grid_for(ngroups, 256);
+  if (dev.dbl)
+    k_dm_y<double2><<<grid, 256, 0, dev.stream>>>(st<double2>(dev), m0, m1, 1ULL << qa, 1ULL << qb, ngroups);
+  else
+    k_dm_y<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), m0, m1, 1ULL << qa, 1ULL << qb, ngroups);
+  check_launch("density-matrix Y kernel");
+}
+
+void launch_scale(Device &dev, cd s) {
+  const int grid = grid_for(dev.amps(), 256);
+  if (dev.dbl)
+    k_scale<double2><<<grid, 256, 0, dev.stream>>>(st<double2>(dev), to_dev<double2>(s), dev.amps());
+  else
+    k_scale<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), to_dev<float2>(s), dev.amps());
+  check_launch("scale kernel");
+}
+
+void launch_set_basis(Device &dev, uint64_t index, cd value) {
+  const int grid = grid_for(dev.amps(), 256);
+  if (dev.dbl)
+    k_set_basis<double2><<<grid, 256, 0, dev.stream>>>(st<double2>(dev), index, to_dev<double2>(value), dev.amps());
+  else
+    k_set_basis<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), index, to_dev<float2>(value), dev.amps());
+  check_launch("initialize kernel");
+}
+
+void reduce_norm(Device &dev) {
+  ensure_partials(dev, 1);
+  if (dev.dbl)
+    k_norm<double2><<<kReduceBlocks, kReduceThreads, 0, dev.stream>>>(st<double2>(dev), dev.amps(), dev.partials);
+  else
+    k_norm<float2><<<kReduceBlocks, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), dev.amps(), dev.partials);
+  check_launch("norm kernel");
+  finish(dev, 1);
+}
+
+void reduce_norm_matrix(Device &dev, const reg_t &qubits, const cd *mat) {
+  ensure_partials(dev, 1);
+  DISPATCH(dev, dense_any, dev, qubits, mat, true);
+  finish(dev, 1);
+}
+
+static void upload_terms(Device &dev, const std::vector<PauliTerm> &terms, TermDev **d_terms) {
+  const size_t bytes = sizeof(TermDev) * terms.size();
+  grow(dev.aux2, dev.aux2_cap, bytes);
+  std::vector<TermDev> h(terms.size());
+  for (size_t i = 0; i < terms.size(); ++i)
+    h[i] = TermDev{terms[i].x_mask, terms[i].z_mask, terms[i].x_max, terms[i].ph_re, terms[i].ph_im, terms[i].diag_only};
+  cuda_check(cudaMemcpyAsync(dev.aux2, h.data(), bytes, cudaMemcpyHostToDevice, dev.stream), "term upload");
+  *d_terms = reinterpret_cast<TermDev *>(dev.aux2);
+}
+
+void reduce_expval(Device &dev, const std::vector<PauliTerm> &terms) {
+  if (terms.empty()) return;
+  if (terms.size() > (size_t)kMaxTerms) throw Error(1, "too many Pauli terms in one call");
+  ensure_partials(dev, terms.size());
+  TermDev *d_terms;
+  upload_terms(dev, terms, &d_terms);
+  dim3 grid(kReduceBlocks / 4, (unsigned)terms.size());
+  if (dev.dbl)
+    k_expval<double2><<<grid, kReduceThreads, 0, dev.stream>>>(st<double2>(dev), dev.n, d_terms, dev.partials);
+  else
+    k_expval<float2><<<grid, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), dev.n, d_terms, dev.partials);
+  check_launch("expval kernel");
+  finish(dev, (int)terms.size(), kReduceBlocks / 4);
+}
+
+void reduce_dm_expval(Device &dev, const std::vector<PauliTerm> &terms) {
+  if (terms.empty()) return;
+  if (terms.size() > (size_t)kMaxTerms) throw Error(1, "too many Pauli terms in one call");
+  ensure_partials(dev, terms.size());
+  TermDev *d_terms;
+  upload_terms(dev, terms, &d_terms);
+  dim3 grid(kReduceBlocks / 4, (unsigned)terms.size());
+  if (dev.dbl)
+    k_dm_expval<double2><<<grid, kReduceThreads, 0, dev.stream>>>(st<double2>(dev), dev.nq, d_terms, dev.partials);
+  else
+    k_dm_expval<float2><<<grid, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), dev.nq, d_terms, dev.partials);
+  check_launch("density-matrix expval kernel");
+  finish(dev, (int)terms.size(), kReduceBlocks / 4);
+}
+
+void reduce_inner_product(Device &dev) {
+  ensure_partials(dev, 2);
+  if (dev.dbl)
+    k_inner<double2><<<kReduceBlocks, kReduceThreads, 0, dev.stream>>>(
+        st<double2>(dev), reinterpret_cast<const double2 *>(dev.ckpt), dev.amps(), dev.partials);
+  else
+    k_inner<float2><<<kReduceBlocks, kReduceThreads, 0, dev.stream>>>(
+        st<float2>(dev), reinterpret_cast<const float2 *>(dev.ckpt), dev.amps(), dev.partials);
+  check_launch("inner product kernel");
+  finish(dev, 2);
+}
+
+void reduce_dm_trace(Device &dev) {
+  ensure_partials(dev, 2);
+  const uint64_t nrows = 1ULL << dev.nq;
+  if (dev.dbl)
+    k_dm_trace<double2><<<kReduceBlocks, kReduceThreads, 0, dev.stream>>>(st<double2>(dev), nrows, dev.partials);
+  else
+    k_dm_trace<float2><<<kReduceBlocks, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), nrows, dev.partials);
+  check_launch("trace kernel");
+  finish(dev, 2);
+}
+
+void reduce_probabilities(Device &dev, const reg_t &qubits) {
+  const int k = (int)qubits.size();
+  if (k < 1 || k > 10) throw Error(1, "marginal probabilities support 1..10 qubits");
+  const int D = 1 << k;
+  ensure_partials(dev, D);
+  auto p = std::make_unique<ProbParams>();
+  local_offsets(qubits, p->offs);
+  sorted_masks(qubits, p->lowmask);
+  p->k = k;
+  const int nbits = sample_bits(dev);
+  p->ngroups = (1ULL << nbits) >> k;
+  p->diag_stride = diag_stride(dev);
+  grow(dev.aux2, dev.aux2_cap, sizeof(ProbParams));
+  cuda_check(cudaMemcpyAsync(dev.aux2, p.get(), sizeof(ProbParams), cudaMemcpyHostToDevice, dev.stream),
+             "probabilities upload");
+  dim3 grid(kReduceBlocks / 4, (D + 31) / 32);
+  if (dev.dbl)
+    k_probs<double2><<<grid, kReduceThreads, 0, dev.stream>>>(st<double2>(dev),
+                                                              reinterpret_cast<const ProbParams *>(dev.aux2), dev.partials);
+  else
+    k_probs<float2><<<grid, kReduceThreads, 0, dev.stream>>>(st<float2>(dev),
+                                                             reinterpret_cast<const ProbParams *>(dev.aux2), dev.partials);
+  check_launch("probabilities kernel");
+  finish(dev, D, kReduceBlocks / 4);
+}
+
+void probabilities_all(Device &dev, double *d_out) {
+  const uint64_t count = 1ULL << sample_bits(dev);
+  const int grid = grid_for(count, 256);
+  if (dev.dbl)
+    k_probs_all<double2><<<grid, 256, 0, dev.stream>>>(st<double2>(dev), count, diag_stride(dev), d_out);
+  else
+    k_probs_all<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), count, diag_stride(dev), d_out);
+  check_launch("probabilities kernel");
+}
+
+void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out) {
+  const int n = sample_bits(dev);
+  const int bb = std::min(n, kSampleBlockBits);
+  const uint64_t nblocks = 1ULL << (n - bb);
+  const uint64_t nchunks = (nblocks + 1023) / 1024;
+  grow(dev.aux, dev.aux_cap, sizeof(double) * (nblocks + nchunks));
+  double *cdf = reinterpret_cast<double *>(dev.aux);
+  double *tot = cdf + nblocks;
+  const uint64_t ds = diag_stride(dev);
+  const int g1 = grid_for(nblocks * 32, 256);
+  if (dev.dbl)
+    k_block_sums<double2><<<g1, 256, 0, dev.stream>>>(st<double2>(dev), nblocks, bb, ds, cdf);
+  else
+    k_block_sums<float2><<<g1, 256, 0, dev.stream>>>(st<float2>(dev), nblocks, bb, ds, cdf);
+  check_launch("sampling block sums");
+  k_scan_chunks<<<(unsigned)nchunks, 1024, 0, dev.stream>>>(cdf, nblocks, tot);
+  k_scan_totals<<<1, 32, 0, dev.stream>>>(tot, nchunks);
+  k_add_offsets<<<grid_for(nblocks, 256), 256, 0, dev.stream>>>(cdf, nblocks, tot);
+  check_launch("sampling prefix");
+  const int g2 = grid_for(shots * 32, 256, 16);
+  if (dev.dbl)
+    k_sample<double2><<<g2, 256, 0, dev.stream>>>(st<double2>(dev), n, cdf, nblocks, bb, ds, d_rnds, shots, d_out);
+  else
+    k_sample<float2><<<g2, 256, 0, dev.stream>>>(st<float2>(dev), n, cdf, nblocks, bb, ds, d_rnds, shots, d_out);
+  check_launch("sampling search");
+}
+
+// ============================ adjoint-gradient kernels ============================
+// (Pψ)[i] = phase * (-1)^{popcount(i & z)} * ψ[i ^ x] for a Pauli string with
+// masks (x, z) and phase (-i)^{num_y} (QubitVector::apply_pauli,
+// qubitvector.hpp:2392-2433, written as a gather).
+namespace {
+
+struct HamTermDev {
+  uint64_t x_mask, z_mask;
+  double re, im;  // coeff * (-i)^{num_y}
+};
+
+// out = sum_t c_t P_t psi  (one pass writing out, gathers from psi per term)
+template <typename T>
+__global__ void __launch_bounds__(256) k_ham_apply(const T *__restrict__ psi, T *__restrict__ out, uint64_t count,
+                                                   const HamTermDev *__restrict__ terms, int nterms) {
+  using R = decltype(T::x);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    double ar = 0.0, ai = 0.0;
+    for (int t = 0; t < nterms; ++t) {
+      const HamTermDev h = terms[t];
+      const T a = psi[i ^ h.x_mask];
+      double cr = h.re, ci = h.im;
+      if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
+      ar += cr * (double)a.x - ci * (double)a.y;
+      ai += cr * (double)a.y + ci * (double)a.x;
+    }
+    T o;
+    o.x = (R)ar;
+    o.y = (R)ai;
+    out[i] = o;
+  }
+}
+
+// sum_i conj(lam[i]) (P psi)[i] for one Pauli string, FP64 partials [re | im]
+template <typename T>
+__global__ void __launch_bounds__(256) k_pauli_inner(const T *__restrict__ lam, const T *__restrict__ psi, uint64_t count,
+                                                     uint64_t x_mask, uint64_t z_mask, double ph_re, double ph_im,
+                                                     double *__restrict__ partials) {
+  double re = 0.0, im = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const T l = lam[i], a = psi[i ^ x_mask];
+    // conj(l) * a
+    double zr = (double)l.x * a.x + (double)l.y * a.y;
+    double zi = (double)l.x * a.y - (double)l.y * a.x;
+    if (__popcll(i & z_mask) & 1) { zr = -zr; zi = -zi; }
+    re += zr;
+    im += zi;
+  }
+  // times the phase
+  const double pr = re * ph_re - im * ph_im, pi = re * ph_im + im * ph_re;
+  const double r = block_sum(pr);
+  if (threadIdx.x == 0) partials[blockIdx.x] = r;
+  const double q = block_sum(pi);
+  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = q;
+}
+
+}  // namespace
+
+void ham_apply(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms) {
+  const size_t bytes = sizeof(HamTermDev) * terms.size();
+  grow(dev.aux2, dev.aux2_cap, bytes);
+  std::vector<HamTermDev> h(terms.size());
+  for (size_t i = 0; i < terms.size(); ++i) h[i] = HamTermDev{terms[i].x_mask, terms[i].z_mask, terms[i].re, terms[i].im};
+  cuda_check(cudaMemcpyAsync(dev.aux2, h.data(), bytes, cudaMemcpyHostToDevice, dev.stream), "hamiltonian upload");
+  const int grid = grid_for(dev.amps(), 256);
+  if (dev.dbl)
+    k_ham_apply<double2><<<grid, 256, 0, dev.stream>>>(reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst),
+                                                       dev.amps(), reinterpret_cast<const HamTermDev *>(dev.aux2), (int)terms.size());
+  else
+    k_ham_apply<float2><<<grid, 256, 0, dev.stream>>>(reinterpret_cast<const float2 *>(src), reinterpret_cast<float2 *>(dst),
+                                                      dev.amps(), reinterpret_cast<const HamTermDev *>(dev.aux2), (int)terms.size());
+  check_launch("hamiltonian kernel");
+}
+
+void reduce_pauli_inner(Device &dev, const void *lam, const void *psi, uint64_t x_mask, uint64_t z_mask, cd phase,
+                        int slot) {
+  // slot: write the (re, im) pair at results[2*slot], [2*slot+1]
+  const int blocks = kReduceBlocks;
+  grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * blocks * 2);
+  if (dev.dbl)
+    k_pauli_inner<double2><<<blocks, kReduceThreads, 0, dev.stream>>>(
+        reinterpret_cast<const double2 *>(lam), reinterpret_cast<const double2 *>(psi), dev.amps(), x_mask, z_mask,
+        phase.real(), phase.imag(), dev.partials);
+  else
+    k_pauli_inner<float2><<<blocks, kReduceThreads, 0, dev.stream>>>(
+        reinterpret_cast<const float2 *>(lam), reinterpret_cast<const float2 *>(psi), dev.amps(), x_mask, z_mask,
+        phase.real(), phase.imag(), dev.partials);
+  check_launch("pauli inner product kernel");
+  k_finish<<<2, 256, 0, dev.stream>>>(dev.partials, blocks, 2, dev.results + 2 * slot);
+  check_launch("reduction finish");
+}
+
+// ============================ cache-blocked runs ============================
+// A run is a sequence of dense (k <= 5) / diagonal ops whose qubits all lie in
+// one tile of kRunTileBits vector qubits.  A persistent CTA loads a tile
+// (the kRunLowBits lowest qubits are always part of it, so a tile is
+// 2^(m - c) contiguous segments of 2^c amplitudes: coalesced 16-byte loads),
+// applies every op of the run in shared memory, and writes the tile back:
+// one HBM read + write for the whole run instead of one per op.
+namespace {
+
+constexpr int kRunMaxOps = 24;
+
+struct RunOpDev {
+  int kind;                 // 0 dense, 1 diagonal
+  int k;
+  int mat_off;              // offset into the matrix pool (complex entries)
+  uint32_t lowmask[5];      // sorted local positions as masks, for zero insertion
+  uint32_t offs[32];        // local offset of matrix index a
+  uint32_t qbit[5];         // local bit of op qubit j (diagonal index)
+};
+
+struct RunParams {
+  int m, c, nops, pool_elems;
+  uint64_t ntiles;
+  uint64_t tile_lowmask[kMaxQubits];  // sorted tile qubits (zero insertion of the tile id)
+  int nt;                             // number of tile qubits = m
+  int T[24];                          // T[j]: global qubit of local bit j
+  RunOpDev ops[kRunMaxOps];
+};
+
+__device__ __forceinline__ uint32_t ins32(uint32_t i, const uint32_t *lowmask, int k) {
+  for (int j = 0; j < k; ++j) {
+    const uint32_t msk = lowmask[j];
+    i = ((i & ~msk) << 1) | (i & msk);
+  }
+  return i;
+}
+
+template <typename T, int K>
+__device__ __forceinline__ void run_dense(T *tile, const T *mat, const RunOpDev &op, int m) {
+  constexpr int D = 1 << K;
+  const uint32_t G = 1u << (m - K);
+  for (uint32_t g = threadIdx.x; g < G; g += blockDim.x) {
+    const uint32_t base = ins32(g, op.lowmask, K);
+    T v[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) v[a] = tile[base + op.offs[a]];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      T acc;
+      acc.x = 0;
+      acc.y = 0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) cfma(acc, mat[r + D * c], v[c]);
+      tile[base + op.offs[r]] = acc;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void run_diag(T *tile, const T *diag, const RunOpDev &op, int m) {
+  const uint32_t L = 1u << m;
+  for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) {
+    uint32_t iv = 0;
+    for (int j = 0; j < op.k; ++j) iv |= ((l & op.qbit[j]) != 0) << j;
+    const T d = diag[iv];
+    if (!is_one(d)) tile[l] = cmul(tile[l], d);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 2) k_run(T *__restrict__ psi, const RunParams *__restrict__ P,
+                                             const T *__restrict__ pool) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = P->m, c = P->c;
+  T *tile = reinterpret_cast<T *>(smem_raw);
+  T *mats = tile + (1u << m);
+  uint64_t *hi = reinterpret_cast<uint64_t *>(mats + P->pool_elems);
+  for (int i = threadIdx.x; i < P->pool_elems; i += blockDim.x) mats[i] = pool[i];
+  const uint32_t nhi = 1u << (m - c);
+  for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
+    uint64_t a = 0;
+    for (int j = c; j < m; ++j)
+      if ((h >> (j - c)) & 1) a |= 1ULL << P->T[j];
+    hi[h] = a;
+  }
+  __syncthreads();
+  const uint32_t L = 1u << m, cmask = (1u << c) - 1;
+  for (uint64_t t = blockIdx.x; t < P->ntiles; t += gridDim.x) {
+    const uint64_t gbase = insert_zeros(t, P->tile_lowmask, P->nt);
+    for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) tile[l] = psi[gbase | hi[l >> c] | (l & cmask)];
+    __syncthreads();
+    for (int o = 0; o < P->nops; ++o) {
+      const RunOpDev &op = P->ops[o];
+      const T *mat = mats + op.mat_off;
+      if (op.kind == 1) {
+        run_diag(tile, mat, op, m);
+      } else {
+        switch (op.k) {
+          case 1: run_dense<T, 1>(tile, mat, op, m); break;
+          case 2: run_dense<T, 2>(tile, mat, op, m); break;
+          case 3: run_dense<T, 3>(tile, mat, op, m); break;
+          case 4: run_dense<T, 4>(tile, mat, op, m); break;
+          case 5: run_dense<T, 5>(tile, mat, op, m); break;
+        }
+      }
+      __syncthreads();
+    }
+    for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) psi[gbase | hi[l >> c] | (l & cmask)] = tile[l];
+    __syncthreads();
+  }
+}
+
+int run_tile_bits(const Device &dev) { return dev.dbl ? 12 : 13; }
+constexpr int kRunLowBits = 4;
+constexpr int kRunPoolBytes = 32 * 1024;
+
+template <typename T>
+void launch_run_t(Device &dev, const std::vector<const RunOp *> &ops) {
+  const int n = dev.n;
+  const int m = std::min(run_tile_bits(dev), n);
+  // tile qubits: the low c qubits, the ops' qubits, then padding from the bottom
+  std::vector<bool> in(n, false);
+  const int c = std::min(kRunLowBits, m);
+  for (int q = 0; q < c; ++q) in[q] = true;
+  for (auto *op : ops)
+    for (auto q : op->qubits) in[q] = true;
+  int cnt = 0;
+  for (int q = 0; q < n; ++q) cnt += in[q];
+  if (cnt > m) throw Error(1, "run does not fit in a tile");
+  for (int q = 0; q < n && cnt < m; ++q)
+    if (!in[q]) { in[q] = true; ++cnt; }
+  auto P = std::make_unique<RunParams>();
+  std::memset(P.get(), 0, sizeof(RunParams));
+  std::vector<int> tq, local(n, -1);
+  for (int q = 0; q < n; ++q)
+    if (in[q]) { local[q] = (int)tq.size(); tq.push_back(q); }
+  // cc = length of the contiguous low prefix of the tile qubits
+  int cc = 0;
+  while (cc < m && tq[cc] == cc) ++cc;
+  P->m = m;
+  P->c = cc;
+  P->nt = m;
+  for (int j = 0; j < m; ++j) { P->T[j] = tq[j]; P->tile_lowmask[j] = (1ULL << tq[j]) - 1; }
+  P->ntiles = 1ULL << (n - m);
+  if ((int)ops.size() > kRunMaxOps) throw Error(1, "run too long");
+  std::vector<T> pool;
+  for (size_t o = 0; o < ops.size(); ++o) {
+    const RunOp &op = *ops[o];
+    RunOpDev &d = P->ops[o];
+    d.kind = op.kind;
+    d.k = (int)op.qubits.size();
+    d.mat_off = (int)pool.size();
+    reg_t lq;
+    for (auto q : op.qubits) lq.push_back(local[q]);
+    reg_t sq = lq;
+    std::sort(sq.begin(), sq.end());
+    for (int j = 0; j < d.k; ++j) { d.lowmask[j] = (1u << sq[j]) - 1; d.qbit[j] = 1u << lq[j]; }
+    d.offs[0] = 0;
+    for (int j = 0; j < d.k; ++j) {
+      const uint32_t nn = 1u << j, bit = 1u << lq[j];
+      for (uint32_t a = 0; a < nn; ++a) d.offs[nn + a] = d.offs[a] | bit;
+    }
+    for (const cd &z : op.mat) pool.push_back(to_dev<T>(z));
+  }
+  P->nops = (int)ops.size();
+  P->pool_elems = (int)pool.size();
+  if (pool.size() * sizeof(T) > (size_t)kRunPoolBytes) throw Error(1, "run matrices exceed the pool");
+  const size_t pbytes = sizeof(RunParams), poolb = pool.size() * sizeof(T);
+  grow(dev.mat, dev.mat_cap, pbytes + poolb + 256);
+  char *base = reinterpret_cast<char *>(dev.mat);
+  cuda_check(cudaMemcpyAsync(base, P.get(), pbytes, cudaMemcpyHostToDevice, dev.stream), "run upload");
+  const size_t pool_off = (pbytes + 255) & ~size_t(255);
+  if (poolb)
+    cuda_check(cudaMemcpyAsync(base + pool_off, pool.data(), poolb, cudaMemcpyHostToDevice, dev.stream), "run upload");
+  const size_t smem = sizeof(T) * ((1u << m) + pool.size()) + sizeof(uint64_t) * (1u << (m - cc));
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[dev.dbl]) {
+    cuda_check(cudaFuncSetAttribute(k_run<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+               "run kernel attribute");
+    attr_set[dev.dbl] = true;
+  }
+  int per_sm = 0;
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<T>, 256, smem), "occupancy");
+  per_sm = std::max(per_sm, 1);
+  const uint64_t grid = std::min<uint64_t>(P->ntiles, 152ULL * per_sm);
+  k_run<T><<<(unsigned)grid, 256, smem, dev.stream>>>(reinterpret_cast<T *>(dev.state),
+                                                     reinterpret_cast<const RunParams *>(base),
+                                                     reinterpret_cast<const T *>(base + pool_off));
+  check_launch("run kernel");
+}
+
+}  // namespace
+
+int run_tile_qubits(const Device &dev) { return std::min(run_tile_bits(dev), dev.n); }
+int run_low_qubits(const Device &dev) { return std::min(kRunLowBits, dev.n); }
+size_t run_pool_bytes(const Device &dev) { return kRunPoolBytes / dev.amp_bytes() * 16; }
+int run_max_ops() { return kRunMaxOps; }
+
+void launch_run(Device &dev, const std::vector<const RunOp *> &ops) {
+  if (dev.dbl)
+    launch_run_t<double2>(dev, ops);
+  else
+    launch_run_t<float2>(dev, ops);
+}
+
+}  // namespace gbqv

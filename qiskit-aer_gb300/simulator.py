@@ -1,0 +1,197 @@
+"""``AerSimulator``-shaped front end over the GB300 engine.
+
+Mirrors the drop-in site ``AerSimulator(method='statevector'|'density_matrix',
+device='GPU', precision=...)`` (qiskit_aer/backends/aer_simulator.py:713-716)
+and the controller path it drives: per-circuit seeds
+``seed_simulator + 2113*i`` (src/controllers/controller_execute.hpp:188-210),
+the Fusion pass with the per-method defaults of
+``Executor::transpile_fusion`` (simulators/circuit_executor.hpp:1228-1287),
+noise inserted as superoperators for the density-matrix method, ops applied
+in order (State::apply_ops, state.hpp:295-340), final measurements sampled
+from ``shots`` uniforms of one RngEngine stream
+(statevector_state.hpp:1016-1052), and save instructions evaluated where
+they sit.  Result metadata carries the reference's fusion keys
+(fusion.hpp:864-945).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _capi as A
+from .circuit import Instruction, NativeCircuit, QuantumCircuit
+from .qubitvector import DensityMatrix, QubitVector
+
+
+def uniforms(seed: int, count: int) -> np.ndarray:
+    """RngEngine::rand(0,1) stream for `seed` (std::mt19937_64)."""
+    out = np.empty(int(count), dtype=np.float64)
+    A.check(A.lib().gbqv_uniforms(int(seed) & (2**64 - 1), out.size, out.ctypes.data_as(A.dp)))
+    return out
+
+
+class Result:
+    def __init__(self, results, time_taken):
+        self.results = results
+        self.time_taken = time_taken
+
+    def get_counts(self, i=0):
+        return self.results[i]["counts"]
+
+    def data(self, i=0):
+        return self.results[i]["data"]
+
+    def metadata(self, i=0):
+        return self.results[i]["metadata"]
+
+    def get_statevector(self, i=0):
+        return self.results[i]["data"]["statevector"]
+
+
+class AerSimulator:
+    METHODS = ("statevector", "density_matrix")
+
+    def __init__(self, method: str = "statevector", device: str = "GPU", precision: str = "double",
+                 noise_model=None, fusion_enable: bool = True, fusion_max_qubit: int | None = None,
+                 fusion_threshold: int | None = None, fusion_cost_factor: float = 1.8,
+                 fusion_avx2_costs: bool = True, blocking_enable: bool = True, seed_simulator: int | None = None):
+        if method not in self.METHODS:
+            raise ValueError(f"method must be one of {self.METHODS}")
+        if device != "GPU":
+            raise ValueError("this engine runs on the GPU only (device='GPU')")
+        self.method = method
+        self.precision = precision
+        self.noise_model = noise_model
+        self.options = dict(fusion_enable=fusion_enable, fusion_max_qubit=fusion_max_qubit,
+                            fusion_threshold=fusion_threshold, fusion_cost_factor=fusion_cost_factor,
+                            fusion_avx2_costs=fusion_avx2_costs, blocking_enable=blocking_enable,
+                            seed_simulator=seed_simulator)
+
+    # ---- fusion configuration ----
+    def fusion_config(self, has_superop=False, has_kraus=False) -> A.FusionConfig:
+        cfg = A.FusionConfig()
+        A.check(A.lib().gbqv_fusion_default_config(1 if self.method == "density_matrix" else 0, C.byref(cfg)))
+        o = self.options
+        # Executor::transpile_fusion: flags from the circuit's op set, then halving
+        # for Kraus on statevector, then the user config overrides
+        cfg.allow_superop = int(has_superop)
+        cfg.allow_kraus = int(has_kraus)
+        if self.method == "statevector" and has_kraus:
+            cfg.max_qubit //= 2
+        cfg.enable = int(o["fusion_enable"])
+        if o["fusion_max_qubit"] is not None:
+            cfg.max_qubit = int(o["fusion_max_qubit"])
+        if o["fusion_threshold"] is not None:
+            cfg.threshold = int(o["fusion_threshold"])
+        cfg.cost_factor = float(o["fusion_cost_factor"])
+        cfg.avx2_costs = int(o["fusion_avx2_costs"])
+        return cfg
+
+    def _with_noise(self, body, positions=None):
+        """Insert the noise model's superoperators after each matching gate.
+        `positions` (op indices into `body`) are mapped to the new list."""
+        if self.noise_model is None or self.noise_model.is_ideal():
+            return (body, list(positions)) if positions is not None else body
+        if self.method != "density_matrix":
+            raise ValueError("noise is supported with method='density_matrix' (superoperator noise)")
+        out, new_index = [], []
+        for ins in body:
+            new_index.append(len(out))
+            out.append(ins)
+            if ins.kind == "gate":
+                err = self.noise_model.error_for(ins.name)
+                if err is not None:
+                    if err.num_qubits != len(ins.qubits):
+                        raise ValueError(f"error on '{ins.name}' acts on {err.num_qubits} qubits")
+                    out.append(Instruction("superop", "superop", list(ins.qubits), data=err.superop))
+        if positions is None:
+            return out
+        new_index.append(len(out))
+        return out, [new_index[p] for p in positions]
+
+    def compile(self, circuit: QuantumCircuit):
+        """Assemble + fuse; returns (NativeCircuit list per save segment,
+        measures, saves, metadata)."""
+        body, meas, saves = circuit.split_final()
+        body, pos = self._with_noise(body, [p for p, _ in saves])
+        saves = [(p, ins) for p, (_, ins) in zip(pos, saves)]
+        kinds = {i.kind for i in body}
+        cfg = self.fusion_config(has_superop="superop" in kinds, has_kraus="kraus" in kinds)
+        meta = {"fusion": {"enabled": bool(cfg.enable)}}
+        # saves split the op list: fuse each segment separately
+        bounds = sorted({pos for pos, _ in saves} | {len(body)})
+        segments, start, applied_any, method_name = [], 0, False, ""
+        t0 = time.perf_counter()
+        for b in bounds:
+            nc = NativeCircuit(circuit.num_qubits, body[start:b])
+            applied, method_name = nc.fuse(cfg)
+            applied_any |= applied
+            segments.append((b, nc))
+            start = b
+        if cfg.enable:
+            meta["fusion"].update({"threshold": cfg.threshold, "max_fused_qubits": cfg.max_qubit,
+                                   "applied": applied_any, "cost_factor": cfg.cost_factor,
+                                   "time_taken": time.perf_counter() - t0})
+            if method_name:
+                meta["fusion"]["method"] = method_name
+        return segments, meas, saves, meta
+
+    def run(self, circuits, shots: int = 1024, seed_simulator: int | None = None, **_):
+        if isinstance(circuits, QuantumCircuit):
+            circuits = [circuits]
+        seed = seed_simulator if seed_simulator is not None else self.options["seed_simulator"]
+        if seed is None:
+            seed = int(np.random.SeedSequence().entropy & 0x7FFFFFFF)
+        t0 = time.perf_counter()
+        results = [self._run_one(c, shots, seed + 2113 * i) for i, c in enumerate(circuits)]
+        return Result(results, time.perf_counter() - t0)
+
+    def _run_one(self, circuit: QuantumCircuit, shots: int, seed: int):
+        segments, meas, saves, meta = self.compile(circuit)
+        cls = DensityMatrix if self.method == "density_matrix" else QubitVector
+        data = {}
+        with cls(circuit.num_qubits, self.precision) as st:
+            if not self.options["blocking_enable"]:
+                A.check(st._L.gbqv_set_blocking(st.handle, 0))
+            save_iter = iter(saves)
+            pending = next(save_iter, None)
+            for bound, nc in segments:
+                A.check(st._L.gbqv_execute(st.handle, nc.handle), st.handle)
+                while pending is not None and pending[0] == bound:
+                    self._save(st, pending[1], data)
+                    pending = next(save_iter, None)
+            counts = None
+            if meas:
+                qubits = [q for m in meas for q in m.qubits]
+                clbits = [c for m in meas for c in m.clbits]
+                rnds = uniforms(seed, shots)
+                samples = st.sample_measure(rnds)
+                counts = self._counts(samples, qubits, clbits, circuit.num_clbits)
+            st.synchronize()
+        return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
+
+    @staticmethod
+    def _counts(samples, qubits, clbits, num_clbits):
+        memory = np.zeros(samples.size, dtype=np.uint64)
+        for q, c in zip(qubits, clbits):
+            memory |= ((samples >> np.uint64(q)) & np.uint64(1)) << np.uint64(c)
+        vals, cnt = np.unique(memory, return_counts=True)
+        return {format(int(v), f"0{num_clbits}b"): int(n) for v, n in zip(vals, cnt)}
+
+    def _save(self, st, ins, data):
+        if ins.name == "statevector":
+            data[ins.data] = st.copy_to_vector()
+        elif ins.name == "density_matrix":
+            data[ins.data] = st.copy_to_matrix()
+        elif ins.name == "probabilities":
+            data[ins.data] = st.probabilities(ins.qubits)
+        elif ins.name == "expval":
+            label, terms = ins.data
+            pairs = [(q, lab) for _, lab, q in terms]
+            coeffs = [complex(c).real for c, _, _ in terms]
+            vals, total = st.expval_pauli_many(pairs, coeffs)
+            # Base::apply_save_expval adds the imaginary part of complex coefficients too
+            imag = sum(complex(c).imag * v for (c, _, _), v in zip(terms, vals))
+            data[label] = total if imag == 0 else complex(total, imag)
