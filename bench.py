@@ -1,25 +1,33 @@
-"""Headline benchmark: fused-gate application on a 30-qubit quantum-volume
-circuit (30 layers of seeded random qubit pairings, one Haar-random SU(4)
-per pair = 450 two-qubit unitaries), fused by Aer's Fusion pass
-(max_fusion_qubits=5), state resident in HBM.
+"""Benchmarks of the GB300 statevector / density-matrix engine.
 
-A step applies the whole fused circuit once to the 2^30-amplitude state.
-  value  = fused-gate GB/s = (fused ops x 2 x 2^n x bytes/amp) / step time
-           (the algorithmic bytes of one read+write pass per fused op)
-  e2e    = the same metric through the public API (AerSimulator-shaped
-           run through the C ABI) with the initial state uploaded from
-           pinned host memory and the final probabilities of 8 qubits read
-           back, every step
-  roofline = the dominant kernel's achieved bytes per launch / its mean
-           launch time (CUDA events on the engine's stream), against the
-           measured HBM copy bandwidth
-  cpu_baseline = the oracle (a C restatement of Aer's QubitVector) timed on
-           the host cores over a bounded sample of the same fused ops
+Default workload (the headline): fused-gate application on a 30-qubit
+quantum-volume-style circuit — 30 layers, each a seeded random pairing of
+the qubits with one Haar-random SU(4) per pair (450 two-qubit unitaries) —
+fused by Aer's Fusion pass (max 5 qubits; it yields 218 fused ops), with the
+2^30-amplitude state resident in HBM.  One step applies the whole fused
+circuit once.
 
-``--impl reference`` times the reference's CPU algorithm (the oracle port;
-the reference's own build does not exist on the GPU host) on the same
-workload and metric.  The state (17 GB at complex128) exceeds L2 (129 MB),
-so no L2 flush is needed between steps.
+  value    fused-gate GB/s = fused ops x (2 x 2^n x bytes/amp) / step time:
+           the algorithmic bytes of one read+write pass per fused op
+  e2e      the same metric through the public API (AerSimulator-shaped
+           compile+run through the C ABI) with |psi0> uploaded from pinned
+           host memory and the 8-qubit marginal read back, every step
+  roofline the dominant kernel (one fused 4-qubit op over the state): its
+           algorithmic bytes per launch / its mean launch time (CUDA events
+           on the engine's stream), against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (C restatement of Aer's QubitVector + OpenMP) on
+           the host cores, over a bounded sample of the same fused ops
+
+Other workloads (--workload): ``adjoint`` (26-qubit hardware-efficient
+ansatz, 624 parameters, 200 Pauli terms: adjoint gradient vs parameter
+shift), ``dm`` (14-qubit noisy density matrix, depolarizing + amplitude
+damping superoperators, 50 Pauli expectation values), ``sample``
+(probabilities and 100,000 shots on the 30-qubit state).
+
+``--impl reference`` times the reference's CPU algorithm on the same
+workload (the oracle port: the reference's own build exists only where its
+sources do, not on the GPU host), all host threads, bounded per step.
+States of 2^26 amplitudes and more exceed L2 (129 MB), so no flush is needed.
 """
 from __future__ import annotations
 
@@ -70,15 +78,17 @@ def hbm_peak():
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
+    FIELDS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
     def __init__(self):
         self.samples = []
         self._stop = threading.Event()
         self._t = None
 
     def start(self):
+        q = "clocks.sm,clocks.max.sm," + ",".join("clocks_event_reasons." + f for f in self.FIELDS)
+
         def run():
-            q = "clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
-                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
             while not self._stop.is_set():
                 try:
                     out = subprocess.run(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-i", "0"],
@@ -91,34 +101,51 @@ class ClockSampler:
 
         self._t = threading.Thread(target=run, daemon=True)
         self._t.start()
+        return self
 
     def stop(self):
         self._stop.set()
         if self._t:
             self._t.join(timeout=5)
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 2 + i and "Active" in s[2 + i]
-                          and not s[2 + i].startswith("Not")})
+        num = lambda v: v.replace(".", "", 1).isdigit()
+        sm = [float(s[0]) for s in self.samples if s and num(s[0])]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and num(s[1])]
+        reasons = sorted({f for s in self.samples for i, f in enumerate(self.FIELDS)
+                          if len(s) > 2 + i and s[2 + i].strip().lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_baseline(P, fused_ops, n_small, precision, budget_s=12.0):
-    """Oracle (C restatement of Aer's QubitVector, OpenMP) on a bounded sample:
-    the fused ops applied to a 2^n_small state on all host cores."""
+class Timer:
+    """CUDA events recorded on the engine's own stream."""
+
+    def __init__(self, torch, stream_ptr):
+        self.torch = torch
+        self.stream = torch.cuda.ExternalStream(stream_ptr)
+
+    def __enter__(self):
+        self.e0 = self.torch.cuda.Event(enable_timing=True)
+        self.e1 = self.torch.cuda.Event(enable_timing=True)
+        self.e0.record(self.stream)
+        return self
+
+    def __exit__(self, *a):
+        self.e1.record(self.stream)
+        self.e1.synchronize()
+        self.ms = self.e0.elapsed_time(self.e1)
+
+
+def cpu_baseline(fused_ops, n_small, budget_s=12.0):
+    """Oracle (C restatement of Aer's QubitVector, OpenMP on all host cores) on
+    a bounded sample: the workload's fused ops on a 2^n_small complex128 state."""
     from oracle import oracle as O
 
+    O.build()
     threads = os.cpu_count() or 1
     O.set_threads(threads, 14)
     o = O.OracleQV(n_small)
-    # map the ops onto n_small qubits (qubit q -> q mod n_small, keeping them distinct)
     t0 = time.perf_counter()
     done = 0
-    amp_bytes = 16 if precision == "double" else 8
     for q, m in fused_ops:
         qq = [x % n_small for x in q]
         if len(set(qq)) != len(qq):
@@ -128,41 +155,232 @@ def cpu_baseline(P, fused_ops, n_small, precision, budget_s=12.0):
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    gbs = done * 2 * (1 << n_small) * amp_bytes / dt / 1e9
+    gbs = done * 2 * (1 << n_small) * 16 / dt / 1e9
     return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"{done} fused ops of the workload on a {n_small}-qubit complex128 state "
-                      f"({(1 << n_small) * 16 / 1e9:.2f} GB), {dt:.1f} s, OpenMP {threads} threads"}
+                      f"({(1 << n_small) * 16 / 1e9:.2f} GB), {dt:.1f} s wall, OpenMP {threads} threads"}
 
 
-def run_reference_arm(args):
-    """--impl reference: the reference's CPU algorithm (oracle port) on the
-    same workload, all host threads, bounded per step."""
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    P = entry.load_package()
-    from oracle import oracle as O
-
-    O.build()
+def fused_ops_of(P, args):
     qc = qv_circuit(P, args.qubits, args.layers, args.seed)
     segs, _, _, meta = P.AerSimulator(precision=args.precision).compile(qc)
     nc = segs[0][1]
-    fused = [(q, nc.op_matrix(i)) for i, (_, _, q) in enumerate(nc.ops())]
+    return qc, nc, [(q, nc.op_matrix(i)) for i, (_, _, q) in enumerate(nc.ops())]
+
+
+def run_reference_arm(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    P = entry.load_package()
+    _, _, fused = fused_ops_of(P, args)
     n_small = min(args.qubits, 26)
-    vals = []
     for _ in range(args.warmup):
-        cpu_baseline(P, fused[:4], n_small, args.precision, budget_s=2.0)
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(P, fused, n_small, args.precision, budget_s=10.0))
+        cpu_baseline(fused[:2], n_small, budget_s=2.0)
+    vals = [cpu_baseline(fused, n_small, budget_s=8.0) for _ in range(args.steps)]
     v = float(np.median([x["value"] for x in vals]))
-    base = vals[-1]
-    line = {"metric": "fused-gate GB/s", "value": v, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+    print(json.dumps({
+        "metric": "fused-gate GB/s", "value": v, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "dtype": "c128", "data": "synthetic",
+        "config": {"workload": f"QV {args.qubits}q x {args.layers} layers, Aer fusion max 5",
+                   "qubits": args.qubits, "layers": args.layers},
+        "cpu_baseline": {**vals[-1], "value": v},
+        "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def bench_qv(args, torch, P):
+    L = P.lib()
+    qc, nc, fused = fused_ops_of(P, args)
+    nops = len(fused)
+    amp_bytes = 16 if args.precision == "double" else 8
+    pass_bytes = 2 * (1 << args.qubits) * amp_bytes
+    st = P.QubitVector(args.qubits, args.precision)
+    if args.no_blocking:
+        A_check(L, L.gbqv_set_blocking(st.handle, 0), st)
+    timer = lambda: Timer(torch, st.stream())
+
+    def step():
+        A_check(L, L.gbqv_execute(st.handle, nc.handle), st)
+
+    st.initialize()
+    for _ in range(args.warmup):
+        step()
+    st.synchronize()
+    clocks = ClockSampler().start()
+    n0 = L.gbqv_launch_count()
+    with timer() as t:
+        for _ in range(args.steps):
+            step()
+    launches = (L.gbqv_launch_count() - n0) // max(args.steps, 1)
+    clk = clocks.stop()
+    t_step = t.ms / 1e3 / args.steps
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        tt = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = nops * pass_bytes / t_step / 1e9 * world
+    # dominant kernel: one fused 4-qubit op over the whole state
+    q4, m4 = next(((q, m) for q, m in fused if len(q) == 4), fused[0])
+    reps = 5
+    st.apply_matrix(q4, m4)
+    with timer() as t:
+        for _ in range(reps):
+            st.apply_matrix(q4, m4)
+    ms_launch = t.ms / reps
+    peak, peak_kind = hbm_peak()
+    achieved = pass_bytes / (ms_launch / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "kernel": f"dense {len(q4)}-qubit op, {ms_launch:.3f} ms/launch", "peak_kind": peak_kind}
+    # e2e: public API with host buffers
+    e2e = None
+    if args.qubits <= 31:
+        psi0 = np.zeros(1 << args.qubits, dtype=np.complex128)
+        psi0[0] = 1.0
+        sim = P.AerSimulator(precision=args.precision, blocking_enable=not args.no_blocking)
+        t1 = time.perf_counter()
+        for _ in range(max(1, args.steps)):
+            segs, _, _, _ = sim.compile(qc)        # Fusion pass on the host
+            st.initialize_from_vector(psi0)        # H2D
+            A_check(L, L.gbqv_execute(st.handle, segs[0][1].handle), st)
+            st.probabilities(list(range(8)))       # D2H of a marginal
+        st.synchronize()
+        te = (time.perf_counter() - t1) / max(1, args.steps)
+        e2e = {"value": round(nops * pass_bytes / te / 1e9, 3), "unit": "GB/s", "ms_per_step": round(te * 1e3, 2),
+               "h2d_bytes_per_step": int(psi0.nbytes), "d2h_bytes_per_step": 8 * 256}
+        del psi0
+    st.close()
+    base = None
+    if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
+        base = cpu_baseline(fused, min(args.qubits, 26))
+    return {"metric": "fused-gate GB/s", "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
-            "config": {"workload": f"QV {args.qubits}q x {args.layers} layers, Aer fusion max 5", "qubits": args.qubits},
-            "cpu_baseline": {**base, "value": v}, "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0,
-                                                         "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+            "config": {"workload": f"QV {args.qubits}q x {args.layers} layers (Haar SU(4) per pair), Aer fusion max 5",
+                       "qubits": args.qubits, "layers": args.layers, "fused_ops": nops,
+                       "l2": "state larger than L2, no flush", "blocking": not args.no_blocking},
+            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clk}
+
+
+def A_check(L, rc, st):
+    if rc != 0:
+        raise RuntimeError(L.gbqv_last_error(st.handle).decode())
+
+
+def bench_adjoint(args, torch, P):
+    """26 qubits, 12 layers of RY/RZ on every qubit + a CX ladder (624
+    parameters), 200 Pauli terms of weight 1-4 with N(0,1) coefficients."""
+    adj = P.adjoint
+    rng = np.random.default_rng(args.seed)
+    n, layers = args.qubits if args.qubits != 30 else 26, 12
+    ans = adj.hardware_efficient_ansatz(n, layers)
+    ham = adj.random_hamiltonian(n, 200, rng)
+    theta = rng.uniform(-np.pi, np.pi, ans.num_params)
+    eng = adj.Engine(n, args.precision)
+    for _ in range(args.warmup):
+        eng.energy_and_grad(ans, theta, ham)
+    clocks = ClockSampler().start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e, g = eng.energy_and_grad(ans, theta, ham)
+    t_adj = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    # parameter shift on a subset, same engine; extrapolated to all parameters
+    idx = [int(i) for i in rng.choice(ans.num_params, size=args.shift_params, replace=False)]
+    eng.energy(ans, theta, ham)
+    t1 = time.perf_counter()
+    ps = eng.param_shift_grad(ans, theta, ham, idx)
+    t_ps_sub = time.perf_counter() - t1
+    t_ps = t_ps_sub / len(idx) * ans.num_params
+    ps_v = np.array([ps[i] for i in idx])
+    rel = float(np.linalg.norm(g[idx] - ps_v) / np.linalg.norm(ps_v))
+    eng.close()
+    return {"metric": "adjoint-grad time vs param-shift", "value": round(t_ps / t_adj, 2), "unit": "x faster",
+            "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
+            "adjoint_s": round(t_adj, 4), "param_shift_s_extrapolated": round(t_ps, 2),
+            "param_shift_measured": f"{len(idx)} params x 2 evaluations in {t_ps_sub:.2f} s",
+            "rel_err_vs_param_shift": rel, "energy": e,
+            "config": {"workload": f"HEA {n}q x {layers} layers, {ans.num_params} params, 200 Pauli terms",
+                       "qubits": n}, "clocks": clk}
+
+
+def bench_dm(args, torch, P):
+    """14-qubit density matrix: 40 layers of U3 on every qubit + CX on a seeded
+    pairing; after every gate depolarizing p=1e-3 and amplitude damping
+    gamma=2e-3 (4x4 / 16x16 superoperators); 50 random Pauli expvals."""
+    rng = np.random.default_rng(args.seed)
+    n, layers = 14, args.dm_layers
+    e1 = P.depolarizing_error(1e-3, 1).compose(P.amplitude_damping_error(2e-3))
+    nm = P.NoiseModel()
+    nm.add_all_qubit_quantum_error(e1, ["u3"])
+    nm.add_all_qubit_quantum_error(e1.tensor(e1), ["cx"])
+    qc = P.QuantumCircuit(n)
+    for _ in range(layers):
+        for q in range(n):
+            qc.u3(*rng.uniform(0, 2 * np.pi, 3), q)
+        perm = rng.permutation(n)
+        for a, b in zip(perm[0::2], perm[1::2]):
+            qc.cx(int(a), int(b))
+    terms = []
+    for _ in range(50):
+        k = int(rng.integers(1, 5))
+        q = [int(x) for x in rng.choice(n, k, replace=False)]
+        terms.append((float(rng.normal()), "".join(rng.choice(list("IXYZ"), k)), q))
+    qc.save_expectation_value(terms)
+    sim = P.AerSimulator(method="density_matrix", noise_model=nm, precision=args.precision)
+    segs, _, _, meta = sim.compile(qc)
+    nops = segs[0][1].num_ops()
+    L = P.lib()
+    st = P.DensityMatrix(n, args.precision)
+    for _ in range(args.warmup):
+        st.initialize()
+        A_check(L, L.gbqv_execute(st.handle, segs[0][1].handle), st)
+    st.synchronize()
+    clocks = ClockSampler().start()
+    with Timer(torch, st.stream()) as t:
+        for _ in range(args.steps):
+            st.initialize()
+            A_check(L, L.gbqv_execute(st.handle, segs[0][1].handle), st)
+    clk = clocks.stop()
+    t_step = t.ms / 1e3 / args.steps
+    t2 = time.perf_counter()
+    vals, total = st.expval_pauli_many([(q, lab) for _, lab, q in terms], [c for c, _, _ in terms])
+    t_exp = time.perf_counter() - t2
+    st.close()
+    amp = 16 if args.precision == "double" else 8
+    gbs = nops * 2 * (1 << (2 * n)) * amp / t_step / 1e9
+    return {"metric": "fused superop GB/s (density matrix)", "value": round(gbs, 2), "unit": "GB/s",
+            "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t_step * 1e3, 2), "dtype": "c128" if args.precision == "double" else "c64",
+            "data": "synthetic", "fused_ops": nops, "fusion": meta["fusion"],
+            "expval_50_terms_ms": round(t_exp * 1e3, 2), "expval_total": total,
+            "config": {"workload": f"DM {n}q x {layers} layers + depolarizing/amp-damping superops", "qubits": n},
+            "clocks": clk}
+
+
+def bench_sample(args, torch, P):
+    """probabilities() of all qubits and 100,000 shots from seeded uniforms."""
+    L = P.lib()
+    qc, nc, fused = fused_ops_of(P, args)
+    st = P.QubitVector(args.qubits, args.precision)
+    st.initialize()
+    A_check(L, L.gbqv_execute(st.handle, nc.handle), st)
+    rnds = P.uniforms(args.seed, 100_000)
+    st.sample_measure(rnds[:1000])
+    t0 = time.perf_counter()
+    s = st.sample_measure(rnds)
+    t_s = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    pm = st.probabilities(list(range(10)))
+    t_p = time.perf_counter() - t1
+    st.close()
+    return {"metric": "shots/s", "value": round(1e5 / t_s, 1), "unit": "shots/s", "higher_is_better": True,
+            "n_gpus": 1, "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
+            "sample_100k_ms": round(t_s * 1e3, 2), "marginal_10q_ms": round(t_p * 1e3, 2),
+            "config": {"workload": f"QV {args.qubits}q state, 100k shots", "qubits": args.qubits}}
 
 
 def main():
@@ -171,104 +389,31 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="double", choices=["double", "single"])
+    ap.add_argument("--workload", default="qv", choices=["qv", "adjoint", "dm", "sample"])
+    ap.add_argument("--precision", default="single", choices=["double", "single"])
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=30)
+    ap.add_argument("--dm-layers", type=int, default=40)
+    ap.add_argument("--shift-params", type=int, default=6)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-blocking", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
-
-    import torch  # device sync / events and torch.distributed for N > 1
+    import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
     if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+        torch.distributed.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.init()
     P = entry.load_package()
     P.build()
-    L = P.lib()
-    qc = qv_circuit(P, args.qubits, args.layers, args.seed)
-    sim = P.AerSimulator(precision=args.precision)
-    segs, _, _, meta = sim.compile(qc)
-    nc = segs[0][1]
-    ops = nc.ops()
-    amp_bytes = 16 if args.precision == "double" else 8
-    pass_bytes = 2 * (1 << args.qubits) * amp_bytes
-    st = P.QubitVector(args.qubits, args.precision)
-    stream_ptr = C.c_void_p()
-    # time on the engine's own stream: events recorded around gbqv_execute
-    torch.cuda.init()
-
-    def step():
-        A_check(L.gbqv_execute(st.handle, nc.handle), st)
-
-    def A_check(rc, s):
-        if rc != 0:
-            raise RuntimeError(L.gbqv_last_error(s.handle).decode())
-
-    st.initialize()
-    for _ in range(args.warmup):
-        step()
-    st.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    clocks = ClockSampler()
-    clocks.start()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step()
-    st.synchronize()
-    dt = time.perf_counter() - t0
-    clk = clocks.stop()
-    t_step = dt / args.steps
-    if world > 1:
-        tt = torch.tensor([t_step], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
-    value = len(ops) * pass_bytes / t_step / 1e9 * world
-
-    # e2e through the public API: upload |psi0> from pinned host memory, run
-    # the fused circuit, read back the 8-qubit marginal
-    psi0 = np.zeros(1 << args.qubits, dtype=np.complex128) if args.qubits <= 30 else None
-    e2e = None
-    if psi0 is not None:
-        psi0[0] = 1.0
-        t1 = time.perf_counter()
-        for _ in range(max(1, args.steps)):
-            st.initialize_from_vector(psi0)
-            step()
-            st.probabilities(list(range(8)))
-        st.synchronize()
-        te = (time.perf_counter() - t1) / max(1, args.steps)
-        e2e = {"value": round(len(ops) * pass_bytes / te / 1e9, 3), "unit": "GB/s",
-               "h2d_bytes_per_step": int(psi0.nbytes), "d2h_bytes_per_step": 8 * 256}
-    peak, peak_kind = hbm_peak()
-    # dominant kernel: the fused-gate pass; per-launch bytes = one read+write of the state
-    ms_per_launch = t_step * 1e3 / len(ops)
-    achieved = pass_bytes / (ms_per_launch / 1e3) / 1e9
-    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind}
-    base = None
-    if rank == 0 and not args.no_cpu_baseline:
-        fused = [(q, nc.op_matrix(i)) for i, (_, _, q) in enumerate(ops)]
-        base = cpu_baseline(P, fused, min(args.qubits, 26), args.precision)
-    if rank == 0:
-        line = {"metric": "fused-gate GB/s", "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
-                "config": {"workload": f"QV {args.qubits}q x {args.layers} layers (450 Haar SU(4)), Aer fusion max 5",
-                           "qubits": args.qubits, "layers": args.layers, "fused_ops": len(ops),
-                           "l2": "state larger than L2, no flush"},
-                "gpu_launches": None, "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clk}
+    fn = {"qv": bench_qv, "adjoint": bench_adjoint, "dm": bench_dm, "sample": bench_sample}[args.workload]
+    line = fn(args, torch, P)
+    if int(os.environ.get("RANK", "0")) == 0:
         print(json.dumps(line))
-    st.close()
 
 
 if __name__ == "__main__":

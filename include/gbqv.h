@@ -103,6 +103,13 @@ int gbqv_num_vector_qubits(gbqv_handle h, int *out);
 int gbqv_synchronize(gbqv_handle h);
 /* Device pointer of the amplitudes (complex<double> or complex<float>). */
 int gbqv_device_data(gbqv_handle h, void **out);
+/* The handle's cudaStream_t (every kernel of the handle runs on it), for
+ * callers that order their own work or record events around the engine's
+ * (the reference keeps its streams private, device_chunk_container.hpp:422). */
+int gbqv_get_stream(gbqv_handle h, void **out);
+/* Kernels this library has launched since load, all handles (a counter the
+ * benchmark reads around its timed region). */
+uint64_t gbqv_launch_count(void);
 
 /* QubitVector::zero (qubitvector.hpp:973-979). */
 int gbqv_zero(gbqv_handle h);

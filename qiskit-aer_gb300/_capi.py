@@ -54,6 +54,8 @@ _SIGS = {
     "gbqv_num_vector_qubits": (C.c_int, [H, C.POINTER(C.c_int)]),
     "gbqv_synchronize": (C.c_int, [H]),
     "gbqv_device_data": (C.c_int, [H, C.POINTER(vp)]),
+    "gbqv_get_stream": (C.c_int, [H, C.POINTER(vp)]),
+    "gbqv_launch_count": (C.c_uint64, []),
     "gbqv_zero": (C.c_int, [H]),
     "gbqv_initialize": (C.c_int, [H]),
     "gbqv_initialize_from_vector": (C.c_int, [H, vp, C.c_uint64]),

@@ -296,6 +296,12 @@ extern "C" int gbqv_device_data(gbqv_handle h, void **out) {
   return guard(h, [&] { need_handle(h); *out = h->dev.state; });
 }
 
+extern "C" int gbqv_get_stream(gbqv_handle h, void **out) {
+  return guard(h, [&] { need_handle(h); REQUIRE(out, GBQV_ERR_ARG, "null output"); *out = (void *)h->dev.stream; });
+}
+
+extern "C" uint64_t gbqv_launch_count(void) { return launch_count(); }
+
 extern "C" int gbqv_zero(gbqv_handle h) {
   return guard(h, [&] {
     need_handle(h);

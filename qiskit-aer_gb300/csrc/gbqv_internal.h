@@ -25,6 +25,8 @@ struct Error : std::runtime_error {
 };
 
 void cuda_check(cudaError_t e, const char *what);
+// Number of kernels launched by the library (incremented after each launch).
+uint64_t launch_count();
 
 // Limits of the kernels.
 constexpr int kMaxQubits = 40;         // 2^40 c64 = 8 TB: capped by memory anyway

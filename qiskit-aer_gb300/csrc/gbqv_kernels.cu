@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <atomic>
 
 namespace gbqv {
 
@@ -98,7 +99,12 @@ template <typename T> T to_dev(const cd &z);
 template <> double2 to_dev<double2>(const cd &z) { return make_double2(z.real(), z.imag()); }
 template <> float2 to_dev<float2>(const cd &z) { return make_float2((float)z.real(), (float)z.imag()); }
 
-void check_launch(const char *what) { cuda_check(cudaGetLastError(), what); }
+std::atomic<uint64_t> g_launches{0};
+
+void check_launch(const char *what) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  cuda_check(cudaGetLastError(), what);
+}
 
 // -------------------------------------------------------------------------
 // Dense k-qubit matrix, k <= 5: the matrix rides in the kernel parameters
@@ -802,6 +808,8 @@ int sample_bits(const Device &dev) { return dev.density ? dev.nq : dev.n; }
 
 }  // namespace
 
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 // ============================== launchers ==============================
 
 #define DISPATCH(dev, F, ...) ((dev).dbl ? F<double2>(__VA_ARGS__) : F<float2>(__VA_ARGS__))
@@ -987,7 +995,9 @@ void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t 
     k_block_sums<float2><<<g1, 256, 0, dev.stream>>>(st<float2>(dev), nblocks, bb, ds, cdf);
   check_launch("sampling block sums");
   k_scan_chunks<<<(unsigned)nchunks, 1024, 0, dev.stream>>>(cdf, nblocks, tot);
+  check_launch("sampling prefix");
   k_scan_totals<<<1, 32, 0, dev.stream>>>(tot, nchunks);
+  check_launch("sampling prefix");
   k_add_offsets<<<grid_for(nblocks, 256), 256, 0, dev.stream>>>(cdf, nblocks, tot);
   check_launch("sampling prefix");
   const int g2 = grid_for(shots * 32, 256, 16);

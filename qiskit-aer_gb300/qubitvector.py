@@ -74,6 +74,12 @@ class QubitVector:
     def synchronize(self) -> None:
         self._c(self._L.gbqv_synchronize(self._h))
 
+    def stream(self) -> int:
+        """The handle's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        p = C.c_void_p()
+        self._c(self._L.gbqv_get_stream(self._h, C.byref(p)))
+        return p.value or 0
+
     def device_pointer(self) -> int:
         p = C.c_void_p()
         self._c(self._L.gbqv_device_data(self._h, C.byref(p)))
