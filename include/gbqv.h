@@ -304,6 +304,12 @@ int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const int *param_o
  * one op per pass).  blocking = 0 applies one kernel per op. */
 int gbqv_set_blocking(gbqv_handle h, int blocking);
 
+/* Arithmetic of complex128 dense gates on 4 or 5 qubits (no reference
+ * counterpart).  1 (default): exact digit slices on the tensor cores, error
+ * <= ~1e-13 of (row max x group max) per gate; 0: native FP64 FMAs (the
+ * reference's arithmetic, 1.2 TFLOP/s on GB300). */
+int gbqv_set_tensor_c128(gbqv_handle h, int enable);
+
 #ifdef __cplusplus
 }
 #endif

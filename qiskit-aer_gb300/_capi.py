@@ -111,6 +111,7 @@ _SIGS = {
     "gbqv_circuit_fuse": (C.c_int, [H, C.POINTER(FusionConfig), C.POINTER(C.c_int), C.c_char_p, C.c_int]),
     "gbqv_execute": (C.c_int, [H, H]),
     "gbqv_set_blocking": (C.c_int, [H, C.c_int]),
+    "gbqv_set_tensor_c128": (C.c_int, [H, C.c_int]),
     "gbqv_adjoint_expval_grad": (C.c_int, [H, H, C.POINTER(C.c_int), dp, C.c_int, C.c_int, u64p, C.POINTER(C.c_int),
                                            C.POINTER(C.c_char_p), dp, dp, dp]),
 }

@@ -151,6 +151,10 @@ void apply_matrix_impl(Device &dev, const reg_t &q, const cd *mat) {
     }
   }
   REQUIRE((int)q.size() <= kMaxDenseK, GBQV_ERR_ARG, "apply_matrix supports at most 10 qubits");
+  if (tensor_dense_available(dev, (int)q.size())) {
+    launch_dense_tensor(dev, q, mat);
+    return;
+  }
   launch_dense(dev, q, mat);
 }
 
@@ -823,6 +827,13 @@ extern "C" int gbqv_dm_trace(gbqv_handle h, gbqv_c128 *out) {
     read_results(h->dev, r, 2);
     out->re = r[0];
     out->im = r[1];
+  });
+}
+
+extern "C" int gbqv_set_tensor_c128(gbqv_handle h, int enable) {
+  return guard(h, [&] {
+    need_handle(h);
+    h->dev.tensor_c128 = enable != 0;
   });
 }
 

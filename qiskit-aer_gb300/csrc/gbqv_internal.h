@@ -47,6 +47,7 @@ struct Device {
   bool dbl = true;      // complex128 (true) or complex64 (false)
   bool density = false;
   int blocking = 1;
+  bool tensor_c128 = true;  // dense k = 4, 5 complex128 gates on the tensor pipe
   void *state = nullptr;
   void *ckpt = nullptr;
   cudaStream_t stream = nullptr;
@@ -106,6 +107,11 @@ struct RunOp {
   reg_t qubits;
   std::vector<cd> mat;
 };
+// complex128 dense gates of 4 / 5 qubits on the tensor cores (exact digit
+// slices, gbqv_ozaki.h)
+bool tensor_dense_available(const Device &dev, int k);
+void launch_dense_tensor(Device &dev, const reg_t &qubits, const cd *mat);
+
 // Dispatch rules of the reference members, shared by the C ABI and the
 // circuit executor (gbqv_capi.cpp).
 void apply_matrix_impl(Device &dev, const reg_t &q, const cd *mat);

@@ -20,6 +20,7 @@
 // warp shuffles, and combine the CTA partials in a fixed order in a second
 // launch, so results are deterministic run to run.
 #include "gbqv_internal.h"
+#include "gbqv_ozaki.h"
 
 #include <algorithm>
 #include <cstring>
@@ -1006,6 +1007,264 @@ void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t 
   else
     k_sample<float2><<<g2, 256, 0, dev.stream>>>(st<float2>(dev), n, cdf, nblocks, bb, ds, d_rnds, shots, d_out);
   check_launch("sampling search");
+}
+
+// ============================ complex128 on tensor cores ============================
+// Dense k-qubit gates (k = 4, 5) on a complex128 state with FP64 emulated by
+// exact digit slices (gbqv_ozaki.h): each group's 2^(k+1) real parts are
+// split into six bf16 digit planes against the group's exponent, the real
+// form of the matrix [[Re U, -Im U], [Im U, Re U]] into six planes against
+// each row's exponent (host), the 21 plane products with s + t <= 5 run as
+// bf16 MMAs with exact FP32 accumulation per level, and the six level sums
+// are recombined exactly in int64 and rounded once to double.  GB300 runs
+// DFMA at 1.2 TFLOP/s; this path uses the tensor pipe and integer units.
+namespace {
+
+template <int KQ>
+struct OzCfg {
+  static constexpr int D = 1 << KQ;          // amplitudes per group
+  static constexpr int R = 2 * D;            // reals per group (matrix dim)
+  static constexpr int MT = R / 16;          // m-tiles of the real matrix
+  static constexpr int KS = R / 16;          // k-steps
+  static constexpr int NT = KQ == 4 ? 2 : 1; // n-tiles (8 groups each) per warp
+  static constexpr int G = 8 * 8 * NT;       // groups per CTA iteration (8 warps)
+  static constexpr int TPG = 256 / G;        // threads per group in load/store
+  static constexpr int APT = D / TPG;        // amplitudes per thread (8)
+  static constexpr int PSTRIDE = R + 8;      // bf16 per digit-plane row (bank-conflict pad)
+  static constexpr size_t plane_bytes = sizeof(uint16_t) * 6 * G * PSTRIDE;
+  static constexpr size_t frag_bytes = sizeof(uint4) * 6 * MT * KS * 32;
+  static constexpr size_t stage_bytes = sizeof(double2) * G * (D + 1);
+  static constexpr size_t smem = (plane_bytes > stage_bytes ? plane_bytes : stage_bytes) + frag_bytes +
+                                 sizeof(int) * (G + R);
+};
+
+template <int KQ>
+struct OzParams {
+  uint64_t offs[1 << KQ];
+  uint64_t lowmask[KQ];
+  uint64_t ngroups;
+  int rowkey[2 << KQ];
+};
+
+// bf16 bits of a small integer (|v| <= 256, exact): float via the 2^23 magic
+// add (FP32 pipe), then the top half of the float word.
+__device__ __forceinline__ uint32_t int_to_bf16(int v) {
+  const float f = __int_as_float(0x4B000000 + v + 512) - 8389120.0f;  // 2^23 + 512
+  return (uint32_t)__float_as_uint(f) >> 16;
+}
+
+__device__ __forceinline__ void mma_bf16(float *c, const uint4 &a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
+}
+
+template <int KQ>
+__global__ void __launch_bounds__(256) k_dense_oz(double2 *__restrict__ psi, const __grid_constant__ OzParams<KQ> p,
+                                                  const uint4 *__restrict__ gfrag) {
+  using Cfg = OzCfg<KQ>;
+  constexpr int D = Cfg::D, R = Cfg::R, MT = Cfg::MT, KS = Cfg::KS, NT = Cfg::NT, G = Cfg::G;
+  constexpr int TPG = Cfg::TPG, APT = Cfg::APT, PS = Cfg::PSTRIDE;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint16_t *planes = reinterpret_cast<uint16_t *>(smem_raw);
+  double2 *stage = reinterpret_cast<double2 *>(smem_raw);
+  constexpr size_t big = Cfg::plane_bytes > Cfg::stage_bytes ? Cfg::plane_bytes : Cfg::stage_bytes;
+  uint4 *frag = reinterpret_cast<uint4 *>(smem_raw + big);
+  int *colkey = reinterpret_cast<int *>(smem_raw + big + Cfg::frag_bytes);
+  int *rowkey = colkey + G;
+  for (int i = threadIdx.x; i < 6 * MT * KS * 32; i += blockDim.x) frag[i] = gfrag[i];
+  for (int i = threadIdx.x; i < R; i += blockDim.x) rowkey[i] = p.rowkey[i];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, gid = lane >> 2, tig = lane & 3;
+  const uint64_t ntiles = (p.ngroups + G - 1) / G;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // ---- load + split: thread handles APT amplitudes of group g ----
+    const int g = tid / TPG, a0 = (tid % TPG) * APT;
+    const uint64_t grp = tile * G + g;
+    const bool valid = grp < p.ngroups;
+    const uint64_t base = valid ? insert_zeros_k<KQ>(grp, p.lowmask) : 0;
+    double2 v[APT];
+    int key = 0;
+#pragma unroll
+    for (int i = 0; i < APT; ++i) {
+      v[i] = valid ? psi[base + p.offs[a0 + i]] : make_double2(0.0, 0.0);
+      key = max(key, max(oz::exp_key(v[i].x), oz::exp_key(v[i].y)));
+    }
+#pragma unroll
+    for (int o = 1; o < TPG; o <<= 1) key = max(key, __shfl_xor_sync(0xffffffffu, key, o));
+    __syncthreads();  // previous tile's staging reads are done
+    if (tid % TPG == 0) colkey[g] = key;
+#pragma unroll
+    for (int i = 0; i < APT; i += 2) {
+      int32_t dr0[6], dr1[6], di0[6], di1[6];
+      oz::split6(v[i].x, key, dr0);
+      oz::split6(v[i + 1].x, key, dr1);
+      oz::split6(v[i].y, key, di0);
+      oz::split6(v[i + 1].y, key, di1);
+#pragma unroll
+      for (int sl = 0; sl < 6; ++sl) {
+        uint32_t *row = reinterpret_cast<uint32_t *>(planes + ((size_t)sl * G + g) * PS);
+        row[(a0 + i) >> 1] = int_to_bf16(dr0[sl]) | (int_to_bf16(dr1[sl]) << 16);
+        row[(D + a0 + i) >> 1] = int_to_bf16(di0[sl]) | (int_to_bf16(di1[sl]) << 16);
+      }
+    }
+    __syncthreads();
+    // ---- tensor-core products, level by level ----
+    int64_t acc64[MT][NT][4];
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc64[mt][nt][c] = 0;
+#pragma unroll
+    for (int l = 0; l < 6; ++l) {
+      float acc[MT][NT][4];
+#pragma unroll
+      for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[mt][nt][c] = 0.f;
+#pragma unroll
+      for (int t = 0; t <= l; ++t) {
+        const int sl = l - t;
+#pragma unroll
+        for (int ks = 0; ks < KS; ++ks) {
+          uint32_t b0[NT], b1[NT];
+#pragma unroll
+          for (int nt = 0; nt < NT; ++nt) {
+            const int gg = (warp * NT + nt) * 8 + gid;
+            const uint32_t *row = reinterpret_cast<const uint32_t *>(planes + ((size_t)sl * G + gg) * PS);
+            b0[nt] = row[ks * 8 + tig];
+            b1[nt] = row[ks * 8 + 4 + tig];
+          }
+#pragma unroll
+          for (int mt = 0; mt < MT; ++mt) {
+            const uint4 af = frag[((t * MT + mt) * KS + ks) * 32 + lane];
+#pragma unroll
+            for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[mt][nt], af, b0[nt], b1[nt]);
+          }
+        }
+      }
+      const int sh = 8 * (5 - l);
+#pragma unroll
+      for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc64[mt][nt][c] += (int64_t)__float2int_rn(acc[mt][nt][c]) * ((int64_t)1 << sh);
+    }
+    __syncthreads();  // planes are dead; reuse the space as output staging
+    // ---- recombine to double into staging [group][amp] ----
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int r = mt * 16 + gid + 8 * (c >> 1);
+          const int gg = (warp * NT + nt) * 8 + 2 * tig + (c & 1);
+          const int ck = colkey[gg];
+          const double y = (ck == 0) ? 0.0 : oz::i64_to_double(acc64[mt][nt][c], oz::out_scale(rowkey[r], ck));
+          double *slot = reinterpret_cast<double *>(&stage[gg * (D + 1) + (r % D)]);
+          slot[r < D ? 0 : 1] = y;
+        }
+    __syncthreads();
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < APT; ++i) psi[base + p.offs[a0 + i]] = stage[g * (D + 1) + a0 + i];
+    }
+  }
+}
+
+// Host: digit planes of the real matrix, in mma.sync A-fragment order.
+template <int KQ>
+void oz_matrix(const cd *mat, std::vector<uint4> &frag, int *rowkey) {
+  using Cfg = OzCfg<KQ>;
+  constexpr int D = Cfg::D, R = Cfg::R, MT = Cfg::MT, KS = Cfg::KS;
+  std::vector<double> A((size_t)R * R);
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) {
+      const cd z = mat[r + (size_t)D * c];
+      A[(size_t)r * R + c] = z.real();
+      A[(size_t)r * R + c + D] = -z.imag();
+      A[(size_t)(r + D) * R + c] = z.imag();
+      A[(size_t)(r + D) * R + c + D] = z.real();
+    }
+  std::vector<int32_t> dig((size_t)6 * R * R);
+  for (int r = 0; r < R; ++r) {
+    int key = 0;
+    for (int c = 0; c < R; ++c) key = std::max(key, oz::exp_key(A[(size_t)r * R + c]));
+    rowkey[r] = key;
+    for (int c = 0; c < R; ++c) {
+      int32_t d[6];
+      oz::split6(A[(size_t)r * R + c], key, d);
+      for (int sl = 0; sl < 6; ++sl) dig[((size_t)sl * R + r) * R + c] = d[sl];
+    }
+  }
+  auto bf = [](int32_t v) -> uint32_t {
+    float f = (float)v;
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u >> 16;
+  };
+  auto pk = [&](int sl, int r, int c) -> uint32_t {
+    return bf(dig[((size_t)sl * R + r) * R + c]) | (bf(dig[((size_t)sl * R + r) * R + c + 1]) << 16);
+  };
+  frag.resize((size_t)6 * MT * KS * 32);
+  for (int sl = 0; sl < 6; ++sl)
+    for (int mt = 0; mt < MT; ++mt)
+      for (int ks = 0; ks < KS; ++ks)
+        for (int lane = 0; lane < 32; ++lane) {
+          const int gid = lane >> 2, tig = lane & 3;
+          const int r0 = mt * 16 + gid, c0 = ks * 16 + 2 * tig;
+          uint4 f;
+          f.x = pk(sl, r0, c0);
+          f.y = pk(sl, r0 + 8, c0);
+          f.z = pk(sl, r0, c0 + 8);
+          f.w = pk(sl, r0 + 8, c0 + 8);
+          frag[((sl * MT + mt) * KS + ks) * 32 + lane] = f;
+        }
+}
+
+template <int KQ>
+void dense_oz(Device &dev, const reg_t &qubits, const cd *mat) {
+  using Cfg = OzCfg<KQ>;
+  OzParams<KQ> p;
+  local_offsets(qubits, p.offs);
+  sorted_masks(qubits, p.lowmask);
+  p.ngroups = dev.amps() >> KQ;
+  std::vector<uint4> frag;
+  oz_matrix<KQ>(mat, frag, p.rowkey);
+  const size_t fb = frag.size() * sizeof(uint4);
+  grow(dev.mat, dev.mat_cap, fb);
+  cuda_check(cudaMemcpyAsync(dev.mat, frag.data(), fb, cudaMemcpyHostToDevice, dev.stream), "matrix upload");
+  static bool attr[2] = {false, false};
+  if (!attr[KQ - 4]) {
+    cuda_check(cudaFuncSetAttribute(k_dense_oz<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::smem),
+               "tensor-core kernel attribute");
+    attr[KQ - 4] = true;
+  }
+  int per_sm = 1;
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_oz<KQ>, 256, Cfg::smem), "occupancy");
+  const uint64_t ntiles = (p.ngroups + Cfg::G - 1) / Cfg::G;
+  const uint64_t grid = std::min<uint64_t>(ntiles, 152ULL * std::max(per_sm, 1));
+  k_dense_oz<KQ><<<(unsigned)grid, 256, Cfg::smem, dev.stream>>>(reinterpret_cast<double2 *>(dev.state), p,
+                                                                 reinterpret_cast<const uint4 *>(dev.mat));
+  check_launch("tensor-core complex128 dense kernel");
+}
+
+}  // namespace
+
+bool tensor_dense_available(const Device &dev, int k) { return dev.dbl && dev.tensor_c128 && (k == 4 || k == 5); }
+
+void launch_dense_tensor(Device &dev, const reg_t &qubits, const cd *mat) {
+  if (qubits.size() == 4)
+    dense_oz<4>(dev, qubits, mat);
+  else
+    dense_oz<5>(dev, qubits, mat);
 }
 
 // ============================ adjoint-gradient kernels ============================

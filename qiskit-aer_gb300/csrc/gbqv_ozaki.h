@@ -1,0 +1,145 @@
+// gbqv_ozaki.h — exact digit-slice arithmetic for complex128 gates on tensor
+// cores (the "Ozaki" error-free splitting, Ozaki et al., Numer. Algorithms
+// 59 (2012)), written as __host__ __device__ helpers so the host test suite
+// can check them bit for bit.
+//
+// A real value x of a column (the 2^(k+1) real parts of one gate group) is
+// written against the column's exponent E (max over the column of the
+// exponent of 2^e > |x|):
+//     x ~= sum_{s=0..5} d_s * 2^(40 - 8 s) * 2^(E - 1071)
+// with balanced digits d_0 in [0, 256], d_1..5 in [-128, 127] (times the
+// sign of x): its significand aligned to the column maximum, rounded to 48
+// bits.
+// Matrix rows get the same treatment with their own row exponent R.  Every
+// product of two digits is <= 2^16, a dot product over K reals is
+// <= K * 2^16 (level 0) or <= K * 2^15 (levels >= 1, one digit is
+// balanced), and level l = s + t sums min(l, 5) + 1 such products: for
+// K <= 64 (gates of up to 5 qubits) every level sum stays below 2^24, so
+// FP32 accumulation on a tensor core is exact.  Levels
+// 0..5 are recombined exactly in int64:
+//     v = sum_l T_l * 2^(8 (5 - l))   (|v| < 2^63)
+// and y = v * 2^(R + E - 2102), rounded once to double.  The dropped levels
+// (l >= 6) and the 5 truncated significand bits bound the error by about
+// 2^-44 of (row max * column max): ~6e-14 relative to the group's largest
+// amplitude, far inside the 1e-12 parity tolerance.
+#pragma once
+
+#include <cstdint>
+
+#ifndef __CUDACC__
+#ifndef __host__
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+#endif
+
+namespace gbqv {
+namespace oz {
+
+constexpr int kSlices = 6;
+constexpr int kLevels = 6;
+
+__host__ __device__ __forceinline__ uint64_t dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  __builtin_memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+
+__host__ __device__ __forceinline__ double bitsd(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  __builtin_memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+
+__host__ __device__ __forceinline__ int clz64(uint64_t v) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)v);
+#else
+  return v ? __builtin_clzll(v) : 64;
+#endif
+}
+
+// Exponent key of |x|: the e with 2^(e-1) <= |x| < 2^e for normal x, as a
+// biased value (biased exponent field + 1); 0 for zero / subnormal.
+__host__ __device__ __forceinline__ int exp_key(double x) {
+  const int ex = (int)((dbits(x) >> 52) & 0x7ff);
+  return ex == 0 ? 0 : ex + 1;
+}
+
+// Balanced digits of x against the column key E (E >= exp_key(x)): writes
+// d[0] in [0, 256] and d[1..5] in [-128, 127] (then all times the sign of x).
+__host__ __device__ __forceinline__ void split6(double x, int E, int32_t *d) {
+  const uint64_t b = dbits(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  uint64_t m = ex ? ((b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52)) : 0;  // subnormals flush to 0
+  // x = m * 2^(ex - 1075); align to the column top 2^(E - 1023): shift by (E - 1) - ex
+  const int sh = (E - 1) - ex;
+  m = (sh >= 53 || m == 0) ? 0 : (m >> sh);
+  uint64_t a = (m + 16) >> 5;  // the top 48 of the 53 aligned bits, rounded (<= 2^48)
+  int32_t dd[6];
+#pragma unroll
+  for (int s = 5; s >= 1; --s) {
+    int32_t v = (int32_t)(a & 255u);
+    a >>= 8;
+    if (v >= 128) {
+      v -= 256;
+      ++a;
+    }
+    dd[s] = v;
+  }
+  dd[0] = (int32_t)a;  // <= 256
+  const int32_t sg = (b >> 63) ? -1 : 1;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) d[s] = sg * dd[s];
+}
+
+// Round a signed int64 times 2^scale to the nearest double (ties to even).
+__host__ __device__ __forceinline__ double i64_to_double(int64_t v, int scale) {
+  if (v == 0) return 0.0;
+  const uint64_t neg = v < 0 ? 1 : 0;
+  uint64_t u = neg ? (uint64_t)(-v) : (uint64_t)v;
+  const int lz = clz64(u);
+  const int top = 63 - lz;  // index of the leading bit
+  uint64_t mant;
+  int e = top;              // value = 1.mant * 2^(top + scale)
+  if (top > 52) {
+    const int drop = top - 52;
+    mant = u >> drop;
+    const uint64_t rem = u & ((1ULL << drop) - 1), half = 1ULL << (drop - 1);
+    if (rem > half || (rem == half && (mant & 1))) {
+      ++mant;
+      if (mant == (1ULL << 53)) {
+        mant >>= 1;
+        ++e;
+      }
+    }
+  } else {
+    mant = u << (52 - top);
+  }
+  const int biased = e + scale + 1023;
+  if (biased <= 0) return 0.0;  // below the normal range: |y| < 2^-1022, flush
+  return bitsd((neg << 63) | ((uint64_t)biased << 52) | (mant & 0xFFFFFFFFFFFFFULL));
+}
+
+// Scale exponent of the recombined v for a row key R and column key E:
+// x = a48 * 2^(E - 1 - 1023 - 47) per input, matrix likewise; the product of
+// the two level-0 weights 2^40 * 2^40 is folded into v's 2^(8*(5-l)) shifts.
+__host__ __device__ __forceinline__ int out_scale(int R, int E) {
+  // input unit: 2^(E - 1 - 1023 - 47) per unit of a48; a48 = sum d_s 2^(40-8s)
+  // => per digit unit at level s: 2^(40-8s) * 2^(E - 1071)
+  // product of row digit t and column digit s: 2^(80 - 8l) * 2^(R - 1071 + E - 1071)
+  // v = sum_l T_l 2^(8(5-l)) = sum_l T_l 2^(40 - 8l)  => y = v * 2^(40) * 2^(R + E - 2142)
+  return R + E - 2142 + 40;
+}
+
+}  // namespace oz
+}  // namespace gbqv

@@ -80,6 +80,10 @@ class QubitVector:
         self._c(self._L.gbqv_get_stream(self._h, C.byref(p)))
         return p.value or 0
 
+    def set_tensor_c128(self, enable: bool) -> None:
+        """complex128 dense 4/5-qubit gates on the tensor cores (default) or FP64 FMAs."""
+        self._c(self._L.gbqv_set_tensor_c128(self._h, int(bool(enable))))
+
     def device_pointer(self) -> int:
         p = C.c_void_p()
         self._c(self._L.gbqv_device_data(self._h, C.byref(p)))

@@ -1,0 +1,80 @@
+// Host check of the digit-slice scheme in qiskit-aer_gb300/csrc/gbqv_ozaki.h:
+// the tensor-core level sums are emulated with exact integer dot products
+// (what FP32 accumulation yields for these bounded integers) and the result
+// is compared against a __float128 matrix-vector product.  Prints the worst
+// error relative to (row max * column max) and the worst absolute error.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#include <vector>
+
+#include "gbqv_ozaki.h"
+
+using namespace gbqv::oz;
+
+int main(int argc, char **argv) {
+  const int K = argc > 1 ? atoi(argv[1]) : 32;   // reals per column
+  const int trials = argc > 2 ? atoi(argv[2]) : 2000;
+  std::mt19937_64 rng(12345);
+  std::normal_distribution<double> nd(0.0, 1.0);
+  std::uniform_int_distribution<int> ed(-60, 2);
+  double worst_rel = 0, worst_abs = 0;
+  for (int t = 0; t < trials; ++t) {
+    std::vector<double> A(K * K), x(K);
+    for (auto &a : A) a = nd(rng) / std::sqrt((double)K);
+    const int mode = t % 4;
+    for (int j = 0; j < K; ++j) {
+      double v = nd(rng) * 1e-4;
+      if (mode == 1) v = std::ldexp(nd(rng), ed(rng));          // wide dynamic range
+      if (mode == 2 && j % 3 == 0) v = 0.0;                       // zeros
+      if (mode == 3) v = (j == 0 ? 1.0 : nd(rng) * 1e-9);         // one dominant entry
+      x[j] = v;
+    }
+    int E = 0;
+    for (double v : x) E = E > exp_key(v) ? E : exp_key(v);
+    std::vector<int64_t> dx(K * kSlices);
+    for (int j = 0; j < K; ++j) {
+      int32_t d[6];
+      split6(x[j], E, d);
+      for (int s = 0; s < 6; ++s) dx[j * 6 + s] = d[s];
+    }
+    for (int r = 0; r < K; ++r) {
+      int R = 0;
+      for (int j = 0; j < K; ++j) R = R > exp_key(A[r * K + j]) ? R : exp_key(A[r * K + j]);
+      std::vector<int64_t> da(K * 6);
+      for (int j = 0; j < K; ++j) {
+        int32_t d[6];
+        split6(A[r * K + j], R, d);
+        for (int s = 0; s < 6; ++s) da[j * 6 + s] = d[s];
+      }
+      int64_t v = 0;
+      for (int l = 0; l < kLevels; ++l) {
+        int64_t T = 0;
+        for (int tt = 0; tt <= l; ++tt) {
+          const int s = l - tt;
+          for (int j = 0; j < K; ++j) T += da[j * 6 + tt] * dx[j * 6 + s];
+        }
+        if (T >= (1 << 24) || T <= -(1 << 24)) {  // FP32 accumulation would round here
+          printf("level sum out of the exact range\n");
+          return 1;
+        }
+        v += T * (int64_t(1) << (8 * (5 - l)));
+      }
+      const double y = (R == 0 || E == 0) ? 0.0 : i64_to_double(v, out_scale(R, E));
+      __float128 ref = 0;
+      double amax = 0, xmax = 0;
+      for (int j = 0; j < K; ++j) {
+        ref += (__float128)A[r * K + j] * (__float128)x[j];
+        amax = std::fmax(amax, std::fabs(A[r * K + j]));
+        xmax = std::fmax(xmax, std::fabs(x[j]));
+      }
+      const double err = std::fabs((double)((__float128)y - ref));
+      const double scale = amax * xmax;
+      if (scale > 0) worst_rel = std::fmax(worst_rel, err / scale);
+      worst_abs = std::fmax(worst_abs, err);
+    }
+  }
+  printf("%.3e %.3e\n", worst_rel, worst_abs);
+  return 0;
+}
