@@ -191,6 +191,24 @@ int gbqv_expval_pauli_many(gbqv_handle h, int nterms, const uint64_t *qubits,
                            const int *offsets, const char *const *labels,
                            const double *coeffs, double *out, double *total);
 
+/* Expectation values of up to 64 Pauli strings on a statevector that the
+ * caller owns in device memory (state: 2^num_qubits complex<double> or
+ * complex<float>, precision GBQV_C128 / GBQV_C64), for callers that cannot
+ * allocate device memory: a framework whose allocator already owns the GPU's
+ * memory, or a loop that must not pay the device synchronisation of
+ * cudaMalloc / cudaFree.  No counterpart in the reference.  It allocates
+ * nothing: its partial sums live in a static __device__ array of 78 KB that
+ * every GPU loading the library holds until exit.  Terms as in
+ * gbqv_expval_pauli_many; work is queued on `stream` (a cudaStream_t, NULL =
+ * default stream) and the call returns once out / *total are written.  More
+ * than 64 terms is GBQV_ERR_ARG.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) with that device current: make it
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race; serialise them. */
+int gbqv_expval_pauli_many_noalloc(const void *state, int num_qubits, int precision, int nterms,
+                                   const uint64_t *qubits, const int *offsets, const char *const *labels,
+                                   const double *coeffs, void *stream, double *out, double *total);
+
 /* ------------------------------------------------------------------ */
 /* Density-matrix surface (GBQV_DENSITY_MATRIX handles only)            */
 /* ------------------------------------------------------------------ */

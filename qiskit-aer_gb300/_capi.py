@@ -81,6 +81,8 @@ _SIGS = {
     "gbqv_sample_measure": (C.c_int, [H, dp, C.c_uint64, u64p]),
     "gbqv_expval_pauli": (C.c_int, [H, u64p, C.c_int, C.c_char_p, c128, dp]),
     "gbqv_expval_pauli_many": (C.c_int, [H, C.c_int, u64p, C.POINTER(C.c_int), C.POINTER(C.c_char_p), dp, dp, dp]),
+    "gbqv_expval_pauli_many_noalloc": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, u64p, C.POINTER(C.c_int),
+                                                 C.POINTER(C.c_char_p), dp, vp, dp, dp]),
     "gbqv_dm_apply_superop_matrix": (C.c_int, [H, u64p, C.c_int, vp]),
     "gbqv_dm_apply_diagonal_superop_matrix": (C.c_int, [H, u64p, C.c_int, vp]),
     "gbqv_dm_apply_unitary_matrix": (C.c_int, [H, u64p, C.c_int, vp]),
