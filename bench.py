@@ -22,7 +22,9 @@ Other workloads (--workload): ``adjoint`` (26-qubit hardware-efficient
 ansatz, 624 parameters, 200 Pauli terms: adjoint gradient vs parameter
 shift), ``dm`` (14-qubit noisy density matrix, depolarizing + amplitude
 damping superoperators, 50 Pauli expectation values), ``sample``
-(probabilities and 100,000 shots on the 30-qubit state).
+(probabilities and 100,000 shots on the 30-qubit state), ``batch`` (2,048
+uneven instances of 12-22 qubits with gradients and 4,096 shots each in one
+graph-captured persistent launch, next to one instance per launch).
 
 ``--impl reference`` times the reference's CPU algorithm on the same
 workload (the oracle port: the reference's own build exists only where its
@@ -383,13 +385,64 @@ def bench_sample(args, torch, P):
             "config": {"workload": f"QV {args.qubits}q state, 100k shots", "qubits": args.qubits}}
 
 
+def bench_batch(args, torch, P):
+    """2,048 instances: n ~ U{12..22}, depth ~ U{4..16} layers of the RY/RZ +
+    CX-ladder ansatz, own theta, 20-60-term Pauli H, 4,096 shots each; <H>,
+    gradient and shots per instance in one graph-captured persistent launch,
+    next to one instance per launch (the per-instance engine) on a sample."""
+    B, adj = P.batched, P.adjoint
+    insts = B.config5_instances(args.instances, seed=args.seed)
+    b = B.Batch(args.precision)
+    for inst in insts:
+        b.add(inst["n"], inst["gates"], inst["theta"], inst["terms"], inst["coeffs"], inst["shots"], inst["seed"])
+    for _ in range(max(1, args.warmup)):
+        b.run(want_grad=True)          # first call builds, uploads and captures the graph
+    clocks = ClockSampler().start()
+    times = [b.run(want_grad=True) for _ in range(args.steps)]
+    clk = clocks.stop()
+    ms = float(np.median(times))
+    lat = np.array([b.result(i)[3] for i in range(len(insts))])
+    # one instance per launch: the same work through the per-instance engine, on a sample
+    rng = np.random.default_rng(args.seed + 1)
+    sample = [int(i) for i in rng.choice(len(insts), size=min(args.per_launch_sample, len(insts)), replace=False)]
+    kinds = {0: "rx", 1: "ry", 2: "rz", 3: "cx", 4: "cz", 5: "h"}
+    t_single = 0.0
+    for i in sample:
+        inst = insts[i]
+        gates = [(kinds[k], [q0, q1] if k in (3, 4) else [q0], p if p >= 0 else None, None)
+                 for k, q0, q1, p in inst["gates"]]
+        ans = adj.Ansatz(inst["n"], gates)
+        ham = adj.Hamiltonian(inst["terms"], inst["coeffs"])
+        eng = adj.Engine(inst["n"], args.precision)
+        t0 = time.perf_counter()
+        e, g = eng.energy_and_grad(ans, inst["theta"], ham)
+        eng.energy(ans, inst["theta"], ham)
+        eng.qv.sample_measure(P.uniforms(inst["seed"], inst["shots"]))
+        t_single += time.perf_counter() - t0
+        eng.close()
+    est_single = t_single / len(sample) * len(insts)
+    b.close()
+    return {"metric": "circuits/s (batched uneven, adjoint gradients + shots)", "value": round(len(insts) / (ms / 1e3), 2),
+            "unit": "circuits/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
+            "launch_ms": round(ms, 2), "latency_ms_p50": round(float(np.percentile(lat, 50)), 3),
+            "latency_ms_p99": round(float(np.percentile(lat, 99)), 3),
+            "one_instance_per_launch_s_estimated": round(est_single, 2),
+            "one_instance_per_launch_measured": f"{len(sample)} instances in {t_single:.2f} s",
+            "speedup_vs_per_launch": round(est_single / (ms / 1e3), 2),
+            "config": {"workload": f"{len(insts)} instances, 12-22 qubits, depth 4-16, 20-60 Paulis, 4096 shots",
+                       "instances": len(insts)}, "clocks": clk}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="qv", choices=["qv", "adjoint", "dm", "sample"])
+    ap.add_argument("--workload", default="qv", choices=["qv", "adjoint", "dm", "sample", "batch"])
+    ap.add_argument("--instances", type=int, default=2048)
+    ap.add_argument("--per-launch-sample", type=int, default=24)
     ap.add_argument("--precision", default="single", choices=["double", "single"])
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=30)
@@ -410,7 +463,8 @@ def main():
     torch.cuda.init()
     P = entry.load_package()
     P.build()
-    fn = {"qv": bench_qv, "adjoint": bench_adjoint, "dm": bench_dm, "sample": bench_sample}[args.workload]
+    fn = {"qv": bench_qv, "adjoint": bench_adjoint, "dm": bench_dm, "sample": bench_sample,
+          "batch": bench_batch}[args.workload]
     line = fn(args, torch, P)
     if int(os.environ.get("RANK", "0")) == 0:
         print(json.dumps(line))

@@ -46,6 +46,7 @@ extern "C" {
 
 typedef struct gbqv_state *gbqv_handle;
 typedef struct gbqv_circuit *gbqv_circuit_t;
+typedef struct gbqv_batch *gbqv_batch_t;
 
 /* Interleaved complex double, layout-compatible with std::complex<double>. */
 typedef struct {
@@ -317,6 +318,35 @@ int gbqv_execute(gbqv_handle h, gbqv_circuit_t c);
 int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const int *param_of_op, const double *params,
                              int nparams, int nterms, const uint64_t *qubits, const int *offsets,
                              const char *const *labels, const double *coeffs, double *energy, double *grad);
+
+/* ------------------------------------------------------------------ */
+/* Batches of independent instances of uneven size in one launch        */
+/* (the role of the batched-shots / parameter-bind executor,            */
+/* src/simulators/batch_shots_executor.hpp:39-314, which batches        */
+/* equal-size states only).                                             */
+/* ------------------------------------------------------------------ */
+
+/* Gate kinds of a batch instance: 0 RX, 1 RY, 2 RZ (rotations reading
+ * params[param_of_gate[i]]), 3 CX, 4 CZ (control, target), 5 H. */
+int gbqv_batch_create(int precision, gbqv_batch_t *out);
+int gbqv_batch_destroy(gbqv_batch_t b);
+/* Add an instance: num_qubits <= 30; ngates gates with kinds[i], qubits
+ * [2*i, 2*i+1] (the second is ignored for 1-qubit kinds); a Hamiltonian laid
+ * out as in gbqv_expval_pauli_many; `shots` samples from the RngEngine stream
+ * of `seed` (gbqv_uniforms).  *index receives the instance number. */
+int gbqv_batch_add(gbqv_batch_t b, int num_qubits, int ngates, const int *kinds, const uint64_t *qubits,
+                   const int *param_of_gate, const double *params, int nparams, int nterms, const uint64_t *tq,
+                   const int *toffsets, const char *const *labels, const double *coeffs, uint64_t shots,
+                   uint64_t seed, int *index);
+/* Run every instance in one persistent kernel launch (captured once as a CUDA
+ * graph and replayed on later calls): forward pass, `shots` samples of the
+ * final state, E = <H>, and with want_grad the adjoint gradient dE/dparams.
+ * *elapsed_ms gets the device time of the launch. */
+int gbqv_batch_run(gbqv_batch_t b, int want_grad, double *elapsed_ms);
+/* Results of instance i (any pointer may be NULL); latency = device time
+ * from the instance's start to its end inside the launch. */
+int gbqv_batch_result(gbqv_batch_t b, int i, double *energy, double *grad, int nparams, uint64_t *samples,
+                      uint64_t shots, double *latency_ms);
 
 /* Execution policy for gbqv_execute (no reference counterpart: Aer applies
  * one op per pass).  blocking = 0 applies one kernel per op. */

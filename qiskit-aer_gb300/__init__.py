@@ -17,10 +17,10 @@ from .noise import (NoiseModel, QuantumError, amplitude_damping_error, depolariz
                     phase_amplitude_damping_error)
 from .qubitvector import DensityMatrix, QubitVector
 from .simulator import AerSimulator, Result, uniforms
-from . import adjoint
+from . import adjoint, batched
 
 __all__ = [
-    "AerSimulator", "adjoint", "DensityMatrix", "GBQVError", "NativeCircuit", "NoiseModel", "QuantumCircuit",
+    "AerSimulator", "adjoint", "batched", "DensityMatrix", "GBQVError", "NativeCircuit", "NoiseModel", "QuantumCircuit",
     "QuantumError", "QubitVector", "Result", "amplitude_damping_error", "depolarizing_error", "lib",
     "phase_amplitude_damping_error", "uniforms",
 ]

@@ -114,6 +114,13 @@ _SIGS = {
     "gbqv_execute": (C.c_int, [H, H]),
     "gbqv_set_blocking": (C.c_int, [H, C.c_int]),
     "gbqv_set_tensor_c128": (C.c_int, [H, C.c_int]),
+    "gbqv_batch_create": (C.c_int, [C.c_int, C.POINTER(H)]),
+    "gbqv_batch_destroy": (C.c_int, [H]),
+    "gbqv_batch_add": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_int), u64p, C.POINTER(C.c_int), dp, C.c_int,
+                                 C.c_int, u64p, C.POINTER(C.c_int), C.POINTER(C.c_char_p), dp, C.c_uint64,
+                                 C.c_uint64, C.POINTER(C.c_int)]),
+    "gbqv_batch_run": (C.c_int, [H, C.c_int, dp]),
+    "gbqv_batch_result": (C.c_int, [H, C.c_int, dp, dp, C.c_int, u64p, C.c_uint64, dp]),
     "gbqv_adjoint_expval_grad": (C.c_int, [H, H, C.POINTER(C.c_int), dp, C.c_int, C.c_int, u64p, C.POINTER(C.c_int),
                                            C.POINTER(C.c_char_p), dp, dp, dp]),
 }

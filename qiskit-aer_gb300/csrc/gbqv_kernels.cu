@@ -120,8 +120,14 @@ struct DenseParams {
   uint64_t ngroups;
 };
 
+// (Capping complex64 k <= 4 at 3 CTAs per SM spills and measured slower
+// than 2 CTAs per SM, so every variant keeps the default register budget.)
+template <typename T>
+constexpr int dense_min_blocks(int K) { return 1; }
+
 template <typename T, int K, bool NORM>
-__global__ void __launch_bounds__(256) k_dense(T *__restrict__ psi, const __grid_constant__ DenseParams<T, K> p,
+__global__ void __launch_bounds__(256, dense_min_blocks<T>(K)) k_dense(T *__restrict__ psi,
+                                                                        const __grid_constant__ DenseParams<T, K> p,
                                                double *__restrict__ partials) {
   constexpr int D = 1 << K;
   double nacc = 0.0;
@@ -1026,10 +1032,10 @@ struct OzCfg {
   static constexpr int R = 2 * D;            // reals per group (matrix dim)
   static constexpr int MT = R / 16;          // m-tiles of the real matrix
   static constexpr int KS = R / 16;          // k-steps
-  static constexpr int NT = KQ == 4 ? 2 : 1; // n-tiles (8 groups each) per warp
-  static constexpr int G = 8 * 8 * NT;       // groups per CTA iteration (8 warps)
-  static constexpr int TPG = 256 / G;        // threads per group in load/store
-  static constexpr int APT = D / TPG;        // amplitudes per thread (8)
+  static constexpr int MC = 2;               // m-tiles whose level sums are live at once
+  static constexpr int G = 64;               // groups per CTA iteration: 8 warps x 8 (one n-tile)
+  static constexpr int TPG = 256 / G;        // threads per group in load / store (4)
+  static constexpr int APT = D / TPG;        // amplitudes per thread
   static constexpr int PSTRIDE = R + 8;      // bf16 per digit-plane row (bank-conflict pad)
   static constexpr size_t plane_bytes = sizeof(uint16_t) * 6 * G * PSTRIDE;
   static constexpr size_t frag_bytes = sizeof(uint4) * 6 * MT * KS * 32;
@@ -1061,11 +1067,16 @@ __device__ __forceinline__ void mma_bf16(float *c, const uint4 &a, uint32_t b0, 
       : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
 }
 
+// Each warp owns 8 groups (one 8-column n-tile).  For a pair of m-tiles the
+// six level sums stay live in registers (48 floats) while the k-steps run:
+// a matrix fragment of plane t feeds the MMAs with every state plane s <=
+// 5 - t, each into a different level accumulator, so consecutive MMAs are
+// independent.
 template <int KQ>
-__global__ void __launch_bounds__(256) k_dense_oz(double2 *__restrict__ psi, const __grid_constant__ OzParams<KQ> p,
-                                                  const uint4 *__restrict__ gfrag) {
+__global__ void __launch_bounds__(256, 2) k_dense_oz(double2 *__restrict__ psi, const __grid_constant__ OzParams<KQ> p,
+                                                     const uint4 *__restrict__ gfrag) {
   using Cfg = OzCfg<KQ>;
-  constexpr int D = Cfg::D, R = Cfg::R, MT = Cfg::MT, KS = Cfg::KS, NT = Cfg::NT, G = Cfg::G;
+  constexpr int D = Cfg::D, R = Cfg::R, MT = Cfg::MT, KS = Cfg::KS, MC = Cfg::MC, G = Cfg::G;
   constexpr int TPG = Cfg::TPG, APT = Cfg::APT, PS = Cfg::PSTRIDE;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint16_t *planes = reinterpret_cast<uint16_t *>(smem_raw);
@@ -1110,67 +1121,60 @@ __global__ void __launch_bounds__(256) k_dense_oz(double2 *__restrict__ psi, con
       }
     }
     __syncthreads();
-    // ---- tensor-core products, level by level ----
-    int64_t acc64[MT][NT][4];
+    // ---- tensor-core level sums, then exact recombination ----
+    const int gw = warp * 8 + gid;  // this lane's B column (group)
+    int64_t out64[MT][4];
 #pragma unroll
-    for (int mt = 0; mt < MT; ++mt)
+    for (int mc = 0; mc < MT; mc += MC) {
+      float acc[6][MC][4];
 #pragma unroll
-      for (int nt = 0; nt < NT; ++nt)
+      for (int l = 0; l < 6; ++l)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc64[mt][nt][c] = 0;
+        for (int j = 0; j < MC; ++j)
 #pragma unroll
-    for (int l = 0; l < 6; ++l) {
-      float acc[MT][NT][4];
+          for (int c = 0; c < 4; ++c) acc[l][j][c] = 0.f;
 #pragma unroll
-      for (int mt = 0; mt < MT; ++mt)
+      for (int ks = 0; ks < KS; ++ks) {
+        uint32_t b0[6], b1[6];
 #pragma unroll
-        for (int nt = 0; nt < NT; ++nt)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) acc[mt][nt][c] = 0.f;
-#pragma unroll
-      for (int t = 0; t <= l; ++t) {
-        const int sl = l - t;
-#pragma unroll
-        for (int ks = 0; ks < KS; ++ks) {
-          uint32_t b0[NT], b1[NT];
-#pragma unroll
-          for (int nt = 0; nt < NT; ++nt) {
-            const int gg = (warp * NT + nt) * 8 + gid;
-            const uint32_t *row = reinterpret_cast<const uint32_t *>(planes + ((size_t)sl * G + gg) * PS);
-            b0[nt] = row[ks * 8 + tig];
-            b1[nt] = row[ks * 8 + 4 + tig];
-          }
-#pragma unroll
-          for (int mt = 0; mt < MT; ++mt) {
-            const uint4 af = frag[((t * MT + mt) * KS + ks) * 32 + lane];
-#pragma unroll
-            for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[mt][nt], af, b0[nt], b1[nt]);
-          }
+        for (int sl = 0; sl < 6; ++sl) {
+          const uint32_t *row = reinterpret_cast<const uint32_t *>(planes + ((size_t)sl * G + gw) * PS);
+          b0[sl] = row[ks * 8 + tig];
+          b1[sl] = row[ks * 8 + 4 + tig];
         }
+#pragma unroll
+        for (int t = 0; t < 6; ++t)
+#pragma unroll
+          for (int j = 0; j < MC; ++j) {
+            const uint4 af = frag[((t * MT + mc + j) * KS + ks) * 32 + lane];
+#pragma unroll
+            for (int sl = 0; sl + t < 6; ++sl) mma_bf16(acc[t + sl][j], af, b0[sl], b1[sl]);
+          }
       }
-      const int sh = 8 * (5 - l);
 #pragma unroll
-      for (int mt = 0; mt < MT; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < NT; ++nt)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) acc64[mt][nt][c] += (int64_t)__float2int_rn(acc[mt][nt][c]) * ((int64_t)1 << sh);
-    }
-    __syncthreads();  // planes are dead; reuse the space as output staging
-    // ---- recombine to double into staging [group][amp] ----
-#pragma unroll
-    for (int mt = 0; mt < MT; ++mt)
-#pragma unroll
-      for (int nt = 0; nt < NT; ++nt)
+      for (int j = 0; j < MC; ++j)
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          const int r = mt * 16 + gid + 8 * (c >> 1);
-          const int gg = (warp * NT + nt) * 8 + 2 * tig + (c & 1);
-          const int ck = colkey[gg];
-          const double y = (ck == 0) ? 0.0 : oz::i64_to_double(acc64[mt][nt][c], oz::out_scale(rowkey[r], ck));
-          double *slot = reinterpret_cast<double *>(&stage[gg * (D + 1) + (r % D)]);
-          slot[r < D ? 0 : 1] = y;
+          // level sums are exact integers below 2^22 in magnitude, so a pair
+          // (l, l+1) combines exactly in int32: T_l * 256 + T_{l+1} < 2^31
+          const int32_t p01 = __float2int_rn(acc[0][j][c]) * 256 + __float2int_rn(acc[1][j][c]);
+          const int32_t p23 = __float2int_rn(acc[2][j][c]) * 256 + __float2int_rn(acc[3][j][c]);
+          const int32_t p45 = __float2int_rn(acc[4][j][c]) * 256 + __float2int_rn(acc[5][j][c]);
+          out64[mc + j][c] = (int64_t)p01 * 4294967296LL + (int64_t)p23 * 65536LL + (int64_t)p45;
         }
+    }
+    __syncthreads();  // planes are dead; reuse the space as output staging
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int r = mt * 16 + gid + 8 * (c >> 1);
+        const int gg = warp * 8 + 2 * tig + (c & 1);
+        const int ck = colkey[gg];
+        const double y = (ck == 0) ? 0.0 : oz::i64_to_double(out64[mt][c], oz::out_scale(rowkey[r], ck));
+        double *slot = reinterpret_cast<double *>(&stage[gg * (D + 1) + (r % D)]);
+        slot[r < D ? 0 : 1] = y;
+      }
     __syncthreads();
     if (valid) {
 #pragma unroll

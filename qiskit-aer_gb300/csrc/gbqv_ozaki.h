@@ -84,19 +84,14 @@ __host__ __device__ __forceinline__ void split6(double x, int E, int32_t *d) {
   // x = m * 2^(ex - 1075); align to the column top 2^(E - 1023): shift by (E - 1) - ex
   const int sh = (E - 1) - ex;
   m = (sh >= 53 || m == 0) ? 0 : (m >> sh);
-  uint64_t a = (m + 16) >> 5;  // the top 48 of the 53 aligned bits, rounded (<= 2^48)
+  const uint64_t a = (m + 16) >> 5;  // the top 48 of the 53 aligned bits, rounded (<= 2^48)
+  // balanced base-256 digits: adding 128 at digits 1..5 lets one 64-bit add
+  // carry for all of them; digit s is then the byte minus 128
+  const uint64_t bsum = a + 0x8080808080ULL;
   int32_t dd[6];
+  dd[0] = (int32_t)(bsum >> 40);  // <= 256
 #pragma unroll
-  for (int s = 5; s >= 1; --s) {
-    int32_t v = (int32_t)(a & 255u);
-    a >>= 8;
-    if (v >= 128) {
-      v -= 256;
-      ++a;
-    }
-    dd[s] = v;
-  }
-  dd[0] = (int32_t)a;  // <= 256
+  for (int s = 1; s < 6; ++s) dd[s] = (int32_t)((bsum >> (40 - 8 * s)) & 255u) - 128;
   const int32_t sg = (b >> 63) ? -1 : 1;
 #pragma unroll
   for (int s = 0; s < 6; ++s) d[s] = sg * dd[s];

@@ -1,0 +1,59 @@
+"""Batched uneven instances in one persistent launch (gbqv_batch_*): per
+instance <H> and the adjoint gradient against the single-instance adjoint
+engine, and the sampled shots bit-exact against the oracle for the same
+RngEngine seed.  Instances span 3..13 qubits so that some fit one tile and
+some need several tiles per run."""
+import numpy as np
+import pytest
+
+from _pkg import pkg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine_ansatz(adj, inst):
+    kinds = {0: "rx", 1: "ry", 2: "rz", 3: "cx", 4: "cz", 5: "h"}
+    gates = []
+    for k, q0, q1, p in inst["gates"]:
+        q = [q0, q1] if k in (3, 4) else [q0]
+        gates.append((kinds[k], q, p if p >= 0 else None, None))
+    return adj.Ansatz(inst["n"], gates)
+
+
+@pytest.mark.parametrize("precision,tol,gtol", [("double", 1e-11, 1e-9), ("single", 2e-4, 2e-3)])
+def test_batch_matches_single_instance_engine(precision, tol, gtol):
+    P = pkg()
+    B, adj = P.batched, P.adjoint
+    insts = B.config5_instances(10, seed=5, qmin=3, qmax=13, dmin=1, dmax=4, tmin=4, tmax=12, shots=300)
+    b = B.Batch(precision)
+    for inst in insts:
+        b.add(inst["n"], inst["gates"], inst["theta"], inst["terms"], inst["coeffs"], inst["shots"], inst["seed"])
+    ms = b.run(want_grad=True)
+    assert ms > 0
+    for i, inst in enumerate(insts):
+        e, g, s, lat = b.result(i)
+        ans = _engine_ansatz(adj, inst)
+        ham = adj.Hamiltonian(inst["terms"], inst["coeffs"])
+        eng = adj.Engine(inst["n"], "double")
+        e_ref, g_ref = eng.energy_and_grad(ans, inst["theta"], ham)
+        eng.close()
+        assert abs(e - e_ref) < tol * max(1, abs(e_ref)), (i, e, e_ref)
+        np.testing.assert_allclose(g, g_ref, atol=gtol)
+        assert lat > 0
+        if precision == "double":
+            o = O.OracleQV(inst["n"])
+            for k, q0, q1, p in inst["gates"]:
+                if k == 1:
+                    o.apply_rotation([q0], 1, inst["theta"][p])
+                elif k == 2:
+                    o.apply_rotation([q0], 2, inst["theta"][p])
+                elif k == 3:
+                    o.apply_mcx([q0, q1])
+            want = o.sample_measure(O.uniforms(inst["seed"], inst["shots"]))
+            np.testing.assert_array_equal(s, want)
+    # a second run replays the captured graph and gives the same results
+    e0 = b.result(0)[0]
+    b.run(want_grad=True)
+    assert b.result(0)[0] == e0
+    b.close()
