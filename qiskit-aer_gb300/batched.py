@@ -105,3 +105,38 @@ def config5_instances(count: int, seed: int, qmin=12, qmax=22, dmin=4, dmax=16, 
         out.append(dict(n=n, depth=depth, gates=gates, theta=theta, terms=terms, coeffs=coeffs, shots=shots,
                         seed=seed * 100003 + i))
     return out
+
+
+def shard(instances, rank: int, world: int):
+    """Indices of the instances rank `rank` of `world` runs: greedy balance of
+    the per-instance cost (depth x 2^n), no data exchange between ranks."""
+    cost = [inst["depth"] * (1 << inst["n"]) for inst in instances]
+    load = [0] * world
+    owner = [0] * len(instances)
+    for i in sorted(range(len(instances)), key=lambda j: -cost[j]):
+        r = min(range(world), key=lambda k: load[k])
+        owner[i] = r
+        load[r] += cost[i]
+    return [i for i in range(len(instances)) if owner[i] == rank]
+
+
+def run_sharded(instances, runner, group=None):
+    """Run this rank's share with runner(list of instances) -> list of energies
+    and all-gather the energies in instance order (torch.distributed; one
+    gather of the results, nothing during the run)."""
+    import torch
+    import torch.distributed as dist
+
+    rank, world = (dist.get_rank(group), dist.get_world_size(group)) if dist.is_initialized() else (0, 1)
+    mine = shard(instances, rank, world)
+    vals = runner([instances[i] for i in mine])
+    out = torch.full((len(instances),), float("nan"), dtype=torch.float64)
+    for i, v in zip(mine, vals):
+        out[i] = v
+    if world > 1:
+        parts = [torch.empty_like(out) for _ in range(world)]
+        dist.all_gather(parts, out, group=group)
+        for p in parts:
+            mask = ~torch.isnan(p)
+            out[mask] = p[mask]
+    return out.numpy()

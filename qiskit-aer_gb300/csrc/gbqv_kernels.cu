@@ -1089,19 +1089,32 @@ __global__ void __launch_bounds__(256, 2) k_dense_oz(double2 *__restrict__ psi, 
   for (int i = threadIdx.x; i < R; i += blockDim.x) rowkey[i] = p.rowkey[i];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, gid = lane >> 2, tig = lane & 3;
   const uint64_t ntiles = (p.ngroups + G - 1) / G;
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    // ---- load + split: thread handles APT amplitudes of group g ----
-    const int g = tid / TPG, a0 = (tid % TPG) * APT;
-    const uint64_t grp = tile * G + g;
-    const bool valid = grp < p.ngroups;
-    const uint64_t base = valid ? insert_zeros_k<KQ>(grp, p.lowmask) : 0;
-    double2 v[APT];
+  // thread -> (group g, amplitude pairs): the thread owns amplitudes
+  // 2*(tid % TPG) + 2*TPG*i + {0, 1}, i < APT/2 (adjacent pairs pack into one
+  // 32-bit word of a digit plane)
+  const int g = tid / TPG, pr0 = 2 * (tid % TPG);
+  auto amp_of = [&](int i) { return pr0 + 2 * TPG * (i >> 1) + (i & 1); };
+  double2 v[APT];
+  uint64_t tile = blockIdx.x;
+  uint64_t base = 0;
+  bool valid = false;
+  auto load_tile = [&](uint64_t t, double2 *dst, uint64_t &b, bool &ok) {
+    const uint64_t grp = t * G + g;
+    ok = t < ntiles && grp < p.ngroups;
+    b = ok ? insert_zeros_k<KQ>(grp, p.lowmask) : 0;
+#pragma unroll
+    for (int i = 0; i < APT; ++i) dst[i] = ok ? psi[b + p.offs[amp_of(i)]] : make_double2(0.0, 0.0);
+  };
+  // 4-qubit gates prefetch the next tile into registers (APT = 4 keeps it
+  // spill-free); 5-qubit gates (APT = 8) load at the top of each iteration
+  constexpr bool kPrefetch = KQ == 4;
+  if (kPrefetch) load_tile(tile, v, base, valid);
+  for (; tile < ntiles; tile += gridDim.x) {
+    if (!kPrefetch) load_tile(tile, v, base, valid);
+    // ---- split the tile loaded (or prefetched) for this iteration ----
     int key = 0;
 #pragma unroll
-    for (int i = 0; i < APT; ++i) {
-      v[i] = valid ? psi[base + p.offs[a0 + i]] : make_double2(0.0, 0.0);
-      key = max(key, max(oz::exp_key(v[i].x), oz::exp_key(v[i].y)));
-    }
+    for (int i = 0; i < APT; ++i) key = max(key, max(oz::exp_key(v[i].x), oz::exp_key(v[i].y)));
 #pragma unroll
     for (int o = 1; o < TPG; o <<= 1) key = max(key, __shfl_xor_sync(0xffffffffu, key, o));
     __syncthreads();  // previous tile's staging reads are done
@@ -1113,13 +1126,18 @@ __global__ void __launch_bounds__(256, 2) k_dense_oz(double2 *__restrict__ psi, 
       oz::split6(v[i + 1].x, key, dr1);
       oz::split6(v[i].y, key, di0);
       oz::split6(v[i + 1].y, key, di1);
+      const int a = amp_of(i);
 #pragma unroll
       for (int sl = 0; sl < 6; ++sl) {
         uint32_t *row = reinterpret_cast<uint32_t *>(planes + ((size_t)sl * G + g) * PS);
-        row[(a0 + i) >> 1] = int_to_bf16(dr0[sl]) | (int_to_bf16(dr1[sl]) << 16);
-        row[(D + a0 + i) >> 1] = int_to_bf16(di0[sl]) | (int_to_bf16(di1[sl]) << 16);
+        row[a >> 1] = int_to_bf16(dr0[sl]) | (int_to_bf16(dr1[sl]) << 16);
+        row[(D + a) >> 1] = int_to_bf16(di0[sl]) | (int_to_bf16(di1[sl]) << 16);
       }
     }
+    const uint64_t cur_base = base;
+    const bool cur_valid = valid;
+    // ---- prefetch the next tile: its loads fly during the MMAs below ----
+    if (kPrefetch) load_tile(tile + gridDim.x, v, base, valid);
     __syncthreads();
     // ---- tensor-core level sums, then exact recombination ----
     const int gw = warp * 8 + gid;  // this lane's B column (group)
@@ -1176,9 +1194,9 @@ __global__ void __launch_bounds__(256, 2) k_dense_oz(double2 *__restrict__ psi, 
         slot[r < D ? 0 : 1] = y;
       }
     __syncthreads();
-    if (valid) {
+    if (cur_valid) {
 #pragma unroll
-      for (int i = 0; i < APT; ++i) psi[base + p.offs[a0 + i]] = stage[g * (D + 1) + a0 + i];
+      for (int i = 0; i < APT; ++i) psi[cur_base + p.offs[amp_of(i)]] = stage[g * (D + 1) + amp_of(i)];
     }
   }
 }
