@@ -354,8 +354,12 @@ int gbqv_set_blocking(gbqv_handle h, int blocking);
 
 /* Arithmetic of complex128 dense gates on 4 or 5 qubits (no reference
  * counterpart).  1 (default): exact digit slices on the tensor cores, error
- * <= ~1e-13 of (row max x group max) per gate; 0: native FP64 FMAs (the
- * reference's arithmetic, 1.2 TFLOP/s on GB300). */
+ * <= ~1e-13 of (row max x group max) per gate (4-qubit gates on tcgen05 with
+ * TMEM accumulators for states of >= 11 vector qubits, otherwise warp-level
+ * mma.sync); 2: the same digit slices on mma.sync only; 0: native FP64 FMAs
+ * (the reference's arithmetic, 1.2 TFLOP/s on GB300).  Other values return
+ * GBQV_ERR_ARG.  A tcgen05 kernel whose bounded pipeline wait gave up makes
+ * the next synchronising call return GBQV_ERR_TIMEOUT. */
 int gbqv_set_tensor_c128(gbqv_handle h, int enable);
 
 #ifdef __cplusplus

@@ -106,7 +106,31 @@ cd as_cd(gbqv_c128 z) { return cd(z.re, z.im); }
 
 namespace gbqv {
 
-void sync(Device &dev) { cuda_check(cudaStreamSynchronize(dev.stream), "stream synchronize"); }
+// Raises GBQV_ERR_TIMEOUT when a tcgen05 kernel's bounded wait gave up since
+// the last check (the word is cleared for the next launches).
+void check_tc_status(Device &dev) {
+  if (!dev.tc_status) return;
+  int word = 0;
+  cuda_check(cudaMemcpyAsync(&word, dev.tc_status, sizeof(int), cudaMemcpyDeviceToHost, dev.stream), "status read");
+  cuda_check(cudaStreamSynchronize(dev.stream), "stream synchronize");
+  if (word) {
+    cuda_check(cudaMemsetAsync(dev.tc_status, 0, sizeof(int), dev.stream), "status reset");
+    throw Error(GBQV_ERR_TIMEOUT, "a tensor-core pipeline wait timed out; the results of that gate are invalid");
+  }
+}
+
+int *tc_status_word(Device &dev) {
+  if (!dev.tc_status) {
+    cuda_check(cudaMalloc(&dev.tc_status, sizeof(int)), "status allocation");
+    cuda_check(cudaMemsetAsync(dev.tc_status, 0, sizeof(int), dev.stream), "status reset");
+  }
+  return dev.tc_status;
+}
+
+void sync(Device &dev) {
+  cuda_check(cudaStreamSynchronize(dev.stream), "stream synchronize");
+  check_tc_status(dev);
+}
 
 // Copies n doubles of dev.results into out (host) and waits.
 void read_results(Device &dev, double *out, size_t n) {
@@ -275,7 +299,8 @@ extern "C" int gbqv_destroy(gbqv_handle h) {
   if (!h) return GBQV_OK;
   Device &d = h->dev;
   cudaStreamSynchronize(d.stream);
-  for (void *p : {d.state, d.ckpt, (void *)d.partials, (void *)d.results, d.mat, d.aux, d.aux2, (void *)h->io})
+  for (void *p : {d.state, d.ckpt, (void *)d.partials, (void *)d.results, d.mat, d.aux, d.aux2, (void *)h->io,
+                  (void *)d.tc_status})
     if (p) cudaFree(p);
   if (d.h_results) cudaFreeHost(d.h_results);
   cudaStreamDestroy(d.stream);
@@ -833,7 +858,8 @@ extern "C" int gbqv_dm_trace(gbqv_handle h, gbqv_c128 *out) {
 extern "C" int gbqv_set_tensor_c128(gbqv_handle h, int enable) {
   return guard(h, [&] {
     need_handle(h);
-    h->dev.tensor_c128 = enable != 0;
+    REQUIRE(enable >= 0 && enable <= 2, GBQV_ERR_ARG, "tensor mode must be 0, 1 or 2");
+    h->dev.tensor_c128 = enable;
   });
 }
 

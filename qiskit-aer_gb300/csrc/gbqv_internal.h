@@ -47,7 +47,8 @@ struct Device {
   bool dbl = true;      // complex128 (true) or complex64 (false)
   bool density = false;
   int blocking = 1;
-  bool tensor_c128 = true;  // dense k = 4, 5 complex128 gates on the tensor pipe
+  int tensor_c128 = 1;      // complex128 dense k = 4, 5: 0 FP64 cores, 1 tensor (tcgen05 for k = 4), 2 mma.sync only
+  int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up
   void *state = nullptr;
   void *ckpt = nullptr;
   cudaStream_t stream = nullptr;
@@ -108,9 +109,23 @@ struct RunOp {
   std::vector<cd> mat;
 };
 // complex128 dense gates of 4 / 5 qubits on the tensor cores (exact digit
-// slices, gbqv_ozaki.h)
+// slices, gbqv_ozaki.h): tcgen05 + TMEM for 4 qubits (gbqv_tc.cu), warp-level
+// mma.sync for 5 qubits and for tensor mode 2.
 bool tensor_dense_available(const Device &dev, int k);
 void launch_dense_tensor(Device &dev, const reg_t &qubits, const cd *mat);
+bool tc_dense_available(const Device &dev, int k);
+void launch_dense_tc(Device &dev, const reg_t &qubits, const cd *mat);
+void tc_matrix4(const cd *mat, uint16_t *planes, int *rowkey);
+// Device word that a bounded wait of a tcgen05 kernel sets when it gives up;
+// sync() turns it into GBQV_ERR_TIMEOUT.
+int *tc_status_word(Device &dev);
+
+// Group geometry shared by the kernels: lowmask[j] = 2^(sorted qubit j) - 1;
+// offs[i] = the amplitude offset of local index i (qubits[j] = bit j of i).
+void sorted_masks(const reg_t &qubits, uint64_t *lowmask);
+void local_offsets(const reg_t &qubits, uint64_t *offs);
+// Counts a launch and turns a launch error into an exception.
+void check_launch(const char *what);
 
 // Dispatch rules of the reference members, shared by the C ABI and the
 // circuit executor (gbqv_capi.cpp).

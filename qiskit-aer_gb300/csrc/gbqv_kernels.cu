@@ -81,6 +81,8 @@ inline int grid_for(uint64_t work, int threads, int per_sm = 8) {
   return (int)blocks;
 }
 
+}  // namespace
+
 void sorted_masks(const reg_t &qubits, uint64_t *lowmask) {
   reg_t s = qubits;
   std::sort(s.begin(), s.end());
@@ -96,16 +98,22 @@ void local_offsets(const reg_t &qubits, uint64_t *offs) {
   }
 }
 
+namespace {
+
 template <typename T> T to_dev(const cd &z);
 template <> double2 to_dev<double2>(const cd &z) { return make_double2(z.real(), z.imag()); }
 template <> float2 to_dev<float2>(const cd &z) { return make_float2((float)z.real(), (float)z.imag()); }
 
 std::atomic<uint64_t> g_launches{0};
 
+}  // namespace
+
 void check_launch(const char *what) {
   g_launches.fetch_add(1, std::memory_order_relaxed);
   cuda_check(cudaGetLastError(), what);
 }
+
+namespace {
 
 // -------------------------------------------------------------------------
 // Dense k-qubit matrix, k <= 5: the matrix rides in the kernel parameters
@@ -1283,7 +1291,9 @@ void dense_oz(Device &dev, const reg_t &qubits, const cd *mat) {
 bool tensor_dense_available(const Device &dev, int k) { return dev.dbl && dev.tensor_c128 && (k == 4 || k == 5); }
 
 void launch_dense_tensor(Device &dev, const reg_t &qubits, const cd *mat) {
-  if (qubits.size() == 4)
+  if (tc_dense_available(dev, (int)qubits.size()))
+    launch_dense_tc(dev, qubits, mat);
+  else if (qubits.size() == 4)
     dense_oz<4>(dev, qubits, mat);
   else
     dense_oz<5>(dev, qubits, mat);

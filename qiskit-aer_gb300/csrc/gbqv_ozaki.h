@@ -136,5 +136,72 @@ __host__ __device__ __forceinline__ int out_scale(int R, int E) {
   return R + E - 2142 + 40;
 }
 
+
+// ---- signed digits (tcgen05 kernel) ----
+// Same value x ~= a * 2^(E - 1071) with a the aligned significand rounded to
+// 48 bits (ties away from zero), but signed: returns bsum = a + 0x8080808080
+// so that digit 0 = bsum >> 40 (arithmetic, in [-256, 256]) and digit s =
+// byte (5 - s) of bsum minus 128 (in [-128, 127]) for s = 1..5, i.e.
+//     a = sum_s d_s * 2^(40 - 8 s).
+// Rounding and the sign come from one identity: with t the significand
+// shifted right by one bit more than needed and S the sign mask (0 or -1),
+// (t ^ S) + 1 is t + 1 for S = 0 and -t for S = -1, and halving
+// 2 * 0x8080808080 + that gives C + round(t / 2) or C - round(t / 2).
+__host__ __device__ __forceinline__ int64_t split_bsum(double x, int E) {
+  const uint64_t b = dbits(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  int sh = E + 3 - ex;
+  sh = sh > 63 ? 63 : sh;
+  sh = ex == 0 ? 63 : sh;  // zero and subnormals give digit 0
+  const uint64_t m = (b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  const uint64_t t = m >> sh;
+  const uint64_t sgn = (uint64_t)((int64_t)b >> 63);
+  return (int64_t)((t ^ sgn) + (1ULL + 2ULL * 0x8080808080ULL)) >> 1;
+}
+
+__host__ __device__ __forceinline__ void bsum_digits(int64_t bs, int32_t *d) {
+  d[0] = (int32_t)(bs >> 40);
+#pragma unroll
+  for (int s = 1; s < 6; ++s) d[s] = (int32_t)((bs >> (40 - 8 * s)) & 255) - 128;
+}
+
+// Signed int64 times 2^scale to double, rounded to nearest with ties away
+// from zero (one normalisation, no branch on the rounding carry: a mantissa
+// that rounds up to 2^53 carries into the exponent field).
+__host__ __device__ __forceinline__ double i64_to_double_fast(int64_t v, int scale) {
+  const uint64_t sgn = (uint64_t)(v >> 63);
+  const uint64_t u = ((uint64_t)v ^ sgn) - sgn;
+  const int lz = clz64(u);
+  const uint64_t nrm = u << (lz & 63);
+  const uint64_t m = ((nrm >> 10) + 1) >> 1;  // 53 bits, or 2^53 after the carry
+  const int be = 63 - lz + scale + 1023;      // biased exponent of the leading bit
+  const uint64_t bits = ((uint64_t)(be - 1) << 52) + m;
+  return (u == 0 || be <= 0) ? 0.0 : bitsd(bits | (sgn << 63));
+}
+
+// Exact level sums (|T_l| <= 2^22, integers held in fp32) to the recombined
+// int64 v = sum_l T_l 2^(40 - 8 l).  Each T_l becomes an integer through the
+// 1.5 * 2^23 magic add (exact for |T| <= 2^22: the sum stays in [2^23, 2^24],
+// spacing 1); pairs (l, l+1) combine in 32-bit arithmetic (|T_l * 256 +
+// T_(l+1)| < 2^31), the magic bias of a pair removed modulo 2^32.
+__host__ __device__ __forceinline__ int64_t levels_to_i64(float t0, float t1, float t2, float t3, float t4,
+                                                         float t5) {
+  constexpr uint32_t kPairBias = 257u * 0x4B400000u;
+  auto u = [](float t) -> uint32_t {
+    const float f = t + 12582912.0f;
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t r;
+    __builtin_memcpy(&r, &f, 4);
+    return r;
+#endif
+  };
+  const int32_t p01 = (int32_t)(u(t0) * 256u + u(t1) - kPairBias);
+  const int32_t p23 = (int32_t)(u(t2) * 256u + u(t3) - kPairBias);
+  const int32_t p45 = (int32_t)(u(t4) * 256u + u(t5) - kPairBias);
+  return (int64_t)p01 * 4294967296LL + (int64_t)p23 * 65536LL + (int64_t)p45;
+}
+
 }  // namespace oz
 }  // namespace gbqv

@@ -80,9 +80,11 @@ class QubitVector:
         self._c(self._L.gbqv_get_stream(self._h, C.byref(p)))
         return p.value or 0
 
-    def set_tensor_c128(self, enable: bool) -> None:
-        """complex128 dense 4/5-qubit gates on the tensor cores (default) or FP64 FMAs."""
-        self._c(self._L.gbqv_set_tensor_c128(self._h, int(bool(enable))))
+    def set_tensor_c128(self, mode) -> None:
+        """complex128 dense 4/5-qubit gates: True / 1 tensor cores (tcgen05 for
+        4 qubits, the default), 2 tensor cores through mma.sync only, False / 0
+        FP64 FMAs."""
+        self._c(self._L.gbqv_set_tensor_c128(self._h, int(mode)))
 
     def device_pointer(self) -> int:
         p = C.c_void_p()

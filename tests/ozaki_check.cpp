@@ -3,10 +3,14 @@
 // (what FP32 accumulation yields for these bounded integers) and the result
 // is compared against a __float128 matrix-vector product.  Prints the worst
 // error relative to (row max * column max) and the worst absolute error.
+// Mode "signed" (third argument) checks the tcgen05 kernel's variant: signed
+// digits from split_bsum, level sums held as fp32 (|T| <= 2^22) and
+// recombined by levels_to_i64 + i64_to_double_fast.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <random>
+#include <string>
 #include <vector>
 
 #include "gbqv_ozaki.h"
@@ -16,6 +20,7 @@ using namespace gbqv::oz;
 int main(int argc, char **argv) {
   const int K = argc > 1 ? atoi(argv[1]) : 32;   // reals per column
   const int trials = argc > 2 ? atoi(argv[2]) : 2000;
+  const bool sgn = argc > 3 && std::string(argv[3]) == "signed";
   std::mt19937_64 rng(12345);
   std::normal_distribution<double> nd(0.0, 1.0);
   std::uniform_int_distribution<int> ed(-60, 2);
@@ -36,7 +41,10 @@ int main(int argc, char **argv) {
     std::vector<int64_t> dx(K * kSlices);
     for (int j = 0; j < K; ++j) {
       int32_t d[6];
-      split6(x[j], E, d);
+      if (sgn)
+        bsum_digits(split_bsum(x[j], E), d);
+      else
+        split6(x[j], E, d);
       for (int s = 0; s < 6; ++s) dx[j * 6 + s] = d[s];
     }
     for (int r = 0; r < K; ++r) {
@@ -45,10 +53,14 @@ int main(int argc, char **argv) {
       std::vector<int64_t> da(K * 6);
       for (int j = 0; j < K; ++j) {
         int32_t d[6];
-        split6(A[r * K + j], R, d);
+        if (sgn)
+          bsum_digits(split_bsum(A[r * K + j], R), d);
+        else
+          split6(A[r * K + j], R, d);
         for (int s = 0; s < 6; ++s) da[j * 6 + s] = d[s];
       }
       int64_t v = 0;
+      float Tf[kLevels];
       for (int l = 0; l < kLevels; ++l) {
         int64_t T = 0;
         for (int tt = 0; tt <= l; ++tt) {
@@ -59,9 +71,24 @@ int main(int argc, char **argv) {
           printf("level sum out of the exact range\n");
           return 1;
         }
+        if (sgn && (T > (1 << 22) || T < -(1 << 22))) {  // outside the magic-add range
+          printf("level sum above 2^22\n");
+          return 1;
+        }
+        Tf[l] = (float)T;
         v += T * (int64_t(1) << (8 * (5 - l)));
       }
-      const double y = (R == 0 || E == 0) ? 0.0 : i64_to_double(v, out_scale(R, E));
+      double y;
+      if (sgn) {
+        const int64_t v2 = levels_to_i64(Tf[0], Tf[1], Tf[2], Tf[3], Tf[4], Tf[5]);
+        if (v2 != v) {
+          printf("levels_to_i64 mismatch\n");
+          return 1;
+        }
+        y = (R == 0 || E == 0) ? 0.0 : i64_to_double_fast(v, out_scale(R, E));
+      } else {
+        y = (R == 0 || E == 0) ? 0.0 : i64_to_double(v, out_scale(R, E));
+      }
       __float128 ref = 0;
       double amax = 0, xmax = 0;
       for (int j = 0; j < K; ++j) {

@@ -2,7 +2,9 @@
 cores (qiskit-aer_gb300/csrc/gbqv_ozaki.h): split -> exact level sums ->
 int64 recombination -> double, against __float128 matrix-vector products,
 for 4- and 5-qubit gates (32 / 64 reals), including zeros, one dominant
-entry and a 2^-60..2^2 dynamic range.  Bound: 1e-13 of (row max x column max)."""
+entry and a 2^-60..2^2 dynamic range.  Bound: 1e-13 of (row max x column max).
+Mode "signed" is the tcgen05 kernel's variant (signed digits, fp32 level
+sums through the magic-add recombination, fast int64 -> double)."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -13,11 +15,13 @@ ROOT = Path(__file__).resolve().parents[1]
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
-@pytest.mark.parametrize("reals,trials", [(32, 3000), (64, 1500)])
-def test_digit_slices_against_quad(tmp_path, reals, trials):
+@pytest.mark.parametrize("reals,trials,mode", [(32, 3000, "rounded"), (64, 1500, "rounded"),
+                                               (32, 3000, "signed")])
+def test_digit_slices_against_quad(tmp_path, reals, trials, mode):
     exe = tmp_path / "ozk"
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "qiskit-aer_gb300" / "csrc"),
                            str(ROOT / "tests" / "ozaki_check.cpp"), "-o", str(exe), "-lquadmath"])
-    out = subprocess.run([str(exe), str(reals), str(trials)], capture_output=True, text=True, check=True).stdout
+    out = subprocess.run([str(exe), str(reals), str(trials), mode], capture_output=True, text=True,
+                         check=True).stdout
     rel, absolute = map(float, out.split())
     assert rel < 1e-13, out
