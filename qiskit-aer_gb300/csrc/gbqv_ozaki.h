@@ -165,28 +165,63 @@ __host__ __device__ __forceinline__ void bsum_digits(int64_t bs, int32_t *d) {
   for (int s = 1; s < 6; ++s) d[s] = (int32_t)((bs >> (40 - 8 * s)) & 255) - 128;
 }
 
-// Signed int64 times 2^scale to double, rounded to nearest with ties away
-// from zero (one normalisation, no branch on the rounding carry: a mantissa
-// that rounds up to 2^53 carries into the exponent field).
-__host__ __device__ __forceinline__ double i64_to_double_fast(int64_t v, int scale) {
-  const uint64_t sgn = (uint64_t)(v >> 63);
-  const uint64_t u = ((uint64_t)v ^ sgn) - sgn;
-  const int lz = clz64(u);
-  const uint64_t nrm = u << (lz & 63);
-  const uint64_t m = ((nrm >> 10) + 1) >> 1;  // 53 bits, or 2^53 after the carry
-  const int be = 63 - lz + scale + 1023;      // biased exponent of the leading bit
-  const uint64_t bits = ((uint64_t)(be - 1) << 52) + m;
-  return (u == 0 || be <= 0) ? 0.0 : bitsd(bits | (sgn << 63));
+// ---- the tcgen05 kernel's arithmetic (host + device, bit-identical) ----
+// PTX shifts clamp the shift amount to the register width; the host
+// versions do the same so both sides agree for every input.
+__host__ __device__ __forceinline__ uint64_t shr64(uint64_t x, uint32_t s) {
+#ifdef __CUDA_ARCH__
+  uint64_t r;
+  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(s));
+  return r;
+#else
+  return s >= 64 ? 0 : x >> s;
+#endif
+}
+__host__ __device__ __forceinline__ uint64_t shl64(uint64_t x, uint32_t s) {
+#ifdef __CUDA_ARCH__
+  uint64_t r;
+  asm("shl.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(s));
+  return r;
+#else
+  return s >= 64 ? 0 : x << s;
+#endif
 }
 
-// Exact level sums (|T_l| <= 2^22, integers held in fp32) to the recombined
-// int64 v = sum_l T_l 2^(40 - 8 l).  Each T_l becomes an integer through the
-// 1.5 * 2^23 magic add (exact for |T| <= 2^22: the sum stays in [2^23, 2^24],
-// spacing 1); pairs (l, l+1) combine in 32-bit arithmetic (|T_l * 256 +
-// T_(l+1)| < 2^31), the magic bias of a pair removed modulo 2^32.
-__host__ __device__ __forceinline__ int64_t levels_to_i64(float t0, float t1, float t2, float t3, float t4,
-                                                         float t5) {
-  constexpr uint32_t kPairBias = 257u * 0x4B400000u;
+// split_bsum's value plus 0x6600 * 2^40, given x's biased exponent field ex
+// and E3 = E + 3: bytes 0..3 and 4 are digits 5..2 and 1 plus 128, bits
+// 40..55 are the fp16 bits of 1536 + d_0 (the kernel subtracts 1536 in
+// packed halves).  The added constant keeps the word positive, so the halving
+// shift is logical.  Zeros (ex = 0) give digit 0 whenever E >= 50; groups
+// whose largest entry is below 2^-973 are the only ones where a zero turns
+// into a value of order 2^-1022.
+constexpr uint64_t kSplitK = 1ULL + 2ULL * 0x8080808080ULL + (0x6600ULL << 41);
+
+__host__ __device__ __forceinline__ uint64_t split_word(double x, uint32_t ex, uint32_t E3) {
+  const uint64_t b = dbits(x);
+  const uint64_t m = (b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  const uint64_t t = shr64(m, E3 - ex);
+  const uint64_t sgn = (uint64_t)((int64_t)b >> 63);
+  return ((t ^ sgn) + kSplitK) >> 1;
+}
+
+__host__ __device__ __forceinline__ void word_digits(uint64_t w, int32_t *d) {
+  d[0] = (int32_t)((w >> 40) & 0xFFFF) - 0x6600;
+#pragma unroll
+  for (int s = 1; s < 6; ++s) d[s] = (int32_t)((w >> (40 - 8 * s)) & 255) - 128;
+}
+
+// Six exact level sums to the output double, v * 2^(ebase - 1085) with
+// v = sum_l T_l 2^(40 - 8 l).  The magic-added words u_l = 0x4B400000 + T_l
+// pair up without wrapping (257 * 0x4B400000 mod 2^32 +- 2^30 stays inside
+// [0, 2^32)), so one 64-bit constant removes all biases.  A negative v is
+// normalised in ones' complement (|v| - 1, an error of one unit in 2^-55 of
+// row max x column max), and the 53-bit mantissa is rounded half up; a
+// mantissa that rounds to 2^53 carries into the exponent field.  Zero and
+// results below 2^-1022 give 0.
+__host__ __device__ __forceinline__ double levels_to_double(float t0, float t1, float t2, float t3, float t4,
+                                                            float t5, int ebase) {
+  constexpr uint32_t kPair = 257u * 0x4B400000u;
+  constexpr uint64_t kBias = (uint64_t)kPair * 0x100010001ULL;  // kPair * (2^32 + 2^16 + 1) mod 2^64
   auto u = [](float t) -> uint32_t {
     const float f = t + 12582912.0f;
 #ifdef __CUDA_ARCH__
@@ -197,10 +232,16 @@ __host__ __device__ __forceinline__ int64_t levels_to_i64(float t0, float t1, fl
     return r;
 #endif
   };
-  const int32_t p01 = (int32_t)(u(t0) * 256u + u(t1) - kPairBias);
-  const int32_t p23 = (int32_t)(u(t2) * 256u + u(t3) - kPairBias);
-  const int32_t p45 = (int32_t)(u(t4) * 256u + u(t5) - kPairBias);
-  return (int64_t)p01 * 4294967296LL + (int64_t)p23 * 65536LL + (int64_t)p45;
+  const uint32_t p01 = u(t0) * 256u + u(t1), p23 = u(t2) * 256u + u(t3), p45 = u(t4) * 256u + u(t5);
+  const uint64_t v = ((uint64_t)p01 << 32) + ((uint64_t)p23 << 16) + (uint64_t)p45 - kBias;
+  const uint32_t sg = (uint32_t)((int32_t)(uint32_t)(v >> 32) >> 31);
+  const uint64_t a = v ^ (((uint64_t)sg << 32) | sg);
+  const int lz = clz64(a);
+  const uint64_t n = shl64(a, (uint32_t)lz);
+  const uint64_t mant = (n >> 11) + ((n >> 10) & 1);
+  const int e1 = ebase - lz;  // biased exponent - 1
+  const uint64_t bits = mant + ((uint64_t)(((uint32_t)e1 << 20) | (sg & 0x80000000u)) << 32);
+  return (a == 0 || e1 < 0) ? 0.0 : bitsd(bits);
 }
 
 }  // namespace oz

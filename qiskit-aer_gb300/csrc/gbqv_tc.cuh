@@ -44,11 +44,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 // Waits for the completion of the phase with the given parity.  Returns false
 // (and raises *abort) after kWaitNs, or returns false at once when *abort is
-// already raised by another thread.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
+// already raised by another thread.  sleep_ns > 0 backs off between polls
+// (single-thread roles, so that they leave issue slots to the warps sharing
+// their SM sub-partition).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort,
+                                          unsigned sleep_ns = 0) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 1; it < (1u << 26); ++it) {
+    if (sleep_ns) __nanosleep(sleep_ns);
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 31) == 0) {
       if (*abort) return false;
@@ -119,6 +123,20 @@ __host__ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t l
 // (bits 7-9, 10-12 = 0), both K-major, N>>3 at [17,23), M>>4 at [24,29).
 __host__ __device__ __forceinline__ uint32_t idesc_f16_f32(int m, int n) {
   return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// ---- bulk (TMA) copies global -> shared, completing on an mbarrier ----
+// One arrival that also raises the phase's expected transaction bytes.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
+// dst and src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
 }
 
 // ---- packed half arithmetic ----

@@ -3,9 +3,10 @@
 // (what FP32 accumulation yields for these bounded integers) and the result
 // is compared against a __float128 matrix-vector product.  Prints the worst
 // error relative to (row max * column max) and the worst absolute error.
-// Mode "signed" (third argument) checks the tcgen05 kernel's variant: signed
-// digits from split_bsum, level sums held as fp32 (|T| <= 2^22) and
-// recombined by levels_to_i64 + i64_to_double_fast.
+// Mode "signed" (third argument) checks the tcgen05 kernel's arithmetic: the
+// state's digits from split_word (checked equal to split_bsum's), the
+// matrix's from split_bsum, level sums held as fp32 (|T| <= 2^22) and turned
+// into the double by levels_to_double.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -41,9 +42,17 @@ int main(int argc, char **argv) {
     std::vector<int64_t> dx(K * kSlices);
     for (int j = 0; j < K; ++j) {
       int32_t d[6];
-      if (sgn)
-        bsum_digits(split_bsum(x[j], E), d);
-      else
+      if (sgn) {
+        const uint32_t ex = (uint32_t)((dbits(x[j]) >> 52) & 0x7ff);
+        word_digits(split_word(x[j], ex, (uint32_t)E + 3), d);
+        int32_t d2[6];
+        bsum_digits(split_bsum(x[j], E), d2);
+        for (int s = 0; s < 6; ++s)
+          if (d[s] != d2[s] && (ex != 0 || E >= 50)) {
+            printf("split_word digits differ from split_bsum\n");
+            return 1;
+          }
+      } else
         split6(x[j], E, d);
       for (int s = 0; s < 6; ++s) dx[j * 6 + s] = d[s];
     }
@@ -80,12 +89,7 @@ int main(int argc, char **argv) {
       }
       double y;
       if (sgn) {
-        const int64_t v2 = levels_to_i64(Tf[0], Tf[1], Tf[2], Tf[3], Tf[4], Tf[5]);
-        if (v2 != v) {
-          printf("levels_to_i64 mismatch\n");
-          return 1;
-        }
-        y = (R == 0 || E == 0) ? 0.0 : i64_to_double_fast(v, out_scale(R, E));
+        y = (R == 0 || E == 0) ? 0.0 : levels_to_double(Tf[0], Tf[1], Tf[2], Tf[3], Tf[4], Tf[5], R + E - 1017);
       } else {
         y = (R == 0 || E == 0) ? 0.0 : i64_to_double(v, out_scale(R, E));
       }
