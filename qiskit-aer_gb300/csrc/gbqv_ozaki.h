@@ -187,41 +187,82 @@ __host__ __device__ __forceinline__ uint64_t shl64(uint64_t x, uint32_t s) {
 #endif
 }
 
-// split_bsum's value plus 0x6600 * 2^40, given x's biased exponent field ex
-// and E3 = E + 3: bytes 0..3 and 4 are digits 5..2 and 1 plus 128, bits
-// 40..55 are the fp16 bits of 1536 + d_0 (the kernel subtracts 1536 in
-// packed halves).  The added constant keeps the word positive, so the halving
-// shift is logical.  Zeros (ex = 0) give digit 0 whenever E >= 50; groups
-// whose largest entry is below 2^-973 are the only ones where a zero turns
-// into a value of order 2^-1022.
+// Digit word of |x| against the column key E (E3 = E + 3), given x's biased
+// exponent field ex: the aligned significand rounded half up to 48 bits
+// (a <= 2^48, x ~= sign * a * 2^(E - 1071); symmetric in the sign, so no
+// drift of the norm, and exact values stay exact) plus 0x8080808080 +
+// 0x6600 * 2^40, so that bytes 0..3 and 4 are digits 5..2 and 1 plus 128 and
+// bits 40..55 are the fp16 bits of 1536 + d_0 (d_0 in [0, 256]); the digits
+// of x are these times the sign of x (balanced digits negate digit by
+// digit).  Rounding and the constant come from one add before the halving
+// shift.  Zeros (ex = 0) give digit 0 whenever E >= 50; groups whose
+// largest entry is below 2^-973 are the only ones where a zero turns into a
+// value of order 2^-1022.
 constexpr uint64_t kSplitK = 1ULL + 2ULL * 0x8080808080ULL + (0x6600ULL << 41);
 
-__host__ __device__ __forceinline__ uint64_t split_word(double x, uint32_t ex, uint32_t E3) {
-  const uint64_t b = dbits(x);
-  const uint64_t m = (b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
-  const uint64_t t = shr64(m, E3 - ex);
-  const uint64_t sgn = (uint64_t)((int64_t)b >> 63);
-  return ((t ^ sgn) + kSplitK) >> 1;
+__host__ __device__ __forceinline__ uint64_t split_word_abs(double x, uint32_t ex, uint32_t E3) {
+  const uint64_t m = (dbits(x) & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  return (shr64(m, E3 - ex) + kSplitK) >> 1;
 }
 
-__host__ __device__ __forceinline__ void word_digits(uint64_t w, int32_t *d) {
+// Signed digits of x from its word (host side of the kernel's fp16 planes).
+__host__ __device__ __forceinline__ void word_digits(uint64_t w, bool negative, int32_t *d) {
   d[0] = (int32_t)((w >> 40) & 0xFFFF) - 0x6600;
 #pragma unroll
   for (int s = 1; s < 6; ++s) d[s] = (int32_t)((w >> (40 - 8 * s)) & 255) - 128;
+  if (negative)
+#pragma unroll
+    for (int s = 0; s < 6; ++s) d[s] = -d[s];
 }
 
 // Six exact level sums to the output double, v * 2^(ebase - 1085) with
-// v = sum_l T_l 2^(40 - 8 l).  The magic-added words u_l = 0x4B400000 + T_l
-// pair up without wrapping (257 * 0x4B400000 mod 2^32 +- 2^30 stays inside
-// [0, 2^32)), so one 64-bit constant removes all biases.  A negative v is
-// normalised in ones' complement (|v| - 1, an error of one unit in 2^-55 of
-// row max x column max), and the 53-bit mantissa is rounded half up; a
-// mantissa that rounds to 2^53 carries into the exponent field.  Zero and
-// results below 2^-1022 give 0.
-__host__ __device__ __forceinline__ double levels_to_double(float t0, float t1, float t2, float t3, float t4,
-                                                            float t5, int ebase) {
+// v = sum_l T_l 2^(40 - 8 l), from the fp32 words u_l = bits(1.5 * 2^23 +
+// T_l) = 0x4B400000 + T_l (exact for |T_l| <= 2^22: the sum stays in [2^23,
+// 2^24], spacing 1).  The words pair up without wrapping (257 * 0x4B400000
+// mod 2^32 +- 2^30 stays inside [0, 2^32)), so one 64-bit constant removes
+// all biases.  |v| is taken in ones' complement (|v| - 1 for v < 0) and its
+// 53 leading bits are kept (truncation); both errors are below 2^-52 of the
+// result or 2^-55 of row max x column max.  Zero and results below 2^-1022
+// give 0.  When the high word of |v| is non-zero (every output above 2^-23
+// of row max x column max) and ebase >= 32, the normalisation is two 32-bit
+// funnel shifts and no range check is needed; the other path gives the same
+// bits.
+__host__ __device__ __forceinline__ uint32_t funnel_l(uint32_t lo, uint32_t hi, uint32_t s) {  // s in [0, 31]
+#ifdef __CUDA_ARCH__
+  return __funnelshift_l(lo, hi, s);
+#else
+  return s == 0 ? hi : (hi << s) | (lo >> (32 - s));
+#endif
+}
+
+__host__ __device__ __forceinline__ double words_to_double(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3,
+                                                           uint32_t u4, uint32_t u5, int ebase) {
   constexpr uint32_t kPair = 257u * 0x4B400000u;
   constexpr uint64_t kBias = (uint64_t)kPair * 0x100010001ULL;  // kPair * (2^32 + 2^16 + 1) mod 2^64
+  const uint32_t p01 = u0 * 256u + u1, p23 = u2 * 256u + u3, p45 = u4 * 256u + u5;
+  const uint64_t v = ((uint64_t)p01 << 32) + ((uint64_t)p23 << 16) + (uint64_t)p45 - kBias;
+  const uint32_t sg = (uint32_t)((int32_t)(uint32_t)(v >> 32) >> 31);
+  const uint32_t ah = (uint32_t)(v >> 32) ^ sg, al = (uint32_t)v ^ sg;
+  if (ah != 0 && ebase >= 32) {
+    const uint32_t lz = (uint32_t)clz64((uint64_t)ah << 32);
+    const uint32_t nh = funnel_l(al, ah, lz), nl = al << lz;
+    // mantissa bits 52..0 = n >> 11; the implicit bit adds one to the
+    // exponent field, hence e1 = biased exponent - 1
+    const uint32_t mhi = nh >> 11, mlo = (nh << 21) | (nl >> 11);
+    const uint32_t e1 = (uint32_t)(ebase - (int)lz);
+    return bitsd(((uint64_t)(mhi + (e1 << 20) + (sg << 31)) << 32) | mlo);
+  }
+  const uint64_t a = ((uint64_t)ah << 32) | al;
+  const int lz = clz64(a);
+  const uint64_t n = shl64(a, (uint32_t)lz);
+  const int e1 = ebase - lz;
+  const uint64_t bits = (n >> 11) + ((uint64_t)(((uint32_t)e1 << 20) | (sg & 0x80000000u)) << 32);
+  return (a == 0 || e1 < 0) ? 0.0 : bitsd(bits);
+}
+
+// The same from fp32 level sums (the magic add done here).
+__host__ __device__ __forceinline__ double levels_to_double(float t0, float t1, float t2, float t3, float t4,
+                                                            float t5, int ebase) {
   auto u = [](float t) -> uint32_t {
     const float f = t + 12582912.0f;
 #ifdef __CUDA_ARCH__
@@ -232,16 +273,7 @@ __host__ __device__ __forceinline__ double levels_to_double(float t0, float t1, 
     return r;
 #endif
   };
-  const uint32_t p01 = u(t0) * 256u + u(t1), p23 = u(t2) * 256u + u(t3), p45 = u(t4) * 256u + u(t5);
-  const uint64_t v = ((uint64_t)p01 << 32) + ((uint64_t)p23 << 16) + (uint64_t)p45 - kBias;
-  const uint32_t sg = (uint32_t)((int32_t)(uint32_t)(v >> 32) >> 31);
-  const uint64_t a = v ^ (((uint64_t)sg << 32) | sg);
-  const int lz = clz64(a);
-  const uint64_t n = shl64(a, (uint32_t)lz);
-  const uint64_t mant = (n >> 11) + ((n >> 10) & 1);
-  const int e1 = ebase - lz;  // biased exponent - 1
-  const uint64_t bits = mant + ((uint64_t)(((uint32_t)e1 << 20) | (sg & 0x80000000u)) << 32);
-  return (a == 0 || e1 < 0) ? 0.0 : bitsd(bits);
+  return words_to_double(u(t0), u(t1), u(t2), u(t3), u(t4), u(t5), ebase);
 }
 
 }  // namespace oz

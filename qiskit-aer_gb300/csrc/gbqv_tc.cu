@@ -51,7 +51,13 @@ constexpr int kStageBytes = 6 * kPlaneBytes;            // 48 KB
 constexpr int kMatBytes = 6 * kTcReals * kTcReals * 2;  // 12 KB: six matrix planes
 constexpr int kRawStage = kTcGroups * 16 * 16;  // 32 KB: a tile's raw amplitudes, in run order
 constexpr int kRawStages = 3;                    // bulk loads run up to three tiles ahead
-constexpr int kOffStage = kMatBytes;
+// bf16 operands of the accumulator-initialising MMA: A = 128 x 16 (column 0
+// ones), B = 192 x 16 (column 0 = 1.5 * 2^23), K-major, 8-row groups 256 B
+// apart: D = 1.5 * 2^23 everywhere, so every level sum lands in TMEM as the
+// word 0x4B400000 + T
+constexpr int kInitABytes = kTcGroups * 16 * 2, kInitBBytes = 6 * kTcReals * 16 * 2;
+constexpr int kOffInit = kMatBytes;
+constexpr int kOffStage = kOffInit + kInitABytes + kInitBBytes;
 constexpr int kOffRaw = kOffStage + 2 * kStageBytes;
 constexpr int kOffKey = kOffRaw + kRawStages * kRawStage;
 constexpr int kOffBar = kOffKey + 2 * kTcGroups * 4;
@@ -95,11 +101,11 @@ __host__ __device__ constexpr uint32_t core_off(uint32_t row, uint32_t k) {
   return (row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
-// output real i of the loaded chunk; ebase = row key + column key - 1017
-// (the biased exponent - 1 of a value whose leading bit is bit 63 of v)
+// output real i of the loaded chunk (TMEM words 0x4B400000 + T_l); ebase =
+// row key + column key - 1017 (the biased exponent - 1 of a value whose
+// leading bit is bit 63 of v)
 __device__ __forceinline__ double combine(const uint32_t (&T)[6][8], int i, int ebase) {
-  return oz::levels_to_double(__uint_as_float(T[0][i]), __uint_as_float(T[1][i]), __uint_as_float(T[2][i]),
-                              __uint_as_float(T[3][i]), __uint_as_float(T[4][i]), __uint_as_float(T[5][i]), ebase);
+  return oz::words_to_double(T[0][i], T[1][i], T[2][i], T[3][i], T[4][i], T[5][i], ebase);
 }
 
 template <int EH>
@@ -122,7 +128,7 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
   auto acce = [&](int b) { return bar0 + 8u * (6 + b); };
   const uint32_t done = bar0 + 8u * 8;
   // raw ring: raw_full[3] (loader arrival + bulk bytes), raw_empty[3] (256
-  // producer arrivals after the split)
+  // producer arrivals once the tile's amplitudes are in registers)
   auto raw_full = [&](int r) { return bar0 + 8u * (9 + r); };
   auto raw_empty = [&](int r) { return bar0 + 8u * (12 + r); };
 
@@ -149,6 +155,13 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
   {
     uint4 *dst = reinterpret_cast<uint4 *>(smem);
     for (int i = tid; i < kMatBytes / 16; i += kThreads) dst[i] = gmat[i];
+    // init operands: element (row, k) at (row / 8) * 256 + (k / 8) * 128 +
+    // (row % 8) * 16 + (k % 8) * 2; only k = 0 is non-zero
+    uint16_t *ia = reinterpret_cast<uint16_t *>(smem + kOffInit);
+    for (int i = tid; i < (kInitABytes + kInitBBytes) / 2; i += kThreads) ia[i] = 0;
+    __syncthreads();
+    if (tid < kTcGroups) ia[(tid >> 3) * 128 + (tid & 7) * 8] = 0x3F80;  // bf16 1.0
+    if (tid < 6 * kTcReals) ia[kInitABytes / 2 + (tid >> 3) * 128 + (tid & 7) * 8] = 0x4B40;  // bf16 1.5 * 2^23
   }
   tc::fence_async_smem();
   tc::fence_before_sync();
@@ -178,15 +191,22 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       const unsigned char *raw = smem + kOffRaw + slot * kRawStage;
       auto amp = [&](int j) { return *reinterpret_cast<const double2 *>(raw + ro[j]); };
       // the group key: the largest biased exponent field plus one (0 for an
-      // all-zero group, which is never stored)
+      // all-zero group, which is never stored); the fields are kept
       double2 v[8];
+      uint32_t ex[16];
       uint32_t mx = 0;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         v[j] = amp(j);
-        mx = max(mx, max(((uint32_t)__double2hiint(v[j].x) >> 20) & 0x7ff,
-                         ((uint32_t)__double2hiint(v[j].y) >> 20) & 0x7ff));
+        ex[2 * j] = ((uint32_t)__double2hiint(v[j].x) >> 20) & 0x7ff;
+        ex[2 * j + 1] = ((uint32_t)__double2hiint(v[j].y) >> 20) & 0x7ff;
+        mx = max(mx, max(ex[2 * j], ex[2 * j + 1]));
       }
+      // the amplitudes are in registers now: the raw slot goes back to the
+      // loader before the split.  The proxy fence orders these generic-proxy
+      // reads before the loader's next bulk (async-proxy) write to the slot.
+      tc::fence_async_smem();
+      tc::mbar_arrive(raw_empty(slot));
       mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
       const int key = mx ? (int)mx + 1 : 0;
       const uint32_t E3 = (uint32_t)key + 3;
@@ -196,61 +216,69 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       const uint32_t K64 = 0x64646464u;
 #pragma unroll
       for (int q2 = 0; q2 < 2; ++q2) {
-        // the chunk's 8 reals (amplitudes 4q..4q+3, re/im) as split words
-        uint32_t lo[8], hi[8];
+        // the chunk's 8 reals (amplitudes 4q..4q+3, re/im): digit words of
+        // their magnitudes, and per amplitude the (re, im) sign pair as half2
+        // (+-1, +-1) with the bias constants times it, so that one HFMA2 per
+        // plane word both removes the fp16 bias and applies the signs
+        uint32_t lo[8], hi[8], sg[4], c1[4], c0[4];
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const double2 a = v[4 * q2 + jj];
-          const uint64_t rw = oz::split_word(a.x, ((uint32_t)__double2hiint(a.x) >> 20) & 0x7ff, E3);
-          const uint64_t iw = oz::split_word(a.y, ((uint32_t)__double2hiint(a.y) >> 20) & 0x7ff, E3);
+          const int j = 4 * q2 + jj;
+          const uint64_t rw = oz::split_word_abs(v[j].x, ex[2 * j], E3);
+          const uint64_t iw = oz::split_word_abs(v[j].y, ex[2 * j + 1], E3);
           lo[2 * jj] = (uint32_t)rw;
           hi[2 * jj] = (uint32_t)(rw >> 32);
           lo[2 * jj + 1] = (uint32_t)iw;
           hi[2 * jj + 1] = (uint32_t)(iw >> 32);
+          // bit 15 <- sign of re, bit 31 <- sign of im (byte sign replication)
+          const uint32_t sb = tc::prmt((uint32_t)__double2hiint(v[j].x), (uint32_t)__double2hiint(v[j].y), 0xF0B0);
+          sg[jj] = (sb & 0x80008000u) | 0x3C003C00u;
+          c1[jj] = tc::hmul2(sg[jj], 0xE480E480u);  // -1152 * sign
+          c0[jj] = tc::hmul2(sg[jj], 0xE600E600u);  // -1536 * sign
         }
         unsigned char *row = stage + core_off(m, 8 * (2 * h + q2));
-        // digits 1..5 are byte (5 - s) of bsum plus 128: fp16 0x64xx = 1152 + d
-        // after a byte permute; subtract 1152 in packed halves
+        // digits 1..5 are byte (5 - s) of the word plus 128: fp16 0x64xx =
+        // 1152 + |d| after a byte permute
         uint32_t w[4];
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
           const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x5140);
-          w[jj] = tc::hadd2(tc::prmt(g, K64, 0x4140), 0xE480E480u);
+          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 5 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
           const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x5140);
-          w[jj] = tc::hadd2(tc::prmt(g, K64, 0x4342), 0xE480E480u);
+          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 4 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
           const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x7362);
-          w[jj] = tc::hadd2(tc::prmt(g, K64, 0x4140), 0xE480E480u);
+          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 3 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
           const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x7362);
-          w[jj] = tc::hadd2(tc::prmt(g, K64, 0x4342), 0xE480E480u);
+          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 2 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
           const uint32_t g = tc::prmt(hi[2 * jj], hi[2 * jj + 1], 0x0040);
-          w[jj] = tc::hadd2(tc::prmt(g, K64, 0x4140), 0xE480E480u);
+          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 1 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
-        // digit 0: bytes 5-6 of the word are the fp16 bits of 1536 + d_0
+        // digit 0: bytes 5-6 of the word are the fp16 bits of 1536 + |d_0|
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) w[jj] = tc::hadd2(tc::prmt(hi[2 * jj], hi[2 * jj + 1], 0x6521), 0xE600E600u);
+        for (int jj = 0; jj < 4; ++jj)
+          w[jj] = tc::hfma2(tc::prmt(hi[2 * jj], hi[2 * jj + 1], 0x6521), sg[jj], c0[jj]);
         *reinterpret_cast<uint4 *>(row) = make_uint4(w[0], w[1], w[2], w[3]);
       }
       if (h == 0) colkey[b * kTcGroups + m] = key;
       tc::fence_async_smem();
       tc::mbar_arrive(full(b));
-      tc::mbar_arrive(raw_empty(slot));
     }
   } else if (warp < kMmaWarp) {
     // ---------------- epilogues ----------------
@@ -318,13 +346,15 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(smem + kOffStage + b * kStageBytes);
       const uint32_t d0 = tmem + (uint32_t)b * 256u;
+      const uint32_t ini = tc::smem_u32(smem + kOffInit);
+      tc::mma_f16(d0, tc::smem_desc(ini, 128, 256), tc::smem_desc(ini + kInitABytes, 128, 256),
+                  tc::idesc_bf16_f32(128, 6 * kTcReals), 0);
 #pragma unroll
       for (int s = 0; s < 6; ++s)
 #pragma unroll
         for (int kk = 0; kk < 2; ++kk)
           tc::mma_f16(d0 + 32u * s, tc::smem_desc(a0 + s * kPlaneBytes + kk * 256, 128, 512),
-                      tc::smem_desc(mat + kk * 256, 128, 512), tc::idesc_f16_f32(128, 32 * (6 - s)),
-                      (s | kk) != 0);
+                      tc::smem_desc(mat + kk * 256, 128, 512), tc::idesc_f16_f32(128, 32 * (6 - s)), 1);
       tc::mma_commit(accf(b));
     }
     // every MMA issued above has completed once `done` flips (bounded wait,

@@ -139,10 +139,25 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
                : "memory");
 }
 
+// The same for bf16 A and B (bits 7-9 and 10-12 = 1).
+__host__ __device__ __forceinline__ uint32_t idesc_bf16_f32(int m, int n) {
+  return idesc_f16_f32(m, n) | (1u << 7) | (1u << 10);
+}
+
 // ---- packed half arithmetic ----
 __device__ __forceinline__ uint32_t hadd2(uint32_t a, uint32_t b) {
   uint32_t d;
   asm("add.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t hfma2(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ uint32_t hmul2(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
   return d;
 }
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
