@@ -4,8 +4,9 @@ Default workload (the headline): fused-gate application on a 30-qubit
 quantum-volume-style circuit — 30 layers, each a seeded random pairing of
 the qubits with one Haar-random SU(4) per pair (450 two-qubit unitaries) —
 fused by Aer's Fusion pass (max 5 qubits; it yields 218 fused ops), with the
-2^30-amplitude state resident in HBM.  One step applies the whole fused
-circuit once.
+2^30-amplitude complex128 state (17 GB) resident in HBM.  One step applies
+the whole fused circuit once.  The same line carries the complex64 run of the
+same circuit under ``variants``.
 
   value    fused-gate GB/s = fused ops x (2 x 2^n x bytes/amp) / step time:
            the algorithmic bytes of one read+write pass per fused op
@@ -14,7 +15,10 @@ circuit once.
            host memory and the 8-qubit marginal read back, every step
   roofline the dominant kernel (one fused 4-qubit op over the state): its
            algorithmic bytes per launch / its mean launch time (CUDA events
-           on the engine's stream), against the measured HBM copy bandwidth
+           on the engine's stream), against the measured HBM copy bandwidth;
+           traffic = DRAM bytes per launch from an ncu capture of the same
+           kernel on a 26-qubit state, scaled by 16 (traffic grows with the
+           state)
   cpu_baseline  the oracle (C restatement of Aer's QubitVector + OpenMP) on
            the host cores, over a bounded sample of the same fused ops
 
@@ -190,6 +194,12 @@ def run_reference_arm(args):
         "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from
+# `ncu --set full` captures on a 26-qubit state (profiles/k_dense_tc4_c128_26q.md,
+# profiles/k_dense_c64_k4_26q.md), scaled to 2^qubits amplitudes.
+NCU_TRAFFIC_26Q = {("c128", 4): 2.0863e9, ("c64", 4): 1.0117e9}
+
+
 def bench_qv(args, torch, P):
     L = P.lib()
     qc, nc, fused = fused_ops_of(P, args)
@@ -232,9 +242,14 @@ def bench_qv(args, torch, P):
     ms_launch = t.ms / reps
     peak, peak_kind = hbm_peak()
     achieved = pass_bytes / (ms_launch / 1e3) / 1e9
+    dtype = "c128" if args.precision == "double" else "c64"
+    traffic = NCU_TRAFFIC_26Q.get((dtype, len(q4)))
+    kname = {"c128": "k_dense_tc4 (tcgen05, exact digit slices)", "c64": "k_dense<float2, 4>"}[dtype]
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None,
-            "kernel": f"dense {len(q4)}-qubit op, {ms_launch:.3f} ms/launch", "peak_kind": peak_kind}
+            "frac": round(achieved / peak, 4),
+            "traffic": round(traffic * 2.0 ** (args.qubits - 26)) if traffic else None,
+            "kernel": f"{kname}: dense {len(q4)}-qubit op, {ms_launch:.3f} ms/launch, "
+                      f"{pass_bytes / 1e9:.2f} GB algorithmic per launch", "peak_kind": peak_kind}
     # e2e: public API with host buffers
     e2e = None
     if args.qubits <= 31:
@@ -256,6 +271,12 @@ def bench_qv(args, torch, P):
     base = None
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(fused, min(args.qubits, 26))
+    variants = None
+    if args.precision == "double" and not args.no_variants:
+        v64 = argparse.Namespace(**{**vars(args), "precision": "single", "no_cpu_baseline": True,
+                                    "no_variants": True, "steps": max(2, args.steps), "warmup": 3})
+        r = bench_qv(v64, torch, P)
+        variants = {"c64": {k: r[k] for k in ("value", "unit", "ms_per_step", "gpu_launches", "roofline", "e2e")}}
     return {"metric": "fused-gate GB/s", "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -263,7 +284,8 @@ def bench_qv(args, torch, P):
             "config": {"workload": f"QV {args.qubits}q x {args.layers} layers (Haar SU(4) per pair), Aer fusion max 5",
                        "qubits": args.qubits, "layers": args.layers, "fused_ops": nops,
                        "l2": "state larger than L2, no flush", "blocking": not args.no_blocking},
-            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clk}
+            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clk,
+            "variants": variants}
 
 
 def A_check(L, rc, st):
@@ -443,7 +465,7 @@ def main():
     ap.add_argument("--workload", default="qv", choices=["qv", "adjoint", "dm", "sample", "batch"])
     ap.add_argument("--instances", type=int, default=2048)
     ap.add_argument("--per-launch-sample", type=int, default=24)
-    ap.add_argument("--precision", default="single", choices=["double", "single"])
+    ap.add_argument("--precision", default="double", choices=["double", "single"])
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=30)
     ap.add_argument("--dm-layers", type=int, default=40)
@@ -451,6 +473,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-blocking", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the complex64 run of the default workload")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)

@@ -1021,7 +1021,11 @@ bool as_run_op(const Device &d, const Op &op, RunOp &out) {
 // 4*2^k FMAs per amplitude and is already compute-bound in one pass, so it
 // keeps its own streaming kernel; 1-2 qubit dense ops and diagonals are
 // bandwidth-bound and share passes.
-bool worth_batching(const RunOp &r) { return r.kind == 1 || r.qubits.size() <= 2; }
+// Diagonals and 1-2 qubit matrices share a cache-blocked pass; complex128
+// dense matrices that the tensor path takes (padded to 4 qubits) go there.
+bool worth_batching(const Device &d, const RunOp &r) {
+  return r.kind == 1 || (r.qubits.size() <= 2 && !tensor_dense_available(d, (int)r.qubits.size()));
+}
 
 // Greedy cache-blocking schedule: starting from the first pending op, take
 // every later op that (a) touches no qubit of an op left behind (so moving
@@ -1031,7 +1035,7 @@ void execute_blocked(Device &d, const std::vector<Op> &ops) {
   const size_t pool_cap = run_pool_bytes(d) / 16;
   std::vector<RunOp> conv(ops.size());
   std::vector<char> runnable(ops.size()), done(ops.size(), 0);
-  for (size_t i = 0; i < ops.size(); ++i) runnable[i] = as_run_op(d, ops[i], conv[i]) && worth_batching(conv[i]);
+  for (size_t i = 0; i < ops.size(); ++i) runnable[i] = as_run_op(d, ops[i], conv[i]) && worth_batching(d, conv[i]);
   const size_t lookahead = 96;
   size_t first = 0;
   while (first < ops.size()) {

@@ -129,13 +129,11 @@ struct DenseParams {
 };
 
 // (Capping complex64 k <= 4 at 3 CTAs per SM spills and measured slower
-// than 2 CTAs per SM, so every variant keeps the default register budget.)
-template <typename T>
-constexpr int dense_min_blocks(int K) { return 1; }
-
+// than 2 CTAs per SM; an explicit minimum of 1 CTA per SM lets the compiler
+// take 130 registers for complex64 k = 4, which allows only one CTA per SM
+// and cost 35% at 30 qubits.  The plain bound gives 118 registers, 2 CTAs.)
 template <typename T, int K, bool NORM>
-__global__ void __launch_bounds__(256, dense_min_blocks<T>(K)) k_dense(T *__restrict__ psi,
-                                                                        const __grid_constant__ DenseParams<T, K> p,
+__global__ void __launch_bounds__(256) k_dense(T *__restrict__ psi, const __grid_constant__ DenseParams<T, K> p,
                                                double *__restrict__ partials) {
   constexpr int D = 1 << K;
   double nacc = 0.0;
@@ -1288,10 +1286,29 @@ void dense_oz(Device &dev, const reg_t &qubits, const cd *mat) {
 
 }  // namespace
 
-bool tensor_dense_available(const Device &dev, int k) { return dev.dbl && dev.tensor_c128 && (k == 4 || k == 5); }
+// 2- and 3-qubit complex128 gates ride the 4-qubit tcgen05 kernel as U (x) I
+// on idle qubits: one HBM pass at the tensor path's speed instead of an
+// FP64-bound pass (8 2^k flops per amplitude at 1.2 TFLOP/s).
+bool tensor_dense_available(const Device &dev, int k) {
+  return dev.dbl && dev.tensor_c128 && (k == 4 || k == 5 || ((k == 2 || k == 3) && tc_dense_available(dev, 4)));
+}
 
 void launch_dense_tensor(Device &dev, const reg_t &qubits, const cd *mat) {
-  if (tc_dense_available(dev, (int)qubits.size()))
+  const int k = (int)qubits.size();
+  if (k < 4) {
+    // extra targets: the highest qubits not acted on (index bits k..3)
+    reg_t q = qubits;
+    for (int b = dev.n - 1; (int)q.size() < 4; --b)
+      if (std::find(qubits.begin(), qubits.end(), (uint64_t)b) == qubits.end()) q.push_back((uint64_t)b);
+    const int d = 1 << k;
+    std::vector<cd> u(256, cd(0.0, 0.0));
+    for (int i = 0; i < 16; ++i)
+      for (int j = 0; j < 16; ++j)
+        if ((i >> k) == (j >> k)) u[i + 16 * j] = mat[(i & (d - 1)) + (size_t)d * (j & (d - 1))];
+    launch_dense_tc(dev, q, u.data());
+    return;
+  }
+  if (tc_dense_available(dev, k))
     launch_dense_tc(dev, qubits, mat);
   else if (qubits.size() == 4)
     dense_oz<4>(dev, qubits, mat);

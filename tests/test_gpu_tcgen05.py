@@ -113,3 +113,19 @@ def test_tensor_mode_argument_checked():
     with P.QubitVector(11) as qv:
         with pytest.raises(Exception):
             qv.set_tensor_c128(3)
+
+
+@pytest.mark.parametrize("n,k", [(12, 2), (12, 3), (17, 2), (17, 3)])
+def test_small_dense_gates_padded_onto_tcgen05(n, k):
+    """complex128 2- and 3-qubit dense gates run as U (x) I on idle qubits
+    through the 4-qubit kernel: same results as the oracle, including gates
+    on the highest qubits (the padding then picks lower idle qubits)."""
+    P = pkg()
+    rng = np.random.default_rng(700 + 10 * n + k)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    placements = [list(range(n - k, n)), list(range(k)), [n - 1] + list(range(k - 1))]
+    placements += [[int(x) for x in rng.choice(n, k, replace=False)] for _ in range(5)]
+    ops = [(q, haar(rng, 1 << k)) for q in placements]
+    got = run(P, n, psi, ops, 1)
+    np.testing.assert_allclose(got, oracle(n, psi, ops), atol=1e-12, rtol=0)
