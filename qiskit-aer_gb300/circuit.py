@@ -24,6 +24,10 @@ class Instruction:
     params: list = field(default_factory=list)
     data: object = None            # matrix / diagonal / kraus list / save payload
     clbits: list = field(default_factory=list)
+    # classical condition (clbits, value): applied only when the memory bits
+    # clbits[i] equal bit i of value (Operations::Op conditional, checked by
+    # ClassicalRegister::check_conditional before each op)
+    condition: tuple | None = None
 
 
 class QuantumCircuit:
@@ -72,6 +76,33 @@ class QuantumCircuit:
 
     def measure_all(self):
         return self.measure(list(range(self.num_qubits)), list(range(self.num_qubits)))
+
+    def c_if(self, clbits, value: int):
+        """Condition the last instruction on classical bits (qiskit's c_if on
+        a register made of `clbits`, least significant first)."""
+        clbits = [clbits] if np.isscalar(clbits) else clbits
+        if not self.data:
+            raise ValueError("c_if needs an instruction to condition")
+        self.num_clbits = max(self.num_clbits, max(clbits) + 1)
+        self.data[-1].condition = ([int(c) for c in clbits], int(value))
+        return self
+
+    def needs_shots(self, method: str = "statevector") -> bool:
+        """True when measure sampling does not apply and every shot runs the
+        circuit (Executor::check_measure_sampling_opt): a measurement followed
+        by other ops, a classical condition, or, on a statevector, a reset or
+        a Kraus channel."""
+        seen_measure = False
+        for ins in self.data:
+            if ins.condition is not None:
+                return True
+            if ins.kind == "measure":
+                seen_measure = True
+            elif ins.kind not in ("save", "barrier") and seen_measure:
+                return True
+            if method == "statevector" and ins.kind in ("reset", "kraus"):
+                return True
+        return False
 
     def save_statevector(self, label="statevector"):
         self.data.append(Instruction("save", "statevector", [], data=label))

@@ -25,6 +25,20 @@ from .circuit import Instruction, NativeCircuit, QuantumCircuit
 from .qubitvector import DensityMatrix, QubitVector
 
 
+def discrete_draw(probs, u: float) -> int:
+    """RngEngine::rand_int(probs) (rng.hpp:94-96) given the uniform u that the
+    draw consumes: libstdc++'s std::discrete_distribution normalises the
+    weights by their sequential sum, takes sequential partial sums, sets the
+    last to 1 and returns lower_bound(cumulative, u), where u is the same
+    generate_canonical<double, 53> value that uniform_real_distribution(0, 1)
+    yields for the engine's next 64-bit word."""
+    p = np.asarray(probs, dtype=np.float64)
+    total = np.add.accumulate(p)[-1]
+    cp = np.add.accumulate(p / total)
+    cp[-1] = 1.0
+    return int(np.searchsorted(cp, u, side="left"))
+
+
 def uniforms(seed: int, count: int) -> np.ndarray:
     """RngEngine::rand(0,1) stream for `seed` (std::mt19937_64)."""
     out = np.empty(int(count), dtype=np.float64)
@@ -149,6 +163,8 @@ class AerSimulator:
         return Result(results, time.perf_counter() - t0)
 
     def _run_one(self, circuit: QuantumCircuit, shots: int, seed: int):
+        if self.method == "statevector" and circuit.needs_shots("statevector"):
+            return self._run_shots(circuit, shots, seed)
         segments, meas, saves, meta = self.compile(circuit)
         cls = DensityMatrix if self.method == "density_matrix" else QubitVector
         data = {}
@@ -171,6 +187,89 @@ class AerSimulator:
                 counts = self._counts(samples, qubits, clbits, circuit.num_clbits)
             st.synchronize()
         return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
+
+    def _run_shots(self, circuit: QuantumCircuit, shots: int, seed: int):
+        """A circuit that cannot be measure-sampled, one shot at a time
+        (CircuitExecutor::run_circuit_shots, circuit_executor.hpp:880-940):
+        shot i starts from |0...0> with RngEngine seed + i; unitary stretches
+        between measurements, resets and conditional ops are fused once and
+        executed per shot; measure and reset draw one outcome each
+        (State::sample_measure_with_prob) and collapse the state
+        (State::measure_reset_update, statevector_state.hpp:936-1011)."""
+        if self.noise_model is not None and not self.noise_model.is_ideal():
+            raise NotImplementedError("noise on a statevector needs per-shot noise sampling; use density_matrix")
+        cfg = self.fusion_config()
+        items, stretch = [], []
+
+        def flush():
+            if stretch:
+                nc = NativeCircuit(circuit.num_qubits, list(stretch))
+                nc.fuse(cfg)
+                items.append(("ops", nc, None))
+                stretch.clear()
+
+        for ins in circuit.data:
+            if ins.kind == "save":
+                raise NotImplementedError("save instructions in a circuit run shot by shot")
+            if ins.kind == "kraus":
+                raise NotImplementedError("Kraus channels on a statevector need per-shot noise sampling")
+            if ins.kind in ("measure", "reset"):
+                flush()
+                items.append((ins.kind, ins, ins.condition))
+            elif ins.condition is not None:
+                flush()
+                cond = Instruction(ins.kind, ins.name, ins.qubits, ins.params, ins.data, ins.clbits)
+                items.append(("ops", NativeCircuit(circuit.num_qubits, [cond]), ins.condition))
+            elif ins.kind != "barrier":
+                stretch.append(ins)
+        flush()
+        ndraw = sum(1 for kind, _, _ in items if kind in ("measure", "reset"))
+        counts: dict[str, int] = {}
+        with QubitVector(circuit.num_qubits, self.precision) as st:
+            for shot in range(shots):
+                u = uniforms(seed + shot, ndraw) if ndraw else np.empty(0)
+                used, memory = 0, 0
+                st.initialize()
+                for kind, obj, cond in items:
+                    if cond is not None:
+                        cbits, value = cond
+                        if any(((memory >> c) & 1) != ((value >> i) & 1) for i, c in enumerate(cbits)):
+                            continue
+                    if kind == "ops":
+                        A.check(st._L.gbqv_execute(st.handle, obj.handle), st.handle)
+                        continue
+                    qubits = obj.qubits
+                    probs = st.probabilities(qubits)
+                    outcome = discrete_draw(probs, u[used])
+                    used += 1
+                    self._collapse(st, qubits, outcome, outcome if kind == "measure" else 0, probs[outcome])
+                    if kind == "measure":
+                        for i, c in enumerate(obj.clbits):
+                            memory = (memory & ~(1 << c)) | (((outcome >> i) & 1) << c)
+                key = format(memory, f"0{circuit.num_clbits}b") if circuit.num_clbits else ""
+                counts[key] = counts.get(key, 0) + 1
+            st.synchronize()
+        return {"counts": counts if circuit.num_clbits else None, "data": {},
+                "metadata": {"fusion": {"enabled": bool(cfg.enable)}, "shot_branching": False,
+                             "measure_sampling": False},
+                "seed_simulator": seed, "shots": shots}
+
+    @staticmethod
+    def _collapse(st, qubits, meas_state: int, final_state: int, prob: float):
+        """measure_reset_update: project onto meas_state, renormalise by
+        1/sqrt(p), then move meas_state to final_state (X for one qubit, a
+        transposition for several)."""
+        dim = 1 << len(qubits)
+        diag = np.zeros(dim, dtype=complex)
+        diag[meas_state] = 1.0 / np.sqrt(prob)
+        st.apply_diagonal_matrix(qubits, diag)
+        if final_state != meas_state:
+            if len(qubits) == 1:
+                st.apply_mcx(qubits)
+            else:
+                perm = np.eye(dim, dtype=complex)
+                perm[[final_state, meas_state]] = perm[[meas_state, final_state]]
+                st.apply_matrix(qubits, perm)
 
     @staticmethod
     def _counts(samples, qubits, clbits, num_clbits):
