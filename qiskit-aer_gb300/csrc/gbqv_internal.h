@@ -49,6 +49,12 @@ struct Device {
   int blocking = 1;
   int tensor_c128 = 1;      // complex128 dense k = 4, 5: 0 FP64 cores, 1 tensor (tcgen05 for k = 4), 2 mma.sync only
   int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up
+  // tcgen05 kernel: 128-byte-swizzled TMA descriptors of the state viewed as
+  // rows of 8 amplitudes, box height 2^(L-3) for run length L = 7..11; built
+  // on first use, dropped when the state buffer changes
+  const void *tmap_state = nullptr;
+  unsigned tmap_ok = 0;  // bit L-7: tmap[L-7] is valid
+  alignas(128) unsigned char tmap[5][128];  // CUtensorMap storage (128-byte aligned)
   void *state = nullptr;
   void *ckpt = nullptr;
   cudaStream_t stream = nullptr;

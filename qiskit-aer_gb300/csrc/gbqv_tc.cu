@@ -31,6 +31,7 @@
 //
 // Shared-memory operands use the K-major no-swizzle layout: 8 rows x 16
 // bytes core matrices, 128 bytes apart along K, 512 bytes apart per 8 rows.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -64,7 +65,7 @@ constexpr int kOffBar = kOffKey + 2 * kTcGroups * 4;
 constexpr int kOffMisc = kOffBar + 16 * 8;
 // + alignment slack; at least 116 KB so that a second CTA never fits on an SM
 // (each CTA allocates all 512 TMEM columns)
-constexpr int kTcSmemUsed = kOffMisc + 64 + 128;
+constexpr int kTcSmemUsed = kOffMisc + 64 + 1024;
 constexpr int kTcSmem = kTcSmemUsed > 116 * 1024 ? kTcSmemUsed : 116 * 1024;
 // warps: 8 producers, 8 * EH epilogue warps (EH warpgroups per pipeline
 // lane, each taking 4 / EH of the 4 output chunks), 1 MMA issuer, 1 loader
@@ -78,6 +79,12 @@ constexpr uint32_t kTmemCols = 512;
 // amplitudes (one per combination of the targets >= L): at most 16 bulk
 // copies of >= 2 KB, whatever the target qubits.
 struct TcParams {
+  // swz = 1: the loader fetches each run with a 2D tiled TMA (rows of 8
+  // amplitudes) into the 128-byte swizzle layout (16-byte chunk index XOR row
+  // index mod 8), which spreads the producers' reads over all banks for any
+  // targets; swz = 0 (states of >= 34 qubits): 1D bulk copies, plain layout
+  CUtensorMap tmap;  // 128-byte aligned type
+  uint32_t swz;
   uint64_t offs[16];
   uint64_t lowmask[4];
   uint64_t hoff[16];      // amplitude offset of run r from the tile's first amplitude
@@ -113,7 +120,8 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     k_dense_tc4(double2 *psi, const __grid_constant__ TcParams p, const uint4 *__restrict__ gmat, int *status) {
   constexpr int kThreads = tc_threads<EH>(), kMmaWarp = 8 + 8 * EH, kChunks = 4 / EH;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned char *smem = smem_raw + ((128 - (tc::smem_u32(smem_raw) & 127)) & 127);
+  // 1024-byte alignment: the swizzle pattern is taken from address bits 4-9
+  unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   int *colkey = reinterpret_cast<int *>(smem + kOffKey);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kOffBar);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kOffMisc);
@@ -180,7 +188,10 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     // amplitudes sit at fixed offsets of each raw stage
     uint32_t ro[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) ro[j] = p.roff[8 * h + j] + 16u * p.zl[m];
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t off = p.roff[8 * h + j] + 16u * p.zl[m];
+      ro[j] = p.swz ? off ^ (((off >> 7) & 7u) << 4) : off;
+    }
     uint64_t tile = blockIdx.x;
     int slot = 0;
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i, slot = slot == kRawStages - 1 ? 0 : slot + 1) {
@@ -326,8 +337,13 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       const uint64_t first = insert_zeros_k4(tile * kTcGroups, p.lowmask);
       const uint32_t dst = tc::smem_u32(smem + kOffRaw + slot * kRawStage);
       tc::mbar_arrive_expect_tx(raw_full(slot), kRawStage);
-      for (uint32_t r = 0; r < p.nruns; ++r)
-        tc::bulk_g2s(dst + r * p.runbytes, psi + first + p.hoff[r], p.runbytes, raw_full(slot));
+      if (p.swz) {
+        for (uint32_t r = 0; r < p.nruns; ++r)
+          tc::tma_load_2d(dst + r * p.runbytes, &p.tmap, 0, (int)((first + p.hoff[r]) >> 3), raw_full(slot));
+      } else {
+        for (uint32_t r = 0; r < p.nruns; ++r)
+          tc::bulk_g2s(dst + r * p.runbytes, psi + first + p.hoff[r], p.runbytes, raw_full(slot));
+      }
       issued = i + 1;
     }
     // copies still in flight after an abort land before the CTA exits
@@ -422,6 +438,52 @@ void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint1
   }
 }
 
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled() {
+  static EncodeTiled fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(ptr);
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+// The swizzled descriptor for run length L, or false (1D bulk path) when the
+// state is too large for int32 row coordinates or encoding fails.
+bool tc_tensor_map(Device &dev, uint32_t L, CUtensorMap *out) {
+  if (dev.n >= 34 || L < 7 || L > 11) return false;
+  if (dev.tmap_state != dev.state) {
+    dev.tmap_ok = 0;
+    dev.tmap_state = dev.state;
+  }
+  const int i = (int)L - 7;
+  if (!(dev.tmap_ok >> i & 1u)) {
+    const EncodeTiled fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {16, (cuuint64_t)1 << (dev.n - 3)};
+    const cuuint64_t strides[1] = {128};
+    const cuuint32_t box[2] = {16, 1u << (L - 3)};
+    const cuuint32_t es[2] = {1, 1};
+    if (fn(reinterpret_cast<CUtensorMap *>(dev.tmap[i]), CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, dev.state, dims, strides,
+           box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+    dev.tmap_ok |= 1u << i;
+  }
+  std::memcpy(out, dev.tmap[i], sizeof(CUtensorMap));
+  return true;
+}
+
 int sm_count() {
   static int n = 0;
   if (!n) {
@@ -472,6 +534,9 @@ void launch_dense_tc(Device &dev, const reg_t &qubits, const cd *mat) {
   p.ngroups = dev.amps() >> 4;
   p.ntiles = (p.ngroups + kTcGroups - 1) / kTcGroups;
   tc_tile_geometry(qubits, p.hoff, p.roff, p.zl, p.nruns, p.runbytes);
+  uint32_t L = 0;
+  while ((16u << L) < p.runbytes) ++L;
+  p.swz = tc_tensor_map(dev, L, &p.tmap) ? 1u : 0u;
   std::vector<uint16_t> planes(kMatBytes / 2);
   int rowkey[kTcReals];
   tc_matrix4(mat, planes.data(), rowkey);

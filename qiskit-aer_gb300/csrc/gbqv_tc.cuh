@@ -144,6 +144,16 @@ __host__ __device__ __forceinline__ uint32_t idesc_bf16_f32(int m, int n) {
   return idesc_f16_f32(m, n) | (1u << 7) | (1u << 10);
 }
 
+// 2D tiled TMA load of box (x, y) of the tensor map at `tmap` (the address of
+// a __grid_constant__ kernel parameter) into shared memory at dst.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void *tmap, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(tmap), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
 // ---- packed half arithmetic ----
 __device__ __forceinline__ uint32_t hadd2(uint32_t a, uint32_t b) {
   uint32_t d;
