@@ -252,7 +252,8 @@ def bench_qv(args, torch, P):
     q4 = next((q for q, _ in fused if len(q) == 4), fused[0][0])
     dtype = "c128" if args.precision == "double" else "c64"
     traffic = NCU_TRAFFIC_26Q.get((dtype, len(q4)))
-    kname = {"c128": "k_dense_tc4 (tcgen05, exact digit slices)", "c64": "k_dense<float2, 4>"}[dtype]
+    kname = {"c128": "k_dense_tc4 (tcgen05, exact digit slices)",
+             "c64": "k_dense_tc4_c64 (tcgen05, 3xTF32 split precision)"}[dtype]
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4),
             "traffic": round(traffic * 2.0 ** (args.qubits - 26)) if traffic else None,

@@ -357,7 +357,10 @@ int gbqv_set_blocking(gbqv_handle h, int blocking);
  * <= ~1e-13 of (row max x group max) per gate (4-qubit gates on tcgen05 with
  * TMEM accumulators for states of >= 11 vector qubits, otherwise warp-level
  * mma.sync); 2: the same digit slices on mma.sync only; 0: native FP64 FMAs
- * (the reference's arithmetic, 1.2 TFLOP/s on GB300).  Other values return
+ * (the reference's arithmetic, 1.2 TFLOP/s on GB300).  On a complex64 state
+ * the same setting selects, for 4-qubit dense gates on >= 11 vector qubits,
+ * tcgen05 products in split precision (3xTF32, fp32 accumulation; value 1)
+ * or fp32 FMAs (0 or 2).  Other values return
  * GBQV_ERR_ARG.  A tcgen05 kernel whose bounded pipeline wait gave up makes
  * the next synchronising call return GBQV_ERR_TIMEOUT. */
 int gbqv_set_tensor_c128(gbqv_handle h, int enable);

@@ -179,6 +179,10 @@ void apply_matrix_impl(Device &dev, const reg_t &q, const cd *mat) {
     launch_dense_tensor(dev, q, mat);
     return;
   }
+  if (tc64_dense_available(dev, (int)q.size())) {
+    launch_dense_tc64(dev, q, mat);
+    return;
+  }
   launch_dense(dev, q, mat);
 }
 

@@ -122,6 +122,18 @@ void launch_dense_tensor(Device &dev, const reg_t &qubits, const cd *mat);
 bool tc_dense_available(const Device &dev, int k);
 void launch_dense_tc(Device &dev, const reg_t &qubits, const cd *mat);
 void tc_matrix4(const cd *mat, uint16_t *planes, int *rowkey);
+// Shared by the tcgen05 kernels (gbqv_tc.cu, gbqv_tc64.cu): tile run
+// geometry, the swizzled TMA descriptor of the state for run length L
+// (CUtensorMap, 128 bytes), the SM count.
+void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint16_t *zl, uint32_t &nruns,
+                      uint32_t &runbytes, uint32_t amp_bytes);
+bool tc_tensor_map(Device &dev, uint32_t L, void *out);
+bool tc_runs_map(Device &dev, const reg_t &qubits, uint32_t L, void *out, uint32_t &rank, uint32_t &nreq,
+                 uint32_t &row_step);
+int sm_count();
+// complex64 dense 4-qubit gates on tcgen05 (3xTF32, gbqv_tc64.cu)
+bool tc64_dense_available(const Device &dev, int k);
+void launch_dense_tc64(Device &dev, const reg_t &qubits, const cd *mat);
 // Device word that a bounded wait of a tcgen05 kernel sets when it gives up;
 // sync() turns it into GBQV_ERR_TIMEOUT.
 int *tc_status_word(Device &dev);

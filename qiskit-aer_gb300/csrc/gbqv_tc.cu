@@ -396,9 +396,14 @@ uint16_t half_bits(int32_t d) {
   return (uint16_t)(sg | ((e + 15) << 10) | mant);
 }
 
-// Run geometry of a tile for targets `qubits` (see TcParams).
+}  // namespace
+
+// Run geometry of a 128-group tile of a 4-qubit gate on targets `qubits`:
+// run offsets hoff[r] (amplitudes), byte offsets roff[j] of local amplitude j
+// of group 0 in the raw stage, zl[m] = amplitude index of group m inside its
+// run; amp_bytes = 16 (complex128) or 8 (complex64).
 void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint16_t *zl, uint32_t &nruns,
-                      uint32_t &runbytes) {
+                      uint32_t &runbytes, uint32_t amp_bytes) {
   reg_t sq = qubits;
   std::sort(sq.begin(), sq.end());
   uint32_t L = 7;
@@ -408,7 +413,7 @@ void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint1
   for (uint64_t q : sq)
     if (q >= L) high.push_back(q);
   nruns = 1u << high.size();
-  runbytes = 16u << L;
+  runbytes = amp_bytes << L;
   for (uint32_t r = 0; r < nruns; ++r) {
     uint64_t off = 0;
     for (size_t t = 0; t < high.size(); ++t)
@@ -428,9 +433,9 @@ void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint1
         r |= 1u << rank;
       }
     }
-    roff[j] = r * runbytes + (uint32_t)(lowpart * 16);
+    roff[j] = r * runbytes + (uint32_t)(lowpart * amp_bytes);
   }
-  for (uint32_t m = 0; m < (uint32_t)kTcGroups; ++m) {
+  for (uint32_t m = 0; m < 128u; ++m) {
     uint64_t g = m;
     for (uint64_t q : sq)
       if (q < L) g = ((g >> q) << (q + 1)) | (g & ((1ULL << q) - 1));
@@ -442,7 +447,7 @@ using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-EncodeTiled encode_tiled() {
+static EncodeTiled encode_tiled() {
   static EncodeTiled fn = nullptr;
   static bool tried = false;
   if (!tried) {
@@ -458,10 +463,12 @@ EncodeTiled encode_tiled() {
   return fn;
 }
 
-// The swizzled descriptor for run length L, or false (1D bulk path) when the
-// state is too large for int32 row coordinates or encoding fails.
-bool tc_tensor_map(Device &dev, uint32_t L, CUtensorMap *out) {
-  if (dev.n >= 34 || L < 7 || L > 11) return false;
+// The swizzled descriptor for run length L (the state as rows of 128 bytes,
+// box height = the run), or false (1D bulk path) when the state is too large
+// for int32 row coordinates or encoding fails.
+bool tc_tensor_map(Device &dev, uint32_t L, void *out) {
+  const uint32_t amp_log2 = dev.dbl ? 4 : 3, row_amps_log2 = 7 - amp_log2;
+  if ((uint32_t)dev.n - row_amps_log2 >= 31 || L < 7 || L > 11) return false;
   if (dev.tmap_state != dev.state) {
     dev.tmap_ok = 0;
     dev.tmap_state = dev.state;
@@ -470,9 +477,9 @@ bool tc_tensor_map(Device &dev, uint32_t L, CUtensorMap *out) {
   if (!(dev.tmap_ok >> i & 1u)) {
     const EncodeTiled fn = encode_tiled();
     if (!fn) return false;
-    const cuuint64_t dims[2] = {16, (cuuint64_t)1 << (dev.n - 3)};
+    const cuuint64_t dims[2] = {16, (cuuint64_t)1 << (dev.n - row_amps_log2)};
     const cuuint64_t strides[1] = {128};
-    const cuuint32_t box[2] = {16, 1u << (L - 3)};
+    const cuuint32_t box[2] = {16, 1u << (L - row_amps_log2)};
     const cuuint32_t es[2] = {1, 1};
     if (fn(reinterpret_cast<CUtensorMap *>(dev.tmap[i]), CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, dev.state, dims, strides,
            box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -480,8 +487,39 @@ bool tc_tensor_map(Device &dev, uint32_t L, CUtensorMap *out) {
       return false;
     dev.tmap_ok |= 1u << i;
   }
-  std::memcpy(out, dev.tmap[i], sizeof(CUtensorMap));
+  std::memcpy(out, dev.tmap[i], 128);
   return true;
+}
+
+// A descriptor that fetches several runs of a tile in one request: the state
+// as rows of 128 bytes (dims 0, 1) plus one dimension of size 2 and stride
+// 2^q amplitudes for each of the first (up to three) targets q >= L, box
+// height = the run.  Up to three high targets take one request per tile; a
+// fourth takes a second request, `row_step` rows further and 8 runs further
+// in shared memory.  Same shared-memory layout as one request per run (run r
+// = bits of r over the high targets, ascending).  False: use the per-run path.
+bool tc_runs_map(Device &dev, const reg_t &qubits, uint32_t L, void *out, uint32_t &rank, uint32_t &nreq,
+                 uint32_t &row_step) {
+  const uint32_t amp_log2 = dev.dbl ? 4 : 3, row_amps_log2 = 7 - amp_log2;
+  if ((uint32_t)dev.n - row_amps_log2 >= 31 || L < 7 || L > 11) return false;
+  const EncodeTiled fn = encode_tiled();
+  if (!fn) return false;
+  reg_t high;
+  for (uint64_t q : qubits)
+    if (q >= L) high.push_back(q);
+  std::sort(high.begin(), high.end());
+  const uint32_t nd = (uint32_t)std::min<size_t>(high.size(), 3);
+  rank = 2 + nd;
+  nreq = high.size() == 4 ? 2 : 1;
+  row_step = high.size() == 4 ? (uint32_t)(1ULL << (high[3] - row_amps_log2)) : 0;
+  cuuint64_t dims[5] = {16, (cuuint64_t)1 << (dev.n - row_amps_log2), 2, 2, 2};
+  cuuint64_t strides[4] = {128, 0, 0, 0};
+  cuuint32_t box[5] = {16, 1u << (L - row_amps_log2), 2, 2, 2};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  for (uint32_t t = 0; t < nd; ++t) strides[1 + t] = (cuuint64_t)1 << (high[t] + amp_log2);
+  return fn(reinterpret_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_UINT64, rank, dev.state, dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 int sm_count() {
@@ -493,8 +531,6 @@ int sm_count() {
   }
   return n;
 }
-
-}  // namespace
 
 // Host: six fp16 digit planes of the real form of a 16x16 column-major
 // complex matrix, rows ordered (amplitude j, re/im) -> 2j + c and columns
@@ -533,7 +569,7 @@ void launch_dense_tc(Device &dev, const reg_t &qubits, const cd *mat) {
   sorted_masks(qubits, p.lowmask);
   p.ngroups = dev.amps() >> 4;
   p.ntiles = (p.ngroups + kTcGroups - 1) / kTcGroups;
-  tc_tile_geometry(qubits, p.hoff, p.roff, p.zl, p.nruns, p.runbytes);
+  tc_tile_geometry(qubits, p.hoff, p.roff, p.zl, p.nruns, p.runbytes, 16);
   uint32_t L = 0;
   while ((16u << L) < p.runbytes) ++L;
   p.swz = tc_tensor_map(dev, L, &p.tmap) ? 1u : 0u;

@@ -154,6 +154,29 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const void *tmap, int 
       : "memory");
 }
 
+// The same with 3 to 5 dimensions (coordinates beyond y are 0).
+template <int N>
+__device__ __forceinline__ void tma_load_nd(uint32_t dst, const void *tmap, int y, uint32_t bar) {
+  if constexpr (N == 3)
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst),
+        "l"(tmap), "r"(0), "r"(y), "r"(0), "r"(bar)
+        : "memory");
+  else if constexpr (N == 4)
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(tmap), "r"(0), "r"(y), "r"(0), "r"(0), "r"(bar)
+        : "memory");
+  else
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(dst),
+        "l"(tmap), "r"(0), "r"(y), "r"(0), "r"(0), "r"(0), "r"(bar)
+        : "memory");
+}
+
 // ---- packed half arithmetic ----
 __device__ __forceinline__ uint32_t hadd2(uint32_t a, uint32_t b) {
   uint32_t d;
