@@ -197,8 +197,8 @@ def run_reference_arm(args):
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from
 # `ncu --set full` captures on a 26-qubit state (profiles/k_dense_tc4_c128_26q.md,
-# profiles/k_dense_c64_k4_26q.md), scaled to 2^qubits amplitudes.
-NCU_TRAFFIC_26Q = {("c128", 4): 2.0863e9, ("c64", 4): 1.0117e9}
+# profiles/k_dense_tc4_c64_26q.md), scaled to 2^qubits amplitudes.
+NCU_TRAFFIC_26Q = {("c128", 4): 2.0923e9, ("c64", 4): 1.0134e9}
 
 
 def bench_qv(args, torch, P):
