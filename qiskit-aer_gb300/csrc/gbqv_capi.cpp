@@ -347,7 +347,11 @@ extern "C" int gbqv_initialize(gbqv_handle h) {
 }
 
 namespace {
-constexpr uint64_t kChunk = 1ULL << 22;
+// complex64 states move through a device staging slice of kChunk complex128
+// values (256 MB): copy engine for the host <-> device leg, a kernel for the
+// precision change.  One stream orders each copy after the kernel that used
+// the slice before it.
+constexpr uint64_t kChunk = 1ULL << 24;
 
 void upload(Device &d, const cd *src, uint64_t offset, uint64_t count) {
   if (d.dbl) {
@@ -356,14 +360,11 @@ void upload(Device &d, const cd *src, uint64_t offset, uint64_t count) {
                "state upload");
     return;
   }
-  std::vector<std::complex<float>> tmp(std::min(count, kChunk));
+  void *stage = grow(d.aux2, d.aux2_cap, std::min(count, kChunk) * sizeof(cd));
   for (uint64_t o = 0; o < count; o += kChunk) {
     const uint64_t c = std::min(kChunk, count - o);
-    for (uint64_t i = 0; i < c; ++i) tmp[i] = std::complex<float>((float)src[o + i].real(), (float)src[o + i].imag());
-    cuda_check(cudaMemcpyAsync(reinterpret_cast<std::complex<float> *>(d.state) + offset + o, tmp.data(),
-                               c * sizeof(std::complex<float>), cudaMemcpyHostToDevice, d.stream),
-               "state upload");
-    sync(d);
+    cuda_check(cudaMemcpyAsync(stage, src + o, c * sizeof(cd), cudaMemcpyHostToDevice, d.stream), "state upload");
+    launch_narrow(d, stage, offset + o, c);
   }
 }
 }  // namespace
@@ -405,18 +406,13 @@ extern "C" int gbqv_copy_to_host(gbqv_handle h, gbqv_c128 *out, uint64_t len) {
       sync(d);
       return;
     }
-    std::vector<std::complex<float>> tmp(std::min(len, kChunk));
+    void *stage = grow(d.aux2, d.aux2_cap, std::min(len, kChunk) * sizeof(cd));
     for (uint64_t o = 0; o < len; o += kChunk) {
       const uint64_t c = std::min(kChunk, len - o);
-      cuda_check(cudaMemcpyAsync(tmp.data(), reinterpret_cast<std::complex<float> *>(d.state) + o,
-                                 c * sizeof(std::complex<float>), cudaMemcpyDeviceToHost, d.stream),
-                 "state download");
-      sync(d);
-      for (uint64_t i = 0; i < c; ++i) {
-        out[o + i].re = tmp[i].real();
-        out[o + i].im = tmp[i].imag();
-      }
+      launch_widen(d, o, c, stage);
+      cuda_check(cudaMemcpyAsync(out + o, stage, c * sizeof(cd), cudaMemcpyDeviceToHost, d.stream), "state download");
     }
+    sync(d);
   });
 }
 

@@ -85,6 +85,10 @@ void launch_pauli(Device &dev, uint64_t x_mask, uint64_t z_mask, uint64_t x_max,
 void launch_dm_y(Device &dev, uint64_t q);
 void launch_scale(Device &dev, cd s);
 void launch_set_basis(Device &dev, uint64_t index, cd value); // zero + one entry
+// complex64 states: state[offset, +count) <- narrow(src) / dst <- widen(state[offset, +count));
+// src and dst are device buffers of complex128
+void launch_narrow(Device &dev, const void *src, uint64_t offset, uint64_t count);
+void launch_widen(Device &dev, uint64_t offset, uint64_t count, void *dst);
 
 // Reductions: write results into dev.results[0..count) (device), async.
 void reduce_norm(Device &dev);                                   // 1 value

@@ -490,6 +490,25 @@ __global__ void k_set_basis(T *__restrict__ psi, uint64_t index, T value, uint64
   }
 }
 
+// complex128 <-> complex64 copies between a staging slice and the state, so
+// that a complex64 state is filled from (and read back to) the ABI's
+// complex128 host vectors at HBM speed.  Narrowing rounds to nearest, the
+// same value as a C++ double -> float conversion on the host.
+__global__ void k_narrow(const double2 *__restrict__ src, float2 *__restrict__ dst, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const double2 v = src[i];
+    dst[i] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
+  }
+}
+__global__ void k_widen(const float2 *__restrict__ src, double2 *__restrict__ dst, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const float2 v = src[i];
+    dst[i] = make_double2(v.x, v.y);
+  }
+}
+
 // -------------------------------------------------------------------------
 // Reductions
 // -------------------------------------------------------------------------
@@ -875,6 +894,18 @@ void launch_set_basis(Device &dev, uint64_t index, cd value) {
   else
     k_set_basis<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), index, to_dev<float2>(value), dev.amps());
   check_launch("initialize kernel");
+}
+
+void launch_narrow(Device &dev, const void *src, uint64_t offset, uint64_t count) {
+  k_narrow<<<grid_for(count, 256), 256, 0, dev.stream>>>(static_cast<const double2 *>(src),
+                                                          st<float2>(dev) + offset, count);
+  check_launch("state narrowing kernel");
+}
+
+void launch_widen(Device &dev, uint64_t offset, uint64_t count, void *dst) {
+  k_widen<<<grid_for(count, 256), 256, 0, dev.stream>>>(st<float2>(dev) + offset, static_cast<double2 *>(dst),
+                                                         count);
+  check_launch("state widening kernel");
 }
 
 void reduce_norm(Device &dev) {
