@@ -305,6 +305,37 @@ int gbqv_circuit_fuse(gbqv_circuit_t c, const gbqv_fusion_config *cfg, int *appl
  * scheduled into cache-blocked passes over HBM. */
 int gbqv_execute(gbqv_handle h, gbqv_circuit_t c);
 
+/* ------------------------------------------------------------------ */
+/* Runtime parameter binding: one circuit, many parameter sets            */
+/* ------------------------------------------------------------------ */
+/* Gives parameter param_pos of gate op_index one value per binding: the
+ * "parameterizations" table that Controller::execute expands with
+ * runtime_parameter_bind_enable (src/controllers/controller_execute.hpp:
+ * 104-131; the Python side builds it in qiskit_aer/backends/aerbackend.py:
+ * 96-144).  Every call on a circuit passes the same nbind; values[j] is
+ * binding j's value.  Out-of-range positions are GBQV_ERR_ARG with the
+ * reference's messages.  Bound gates are left out of Fusion. */
+int gbqv_circuit_bind_param(gbqv_circuit_t c, int op_index, int param_pos, int nbind, const double *values);
+int gbqv_circuit_num_bindings(gbqv_circuit_t c, int *out);
+
+/* Runs bindings [first, first + count) of a bound circuit of n qubits at
+ * once, the work the batched-shots executor does for parameter bindings on
+ * a GPU (src/simulators/batch_shots_executor.hpp:152-314, ops converted by
+ * transpile/batch_converter.hpp:54-200).  h holds a stack of 2^b states of n
+ * qubits (h has n + b qubits, 2^b >= count): state j, amplitudes
+ * [j 2^n, (j + 1) 2^n), starts in |0...0> and ends as binding first + j
+ * applied to it; states j >= count are zero.  Gates with bound parameters
+ * run as per-binding matrices inside cache-blocked passes.  The circuit must
+ * be unitary (gates, unitary, diagonal, barrier): GBQV_ERR_KIND otherwise. */
+int gbqv_execute_bound(gbqv_handle h, gbqv_circuit_t c, uint64_t first, uint64_t count);
+
+/* <P_t> on each of the first nseg states of such a stack (states of
+ * 2^state_qubits amplitudes, terms on qubits below state_qubits, laid out as
+ * in gbqv_expval_pauli_many): out[t * nseg + s] = <psi_s|P_t|psi_s>
+ * (QubitVector::expval_pauli per state, qubitvector.hpp:2299-2347). */
+int gbqv_expval_pauli_segments(gbqv_handle h, int state_qubits, uint64_t nseg, int nterms, const uint64_t *qubits,
+                               const int *offsets, const char *const *labels, double *out);
+
 /* Adjoint-method gradient of E(theta) = <psi(theta)|H|psi(theta)>, psi =
  * c applied to |0...0>.  No counterpart in the reference (Aer has no gradient
  * code); it extends the statevector surface for the torch.autograd wrapper.

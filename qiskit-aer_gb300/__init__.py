@@ -12,15 +12,17 @@ Package layout:
   adjoint.py      adjoint-method gradients behind torch.autograd
 """
 from ._capi import GBQVError, lib
-from .circuit import NativeCircuit, QuantumCircuit
+from .circuit import NativeCircuit, Parameter, ParameterExpression, QuantumCircuit
 from .noise import (NoiseModel, QuantumError, amplitude_damping_error, depolarizing_error,
                     phase_amplitude_damping_error)
 from .qubitvector import DensityMatrix, QubitVector
 from .simulator import AerSimulator, Result, uniforms
 from . import adjoint, batched
+from .primitives import EstimatorV2
 
 __all__ = [
-    "AerSimulator", "adjoint", "batched", "DensityMatrix", "GBQVError", "NativeCircuit", "NoiseModel", "QuantumCircuit",
+    "AerSimulator", "adjoint", "batched", "DensityMatrix", "EstimatorV2", "GBQVError", "NativeCircuit", "NoiseModel",
+    "Parameter", "ParameterExpression", "QuantumCircuit",
     "QuantumError", "QubitVector", "Result", "amplitude_damping_error", "depolarizing_error", "lib",
     "phase_amplitude_damping_error", "uniforms",
 ]

@@ -112,6 +112,11 @@ _SIGS = {
     "gbqv_fusion_default_config": (C.c_int, [C.c_int, C.POINTER(FusionConfig)]),
     "gbqv_circuit_fuse": (C.c_int, [H, C.POINTER(FusionConfig), C.POINTER(C.c_int), C.c_char_p, C.c_int]),
     "gbqv_execute": (C.c_int, [H, H]),
+    "gbqv_circuit_bind_param": (C.c_int, [H, C.c_int, C.c_int, C.c_int, dp]),
+    "gbqv_circuit_num_bindings": (C.c_int, [H, C.POINTER(C.c_int)]),
+    "gbqv_execute_bound": (C.c_int, [H, H, C.c_uint64, C.c_uint64]),
+    "gbqv_expval_pauli_segments": (C.c_int, [H, C.c_int, C.c_uint64, C.c_int, u64p, C.POINTER(C.c_int),
+                                             C.POINTER(C.c_char_p), dp]),
     "gbqv_set_blocking": (C.c_int, [H, C.c_int]),
     "gbqv_set_tensor_c128": (C.c_int, [H, C.c_int]),
     "gbqv_batch_create": (C.c_int, [C.c_int, C.POINTER(H)]),

@@ -16,6 +16,120 @@ import numpy as np
 from . import _capi as A
 
 
+class ParameterExpression:
+    """A real affine expression c0 + sum_p c_p * p over Parameters: the part of
+    qiskit's ParameterExpression that parameter binding uses (the Python side
+    of the reference evaluates each bound expression per binding,
+    qiskit_aer/backends/aerbackend.py:96-126)."""
+
+    __slots__ = ("_terms", "_const")
+
+    def __init__(self, terms=None, const: float = 0.0):
+        self._terms = dict(terms or {})
+        self._const = float(const)
+
+    @property
+    def parameters(self) -> set:
+        return {p for p, c in self._terms.items() if c != 0.0}
+
+    @staticmethod
+    def _coerce(x) -> "ParameterExpression":
+        if isinstance(x, ParameterExpression):
+            return x
+        if np.ndim(x) != 0 or np.iscomplexobj(x):
+            raise TypeError(f"cannot combine a parameter with {x!r}")
+        return ParameterExpression({}, float(x))
+
+    def _combine(self, other, sign: float) -> "ParameterExpression":
+        o = self._coerce(other)
+        terms = dict(self._terms)
+        for p, c in o._terms.items():
+            terms[p] = terms.get(p, 0.0) + sign * c
+        return ParameterExpression(terms, self._const + sign * o._const)
+
+    def _scale(self, k) -> "ParameterExpression":
+        if isinstance(k, ParameterExpression):
+            if k.parameters and self.parameters:
+                raise TypeError("only affine parameter expressions are supported")
+            if k.parameters:
+                return k._scale(self._const)
+            k = k._const
+        k = float(k)
+        return ParameterExpression({p: c * k for p, c in self._terms.items()}, self._const * k)
+
+    def __add__(self, o): return self._combine(o, 1.0)
+    def __radd__(self, o): return self._combine(o, 1.0)
+    def __sub__(self, o): return self._combine(o, -1.0)
+    def __rsub__(self, o): return self._coerce(o)._combine(self, -1.0)
+    def __mul__(self, k): return self._scale(k)
+    def __rmul__(self, k): return self._scale(k)
+    def __truediv__(self, k): return self._scale(1.0 / float(k))
+    def __neg__(self): return self._scale(-1.0)
+    def __pos__(self): return self
+
+    def bind(self, values: dict) -> "ParameterExpression | float":
+        """Substitute the parameters found in `values`; a float once none is left."""
+        terms, const = {}, self._const
+        for p, c in self._terms.items():
+            if p in values:
+                const += c * float(values[p])
+            else:
+                terms[p] = c
+        return ParameterExpression(terms, const) if any(c != 0.0 for c in terms.values()) else const
+
+    def evaluate(self, binds: dict) -> np.ndarray:
+        """Values of the expression for every binding: binds maps each of its
+        parameters to an array of values (one per binding)."""
+        out = None
+        for p, c in self._terms.items():
+            if c == 0.0:
+                continue
+            if p not in binds:
+                raise ValueError(f"no values bound to parameter '{p.name}'")
+            v = c * np.asarray(binds[p], dtype=np.float64)
+            out = v if out is None else out + v
+        if out is None:
+            raise ValueError("the expression has no parameter")
+        return out + self._const
+
+    def __float__(self):
+        if self.parameters:
+            raise TypeError(f"unbound parameters: {sorted(p.name for p in self.parameters)}")
+        return self._const
+
+    def __repr__(self):
+        parts = [f"{c:g}*{p.name}" for p, c in self._terms.items() if c != 0.0]
+        if self._const or not parts:
+            parts.append(f"{self._const:g}")
+        return " + ".join(parts)
+
+
+class Parameter(ParameterExpression):
+    """A named circuit parameter (qiskit.circuit.Parameter); identity-hashed."""
+
+    __slots__ = ("name",)
+
+    def __init__(self, name: str):
+        super().__init__({}, 0.0)
+        self.name = str(name)
+        self._terms[self] = 1.0
+
+    __hash__ = object.__hash__
+
+    def __eq__(self, other):
+        return self is other
+
+    def __repr__(self):
+        return f"Parameter({self.name})"
+
+
+def _param(x):
+    """A gate parameter as stored: a float, or an expression with parameters."""
+    if isinstance(x, ParameterExpression):
+        return x if x.parameters else float(x)
+    return float(x)
+
+
 @dataclass
 class Instruction:
     kind: str                      # "gate" | "unitary" | "diagonal" | "superop" | "kraus" | "reset" | "barrier" | "measure" | "save"
@@ -31,16 +145,53 @@ class Instruction:
 
 
 class QuantumCircuit:
-    def __init__(self, num_qubits: int, num_clbits: int = 0, name: str = "circuit"):
+    def __init__(self, num_qubits: int, num_clbits: int = 0, name: str = "circuit", metadata: dict | None = None):
         self.num_qubits = int(num_qubits)
         self.num_clbits = int(num_clbits)
         self.name = name
+        self.metadata = dict(metadata or {})
         self.data: list[Instruction] = []
 
     # ---- generic ----
     def append_gate(self, name: str, qubits, params=()):
-        self.data.append(Instruction("gate", name, [int(q) for q in qubits], [float(p) for p in params]))
+        self.data.append(Instruction("gate", name, [int(q) for q in qubits], [_param(p) for p in params]))
         return self
+
+    # ---- parameters ----
+    @property
+    def parameters(self) -> list:
+        """The circuit's unbound parameters, sorted by name (qiskit's order)."""
+        found = {}
+        for ins in self.data:
+            for p in ins.params:
+                if isinstance(p, ParameterExpression):
+                    for q in p.parameters:
+                        found[id(q)] = q
+        return sorted(found.values(), key=lambda q: q.name)
+
+    @property
+    def num_parameters(self) -> int:
+        return len(self.parameters)
+
+    def copy(self) -> "QuantumCircuit":
+        out = QuantumCircuit(self.num_qubits, self.num_clbits, self.name, self.metadata)
+        out.data = [Instruction(i.kind, i.name, list(i.qubits), list(i.params), i.data, list(i.clbits), i.condition)
+                    for i in self.data]
+        return out
+
+    def assign_parameters(self, values) -> "QuantumCircuit":
+        """A copy with parameters replaced: values is a dict {Parameter: value}
+        or a sequence in the order of `parameters`."""
+        if not isinstance(values, dict):
+            params = self.parameters
+            values = list(values)
+            if len(values) != len(params):
+                raise ValueError(f"{len(values)} values for {len(params)} parameters")
+            values = dict(zip(params, values))
+        out = self.copy()
+        for ins in out.data:
+            ins.params = [p.bind(values) if isinstance(p, ParameterExpression) else p for p in ins.params]
+        return out
 
     def unitary(self, mat, qubits, label="unitary"):
         self.data.append(Instruction("unitary", label, [int(q) for q in qubits], data=np.asarray(mat, dtype=complex)))
@@ -176,8 +327,19 @@ class NativeCircuit:
         A.check(self._L.gbqv_circuit_create(int(num_qubits), C.byref(h)))
         self._h = h
         self.num_qubits = num_qubits
+        self.param_slots = []  # (op index, parameter position, expression)
         for ins in instructions:
             self.add(ins)
+
+    def bind(self, binds: dict, nbind: int) -> None:
+        """Runtime parameter binding (gbqv_circuit_bind_param): every
+        parameterised gate parameter gets its value for each of the nbind
+        bindings; binds maps each Parameter to nbind values."""
+        for op_index, pos, expr in self.param_slots:
+            v = np.ascontiguousarray(np.broadcast_to(expr.evaluate(binds), (nbind,)), dtype=np.float64)
+            if v.shape != (nbind,):
+                raise ValueError("every parameter needs one value per binding")
+            A.check(self._L.gbqv_circuit_bind_param(self._h, op_index, pos, nbind, v.ctypes.data_as(A.dp)))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -198,7 +360,15 @@ class NativeCircuit:
         q, qp, k = A.qubits_arg(ins.qubits)
         L = self._L
         if ins.kind == "gate":
-            pa = np.ascontiguousarray(np.asarray(ins.params, dtype=np.float64))
+            vals = []
+            for pos, p in enumerate(ins.params):
+                if isinstance(p, ParameterExpression):
+                    # placeholder until bind(): the op's index is the current op count
+                    self.param_slots.append((self.num_ops(), pos, p))
+                    vals.append(0.0)
+                else:
+                    vals.append(float(p))
+            pa = np.ascontiguousarray(np.asarray(vals, dtype=np.float64))
             A.check(L.gbqv_circuit_gate(self._h, ins.name.encode(), qp, k, pa.ctypes.data_as(A.dp), pa.size))
         elif ins.kind == "unitary":
             m, mp = A.cmat_arg(ins.data)

@@ -692,6 +692,31 @@ extern "C" int gbqv_expval_pauli_many(gbqv_handle h, int nterms, const uint64_t 
   });
 }
 
+extern "C" int gbqv_expval_pauli_segments(gbqv_handle h, int state_qubits, uint64_t nseg, int nterms,
+                                          const uint64_t *qubits, const int *offsets, const char *const *labels,
+                                          double *out) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    REQUIRE(!d.density, GBQV_ERR_KIND, "expval_pauli_segments: statevector stacks only");
+    REQUIRE(nterms >= 0 && offsets && labels && out, GBQV_ERR_ARG, "bad term arrays");
+    REQUIRE(state_qubits >= 1 && state_qubits <= d.n && nseg >= 1 && nseg <= (d.amps() >> state_qubits),
+            GBQV_ERR_ARG, "expval_pauli_segments: the states do not fit the handle's vector");
+    // keep one launch's partial sums bounded: terms x states per launch
+    const uint64_t per_launch = std::max<uint64_t>(1, (1ULL << 22) / nseg);
+    const int step = (int)std::min<uint64_t>((uint64_t)kMaxTerms, per_launch);
+    std::vector<double> vals;
+    for (int t0 = 0; t0 < nterms; t0 += step) {
+      const int cnt = std::min(step, nterms - t0);
+      std::vector<PauliTerm> terms = make_terms(d, cnt, qubits, offsets + t0, labels + t0, state_qubits);
+      reduce_expval_segments(d, terms, state_qubits, nseg);
+      vals.resize((size_t)cnt * nseg);
+      read_results(d, vals.data(), vals.size());
+      std::copy(vals.begin(), vals.end(), out + (size_t)t0 * nseg);
+    }
+  });
+}
+
 // ============================== density matrix ==============================
 
 namespace gbqv {

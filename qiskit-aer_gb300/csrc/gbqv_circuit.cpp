@@ -29,11 +29,16 @@ struct Op {
   std::vector<double> params;
   std::vector<cd> mat;                 // MATRIX 4^k, DIAGONAL 2^k, SUPEROP 16^k (column-major)
   std::vector<std::vector<cd>> kraus;  // KRAUS
+  // Runtime parameter binding (controller_execute.hpp:104-131): binding j's
+  // parameters at [j * params.size(), (j + 1) * params.size()); empty when
+  // every binding uses `params` (which then hold binding 0's values).
+  std::vector<double> bparams;
 };
 }  // namespace
 
 struct gbqv_circuit {
   int num_qubits = 0;
+  int nbind = 0;  // number of parameter bindings (0: none)
   std::vector<Op> ops;
 };
 
@@ -286,6 +291,9 @@ struct Fusion {
     }
   }
   bool can_apply(const Op &op, uint64_t maxq) const {
+    // gates with bound parameters stay unfused: they run as per-binding
+    // members of cache-blocked runs (execute_bound)
+    if (!op.bparams.empty()) return false;
     if (method == FMethod::UNITARY) return unitary_can_apply(op, maxq);
     switch (op.type) {
       case GBQV_OP_KRAUS:
@@ -751,6 +759,38 @@ extern "C" int gbqv_circuit_op_matrix(gbqv_circuit_t c, int i, gbqv_c128 *out, u
   });
 }
 
+extern "C" int gbqv_circuit_bind_param(gbqv_circuit_t c, int op_index, int param_pos, int nbind,
+                                       const double *values) {
+  return guard([&] {
+    REQUIRE(c && values, GBQV_ERR_ARG, "null argument");
+    REQUIRE(nbind >= 1, GBQV_ERR_ARG, "Invalid parameterization: no parameter values");
+    REQUIRE(c->nbind == 0 || c->nbind == nbind, GBQV_ERR_ARG,
+            "Invalid parameterization: every parameter needs the same number of values (" +
+                std::to_string(c->nbind) + ")");
+    REQUIRE(op_index >= 0 && op_index < (int)c->ops.size(), GBQV_ERR_ARG,
+            "Invalid parameterized qobj: instruction position out of range");
+    Op &op = c->ops[op_index];
+    REQUIRE(op.type == GBQV_OP_GATE, GBQV_ERR_ARG, "Invalid parameterized qobj: only gate parameters can be bound");
+    REQUIRE(param_pos >= 0 && param_pos < (int)op.params.size(), GBQV_ERR_ARG,
+            "Invalid parameterized qobj: instruction param position out of range");
+    const size_t stride = op.params.size();
+    if (op.bparams.empty()) {
+      op.bparams.resize(stride * nbind);
+      for (int j = 0; j < nbind; ++j) std::copy(op.params.begin(), op.params.end(), op.bparams.begin() + j * stride);
+    }
+    for (int j = 0; j < nbind; ++j) op.bparams[param_pos + stride * j] = values[j];
+    op.params[param_pos] = values[0];
+    c->nbind = nbind;
+  });
+}
+
+extern "C" int gbqv_circuit_num_bindings(gbqv_circuit_t c, int *out) {
+  return guard([&] {
+    REQUIRE(c && out, GBQV_ERR_ARG, "null argument");
+    *out = c->nbind;
+  });
+}
+
 extern "C" int gbqv_fusion_default_config(int method, gbqv_fusion_config *cfg) {
   return guard([&] {
     REQUIRE(cfg && (method == 0 || method == 1), GBQV_ERR_ARG, "bad fusion method");
@@ -1030,12 +1070,16 @@ bool worth_batching(const Device &d, const RunOp &r) {
 // Greedy cache-blocking schedule: starting from the first pending op, take
 // every later op that (a) touches no qubit of an op left behind (so moving
 // it earlier commutes) and (b) keeps the union of qubits within one tile.
-void execute_blocked(Device &d, const std::vector<Op> &ops) {
-  const int m = run_tile_qubits(d), c = run_low_qubits(d);
-  const size_t pool_cap = run_pool_bytes(d) / 16;
-  std::vector<RunOp> conv(ops.size());
-  std::vector<char> runnable(ops.size()), done(ops.size(), 0);
-  for (size_t i = 0; i < ops.size(); ++i) runnable[i] = as_run_op(d, ops[i], conv[i]) && worth_batching(d, conv[i]);
+// conv/runnable: each op's run form and whether it joins runs.  With `bound`
+// the state is a stack of bound states: tiles stay below bound->state_bits,
+// ops with per-binding matrices fill the per-binding pool, and ops outside
+// runs (exec_op) act on every state of the stack alike.
+void schedule_runs(Device &d, const std::vector<Op> &ops, const std::vector<RunOp> &conv,
+                   const std::vector<char> &runnable, const RunBound *bound) {
+  const int m = bound ? std::min(run_tile_qubits(d), bound->state_bits) : run_tile_qubits(d);
+  const int c = std::min(run_low_qubits(d), m);
+  const size_t pool_cap = run_pool_bytes(d) / 16, bound_cap = run_bound_pool_bytes(d) / 16;
+  std::vector<char> done(ops.size(), 0);
   const size_t lookahead = 96;
   size_t first = 0;
   while (first < ops.size()) {
@@ -1051,7 +1095,7 @@ void execute_blocked(Device &d, const std::vector<Op> &ops) {
     for (int q = 0; q < c; ++q) inT[q] = 1, ++tcount;
     std::vector<const RunOp *> run;
     std::vector<size_t> members;
-    size_t pool = 0;
+    size_t pool = 0, bpool = 0;
     size_t scanned = 0;
     for (size_t i = first; i < ops.size() && scanned < lookahead; ++i) {
       if (done[i]) continue;
@@ -1060,7 +1104,10 @@ void execute_blocked(Device &d, const std::vector<Op> &ops) {
       bool clash = false;
       for (auto x : q) clash |= blocked[x] != 0;
       bool take = false;
-      if (runnable[i] && !clash && (int)run.size() < run_max_ops() && pool + conv[i].mat.size() <= pool_cap) {
+      const bool per_binding = !conv[i].bmat.empty();
+      const size_t msz = conv[i].mat.size();
+      if (runnable[i] && !clash && (int)run.size() < run_max_ops() &&
+          (per_binding ? bpool + msz <= bound_cap : pool + msz <= pool_cap)) {
         int extra = 0;
         for (auto x : q) extra += !inT[x];
         if (tcount + extra <= m) take = true;
@@ -1070,28 +1117,173 @@ void execute_blocked(Device &d, const std::vector<Op> &ops) {
           if (!inT[x]) inT[x] = 1, ++tcount;
         run.push_back(&conv[i]);
         members.push_back(i);
-        pool += conv[i].mat.size();
+        (per_binding ? bpool : pool) += msz;
       } else {
         // a barrier-like op (no qubit list) blocks everything
         if (q.empty() && ops[i].type != GBQV_OP_BARRIER) break;
         for (auto x : q) blocked[x] = 1;
       }
     }
-    if (run.size() == 1 && conv[members[0]].qubits.size() <= 1) {
+    if (run.size() == 1 && conv[members[0]].qubits.size() <= 1 && conv[members[0]].bmat.empty()) {
       exec_op(d, ops[members[0]]);  // a lone 1-qubit op: the streaming kernel is enough
     } else {
-      launch_run(d, run);
+      launch_run(d, run, bound);
     }
     for (auto i : members) done[i] = 1;
   }
 }
 
+void execute_blocked(Device &d, const std::vector<Op> &ops) {
+  std::vector<RunOp> conv(ops.size());
+  std::vector<char> runnable(ops.size());
+  for (size_t i = 0; i < ops.size(); ++i) runnable[i] = as_run_op(d, ops[i], conv[i]) && worth_batching(d, conv[i]);
+  schedule_runs(d, ops, conv, runnable, nullptr);
+}
+
+// ---- runtime parameter binding: many bindings, one stack of states ----
+
+// A gate's prim as a run member: dense / diagonal matrix on its qubits, or a
+// multi-controlled X.  dense_only: a controlled 2x2 becomes a dense matrix
+// even when it is diagonal.  False when it has no run form.
+bool prim_run_form(const Prim &p, bool dense_only, RunOp &out) {
+  out.qubits = p.q;
+  out.mat.clear();
+  const size_t k = p.q.size();
+  if (k == 0 || k > 5) return false;
+  const size_t D = 1ULL << k;
+  auto controlled = [&](const cd *u) {  // identity except the block where every control is set
+    const size_t i0 = (D >> 1) - 1, i1 = D - 1;
+    if (!dense_only && u[1] == 0.0 && u[2] == 0.0) {
+      out.kind = 1;
+      out.mat.assign(D, 1.0);
+      out.mat[i0] = u[0];
+      out.mat[i1] = u[3];
+    } else {
+      out.kind = 0;
+      out.mat = gates::identity(D);
+      out.mat[i0 + D * i0] = u[0];
+      out.mat[i1 + D * i0] = u[1];
+      out.mat[i0 + D * i1] = u[2];
+      out.mat[i1 + D * i1] = u[3];
+    }
+  };
+  switch (p.k) {
+    case P::MCX: out.kind = 2; return true;
+    case P::DIAG: out.kind = 1; out.mat = p.m; return true;
+    case P::MATRIX: out.kind = 0; out.mat = p.m; return true;
+    case P::MCPHASE:
+      out.kind = 1;
+      out.mat.assign(D, 1.0);
+      out.mat[D - 1] = p.m[0];
+      return true;
+    case P::MCU: controlled(p.m.data()); return true;
+    case P::MCY: {
+      const cd y[4] = {0.0, cd(0., 1.), cd(0., -1.), 0.0};
+      controlled(y);
+      return true;
+    }
+    case P::MCSWAP: {
+      if (k < 2) return false;
+      out.kind = 0;
+      out.mat.assign(D * D, 0.0);
+      const size_t a = D >> 2, b = D >> 1, ctrl = a - 1;  // last two qubits at bits k-2, k-1
+      for (size_t i = 0; i < D; ++i) {
+        size_t j = i;
+        if ((i & ctrl) == ctrl && (((i & a) != 0) != ((i & b) != 0))) j = i ^ (a | b);
+        out.mat[j + D * i] = 1.0;
+      }
+      return true;
+    }
+    default: return false;
+  }
+}
+
+// The op's run form over `nbind` bindings: per-binding matrices (bmat) for a
+// gate with bound parameters.  False when it has none (then it must not be
+// bound, and runs on the whole stack through exec_op).
+bool bound_run_op(const Op &op, int nbind, RunOp &out) {
+  out = RunOp{};
+  if (op.type == GBQV_OP_MATRIX || op.type == GBQV_OP_DIAGONAL) {
+    Device dummy;
+    dummy.density = false;
+    return as_run_op(dummy, op, out);
+  }
+  if (op.type != GBQV_OP_GATE) return false;
+  if (op.bparams.empty()) return prim_run_form(sv_prim(op), false, out);
+  const size_t stride = op.params.size();
+  Op b = op;
+  b.bparams.clear();
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool dense_only = pass == 1;
+    bool same = true;
+    for (int j = 0; j < nbind && same; ++j) {
+      b.params.assign(op.bparams.begin() + j * stride, op.bparams.begin() + (j + 1) * stride);
+      RunOp r;
+      if (!prim_run_form(sv_prim(b), dense_only, r) || r.kind == 2)
+        throw Error(GBQV_ERR_KIND, "gate '" + op.name + "' with bound parameters has no per-binding form");
+      if (j == 0) {
+        out.kind = r.kind;
+        out.qubits = r.qubits;
+        out.mat = r.mat;
+        out.bmat.clear();
+        out.bmat.reserve(r.mat.size() * nbind);
+      } else if (r.kind != out.kind || r.mat.size() != out.mat.size()) {
+        same = false;  // a controlled 2x2 diagonal for some bindings only: all dense
+        break;
+      }
+      out.bmat.insert(out.bmat.end(), r.mat.begin(), r.mat.end());
+    }
+    if (same) return true;
+  }
+  throw Error(GBQV_ERR_KIND, "gate '" + op.name + "' with bound parameters has no per-binding form");
+}
+
+void execute_bound(Device &d, const gbqv_circuit &c, uint64_t first, uint64_t count) {
+  const int sb = c.num_qubits;
+  REQUIRE(!d.density, GBQV_ERR_KIND, "parameter binding runs statevectors only");
+  const int nb = std::max(c.nbind, 1);
+  REQUIRE(count >= 1 && first + count <= (uint64_t)nb, GBQV_ERR_ARG,
+          "binding range [" + std::to_string(first) + ", " + std::to_string(first + count) + ") out of " +
+              std::to_string(nb));
+  REQUIRE(d.n >= sb && (d.n - sb) < 63 && (1ULL << (d.n - sb)) >= count, GBQV_ERR_ARG,
+          "the state must stack 2^b states of " + std::to_string(sb) + " qubits, 2^b >= " + std::to_string(count) +
+              " (state has " + std::to_string(d.n) + " qubits)");
+  std::vector<Op> ops;
+  for (const Op &op : c.ops) {
+    if (op.type == GBQV_OP_BARRIER) continue;
+    REQUIRE(op.type == GBQV_OP_GATE || op.type == GBQV_OP_MATRIX || op.type == GBQV_OP_DIAGONAL, GBQV_ERR_KIND,
+            "op '" + op.name + "' is not unitary: bound execution runs unitary circuits");
+    if (op.type == GBQV_OP_GATE && op.bparams.empty() && sv_prim(op).k == P::NONE) continue;
+    ops.push_back(op);
+  }
+  std::vector<RunOp> conv(ops.size());
+  std::vector<char> runnable(ops.size());
+  for (size_t i = 0; i < ops.size(); ++i) {
+    runnable[i] = bound_run_op(ops[i], nb, conv[i]);
+    REQUIRE(runnable[i] || ops[i].bparams.empty(), GBQV_ERR_KIND,
+            "gate '" + ops[i].name + "' with bound parameters acts on more than 5 qubits");
+  }
+  RunBound rb{sb, first, count};
+  launch_set_basis_segments(d, sb, count);
+  schedule_runs(d, ops, conv, runnable, &rb);
+}
+
 }  // namespace
+
+extern "C" int gbqv_execute_bound(gbqv_handle h, gbqv_circuit_t c, uint64_t first, uint64_t count) {
+  return guard(
+      [&] {
+        REQUIRE(h && c, GBQV_ERR_ARG, "null argument");
+        execute_bound(device_of(h), *c, first, count);
+      },
+      h);
+}
 
 extern "C" int gbqv_execute(gbqv_handle h, gbqv_circuit_t c) {
   return guard(
       [&] {
         REQUIRE(h && c, GBQV_ERR_ARG, "null argument");
+        REQUIRE(c->nbind == 0, GBQV_ERR_ARG, "the circuit has parameter bindings: run it with gbqv_execute_bound");
         Device &d = device_of(h);
         REQUIRE(c->num_qubits == d.nq, GBQV_ERR_ARG,
                 "circuit has " + std::to_string(c->num_qubits) + " qubits, state has " + std::to_string(d.nq));

@@ -114,9 +114,20 @@ void reduce_pauli_inner(Device &dev, const void *lam, const void *psi, uint64_t 
 // Fused-run (cache-blocked) execution: a run of dense/diagonal ops whose
 // qubits all lie inside one tile of `tile_bits` vector qubits.
 struct RunOp {
-  int kind;       // 0 dense, 1 diagonal
+  int kind;       // 0 dense, 1 diagonal, 2 multi-controlled X (last qubit the target; no matrix)
   reg_t qubits;
   std::vector<cd> mat;
+  // Bound runs (runtime parameter binding): one matrix per binding, binding
+  // j at [j * mat size, (j + 1) * mat size); empty for an op that all
+  // bindings share (its matrix is `mat`).
+  std::vector<cd> bmat;
+};
+// A run over a stack of bound states: state j holds binding first + j, at
+// amplitudes [j 2^state_bits, (j + 1) 2^state_bits); states j >= count are
+// padding and are left untouched.
+struct RunBound {
+  int state_bits;
+  uint64_t first, count;
 };
 // complex128 dense gates of 4 / 5 qubits on the tensor cores (exact digit
 // slices, gbqv_ozaki.h): tcgen05 + TMEM for 4 qubits (gbqv_tc.cu), warp-level
@@ -165,6 +176,14 @@ int run_tile_qubits(const Device &dev);
 int run_low_qubits(const Device &dev);
 size_t run_pool_bytes(const Device &dev);
 int run_max_ops();
-void launch_run(Device &dev, const std::vector<const RunOp *> &ops);
+void launch_run(Device &dev, const std::vector<const RunOp *> &ops, const RunBound *bound = nullptr);
+// Bytes of per-binding matrices one bound run may hold per binding.
+size_t run_bound_pool_bytes(const Device &dev);
+// Every state of a stack of 2^state_bits-amplitude states: |0...0> for the
+// first `count`, zero for the rest.
+void launch_set_basis_segments(Device &dev, int state_bits, uint64_t count);
+// Expectation values of `terms` on each of the first nseg states of a stack
+// of 2^state_bits-amplitude states, into dev.results[t * nseg + s].
+void reduce_expval_segments(Device &dev, const std::vector<PauliTerm> &terms, int state_bits, uint64_t nseg);
 
 }  // namespace gbqv

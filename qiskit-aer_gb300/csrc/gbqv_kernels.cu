@@ -596,6 +596,61 @@ __global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n
   if (threadIdx.x == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = acc;
 }
 
+// The same per state of a stack of 2^sb-amplitude states (one state per
+// parameter binding): blockIdx.x = state * bps + slice, blockIdx.y = term;
+// the terms act on qubits below sb.
+template <typename T>
+__global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, int sb, int bps,
+                                                    const TermDev *__restrict__ terms, double *__restrict__ partials) {
+  const TermDev t = terms[blockIdx.y];
+  using R = decltype(T::x);
+  const R pr = (R)t.ph_re, pi = (R)t.ph_im;
+  const uint64_t seg = blockIdx.x / bps, slice = blockIdx.x % bps;
+  const T *ps = psi + (seg << sb);
+  double acc = 0.0;
+  const uint64_t stride = (uint64_t)bps * blockDim.x;
+  if (!t.x_mask) {
+    const uint64_t count = 1ULL << sb;
+    for (uint64_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
+      const T a = ps[i];
+      R v = pr * (a.x * a.x + a.y * a.y);
+      if (t.z_mask && (__popcll(i & t.z_mask) & 1)) v = -v;
+      acc += (double)v;
+    }
+  } else {
+    const uint64_t count = 1ULL << (sb - 1);
+    const uint64_t mask_l = (1ULL << t.x_max) - 1;
+    const uint64_t mask_u = ~((1ULL << (t.x_max + 1)) - 1);
+    for (uint64_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
+      const uint64_t i0 = ((i << 1) & mask_u) | (i & mask_l);
+      const uint64_t i1 = i0 ^ t.x_mask;
+      const T a0 = ps[i0], a1 = ps[i1];
+      const R zr = a1.x * a0.x + a1.y * a0.y;
+      const R zi = a1.y * a0.x - a1.x * a0.y;
+      R v0 = pr * zr - pi * zi;
+      R v1 = pr * zr + pi * zi;
+      if (t.z_mask && (__popcll(i0 & t.z_mask) & 1)) v0 = -v0;
+      if (t.z_mask && (__popcll(i1 & t.z_mask) & 1)) v1 = -v1;
+      acc += (double)v0;
+      acc += (double)v1;
+    }
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = acc;
+}
+
+template <typename T>
+__global__ void k_set_basis_seg(T *__restrict__ psi, int sb, uint64_t nvalid, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t low = (1ULL << sb) - 1;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    T z;
+    z.x = ((i & low) == 0 && (i >> sb) < nvalid) ? 1 : 0;
+    z.y = 0;
+    psi[i] = z;
+  }
+}
+
 // DensityMatrix::expval_pauli (densitymatrix.hpp:445-496): rho is 2^nq x 2^nq.
 template <typename T>
 __global__ void __launch_bounds__(256) k_dm_expval(const T *__restrict__ rho, int nq, const TermDev *__restrict__ terms,
@@ -947,6 +1002,39 @@ void reduce_expval(Device &dev, const std::vector<PauliTerm> &terms) {
     k_expval<float2><<<grid, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), dev.n, d_terms, dev.partials);
   check_launch("expval kernel");
   finish(dev, (int)terms.size(), kReduceBlocks / 4);
+}
+
+void reduce_expval_segments(Device &dev, const std::vector<PauliTerm> &terms, int state_bits, uint64_t nseg) {
+  if (terms.empty() || nseg == 0) return;
+  if (terms.size() > (size_t)kMaxTerms) throw Error(1, "too many Pauli terms in one call");
+  // blocks per state: about 8 blocks of 256 threads per SM over the whole launch
+  const uint64_t want = std::max<uint64_t>(1, (uint64_t)kReduceBlocks / 4 / std::max<uint64_t>(nseg, 1));
+  const uint64_t cap = std::max<uint64_t>(1, (1ULL << state_bits) / (2 * 256));
+  const int bps = (int)std::min<uint64_t>(std::min<uint64_t>(want, cap), 1024);
+  if (nseg * (uint64_t)bps > 0x7fffffffULL) throw Error(1, "too many states in one expectation-value launch");
+  const size_t values = terms.size() * nseg;
+  grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * values * bps);
+  grow(reinterpret_cast<void *&>(dev.results), dev.results_cap, sizeof(double) * values);
+  TermDev *d_terms;
+  upload_terms(dev, terms, &d_terms);
+  dim3 grid((unsigned)(nseg * bps), (unsigned)terms.size());
+  if (dev.dbl)
+    k_expval_seg<double2><<<grid, kReduceThreads, 0, dev.stream>>>(st<double2>(dev), state_bits, bps, d_terms,
+                                                                   dev.partials);
+  else
+    k_expval_seg<float2><<<grid, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), state_bits, bps, d_terms,
+                                                                  dev.partials);
+  check_launch("segmented expval kernel");
+  finish(dev, (int)values, bps);
+}
+
+void launch_set_basis_segments(Device &dev, int state_bits, uint64_t count) {
+  const int grid = grid_for(dev.amps(), 256);
+  if (dev.dbl)
+    k_set_basis_seg<double2><<<grid, 256, 0, dev.stream>>>(st<double2>(dev), state_bits, count, dev.amps());
+  else
+    k_set_basis_seg<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), state_bits, count, dev.amps());
+  check_launch("initialize kernel");
 }
 
 void reduce_dm_expval(Device &dev, const std::vector<PauliTerm> &terms) {
@@ -1453,9 +1541,10 @@ namespace {
 constexpr int kRunMaxOps = 24;
 
 struct RunOpDev {
-  int kind;                 // 0 dense, 1 diagonal
+  int kind;                 // 0 dense, 1 diagonal, 2 multi-controlled X
   int k;
-  int mat_off;              // offset into the matrix pool (complex entries)
+  int bound;                // 1: the matrix is in the per-binding block of the tile's state
+  int mat_off;              // offset into the matrix pool / per-binding block (complex entries)
   uint32_t lowmask[5];      // sorted local positions as masks, for zero insertion
   uint32_t offs[32];        // local offset of matrix index a
   uint32_t qbit[5];         // local bit of op qubit j (diagonal index)
@@ -1463,6 +1552,9 @@ struct RunOpDev {
 
 struct RunParams {
   int m, c, nops, pool_elems;
+  int bound_elems;          // complex entries per binding in the per-binding pool (0: none)
+  int state_bits;           // bound runs: log2 of the amplitudes per state of the stack
+  uint64_t nbind;           // bound runs: states of the stack that hold a binding
   uint64_t ntiles;
   uint64_t tile_lowmask[kMaxQubits];  // sorted tile qubits (zero insertion of the tile id)
   int nt;                             // number of tile qubits = m
@@ -1510,14 +1602,36 @@ __device__ __forceinline__ void run_diag(T *tile, const T *diag, const RunOpDev 
   }
 }
 
+// Multi-controlled X inside a tile: swap the pairs that differ in the target
+// bit and have every control bit set (QubitVector::apply_mcx,
+// qubitvector.hpp:1446-1486); no arithmetic.
+template <typename T>
+__device__ __forceinline__ void run_mcx(T *tile, const RunOpDev &op, int m) {
+  const uint32_t tb = op.qbit[op.k - 1], low = tb - 1;
+  uint32_t cm = 0;
+  for (int j = 0; j + 1 < op.k; ++j) cm |= op.qbit[j];
+  const uint32_t half = 1u << (m - 1);
+  for (uint32_t p = threadIdx.x; p < half; p += blockDim.x) {
+    const uint32_t i0 = ((p & ~low) << 1) | (p & low);
+    if ((i0 & cm) == cm) {
+      const T a = tile[i0];
+      tile[i0] = tile[i0 | tb];
+      tile[i0 | tb] = a;
+    }
+  }
+}
+
+// bpool (bound runs only): bound_elems complex entries per binding, binding
+// j of the stack at bpool + j * bound_elems.
 template <typename T>
 __global__ void __launch_bounds__(256, 2) k_run(T *__restrict__ psi, const RunParams *__restrict__ P,
-                                             const T *__restrict__ pool) {
+                                             const T *__restrict__ pool, const T *__restrict__ bpool) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = P->m, c = P->c;
   T *tile = reinterpret_cast<T *>(smem_raw);
   T *mats = tile + (1u << m);
-  uint64_t *hi = reinterpret_cast<uint64_t *>(mats + P->pool_elems);
+  T *bmats = mats + P->pool_elems;
+  uint64_t *hi = reinterpret_cast<uint64_t *>(bmats + P->bound_elems);
   for (int i = threadIdx.x; i < P->pool_elems; i += blockDim.x) mats[i] = pool[i];
   const uint32_t nhi = 1u << (m - c);
   for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
@@ -1530,13 +1644,23 @@ __global__ void __launch_bounds__(256, 2) k_run(T *__restrict__ psi, const RunPa
   const uint32_t L = 1u << m, cmask = (1u << c) - 1;
   for (uint64_t t = blockIdx.x; t < P->ntiles; t += gridDim.x) {
     const uint64_t gbase = insert_zeros(t, P->tile_lowmask, P->nt);
+    if (P->bound_elems) {
+      // the tile lies inside one state of the stack (no tile qubit reaches
+      // state_bits): its binding's matrices, or nothing for a padding state
+      const uint64_t st = gbase >> P->state_bits;
+      if (st >= P->nbind) continue;  // same value in every thread of the CTA
+      const T *src = bpool + st * (uint64_t)P->bound_elems;
+      for (int i = threadIdx.x; i < P->bound_elems; i += blockDim.x) bmats[i] = src[i];
+    }
     for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) tile[l] = psi[gbase | hi[l >> c] | (l & cmask)];
     __syncthreads();
     for (int o = 0; o < P->nops; ++o) {
       const RunOpDev &op = P->ops[o];
-      const T *mat = mats + op.mat_off;
+      const T *mat = (op.bound ? bmats : mats) + op.mat_off;
       if (op.kind == 1) {
         run_diag(tile, mat, op, m);
+      } else if (op.kind == 2) {
+        run_mcx(tile, op, m);
       } else {
         switch (op.k) {
           case 1: run_dense<T, 1>(tile, mat, op, m); break;
@@ -1557,10 +1681,13 @@ int run_tile_bits(const Device &dev) { return dev.dbl ? 12 : 13; }
 constexpr int kRunLowBits = 4;
 constexpr int kRunPoolBytes = 32 * 1024;
 
+constexpr int kRunBoundBytes = 16 * 1024;
+
 template <typename T>
-void launch_run_t(Device &dev, const std::vector<const RunOp *> &ops) {
+void launch_run_t(Device &dev, const std::vector<const RunOp *> &ops, const RunBound *bound) {
   const int n = dev.n;
-  const int m = std::min(run_tile_bits(dev), n);
+  // a bound run's tiles stay inside one state of the stack
+  const int m = std::min(run_tile_bits(dev), bound ? bound->state_bits : n);
   // tile qubits: the low c qubits, the ops' qubits, then padding from the bottom
   std::vector<bool> in(n, false);
   const int c = std::min(kRunLowBits, m);
@@ -1587,12 +1714,15 @@ void launch_run_t(Device &dev, const std::vector<const RunOp *> &ops) {
   P->ntiles = 1ULL << (n - m);
   if ((int)ops.size() > kRunMaxOps) throw Error(1, "run too long");
   std::vector<T> pool;
+  int bound_elems = 0;
   for (size_t o = 0; o < ops.size(); ++o) {
     const RunOp &op = *ops[o];
     RunOpDev &d = P->ops[o];
     d.kind = op.kind;
     d.k = (int)op.qubits.size();
-    d.mat_off = (int)pool.size();
+    d.bound = !op.bmat.empty();
+    if (d.bound && !bound) throw Error(1, "bound run op outside a bound run");
+    d.mat_off = d.bound ? bound_elems : (int)pool.size();
     reg_t lq;
     for (auto q : op.qubits) lq.push_back(local[q]);
     reg_t sq = lq;
@@ -1603,19 +1733,44 @@ void launch_run_t(Device &dev, const std::vector<const RunOp *> &ops) {
       const uint32_t nn = 1u << j, bit = 1u << lq[j];
       for (uint32_t a = 0; a < nn; ++a) d.offs[nn + a] = d.offs[a] | bit;
     }
-    for (const cd &z : op.mat) pool.push_back(to_dev<T>(z));
+    if (d.bound)
+      bound_elems += (int)op.mat.size();
+    else
+      for (const cd &z : op.mat) pool.push_back(to_dev<T>(z));
   }
   P->nops = (int)ops.size();
   P->pool_elems = (int)pool.size();
+  P->bound_elems = bound_elems;
   if (pool.size() * sizeof(T) > (size_t)kRunPoolBytes) throw Error(1, "run matrices exceed the pool");
-  const size_t pbytes = sizeof(RunParams), poolb = pool.size() * sizeof(T);
-  grow(dev.mat, dev.mat_cap, pbytes + poolb + 256);
+  if ((size_t)bound_elems * sizeof(T) > (size_t)kRunBoundBytes) throw Error(1, "run matrices exceed the bound pool");
+  // per-binding matrices of the stack's states, binding-major
+  std::vector<T> bpool;
+  if (bound_elems) {
+    P->state_bits = bound->state_bits;
+    P->nbind = bound->count;
+    bpool.reserve((size_t)bound_elems * bound->count);
+    for (uint64_t j = 0; j < bound->count; ++j)
+      for (const RunOp *op : ops) {
+        if (op->bmat.empty()) continue;
+        const size_t msz = op->mat.size();
+        if (op->bmat.size() < (bound->first + j + 1) * msz) throw Error(1, "bound run op has too few bindings");
+        const cd *src = op->bmat.data() + (bound->first + j) * msz;
+        for (size_t e = 0; e < msz; ++e) bpool.push_back(to_dev<T>(src[e]));
+      }
+  }
+  const size_t pbytes = sizeof(RunParams), poolb = pool.size() * sizeof(T), bpoolb = bpool.size() * sizeof(T);
+  const size_t pool_off = (pbytes + 255) & ~size_t(255);
+  const size_t bpool_off = (pool_off + poolb + 255) & ~size_t(255);
+  grow(dev.mat, dev.mat_cap, bpool_off + bpoolb + 256);
   char *base = reinterpret_cast<char *>(dev.mat);
   cuda_check(cudaMemcpyAsync(base, P.get(), pbytes, cudaMemcpyHostToDevice, dev.stream), "run upload");
-  const size_t pool_off = (pbytes + 255) & ~size_t(255);
   if (poolb)
     cuda_check(cudaMemcpyAsync(base + pool_off, pool.data(), poolb, cudaMemcpyHostToDevice, dev.stream), "run upload");
-  const size_t smem = sizeof(T) * ((1u << m) + pool.size()) + sizeof(uint64_t) * (1u << (m - cc));
+  if (bpoolb)
+    cuda_check(cudaMemcpyAsync(base + bpool_off, bpool.data(), bpoolb, cudaMemcpyHostToDevice, dev.stream),
+               "run upload");
+  const size_t smem =
+      sizeof(T) * ((1u << m) + pool.size() + (size_t)bound_elems) + sizeof(uint64_t) * (1u << (m - cc));
   static bool attr_set[2] = {false, false};
   if (!attr_set[dev.dbl]) {
     cuda_check(cudaFuncSetAttribute(k_run<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
@@ -1628,7 +1783,8 @@ void launch_run_t(Device &dev, const std::vector<const RunOp *> &ops) {
   const uint64_t grid = std::min<uint64_t>(P->ntiles, 152ULL * per_sm);
   k_run<T><<<(unsigned)grid, 256, smem, dev.stream>>>(reinterpret_cast<T *>(dev.state),
                                                      reinterpret_cast<const RunParams *>(base),
-                                                     reinterpret_cast<const T *>(base + pool_off));
+                                                     reinterpret_cast<const T *>(base + pool_off),
+                                                     reinterpret_cast<const T *>(base + bpool_off));
   check_launch("run kernel");
 }
 
@@ -1639,11 +1795,13 @@ int run_low_qubits(const Device &dev) { return std::min(kRunLowBits, dev.n); }
 size_t run_pool_bytes(const Device &dev) { return kRunPoolBytes / dev.amp_bytes() * 16; }
 int run_max_ops() { return kRunMaxOps; }
 
-void launch_run(Device &dev, const std::vector<const RunOp *> &ops) {
+size_t run_bound_pool_bytes(const Device &dev) { return kRunBoundBytes / dev.amp_bytes() * 16; }
+
+void launch_run(Device &dev, const std::vector<const RunOp *> &ops, const RunBound *bound) {
   if (dev.dbl)
-    launch_run_t<double2>(dev, ops);
+    launch_run_t<double2>(dev, ops, bound);
   else
-    launch_run_t<float2>(dev, ops);
+    launch_run_t<float2>(dev, ops, bound);
 }
 
 }  // namespace gbqv

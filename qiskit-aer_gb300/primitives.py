@@ -1,0 +1,230 @@
+"""``EstimatorV2`` over the engine, the shape of qiskit_aer.primitives.EstimatorV2
+(qiskit_aer/primitives/estimator_v2.py:46-159) without the qiskit dependency.
+
+A pub is ``(circuit, observables[, parameter_values[, precision]])``:
+
+* ``observables``: a Pauli label (``"XZI"``, qubit 0 rightmost), a dict
+  ``{label: coeff}``, a list of ``(label, coeff)`` pairs (one observable, the
+  ``SparsePauliOp.to_list()`` form), or a nested list / object array of those
+  (an array of observables);
+* ``parameter_values``: ``None``, an array of shape ``(..., P)`` whose last
+  axis follows ``circuit.parameters`` (sorted by name), or a dict
+  ``{Parameter: array of shape (...)}``;
+* ``precision``: standard deviation of the Gaussian noise added to the
+  expectation values (0: exact).
+
+As in the reference, the parameter and observable shapes broadcast, every
+distinct Pauli gets one ``save_expectation_value`` over all qubits, and the
+circuit runs once with every binding through ``AerSimulator.run(...,
+parameter_binds=[...])`` — which runs all bindings together on one stack of
+states.  ``evs[i] = sum_p coeff_p <p>`` for the broadcast index i; ``stds`` is
+the precision.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .circuit import Parameter, QuantumCircuit
+from .simulator import AerSimulator
+
+
+@dataclass
+class Options:
+    """Options of EstimatorV2 (estimator_v2.py:30-42)."""
+
+    default_precision: float = 0.0
+    backend_options: dict = field(default_factory=dict)
+    run_options: dict = field(default_factory=dict)
+
+
+class DataBin:
+    def __init__(self, **kw):
+        self._fields = list(kw)
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+    def __repr__(self):
+        return "DataBin(" + ", ".join(f"{k}={getattr(self, k)!r}" for k in self._fields) + ")"
+
+
+class PubResult:
+    def __init__(self, data: DataBin, metadata: dict):
+        self.data = data
+        self.metadata = metadata
+
+
+class PrimitiveResult(list):
+    def __init__(self, pub_results, metadata=None):
+        super().__init__(pub_results)
+        self.metadata = metadata or {}
+
+
+class PrimitiveJob:
+    """Runs on submission; result() returns the PrimitiveResult."""
+
+    def __init__(self, fn, *args):
+        self._fn, self._args, self._result = fn, args, None
+
+    def _submit(self):
+        self._result = self._fn(*self._args)
+
+    def result(self):
+        if self._result is None:
+            self._submit()
+        return self._result
+
+    def status(self):
+        return "DONE" if self._result is not None else "INITIALIZING"
+
+
+def _is_label(x) -> bool:
+    return isinstance(x, str)
+
+
+def _one_observable(obs) -> dict | None:
+    """obs as {pauli label: coeff}, or None when it is an array of observables."""
+    if _is_label(obs):
+        return {obs: 1.0}
+    if isinstance(obs, dict):
+        return {str(k): complex(v) if np.iscomplexobj(v) else float(v) for k, v in obs.items()}
+    if (isinstance(obs, (list, tuple)) and obs and all(isinstance(t, tuple) and len(t) == 2 and _is_label(t[0])
+                                                       for t in obs)):
+        out: dict = {}
+        for lab, c in obs:
+            out[lab] = out.get(lab, 0.0) + c
+        return out
+    return None
+
+
+def coerce_observables(obs, num_qubits: int) -> np.ndarray:
+    """An object array of {label: coeff} dicts (ObservablesArray.coerce)."""
+    one = _one_observable(obs)
+    if one is not None:
+        arr = np.empty((), dtype=object)
+        arr[()] = one
+    else:
+        items = [coerce_observables(o, num_qubits) for o in obs]
+        arr = np.empty(len(items), dtype=object)
+        if items and items[0].shape:
+            arr = np.empty((len(items),) + items[0].shape, dtype=object)
+        for i, it in enumerate(items):
+            if it.shape != arr.shape[1:]:
+                raise ValueError("observables array is ragged")
+            if it.shape:
+                arr[i] = it
+            else:
+                arr[i] = it[()]
+    for d in arr.reshape(-1):
+        for lab in d:
+            if len(lab) != num_qubits or set(lab) - set("IXYZ"):
+                raise ValueError(f"observable '{lab}' is not a Pauli label on {num_qubits} qubits")
+    return arr
+
+
+def coerce_parameter_values(values, circuit: QuantumCircuit) -> np.ndarray:
+    """Array of shape (..., P), the last axis in the order of circuit.parameters."""
+    params = circuit.parameters
+    if values is None:
+        if params:
+            raise ValueError(f"the circuit has {len(params)} parameters and no parameter values")
+        return None
+    if isinstance(values, dict):
+        by_name = {}
+        for k, v in values.items():
+            keys = k if isinstance(k, tuple) else (k,)
+            v = np.asarray(v, dtype=np.float64)
+            if len(keys) > 1:
+                for i, kk in enumerate(keys):
+                    by_name[kk.name if isinstance(kk, Parameter) else str(kk)] = v[..., i]
+            else:
+                kk = keys[0]
+                by_name[kk.name if isinstance(kk, Parameter) else str(kk)] = v
+        missing = [p.name for p in params if p.name not in by_name]
+        if missing:
+            raise ValueError(f"no values for parameters {missing}")
+        cols = np.broadcast_arrays(*[by_name[p.name] for p in params])
+        return np.stack(cols, axis=-1)
+    arr = np.asarray(values, dtype=np.float64)
+    if arr.ndim == 0 or arr.shape[-1] != len(params):
+        raise ValueError(f"parameter values of shape {arr.shape} for {len(params)} parameters")
+    return arr
+
+
+class EstimatorV2:
+    """Expectation values of observables on (parameterised) circuits."""
+
+    def __init__(self, *, options: dict | None = None):
+        self._options = Options(**options) if options else Options()
+        self._backend = AerSimulator(**self._options.backend_options)
+
+    @classmethod
+    def from_backend(cls, backend: AerSimulator, **options):
+        est = cls(**options)
+        est._backend = backend
+        return est
+
+    @property
+    def options(self) -> Options:
+        return self._options
+
+    def run(self, pubs, *, precision: float | None = None) -> PrimitiveJob:
+        if precision is None:
+            precision = self._options.default_precision
+        coerced = [self._coerce(pub, precision) for pub in pubs]
+        for i, (_, _, _, prec) in enumerate(coerced):
+            if prec < 0.0:
+                raise ValueError(f"The {i}-th pub has precision less than 0 ({prec}). "
+                                 "But precision should be equal to or larger than 0.")
+        job = PrimitiveJob(self._run, coerced)
+        job._submit()
+        return job
+
+    @staticmethod
+    def _coerce(pub, default_precision):
+        if isinstance(pub, QuantumCircuit):
+            raise ValueError("an estimator pub needs observables")
+        circuit, obs = pub[0], pub[1]
+        values = pub[2] if len(pub) > 2 else None
+        prec = pub[3] if len(pub) > 3 and pub[3] is not None else default_precision
+        observables = coerce_observables(obs, circuit.num_qubits)
+        pv = coerce_parameter_values(values, circuit)
+        return circuit, observables, pv, float(prec)
+
+    def _run(self, pubs) -> PrimitiveResult:
+        return PrimitiveResult([self._run_pub(*pub) for pub in pubs], metadata={"version": 2})
+
+    def _run_pub(self, circuit: QuantumCircuit, observables: np.ndarray, values, precision: float) -> PubResult:
+        circ = circuit.copy()
+        params = circ.parameters
+        param_shape = values.shape[:-1] if values is not None else ()
+        param_indices = np.fromiter(np.ndindex(param_shape), dtype=object).reshape(param_shape) \
+            if param_shape else np.empty((), dtype=object)
+        if not param_shape:
+            param_indices[()] = ()
+        bc_param_ind, bc_obs = np.broadcast_arrays(param_indices, observables)
+        paulis = sorted({lab for d in observables.reshape(-1) for lab in d})
+        n = circ.num_qubits
+        for lab in paulis:
+            circ.save_expectation_value([(1.0, lab, list(range(n)))], label=lab)
+        run_options = dict(self._options.run_options)
+        if params:
+            flat = values.reshape(-1, len(params))
+            binds = [{p: flat[:, i] for i, p in enumerate(params)}]
+            result = self._backend.run(circ, parameter_binds=binds, **run_options)
+        else:
+            result = self._backend.run(circ, **run_options)
+        position = {idx: i for i, idx in enumerate(param_indices.reshape(-1))}
+        evs = np.zeros(bc_param_ind.shape, dtype=float)
+        stds = np.full(bc_param_ind.shape, precision)
+        for index in np.ndindex(*bc_param_ind.shape):
+            data = result.data(position[bc_param_ind[index]] if params else 0)
+            for lab, coeff in bc_obs[index].items():
+                evs[index] += np.real(data[lab] * coeff)
+        if precision > 0:
+            rng = np.random.default_rng(self._options.run_options.get("seed_simulator"))
+            evs = rng.normal(evs, precision, evs.shape)
+        return PubResult(DataBin(evs=evs, stds=stds, shape=evs.shape),
+                         metadata={"target_precision": precision, "circuit_metadata": circuit.metadata,
+                                   "simulator_metadata": result.metadata(0) if result.results else {}})

@@ -236,6 +236,24 @@ class QubitVector:
         return out, total.value
 
 
+    def expval_pauli_segments(self, state_qubits: int, nseg: int, terms) -> np.ndarray:
+        """<P_t> on each of the first nseg states of a stack of
+        2^state_qubits-amplitude states: array [term, state]."""
+        qs, offs, labels = [], [0], []
+        for q, lab in terms:
+            qs.extend(int(x) for x in q)
+            offs.append(len(qs))
+            labels.append(lab.encode())
+        qa = np.ascontiguousarray(np.asarray(qs, dtype=np.uint64))
+        oa = (C.c_int * len(offs))(*offs)
+        la = (C.c_char_p * max(1, len(labels)))(*labels)
+        out = np.empty((len(labels), int(nseg)), dtype=np.float64)
+        if labels:
+            self._c(self._L.gbqv_expval_pauli_segments(self._h, int(state_qubits), int(nseg), len(labels),
+                                                       qa.ctypes.data_as(A.u64p), oa, la, out.ctypes.data_as(A.dp)))
+        return out
+
+
 class DensityMatrix(QubitVector):
     """vec(rho) of n qubits over 2n vector qubits, resident on the GPU."""
 

@@ -152,15 +152,130 @@ class AerSimulator:
                 meta["fusion"]["method"] = method_name
         return segments, meas, saves, meta
 
-    def run(self, circuits, shots: int = 1024, seed_simulator: int | None = None, **_):
-        if isinstance(circuits, QuantumCircuit):
+    def run(self, circuits, shots: int = 1024, seed_simulator: int | None = None, parameter_binds=None, **_):
+        """parameter_binds: one dict {Parameter: values} per circuit (AerBackend.run,
+        qiskit_aer/backends/aerbackend.py:146-185); a parameterised circuit
+        becomes one experiment per binding, in order, and experiment k of the
+        job gets seed seed_simulator + 2113 * k (controller_execute.hpp:188-210)."""
+        single = isinstance(circuits, QuantumCircuit)
+        if single:
             circuits = [circuits]
+        binds = self._check_binds(circuits, parameter_binds, single)
         seed = seed_simulator if seed_simulator is not None else self.options["seed_simulator"]
         if seed is None:
             seed = int(np.random.SeedSequence().entropy & 0x7FFFFFFF)
         t0 = time.perf_counter()
-        results = [self._run_one(c, shots, seed + 2113 * i) for i, c in enumerate(circuits)]
+        results, k = [], 0
+        for c, b in zip(circuits, binds):
+            if not b:
+                results.append(self._run_one(c, shots, seed + 2113 * k))
+                k += 1
+                continue
+            nbind = len(next(iter(b.values())))
+            seeds = [seed + 2113 * (k + j) for j in range(nbind)]
+            if self._bound_batchable(c):
+                results.extend(self._run_bound(c, b, nbind, seeds, shots))
+            else:
+                for j in range(nbind):
+                    results.append(self._run_one(c.assign_parameters({p: v[j] for p, v in b.items()}), shots,
+                                                 seeds[j]))
+            k += nbind
         return Result(results, time.perf_counter() - t0)
+
+    @staticmethod
+    def _check_binds(circuits, parameter_binds, single):
+        """Per circuit, {Parameter: values} restricted to its parameters (empty
+        for a circuit without any), with the reference's validation
+        (AerBackend._convert_binds, aerbackend.py:128-144, and the length
+        check of controller_execute.hpp:104-155)."""
+        if parameter_binds is None:
+            if any(c.parameters for c in circuits):
+                raise ValueError("circuits have parameters but parameter_binds is not specified.")
+            return [{} for _ in circuits]
+        if single and len(parameter_binds) > 1:
+            raise ValueError("More than 1 parameter table provided for a single circuit")
+        if len(parameter_binds) != len(circuits):
+            raise ValueError("Number of input circuits does not match number of input parameter bind dictionaries")
+        out = []
+        for c, table in zip(circuits, parameter_binds):
+            params = c.parameters
+            if not params:
+                out.append({})
+                continue
+            missing = [p.name for p in params if p not in table]
+            if missing:
+                raise ValueError(f"no values bound to parameters {missing}")
+            b = {p: np.atleast_1d(np.asarray(table[p], dtype=np.float64)).reshape(-1) for p in params}
+            lens = {v.size for v in b.values()}
+            if len(lens) != 1 or 0 in lens:
+                raise ValueError("Invalid parameterization: every parameter needs the same number of values")
+            out.append(b)
+        return out
+
+    def _bound_batchable(self, circuit: QuantumCircuit) -> bool:
+        """Bindings run together on one stack of states when the circuit is a
+        unitary statevector circuit whose saves (expectation values,
+        statevectors) all sit at its end."""
+        if self.method != "statevector" or (self.noise_model is not None and not self.noise_model.is_ideal()):
+            return False
+        if circuit.needs_shots("statevector"):
+            return False
+        body, meas, saves = circuit.split_final()
+        if meas:
+            return False
+        if any(ins.kind not in ("gate", "unitary", "diagonal", "barrier") for ins in body):
+            return False
+        return all(pos == len(body) and ins.name in ("expval", "statevector") for pos, ins in saves)
+
+    # largest stack of bound states held at once: 2^31 amplitudes (34 GB at complex128)
+    MAX_STACK_QUBITS = 31
+
+    def _run_bound(self, circuit: QuantumCircuit, binds: dict, nbind: int, seeds, shots: int):
+        """Every binding of a parameterised circuit at once
+        (BatchShotsExecutor over runtime-bound parameters,
+        batch_shots_executor.hpp:152-314): the circuit is assembled once, its
+        parameterised gates get per-binding values (gbqv_circuit_bind_param),
+        and each chunk of bindings runs on one stack of states
+        (gbqv_execute_bound); expectation values are reduced per state."""
+        n = circuit.num_qubits
+        body, _, saves = circuit.split_final()
+        nc = NativeCircuit(n, body)
+        nc.bind(binds, nbind)
+        data = [{} for _ in range(nbind)]
+        chunk = 1 << max(0, self.MAX_STACK_QUBITS - n)
+        L = A.lib()
+        st, st_bits = None, -1
+        try:
+            for first in range(0, nbind, chunk):
+                cnt = min(chunk, nbind - first)
+                b = (cnt - 1).bit_length()
+                if st is None or st_bits != b:
+                    if st is not None:
+                        st.close()
+                    st, st_bits = QubitVector(n + b, self.precision), b
+                A.check(L.gbqv_execute_bound(st.handle, nc.handle, first, cnt), st.handle)
+                for _, ins in saves:
+                    if ins.name == "statevector":
+                        vec = st.copy_to_vector()
+                        for j in range(cnt):
+                            data[first + j][ins.data] = vec[j << n:(j + 1) << n].copy()
+                        continue
+                    label, terms = ins.data
+                    vals = st.expval_pauli_segments(n, cnt, [(q, lab) for _, lab, q in terms])
+                    coeffs = np.array([complex(c) for c, _, _ in terms])
+                    re = coeffs.real @ vals
+                    im = coeffs.imag @ vals
+                    for j in range(cnt):
+                        data[first + j][label] = float(re[j]) if not np.any(coeffs.imag) else complex(re[j], im[j])
+            if st is not None:
+                st.synchronize()
+        finally:
+            if st is not None:
+                st.close()
+        meta = {"fusion": {"enabled": False}, "parameter_binding": {"batched": True, "bindings": nbind,
+                                                                   "stack_qubits": n + max(st_bits, 0)}}
+        return [{"counts": None, "data": data[j], "metadata": dict(meta), "seed_simulator": seeds[j], "shots": shots}
+                for j in range(nbind)]
 
     def _run_one(self, circuit: QuantumCircuit, shots: int, seed: int):
         if self.method == "statevector" and circuit.needs_shots("statevector"):
