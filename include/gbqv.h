@@ -380,7 +380,11 @@ int gbqv_batch_result(gbqv_batch_t b, int i, double *energy, double *grad, int n
                       uint64_t shots, double *latency_ms);
 
 /* Execution policy for gbqv_execute (no reference counterpart: Aer applies
- * one op per pass).  blocking = 0 applies one kernel per op. */
+ * one op per pass).  blocking = 0 applies one kernel per op; 1 (default)
+ * schedules runs of small ops into cache-blocked passes whose tile is held
+ * in registers; 2 the same passes with the tile swept in shared memory op by
+ * op.  Bound execution (gbqv_execute_bound) always uses runs, mode 2 picks
+ * the shared-memory form there too. */
 int gbqv_set_blocking(gbqv_handle h, int blocking);
 
 /* Arithmetic of complex128 dense gates on 4 or 5 qubits (no reference

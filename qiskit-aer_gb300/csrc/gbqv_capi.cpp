@@ -891,6 +891,7 @@ extern "C" int gbqv_set_tensor_c128(gbqv_handle h, int enable) {
 extern "C" int gbqv_set_blocking(gbqv_handle h, int blocking) {
   return guard(h, [&] {
     need_handle(h);
+    REQUIRE(blocking >= 0 && blocking <= 2, GBQV_ERR_ARG, "blocking mode must be 0, 1 or 2");
     h->dev.blocking = blocking;
   });
 }

@@ -40,6 +40,12 @@ struct gbqv_circuit {
   int num_qubits = 0;
   int nbind = 0;  // number of parameter bindings (0: none)
   std::vector<Op> ops;
+  uint64_t version = 0;  // bumped by every change of ops or bindings
+  // bound execution: the run form of every op, built once per version
+  uint64_t bound_version = UINT64_MAX;
+  std::vector<Op> bound_ops;
+  std::vector<RunOp> bound_conv;
+  std::vector<char> bound_runnable;
 };
 
 namespace {
@@ -459,6 +465,7 @@ struct Fusion {
   }
 
   int next_diagonal_end(const std::vector<Op> &ops, int from, int end, std::set<uint64_t> &fq) const {
+    if (!ops[from].bparams.empty()) return -1;  // bound gates stay unfused
     if (is_diagonal_op(ops[from])) {
       for (auto q : ops[from].qubits) fq.insert(q);
       return from;
@@ -650,6 +657,7 @@ extern "C" int gbqv_circuit_gate(gbqv_circuit_t c, const char *name, const uint6
     Prim p = sv_prim(op);
     (void)p;
     c->ops.push_back(std::move(op));
+    ++c->version;
   });
 }
 
@@ -663,6 +671,7 @@ extern "C" int gbqv_circuit_unitary(gbqv_circuit_t c, const uint64_t *qubits, in
     const cd *m = reinterpret_cast<const cd *>(mat);
     op.mat.assign(m, m + (1ULL << (2 * k)));
     c->ops.push_back(std::move(op));
+    ++c->version;
   });
 }
 
@@ -676,6 +685,7 @@ extern "C" int gbqv_circuit_diagonal(gbqv_circuit_t c, const uint64_t *qubits, i
     const cd *m = reinterpret_cast<const cd *>(diag);
     op.mat.assign(m, m + (1ULL << k));
     c->ops.push_back(std::move(op));
+    ++c->version;
   });
 }
 
@@ -689,6 +699,7 @@ extern "C" int gbqv_circuit_superop(gbqv_circuit_t c, const uint64_t *qubits, in
     const cd *m = reinterpret_cast<const cd *>(mat);
     op.mat.assign(m, m + (1ULL << (4 * k)));
     c->ops.push_back(std::move(op));
+    ++c->version;
   });
 }
 
@@ -703,6 +714,7 @@ extern "C" int gbqv_circuit_kraus(gbqv_circuit_t c, const uint64_t *qubits, int 
     const size_t sz = 1ULL << (2 * k);
     for (int i = 0; i < nk; ++i) op.kraus.emplace_back(m + i * sz, m + (i + 1) * sz);
     c->ops.push_back(std::move(op));
+    ++c->version;
   });
 }
 
@@ -713,6 +725,7 @@ extern "C" int gbqv_circuit_reset(gbqv_circuit_t c, const uint64_t *qubits, int 
     op.name = "reset";
     op.qubits = check_q(c, qubits, k);
     c->ops.push_back(std::move(op));
+    ++c->version;
   });
 }
 
@@ -723,6 +736,7 @@ extern "C" int gbqv_circuit_barrier(gbqv_circuit_t c, const uint64_t *qubits, in
     op.name = "barrier";
     op.qubits = check_q(c, qubits, k, 0);
     c->ops.push_back(std::move(op));
+    ++c->version;
   });
 }
 
@@ -781,6 +795,7 @@ extern "C" int gbqv_circuit_bind_param(gbqv_circuit_t c, int op_index, int param
     for (int j = 0; j < nbind; ++j) op.bparams[param_pos + stride * j] = values[j];
     op.params[param_pos] = values[0];
     c->nbind = nbind;
+    ++c->version;
   });
 }
 
@@ -857,6 +872,7 @@ extern "C" int gbqv_circuit_fuse(gbqv_circuit_t c, const gbqv_fusion_config *cfg
       if (s < e) f.cost_based(ops, s, e, m);
     });
     any |= Fusion::compact(c->ops);
+    ++c->version;
     if (applied) *applied = any ? 1 : 0;
   });
 }
@@ -1029,6 +1045,11 @@ bool as_run_op(const Device &d, const Op &op, RunOp &out) {
         out.mat.back() = p.m[0];
         return true;
       }
+      if (p.k == P::MCX) {  // exact swaps inside the tile
+        out.kind = 2;
+        out.qubits = p.q;
+        return true;
+      }
       return false;
     }
     return false;
@@ -1064,7 +1085,7 @@ bool as_run_op(const Device &d, const Op &op, RunOp &out) {
 // Diagonals and 1-2 qubit matrices share a cache-blocked pass; complex128
 // dense matrices that the tensor path takes (padded to 4 qubits) go there.
 bool worth_batching(const Device &d, const RunOp &r) {
-  return r.kind == 1 || (r.qubits.size() <= 2 && !tensor_dense_available(d, (int)r.qubits.size()));
+  return r.kind == 1 || r.kind == 2 || (r.qubits.size() <= 2 && !tensor_dense_available(d, (int)r.qubits.size()));
 }
 
 // Greedy cache-blocking schedule: starting from the first pending op, take
@@ -1198,6 +1219,72 @@ bool prim_run_form(const Prim &p, bool dense_only, RunOp &out) {
   }
 }
 
+// Parameterised gate families whose per-binding matrices are computed
+// directly (the values sv_prim + prim_run_form give, without the name
+// dispatch per binding).
+enum class BF { NONE, MCRX, MCRY, MCRZ, MCP, MCU3, MCU, MCU2, MCR, RXX, RYY, RZZ, RZX };
+
+BF bound_family(const std::string &name) {
+  auto it = sv_gateset().find(name);
+  if (it == sv_gateset().end()) return BF::NONE;
+  static const std::unordered_map<std::string, BF> fam = {
+      {"mcrx", BF::MCRX}, {"mcry", BF::MCRY}, {"mcrz", BF::MCRZ}, {"mcp", BF::MCP}, {"mcu3", BF::MCU3},
+      {"mcu", BF::MCU},   {"mcu2", BF::MCU2}, {"mcr", BF::MCR},   {"rxx", BF::RXX}, {"ryy", BF::RYY},
+      {"rzz", BF::RZZ},   {"rzx", BF::RZX}};
+  auto f = fam.find(it->second);
+  return f == fam.end() ? BF::NONE : f->second;
+}
+
+bool fast_bound_form(const Op &op, int nbind, RunOp &out) {
+  const BF f = bound_family(op.name);
+  if (f == BF::NONE) return false;
+  const size_t k = op.qubits.size(), D = 1ULL << k, stride = op.params.size();
+  if (k == 0 || k > 5) return false;
+  const bool two = f == BF::RXX || f == BF::RYY || f == BF::RZZ || f == BF::RZX;
+  if (two && k != 2) return false;
+  const size_t need = f == BF::MCR || f == BF::MCU2 ? 2 : f == BF::MCU3 ? 3 : f == BF::MCU ? 4 : 1;
+  if (stride < need) return false;
+  const bool diag = f == BF::MCRZ || f == BF::MCP || f == BF::RZZ;
+  out.kind = diag ? 1 : 0;
+  out.qubits = op.qubits;
+  const size_t msz = diag ? D : D * D;
+  std::vector<cd> tmpl = diag ? std::vector<cd>(D, 1.0) : gates::identity(D);
+  out.bmat.resize(msz * nbind);
+  const size_t i0 = (D >> 1) - 1, i1 = D - 1;  // controlled block: every control set
+  for (int j = 0; j < nbind; ++j) {
+    const double *p = op.bparams.data() + (size_t)j * stride;
+    cd *dst = out.bmat.data() + (size_t)j * msz;
+    std::copy(tmpl.begin(), tmpl.end(), dst);
+    gates::mat_t u;
+    switch (f) {
+      case BF::MCRX: u = gates::rx(p[0]); break;
+      case BF::MCRY: u = gates::ry(p[0]); break;
+      case BF::MCRZ: u = gates::rz(p[0]); break;
+      case BF::MCU3: u = gates::u4(p[0], p[1], p[2], 0.); break;
+      case BF::MCU: u = gates::u4(p[0], p[1], p[2], p[3]); break;
+      case BF::MCU2: u = gates::u4(M_PI / 2., p[0], p[1], 0.); break;
+      case BF::MCR: u = gates::r(p[0], p[1]); break;
+      case BF::MCP: dst[D - 1] = std::exp(cd(0, 1) * p[0]); continue;
+      case BF::RXX: u = gates::rxx(p[0]); std::copy(u.begin(), u.end(), dst); continue;
+      case BF::RYY: u = gates::ryy(p[0]); std::copy(u.begin(), u.end(), dst); continue;
+      case BF::RZX: u = gates::rzx(p[0]); std::copy(u.begin(), u.end(), dst); continue;
+      case BF::RZZ: u = gates::rzz_diag(p[0]); std::copy(u.begin(), u.end(), dst); continue;
+      default: return false;
+    }
+    if (diag) {  // controlled rz: diagonal 2x2
+      dst[i0] = u[0];
+      dst[i1] = u[3];
+    } else {
+      dst[i0 + D * i0] = u[0];
+      dst[i1 + D * i0] = u[1];
+      dst[i0 + D * i1] = u[2];
+      dst[i1 + D * i1] = u[3];
+    }
+  }
+  out.mat.assign(out.bmat.begin(), out.bmat.begin() + msz);
+  return true;
+}
+
 // The op's run form over `nbind` bindings: per-binding matrices (bmat) for a
 // gate with bound parameters.  False when it has none (then it must not be
 // bound, and runs on the whole stack through exec_op).
@@ -1210,6 +1297,8 @@ bool bound_run_op(const Op &op, int nbind, RunOp &out) {
   }
   if (op.type != GBQV_OP_GATE) return false;
   if (op.bparams.empty()) return prim_run_form(sv_prim(op), false, out);
+  if (fast_bound_form(op, nbind, out)) return true;
+  out = RunOp{};
   const size_t stride = op.params.size();
   Op b = op;
   b.bparams.clear();
@@ -1238,7 +1327,81 @@ bool bound_run_op(const Op &op, int nbind, RunOp &out) {
   throw Error(GBQV_ERR_KIND, "gate '" + op.name + "' with bound parameters has no per-binding form");
 }
 
-void execute_bound(Device &d, const gbqv_circuit &c, uint64_t first, uint64_t count) {
+// Consecutive 1-qubit dense / diagonal ops on the same qubit (no op on that
+// qubit between them) become one op per binding, their 2x2 product; the
+// kind of fusion Aer's Fusion applies per binding (fusion.hpp:59-101), kept
+// to 1-qubit products so that no binding pays for a wider matrix.
+void merge_one_qubit_runs(int nbind, std::vector<Op> &ops, std::vector<RunOp> &conv, std::vector<char> &runnable) {
+  const size_t nops = ops.size();
+  std::vector<char> gone(nops, 0);
+  std::map<uint64_t, size_t> last;  // qubit -> index of the pending 1-qubit op on it
+  auto is1q = [&](size_t i) { return runnable[i] && conv[i].qubits.size() == 1 && conv[i].kind != 2; };
+  // 2x2 column-major of a 1-qubit run op, binding j
+  auto mat2 = [&](const RunOp &r, int j, cd *m) {
+    const bool b = !r.bmat.empty();
+    const cd *src = b ? r.bmat.data() + (size_t)j * r.mat.size() : r.mat.data();
+    if (r.kind == 1) {
+      m[0] = src[0]; m[1] = 0.0; m[2] = 0.0; m[3] = src[1];
+    } else {
+      std::copy(src, src + 4, m);
+    }
+  };
+  for (size_t k = 0; k < nops; ++k) {
+    if (is1q(k)) {
+      const uint64_t q = conv[k].qubits[0];
+      auto it = last.find(q);
+      if (it != last.end()) {
+        const size_t i = it->second;
+        RunOp &A = conv[i], &Bop = conv[k];
+        const bool both_diag = A.kind == 1 && Bop.kind == 1;
+        const bool bound = !A.bmat.empty() || !Bop.bmat.empty();
+        const int nb = bound ? nbind : 1;
+        RunOp C;
+        C.kind = both_diag ? 1 : 0;
+        C.qubits = Bop.qubits;
+        const size_t msz = both_diag ? 2 : 4;
+        std::vector<cd> out((size_t)nb * msz);
+        for (int j = 0; j < nb; ++j) {
+          cd a[4], b[4];
+          mat2(A, j, a);
+          mat2(Bop, j, b);
+          cd *o = out.data() + (size_t)j * msz;
+          if (both_diag) {
+            o[0] = b[0] * a[0];
+            o[1] = b[3] * a[3];
+          } else {
+            for (int r = 0; r < 2; ++r)
+              for (int cc = 0; cc < 2; ++cc) o[r + 2 * cc] = b[r] * a[2 * cc] + b[r + 2] * a[1 + 2 * cc];
+          }
+        }
+        C.mat.assign(out.begin(), out.begin() + msz);
+        if (bound) C.bmat = std::move(out);
+        conv[k] = std::move(C);
+        gone[i] = 1;
+      }
+      last[q] = k;
+      continue;
+    }
+    const reg_t &qs = runnable[k] ? conv[k].qubits : ops[k].qubits;
+    for (auto x : qs) last.erase(x);
+    if (qs.empty()) last.clear();
+  }
+  size_t w = 0;
+  for (size_t i = 0; i < nops; ++i)
+    if (!gone[i]) {
+      if (w != i) {
+        ops[w] = std::move(ops[i]);
+        conv[w] = std::move(conv[i]);
+        runnable[w] = runnable[i];
+      }
+      ++w;
+    }
+  ops.resize(w);
+  conv.resize(w);
+  runnable.resize(w);
+}
+
+void execute_bound(Device &d, gbqv_circuit &c, uint64_t first, uint64_t count) {
   const int sb = c.num_qubits;
   REQUIRE(!d.density, GBQV_ERR_KIND, "parameter binding runs statevectors only");
   const int nb = std::max(c.nbind, 1);
@@ -1248,24 +1411,31 @@ void execute_bound(Device &d, const gbqv_circuit &c, uint64_t first, uint64_t co
   REQUIRE(d.n >= sb && (d.n - sb) < 63 && (1ULL << (d.n - sb)) >= count, GBQV_ERR_ARG,
           "the state must stack 2^b states of " + std::to_string(sb) + " qubits, 2^b >= " + std::to_string(count) +
               " (state has " + std::to_string(d.n) + " qubits)");
-  std::vector<Op> ops;
-  for (const Op &op : c.ops) {
-    if (op.type == GBQV_OP_BARRIER) continue;
-    REQUIRE(op.type == GBQV_OP_GATE || op.type == GBQV_OP_MATRIX || op.type == GBQV_OP_DIAGONAL, GBQV_ERR_KIND,
-            "op '" + op.name + "' is not unitary: bound execution runs unitary circuits");
-    if (op.type == GBQV_OP_GATE && op.bparams.empty() && sv_prim(op).k == P::NONE) continue;
-    ops.push_back(op);
-  }
-  std::vector<RunOp> conv(ops.size());
-  std::vector<char> runnable(ops.size());
-  for (size_t i = 0; i < ops.size(); ++i) {
-    runnable[i] = bound_run_op(ops[i], nb, conv[i]);
-    REQUIRE(runnable[i] || ops[i].bparams.empty(), GBQV_ERR_KIND,
-            "gate '" + ops[i].name + "' with bound parameters acts on more than 5 qubits");
+  if (c.bound_version != c.version) {  // run forms of every op, once per circuit version
+    std::vector<Op> ops;
+    for (const Op &op : c.ops) {
+      if (op.type == GBQV_OP_BARRIER) continue;
+      REQUIRE(op.type == GBQV_OP_GATE || op.type == GBQV_OP_MATRIX || op.type == GBQV_OP_DIAGONAL, GBQV_ERR_KIND,
+              "op '" + op.name + "' is not unitary: bound execution runs unitary circuits");
+      if (op.type == GBQV_OP_GATE && op.bparams.empty() && sv_prim(op).k == P::NONE) continue;
+      ops.push_back(op);
+    }
+    std::vector<RunOp> conv(ops.size());
+    std::vector<char> runnable(ops.size());
+    for (size_t i = 0; i < ops.size(); ++i) {
+      runnable[i] = bound_run_op(ops[i], nb, conv[i]);
+      REQUIRE(runnable[i] || ops[i].bparams.empty(), GBQV_ERR_KIND,
+              "gate '" + ops[i].name + "' with bound parameters acts on more than 5 qubits");
+    }
+    merge_one_qubit_runs(nb, ops, conv, runnable);
+    c.bound_ops = std::move(ops);
+    c.bound_conv = std::move(conv);
+    c.bound_runnable = std::move(runnable);
+    c.bound_version = c.version;
   }
   RunBound rb{sb, first, count};
   launch_set_basis_segments(d, sb, count);
-  schedule_runs(d, ops, conv, runnable, &rb);
+  schedule_runs(d, c.bound_ops, c.bound_conv, c.bound_runnable, &rb);
 }
 
 }  // namespace

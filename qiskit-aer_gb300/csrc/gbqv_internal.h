@@ -46,7 +46,7 @@ struct Device {
   int nq = 0;           // logical qubits
   bool dbl = true;      // complex128 (true) or complex64 (false)
   bool density = false;
-  int blocking = 1;
+  int blocking = 1;         // 0 one kernel per op, 1 register-tile runs, 2 shared-memory runs
   int tensor_c128 = 1;      // complex128 dense k = 4, 5: 0 FP64 cores, 1 tensor (tcgen05 for k = 4), 2 mma.sync only
   int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up
   // tcgen05 kernel: 128-byte-swizzled TMA descriptors of the state viewed as
@@ -177,6 +177,11 @@ int run_low_qubits(const Device &dev);
 size_t run_pool_bytes(const Device &dev);
 int run_max_ops();
 void launch_run(Device &dev, const std::vector<const RunOp *> &ops, const RunBound *bound = nullptr);
+// The register-tile form of a run (gbqv_runreg.cu), given the tile qubits
+// (ascending) and the length c of their contiguous low prefix; false when the
+// run has an op it does not take or the tile is too small.
+bool launch_run_reg(Device &dev, const std::vector<const RunOp *> &ops, const std::vector<int> &tile_qubits, int c,
+                    const RunBound *bound);
 // Bytes of per-binding matrices one bound run may hold per binding.
 size_t run_bound_pool_bytes(const Device &dev);
 // Every state of a stack of 2^state_bits-amplitude states: |0...0> for the

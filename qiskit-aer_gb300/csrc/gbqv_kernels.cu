@@ -597,17 +597,26 @@ __global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n
 }
 
 // The same per state of a stack of 2^sb-amplitude states (one state per
-// parameter binding): blockIdx.x = state * bps + slice, blockIdx.y = term;
+// parameter binding): blockIdx.y = state, blockIdx.x = term * bps + slice,
+// so that every term of a state runs back to back while the state is in L2;
 // the terms act on qubits below sb.
 template <typename T>
-__global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, int sb, int bps,
-                                                    const TermDev *__restrict__ terms, double *__restrict__ partials) {
-  const TermDev t = terms[blockIdx.y];
+__global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, int sb, int bps, uint64_t nseg,
+                                                    uint64_t seg0, const TermDev *__restrict__ terms,
+                                                    double *__restrict__ partials) {
+  const uint32_t term = blockIdx.x / bps, slice = blockIdx.x % bps;
+  const uint64_t seg = seg0 + blockIdx.y;
+  const TermDev t = terms[term];
   using R = decltype(T::x);
   const R pr = (R)t.ph_re, pi = (R)t.ph_im;
-  const uint64_t seg = blockIdx.x / bps, slice = blockIdx.x % bps;
   const T *ps = psi + (seg << sb);
+  // complex64: short sums in float, then into the double accumulator (the
+  // FP64 add per amplitude would otherwise bound the kernel); complex128:
+  // every value goes into the double accumulator
+  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
   double acc = 0.0;
+  R part = 0;
+  int cnt = 0;
   const uint64_t stride = (uint64_t)bps * blockDim.x;
   if (!t.x_mask) {
     const uint64_t count = 1ULL << sb;
@@ -615,7 +624,8 @@ __global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, i
       const T a = ps[i];
       R v = pr * (a.x * a.x + a.y * a.y);
       if (t.z_mask && (__popcll(i & t.z_mask) & 1)) v = -v;
-      acc += (double)v;
+      part += v;
+      if (++cnt == kChunk) { acc += (double)part; part = 0; cnt = 0; }
     }
   } else {
     const uint64_t count = 1ULL << (sb - 1);
@@ -631,12 +641,13 @@ __global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, i
       R v1 = pr * zr + pi * zi;
       if (t.z_mask && (__popcll(i0 & t.z_mask) & 1)) v0 = -v0;
       if (t.z_mask && (__popcll(i1 & t.z_mask) & 1)) v1 = -v1;
-      acc += (double)v0;
-      acc += (double)v1;
+      part += v0 + v1;
+      if (++cnt == kChunk) { acc += (double)part; part = 0; cnt = 0; }
     }
   }
+  acc += (double)part;
   acc = block_sum(acc);
-  if (threadIdx.x == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = acc;
+  if (threadIdx.x == 0) partials[((size_t)term * nseg + seg) * bps + slice] = acc;
 }
 
 template <typename T>
@@ -1011,20 +1022,21 @@ void reduce_expval_segments(Device &dev, const std::vector<PauliTerm> &terms, in
   const uint64_t want = std::max<uint64_t>(1, (uint64_t)kReduceBlocks / 4 / std::max<uint64_t>(nseg, 1));
   const uint64_t cap = std::max<uint64_t>(1, (1ULL << state_bits) / (2 * 256));
   const int bps = (int)std::min<uint64_t>(std::min<uint64_t>(want, cap), 1024);
-  if (nseg * (uint64_t)bps > 0x7fffffffULL) throw Error(1, "too many states in one expectation-value launch");
   const size_t values = terms.size() * nseg;
   grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * values * bps);
   grow(reinterpret_cast<void *&>(dev.results), dev.results_cap, sizeof(double) * values);
   TermDev *d_terms;
   upload_terms(dev, terms, &d_terms);
-  dim3 grid((unsigned)(nseg * bps), (unsigned)terms.size());
-  if (dev.dbl)
-    k_expval_seg<double2><<<grid, kReduceThreads, 0, dev.stream>>>(st<double2>(dev), state_bits, bps, d_terms,
-                                                                   dev.partials);
-  else
-    k_expval_seg<float2><<<grid, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), state_bits, bps, d_terms,
-                                                                  dev.partials);
-  check_launch("segmented expval kernel");
+  for (uint64_t s0 = 0; s0 < nseg; s0 += 65535) {  // grid y limit
+    dim3 grid((unsigned)(terms.size() * bps), (unsigned)std::min<uint64_t>(65535, nseg - s0));
+    if (dev.dbl)
+      k_expval_seg<double2><<<grid, kReduceThreads, 0, dev.stream>>>(st<double2>(dev), state_bits, bps, nseg, s0,
+                                                                     d_terms, dev.partials);
+    else
+      k_expval_seg<float2><<<grid, kReduceThreads, 0, dev.stream>>>(st<float2>(dev), state_bits, bps, nseg, s0,
+                                                                    d_terms, dev.partials);
+    check_launch("segmented expval kernel");
+  }
   finish(dev, (int)values, bps);
 }
 
@@ -1707,6 +1719,7 @@ void launch_run_t(Device &dev, const std::vector<const RunOp *> &ops, const RunB
   // cc = length of the contiguous low prefix of the tile qubits
   int cc = 0;
   while (cc < m && tq[cc] == cc) ++cc;
+  if (dev.blocking != 2 && launch_run_reg(dev, ops, tq, cc, bound)) return;
   P->m = m;
   P->c = cc;
   P->nt = m;

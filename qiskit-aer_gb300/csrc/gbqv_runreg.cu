@@ -1,0 +1,662 @@
+// gbqv_runreg.cu — cache-blocked runs with the tile held in registers.
+//
+// A run (a sequence of 1-2 qubit dense ops, diagonals and multi-controlled
+// X gates whose qubits all lie in one tile of m vector qubits) costs one
+// HBM read and one write of the state.  Inside the tile the ops used to
+// sweep shared memory one by one with a barrier between them; here each of
+// the 512 threads holds 2^(m-9) amplitudes of the tile in registers.  The m
+// tile bits are split into register bits (the thread's own amplitudes) and
+// 9 thread bits; an op whose dense qubits are register bits is applied in
+// registers, a 1-qubit dense op or an X target on one of the 5 lane bits is
+// applied with warp shuffles, diagonals and controls may sit on any bit.
+// When an op needs a bit that is neither, the tile is re-laid out once
+// through shared memory (a "segment" boundary) so that its bits become
+// register bits; the host picks each segment's register bits by next use.
+// Arithmetic per op is that of the shared-memory run kernel (the same
+// products; a lane op sums its two terms in the order own, partner).
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "gbqv_internal.h"
+
+namespace gbqv {
+namespace {
+
+constexpr int kRegThreads = 512;  // 9 thread bits: one CTA per SM, 128 registers a thread
+constexpr int kThreadBits = 9;
+constexpr int kRegMaxOps = 24;
+constexpr int kRegMaxSegs = kRegMaxOps + 1;
+
+enum RegKind : int {
+  RK_DENSE1 = 0,       // 1-qubit dense, target on register bit a
+  RK_DENSE1_REAL = 1,  // the same with a real matrix (every binding)
+  RK_DENSE1_LANE = 2,  // 1-qubit dense, target on lane bit a
+  RK_DENSE2 = 3,       // 2-qubit dense on register bits a < b (matrix bit 0 <-> a)
+  RK_DIAG1 = 4,        // 1-qubit diagonal on register bit a
+  RK_DIAG = 5,         // diagonal on any bits
+  RK_MCX = 6,          // multi-controlled X, target on register bit a
+  RK_MCX_LANE = 7,     // multi-controlled X, target on lane bit a
+  RK_DIAG_T = 8,       // diagonal whose qubits are all thread bits: one factor per thread
+  RK_DENSE1_REAL_LANE = 9,  // RK_DENSE1_LANE with a real matrix
+};
+
+struct RegOp {
+  int kind, k, a, b;
+  int bound, mat_off;   // matrix in the per-binding block (bound) or the shared pool
+  uint32_t ctm, crm;    // X controls: bits of the thread index / of the register index
+  int8_t dtpos[5];      // diagonal: thread-bit position of op qubit j, -1 on a register bit
+  uint8_t div[32];      // diagonal: index bits that register i contributes
+};
+
+struct RegSeg {
+  int first, count;     // ops [first, first + count)
+  uint16_t rp[32];      // tile index bits of register i
+  uint8_t tb[16];       // tile bit held by thread-index bit q (q < 9)
+};
+static_assert(sizeof(RegSeg) % 8 == 0 && sizeof(RegOp) % 8 == 0, "shared-memory layout keeps 8-byte alignment");
+
+struct RegParams {
+  int m, c, rb, nops, nsegs, pool_elems, bound_elems, state_bits;
+  uint64_t nbind, ntiles;
+  uint64_t tile_lowmask[kMaxQubits];
+  int T[24];
+  RegOp ops[kRegMaxOps];
+  RegSeg segs[kRegMaxSegs];
+};
+
+template <typename T>
+__device__ __forceinline__ T cmul(T a, T b) {
+  T r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ void cfma(T &acc, T a, T b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+template <typename T>
+__device__ __forceinline__ T czero() {
+  T z;
+  z.x = 0;
+  z.y = 0;
+  return z;
+}
+template <typename T>
+__device__ __forceinline__ T shfl_x(T v, int mask) {
+  T r;
+  r.x = __shfl_xor_sync(0xffffffffu, v.x, mask);
+  r.y = __shfl_xor_sync(0xffffffffu, v.y, mask);
+  return r;
+}
+
+// ---- ops on the register-held amplitudes v[0..R) ----
+template <typename T, int R, int J>
+__device__ __forceinline__ void reg_dense1(T (&v)[R], const T *m) {
+  const T m00 = m[0], m10 = m[1], m01 = m[2], m11 = m[3];
+#pragma unroll
+  for (int p = 0; p < R / 2; ++p) {
+    const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
+    const T a0 = v[i0], a1 = v[i1];
+    T r0 = czero<T>(), r1 = czero<T>();
+    cfma(r0, m00, a0);
+    cfma(r0, m01, a1);
+    cfma(r1, m10, a0);
+    cfma(r1, m11, a1);
+    v[i0] = r0;
+    v[i1] = r1;
+  }
+}
+// real matrix: the complex FMAs above with every imaginary matrix term zero
+template <typename T, int R, int J>
+__device__ __forceinline__ void reg_dense1_real(T (&v)[R], const T *m) {
+  const auto m00 = m[0].x, m10 = m[1].x, m01 = m[2].x, m11 = m[3].x;
+#pragma unroll
+  for (int p = 0; p < R / 2; ++p) {
+    const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
+    const T a0 = v[i0], a1 = v[i1];
+    T r0, r1;
+    r0.x = fma(m01, a1.x, m00 * a0.x);
+    r0.y = fma(m01, a1.y, m00 * a0.y);
+    r1.x = fma(m11, a1.x, m10 * a0.x);
+    r1.y = fma(m11, a1.y, m10 * a0.y);
+    v[i0] = r0;
+    v[i1] = r1;
+  }
+}
+template <typename T, int R, int J>
+__device__ __forceinline__ void reg_diag1(T (&v)[R], const T *d) {
+  const T d0 = d[0], d1 = d[1];
+#pragma unroll
+  for (int i = 0; i < R; ++i) v[i] = cmul(v[i], ((i >> J) & 1) ? d1 : d0);
+}
+template <typename T, int R, int J>
+__device__ __forceinline__ void reg_mcx(T (&v)[R], bool tcond, uint32_t crm) {
+#pragma unroll
+  for (int p = 0; p < R / 2; ++p) {
+    const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
+    const bool sw = tcond && (((uint32_t)i0 & crm) == crm);
+    const T a0 = v[i0], a1 = v[i1];
+    v[i0] = sw ? a1 : a0;
+    v[i1] = sw ? a0 : a1;
+  }
+}
+template <typename T, int R, int A, int B>
+__device__ __forceinline__ void reg_dense2(T (&v)[R], const T *m) {
+#pragma unroll
+  for (int q = 0; q < R / 4; ++q) {
+    // insert zeros at A then B (A < B)
+    int i = ((q >> A) << (A + 1)) | (q & ((1 << A) - 1));
+    i = ((i >> B) << (B + 1)) | (i & ((1 << B) - 1));
+    const int idx[4] = {i, i | (1 << A), i | (1 << B), i | (1 << A) | (1 << B)};
+    T x[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) x[c] = v[idx[c]];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      T acc = czero<T>();
+#pragma unroll
+      for (int c = 0; c < 4; ++c) cfma(acc, m[r + 4 * c], x[c]);
+      v[idx[r]] = acc;
+    }
+  }
+}
+
+template <typename T, int R, int A>
+__device__ __forceinline__ void dense2_b(T (&v)[R], const T *m, int b) {
+  constexpr int RB = R == 32 ? 5 : R == 16 ? 4 : R == 8 ? 3 : 2;
+  switch (b) {
+    case 1: if constexpr (A < 1 && 1 < RB) reg_dense2<T, R, A, 1>(v, m); break;
+    case 2: if constexpr (A < 2 && 2 < RB) reg_dense2<T, R, A, 2>(v, m); break;
+    case 3: if constexpr (A < 3 && 3 < RB) reg_dense2<T, R, A, 3>(v, m); break;
+    case 4: if constexpr (A < 4 && 4 < RB) reg_dense2<T, R, A, 4>(v, m); break;
+    default: break;
+  }
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void apply_reg_op(T (&v)[R], const RegOp &op, const T *mat, int tid) {
+  constexpr int RB = R == 32 ? 5 : R == 16 ? 4 : R == 8 ? 3 : 2;
+  const int lane = tid & 31;
+  switch (op.kind) {
+    case RK_DENSE1:
+    case RK_DENSE1_REAL:
+    case RK_DIAG1:
+    case RK_MCX: {
+      const bool tcond = ((uint32_t)tid & op.ctm) == op.ctm;
+#define GBQV_REG_CASE(J)                                                    \
+  case J:                                                                   \
+    if constexpr (J < RB) {                                                 \
+      if (op.kind == RK_DENSE1) reg_dense1<T, R, J>(v, mat);                \
+      else if (op.kind == RK_DENSE1_REAL) reg_dense1_real<T, R, J>(v, mat); \
+      else if (op.kind == RK_DIAG1) reg_diag1<T, R, J>(v, mat);             \
+      else reg_mcx<T, R, J>(v, tcond, op.crm);                              \
+    }                                                                       \
+    break;
+      switch (op.a) {
+        GBQV_REG_CASE(0)
+        GBQV_REG_CASE(1)
+        GBQV_REG_CASE(2)
+        GBQV_REG_CASE(3)
+        GBQV_REG_CASE(4)
+        default: break;
+      }
+#undef GBQV_REG_CASE
+      return;
+    }
+    case RK_DENSE2:
+      switch (op.a) {
+        case 0: dense2_b<T, R, 0>(v, mat, op.b); break;
+        case 1: dense2_b<T, R, 1>(v, mat, op.b); break;
+        case 2: dense2_b<T, R, 2>(v, mat, op.b); break;
+        case 3: dense2_b<T, R, 3>(v, mat, op.b); break;
+        default: break;
+      }
+      return;
+    case RK_DENSE1_LANE: {
+      // this lane holds row `bit` of the pair: new = m[bit][bit] * own + m[bit][1-bit] * partner's
+      const int bit = (lane >> op.a) & 1;
+      const T ms = bit ? mat[3] : mat[0], mo = bit ? mat[1] : mat[2];
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const T o = shfl_x(v[i], 1 << op.a);
+        T r = czero<T>();
+        cfma(r, ms, v[i]);
+        cfma(r, mo, o);
+        v[i] = r;
+      }
+      return;
+    }
+    case RK_DENSE1_REAL_LANE: {
+      const int bit = (lane >> op.a) & 1;
+      const auto ms = bit ? mat[3].x : mat[0].x, mo = bit ? mat[1].x : mat[2].x;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const T o = shfl_x(v[i], 1 << op.a);
+        T r;
+        r.x = fma(mo, o.x, ms * v[i].x);
+        r.y = fma(mo, o.y, ms * v[i].y);
+        v[i] = r;
+      }
+      return;
+    }
+    case RK_DIAG_T: {
+      uint32_t td = 0;
+      for (int j = 0; j < op.k; ++j) td |= (((uint32_t)tid >> op.dtpos[j]) & 1u) << j;
+      const T d = mat[td];
+#pragma unroll
+      for (int i = 0; i < R; ++i) v[i] = cmul(v[i], d);
+      return;
+    }
+    case RK_MCX_LANE: {
+      const bool tcond = ((uint32_t)tid & op.ctm) == op.ctm;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const T o = shfl_x(v[i], 1 << op.a);
+        if (tcond && (((uint32_t)i & op.crm) == op.crm)) v[i] = o;
+      }
+      return;
+    }
+    case RK_DIAG: {
+      uint32_t td = 0;
+      for (int j = 0; j < op.k; ++j)
+        if (op.dtpos[j] >= 0) td |= (((uint32_t)tid >> op.dtpos[j]) & 1u) << j;
+#pragma unroll
+      for (int i = 0; i < R; ++i) v[i] = cmul(v[i], mat[td | op.div[i]]);
+      return;
+    }
+    default: return;
+  }
+}
+
+// 16-byte asynchronous global -> shared copies (LDGSTS): the next tile
+// streams in while the current one is computed.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ uint64_t tile_base(uint64_t t, const uint64_t *lowmask, int m) {
+  for (int j = 0; j < m; ++j) {
+    const uint64_t msk = lowmask[j];
+    t = ((t & ~msk) << 1) | (t & msk);
+  }
+  return t;
+}
+
+// Two tile buffers: tile t + gridDim.x is fetched with cp.async into one while
+// tile t is computed in registers (and re-laid out) through the other.
+template <typename T, int RB>
+__global__ void __launch_bounds__(kRegThreads, 1) k_run_reg(T *__restrict__ psi, const RegParams *__restrict__ P,
+                                                           const T *__restrict__ pool, const T *__restrict__ bpool) {
+  constexpr int R = 1 << RB;
+  constexpr uint32_t kPer = 16 / sizeof(T);  // amplitudes per 16-byte copy
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = P->m, c = P->c, nsegs = P->nsegs, nops = P->nops;
+  const int tid = threadIdx.x;
+  const uint32_t L = 1u << m, cmask = (1u << c) - 1;
+  T *buf0 = reinterpret_cast<T *>(smem_raw);
+  T *buf1 = buf0 + L;
+  T *mats = buf1 + L;
+  T *bmats = mats + P->pool_elems;
+  RegOp *ops = reinterpret_cast<RegOp *>(bmats + P->bound_elems);
+  RegSeg *segs = reinterpret_cast<RegSeg *>(ops + nops);
+  uint64_t *hi = reinterpret_cast<uint64_t *>((reinterpret_cast<uintptr_t>(segs + nsegs) + 7) & ~uintptr_t(7));
+  for (int i = tid; i < P->pool_elems; i += kRegThreads) mats[i] = pool[i];
+  {
+    const int *src = reinterpret_cast<const int *>(P->ops);
+    int *dst = reinterpret_cast<int *>(ops);
+    for (int i = tid; i < nops * (int)(sizeof(RegOp) / 4); i += kRegThreads) dst[i] = src[i];
+    src = reinterpret_cast<const int *>(P->segs);
+    dst = reinterpret_cast<int *>(segs);
+    for (int i = tid; i < nsegs * (int)(sizeof(RegSeg) / 4); i += kRegThreads) dst[i] = src[i];
+  }
+  const uint32_t nhi = 1u << (m - c);
+  for (uint32_t h = tid; h < nhi; h += kRegThreads) {
+    uint64_t a = 0;
+    for (int j = c; j < m; ++j)
+      if ((h >> (j - c)) & 1) a |= 1ULL << P->T[j];
+    hi[h] = a;
+  }
+  __syncthreads();
+  const bool bound = P->bound_elems > 0;
+  // a padding state of a bound stack is neither read nor written
+  auto skip = [&](uint64_t gb) { return bound && (gb >> P->state_bits) >= P->nbind; };
+  auto fetch = [&](uint64_t t, T *buf) {
+    const uint64_t gb = tile_base(t, P->tile_lowmask, m);
+    if (skip(gb)) return;
+    for (uint32_t ch = tid; ch < L / kPer; ch += kRegThreads) {
+      const uint32_t l = ch * kPer;  // kPer consecutive tile indices: consecutive amplitudes (c >= 4)
+      cp_async16(buf + l, psi + (gb | hi[l >> c] | (l & cmask)));
+    }
+  };
+  uint64_t t = blockIdx.x;
+  if (t < P->ntiles) fetch(t, buf0);
+  cp_async_commit();
+  for (int k = 0; t < P->ntiles; t += gridDim.x, ++k) {
+    T *tile = (k & 1) ? buf1 : buf0;
+    if (t + gridDim.x < P->ntiles) fetch(t + gridDim.x, (k & 1) ? buf0 : buf1);
+    cp_async_commit();
+    cp_async_wait<1>();  // this tile's copies (all but the group just issued)
+    __syncthreads();
+    const uint64_t gbase = tile_base(t, P->tile_lowmask, m);
+    if (skip(gbase)) continue;  // same value in every thread of the CTA
+    if (bound) {
+      const T *src = bpool + (gbase >> P->state_bits) * (uint64_t)P->bound_elems;
+      for (int i = tid; i < P->bound_elems; i += kRegThreads) bmats[i] = src[i];
+      __syncthreads();
+    }
+    T v[R];
+    uint32_t tpart = 0;
+    for (int s = 0; s < nsegs; ++s) {
+      const RegSeg &S = segs[s];
+      if (s > 0) {
+        const RegSeg &Sp = segs[s - 1];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < R; ++i) tile[tpart | Sp.rp[i]] = v[i];
+        __syncthreads();
+      }
+      tpart = 0;
+#pragma unroll
+      for (int q = 0; q < kThreadBits; ++q) tpart |= (((uint32_t)tid >> q) & 1u) << S.tb[q];
+#pragma unroll
+      for (int i = 0; i < R; ++i) v[i] = tile[tpart | S.rp[i]];
+      for (int o = S.first; o < S.first + S.count; ++o) {
+        const RegOp &op = ops[o];
+        apply_reg_op<T, R>(v, op, (op.bound ? bmats : mats) + op.mat_off, tid);
+      }
+    }
+    {
+      const RegSeg &Sl = segs[nsegs - 1];
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < R; ++i) tile[tpart | Sl.rp[i]] = v[i];
+    }
+    __syncthreads();
+    for (uint32_t l = tid; l < L; l += kRegThreads) psi[gbase | hi[l >> c] | (l & cmask)] = tile[l];
+    __syncthreads();  // the buffer is fetched into again two tiles later; bmats are rewritten next tile
+  }
+  cp_async_wait<0>();
+}
+
+template <typename T> T to_dev(const cd &z);
+template <> double2 to_dev<double2>(const cd &z) { return make_double2(z.real(), z.imag()); }
+template <> float2 to_dev<float2>(const cd &z) { return make_float2((float)z.real(), (float)z.imag()); }
+
+// dense 2-qubit matrix with its two index bits exchanged
+std::vector<cd> swap_bits2(const cd *m) {
+  static const int s[4] = {0, 2, 1, 3};
+  std::vector<cd> o(16);
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) o[s[r] + 4 * s[c]] = m[r + 4 * c];
+  return o;
+}
+
+template <typename T, int RB>
+void launch_reg_t(Device &dev, RegParams &P, const std::vector<T> &pool, const std::vector<T> &bpool) {
+  const size_t pbytes = sizeof(RegParams), poolb = pool.size() * sizeof(T), bpoolb = bpool.size() * sizeof(T);
+  const size_t pool_off = (pbytes + 255) & ~size_t(255);
+  const size_t bpool_off = (pool_off + poolb + 255) & ~size_t(255);
+  grow(dev.mat, dev.mat_cap, bpool_off + bpoolb + 256);
+  char *base = reinterpret_cast<char *>(dev.mat);
+  cuda_check(cudaMemcpyAsync(base, &P, pbytes, cudaMemcpyHostToDevice, dev.stream), "run upload");
+  if (poolb)
+    cuda_check(cudaMemcpyAsync(base + pool_off, pool.data(), poolb, cudaMemcpyHostToDevice, dev.stream), "run upload");
+  if (bpoolb)
+    cuda_check(cudaMemcpyAsync(base + bpool_off, bpool.data(), bpoolb, cudaMemcpyHostToDevice, dev.stream),
+               "run upload");
+  size_t smem = sizeof(T) * (2 * (1u << P.m) + pool.size() + (size_t)P.bound_elems);
+  smem += sizeof(RegOp) * P.nops + sizeof(RegSeg) * P.nsegs;
+  smem = (smem + 7) & ~size_t(7);
+  smem += sizeof(uint64_t) * (1u << (P.m - P.c));
+  static bool attr_set = false;
+  if (!attr_set) {
+    cuda_check(cudaFuncSetAttribute(k_run_reg<T, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+               "run kernel attribute");
+    attr_set = true;
+  }
+  int per_sm = 0;
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run_reg<T, RB>, kRegThreads, smem),
+             "occupancy");
+  per_sm = std::max(per_sm, 1);
+  const uint64_t grid = std::min<uint64_t>(P.ntiles, (uint64_t)sm_count() * per_sm);
+  k_run_reg<T, RB><<<(unsigned)grid, kRegThreads, smem, dev.stream>>>(
+      reinterpret_cast<T *>(dev.state), reinterpret_cast<const RegParams *>(base),
+      reinterpret_cast<const T *>(base + pool_off), reinterpret_cast<const T *>(base + bpool_off));
+  check_launch("run kernel");
+}
+
+// Register bits for a new segment: `need` plus the tile bits whose next use
+// as a dense / X-target bit comes soonest (ties: higher bits first, so low
+// bits stay thread bits and shared-memory accesses stay contiguous).
+std::vector<int> choose_regs(const std::vector<int> &need, int rb, int m,
+                             const std::vector<std::vector<int>> &dense_bits, size_t from) {
+  std::vector<int> regs = need;
+  std::vector<std::pair<size_t, int>> cand;
+  for (int b = 0; b < m; ++b) {
+    if (std::find(regs.begin(), regs.end(), b) != regs.end()) continue;
+    size_t next = SIZE_MAX;
+    for (size_t o = from; o < dense_bits.size() && next == SIZE_MAX; ++o)
+      if (std::find(dense_bits[o].begin(), dense_bits[o].end(), b) != dense_bits[o].end()) next = o;
+    cand.push_back({next, -b});
+  }
+  std::sort(cand.begin(), cand.end());
+  for (auto &cb : cand) {
+    if ((int)regs.size() >= rb) break;
+    regs.push_back(-cb.second);
+  }
+  return regs;
+}
+
+}  // namespace
+
+// A run on the register-tile kernel; false when the run has an op it does
+// not take (a dense op on more than 2 qubits) or the tile is too small.
+bool launch_run_reg(Device &dev, const std::vector<const RunOp *> &ops, const std::vector<int> &tile_qubits, int c,
+                    const RunBound *bound) {
+  const int m = (int)tile_qubits.size();
+  const int rb = m - kThreadBits;
+  const int maxrb = dev.dbl ? 3 : 4;
+  if (rb < 2 || rb > maxrb || (int)ops.size() > kRegMaxOps || ops.empty()) return false;
+  for (const RunOp *op : ops) {
+    if (op->kind == 0 && op->qubits.size() > 2) return false;
+    if (op->qubits.size() > 5) return false;
+  }
+  const int n = dev.n;
+  std::vector<int> local(n, -1);
+  for (int j = 0; j < m; ++j) local[tile_qubits[j]] = j;
+  // per op: local qubits, and the bits it needs as register bits (dense qubits, X target)
+  std::vector<std::vector<int>> lq(ops.size()), dense_bits(ops.size());
+  for (size_t o = 0; o < ops.size(); ++o) {
+    for (auto q : ops[o]->qubits) lq[o].push_back(local[q]);
+    if (ops[o]->kind == 0) dense_bits[o] = lq[o];
+    if (ops[o]->kind == 2) dense_bits[o] = {lq[o].back()};
+  }
+  auto thread_bits = [&](const std::vector<int> &regs) {
+    std::vector<int> tb;
+    for (int b = 0; b < m; ++b)
+      if (std::find(regs.begin(), regs.end(), b) == regs.end()) tb.push_back(b);
+    return tb;  // ascending: thread-index bit q holds tile bit tb[q]
+  };
+  // segments: one set of register bits each
+  std::vector<std::vector<int>> seg_regs;
+  std::vector<std::vector<size_t>> seg_ops;
+  std::vector<int> regs = choose_regs(dense_bits[0], rb, m, dense_bits, 0);
+  seg_regs.push_back(regs);
+  seg_ops.push_back({});
+  for (size_t o = 0; o < ops.size(); ++o) {
+    const std::vector<int> tb = thread_bits(regs);
+    bool ok = true;
+    for (int b : dense_bits[o]) {
+      const bool in_reg = std::find(regs.begin(), regs.end(), b) != regs.end();
+      const int tpos = (int)(std::find(tb.begin(), tb.end(), b) - tb.begin());
+      const bool lane_ok = dense_bits[o].size() == 1 && tpos < 5;  // 1-qubit dense / X target on a lane bit
+      if (!in_reg && !lane_ok) ok = false;
+    }
+    if (!ok) {
+      regs = choose_regs(dense_bits[o], rb, m, dense_bits, o + 1);
+      seg_regs.push_back(regs);
+      seg_ops.push_back({});
+    }
+    seg_ops.back().push_back(o);
+  }
+  auto P = std::make_unique<RegParams>();
+  std::memset(P.get(), 0, sizeof(RegParams));
+  P->m = m;
+  P->c = c;
+  P->rb = rb;
+  P->nops = (int)ops.size();
+  P->nsegs = (int)seg_regs.size();
+  P->ntiles = 1ULL << (n - m);
+  for (int j = 0; j < m; ++j) {
+    P->T[j] = tile_qubits[j];
+    P->tile_lowmask[j] = (1ULL << tile_qubits[j]) - 1;
+  }
+  using HostMat = std::vector<cd>;
+  std::vector<HostMat> op_mat(ops.size()), op_bmat(ops.size());
+  int bound_elems = 0, pool_elems = 0;
+  size_t oi = 0;
+  for (size_t s = 0; s < seg_regs.size(); ++s) {
+    const std::vector<int> &rg = seg_regs[s];
+    const std::vector<int> tb = thread_bits(rg);
+    RegSeg &S = P->segs[s];
+    S.first = (int)oi;
+    S.count = (int)seg_ops[s].size();
+    for (int i = 0; i < (1 << rb); ++i) {
+      uint32_t a = 0;
+      for (int p = 0; p < rb; ++p)
+        if ((i >> p) & 1) a |= 1u << rg[p];
+      S.rp[i] = (uint16_t)a;
+    }
+    for (int q = 0; q < kThreadBits; ++q) S.tb[q] = (uint8_t)tb[q];
+    auto rpos = [&](int b) { return (int)(std::find(rg.begin(), rg.end(), b) - rg.begin()); };
+    auto tpos = [&](int b) { return (int)(std::find(tb.begin(), tb.end(), b) - tb.begin()); };
+    for (size_t o : seg_ops[s]) {
+      const RunOp &op = *ops[o];
+      RegOp &d = P->ops[oi++];
+      const int k = (int)lq[o].size();
+      d.k = k;
+      d.bound = !op.bmat.empty();
+      op_mat[o] = op.mat;
+      op_bmat[o] = op.bmat;
+      if (op.kind == 0 && k == 1) {
+        const int b = lq[o][0];
+        bool real = true;
+        for (const cd &z : op.mat) real &= z.imag() == 0.0;
+        for (const cd &z : op.bmat) real &= z.imag() == 0.0;
+        if (rpos(b) < rb) {
+          d.kind = real ? RK_DENSE1_REAL : RK_DENSE1;
+          d.a = rpos(b);
+        } else {
+          d.kind = real ? RK_DENSE1_REAL_LANE : RK_DENSE1_LANE;
+          d.a = tpos(b);
+        }
+      } else if (op.kind == 0) {  // k == 2
+        int a = rpos(lq[o][0]), b = rpos(lq[o][1]);
+        if (a > b) {
+          std::swap(a, b);
+          op_mat[o] = swap_bits2(op.mat.data());
+          if (!op.bmat.empty()) {
+            HostMat bm(op.bmat.size());
+            for (size_t j = 0; j < op.bmat.size() / 16; ++j) {
+              HostMat t = swap_bits2(op.bmat.data() + 16 * j);
+              std::copy(t.begin(), t.end(), bm.begin() + 16 * j);
+            }
+            op_bmat[o] = bm;
+          }
+        }
+        d.kind = RK_DENSE2;
+        d.a = a;
+        d.b = b;
+      } else if (op.kind == 1) {
+        if (k == 1 && rpos(lq[o][0]) < rb) {
+          d.kind = RK_DIAG1;
+          d.a = rpos(lq[o][0]);
+        } else {
+          bool thread_only = true;
+          for (int j = 0; j < k; ++j) thread_only &= rpos(lq[o][j]) >= rb;
+          d.kind = thread_only ? RK_DIAG_T : RK_DIAG;
+          for (int j = 0; j < k; ++j) d.dtpos[j] = (int8_t)(rpos(lq[o][j]) < rb ? -1 : tpos(lq[o][j]));
+          for (int i = 0; i < (1 << rb); ++i) {
+            uint32_t x = 0;
+            for (int j = 0; j < k; ++j)
+              if (rpos(lq[o][j]) < rb) x |= (uint32_t)((i >> rpos(lq[o][j])) & 1) << j;
+            d.div[i] = (uint8_t)x;
+          }
+        }
+      } else {  // multi-controlled X
+        const int tq = lq[o].back();
+        if (rpos(tq) < rb) {
+          d.kind = RK_MCX;
+          d.a = rpos(tq);
+        } else {
+          d.kind = RK_MCX_LANE;
+          d.a = tpos(tq);
+        }
+        for (int j = 0; j + 1 < k; ++j) {
+          const int b = lq[o][j];
+          if (rpos(b) < rb)
+            d.crm |= 1u << rpos(b);
+          else
+            d.ctm |= 1u << tpos(b);
+        }
+      }
+      if (op.kind != 2) {
+        d.mat_off = d.bound ? bound_elems : pool_elems;
+        (d.bound ? bound_elems : pool_elems) += (int)op.mat.size();
+      }
+    }
+  }
+  P->pool_elems = pool_elems;
+  P->bound_elems = bound_elems;
+  // matrices in op order, as the offsets above
+  auto fill = [&](auto tag) {
+    using T = decltype(tag);
+    std::vector<T> pool, bpool;
+    std::vector<size_t> order;
+    for (size_t s = 0; s < seg_ops.size(); ++s)
+      for (size_t o : seg_ops[s]) order.push_back(o);
+    for (size_t o : order)
+      if (ops[o]->kind != 2 && op_bmat[o].empty())
+        for (const cd &z : op_mat[o]) pool.push_back(to_dev<T>(z));
+    if (bound_elems) {
+      P->state_bits = bound->state_bits;
+      P->nbind = bound->count;
+      bpool.reserve((size_t)bound_elems * bound->count);
+      for (uint64_t j = 0; j < bound->count; ++j)
+        for (size_t o : order) {
+          if (op_bmat[o].empty()) continue;
+          const size_t msz = op_mat[o].size();
+          if (op_bmat[o].size() < (bound->first + j + 1) * msz) throw Error(1, "bound run op has too few bindings");
+          const cd *src = op_bmat[o].data() + (bound->first + j) * msz;
+          for (size_t e = 0; e < msz; ++e) bpool.push_back(to_dev<T>(src[e]));
+        }
+    }
+    switch (rb) {
+      case 2: launch_reg_t<T, 2>(dev, *P, pool, bpool); break;
+      case 3: launch_reg_t<T, 3>(dev, *P, pool, bpool); break;
+      case 4:
+        if constexpr (sizeof(T) == 8) launch_reg_t<T, 4>(dev, *P, pool, bpool);
+        break;
+      default: break;
+    }
+  };
+  if (bound_elems && !bound) throw Error(1, "bound run op outside a bound run");
+  if (dev.dbl)
+    fill(double2{});
+  else
+    fill(float2{});
+  return true;
+}
+
+}  // namespace gbqv
