@@ -64,7 +64,13 @@ enum gbqv_status {
 };
 
 enum gbqv_precision { GBQV_C64 = 0, GBQV_C128 = 1 };
-enum gbqv_kind { GBQV_STATEVECTOR = 0, GBQV_DENSITY_MATRIX = 1 };
+/* GBQV_UNITARY: QV::UnitaryMatrix<T> (src/simulators/unitary/unitarymatrix.hpp),
+ * the state of the unitary method: a 2^n x 2^n matrix stored column-major as
+ * a vector of 2n qubits (row bits 0..n-1, column bits n..2n-1), starting as
+ * the identity (UnitaryMatrix::initialize, unitarymatrix.hpp:236-247).  Gates
+ * on qubits 0..n-1 give U <- G U (QubitUnitary::State::apply_gate,
+ * unitary_state.hpp:414-545); copy_to_host returns the 4^n entries. */
+enum gbqv_kind { GBQV_STATEVECTOR = 0, GBQV_DENSITY_MATRIX = 1, GBQV_UNITARY = 2 };
 
 /* Rotation axes, QV::Rotation (qubitvector.hpp:50-59). */
 enum gbqv_rotation {

@@ -15,7 +15,7 @@ from ._capi import GBQVError, lib
 from .circuit import NativeCircuit, Parameter, ParameterExpression, QuantumCircuit
 from .noise import (NoiseModel, QuantumError, amplitude_damping_error, depolarizing_error,
                     phase_amplitude_damping_error)
-from .qubitvector import DensityMatrix, QubitVector
+from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
 from .simulator import AerSimulator, Result, uniforms
 from . import adjoint, batched
 from .primitives import EstimatorV2
@@ -23,7 +23,7 @@ from .primitives import EstimatorV2
 __all__ = [
     "AerSimulator", "adjoint", "batched", "DensityMatrix", "EstimatorV2", "GBQVError", "NativeCircuit", "NoiseModel",
     "Parameter", "ParameterExpression", "QuantumCircuit",
-    "QuantumError", "QubitVector", "Result", "amplitude_damping_error", "depolarizing_error", "lib",
+    "QuantumError", "QubitVector", "Result", "UnitaryMatrix", "amplitude_damping_error", "depolarizing_error", "lib",
     "phase_amplitude_damping_error", "uniforms",
 ]
 

@@ -16,7 +16,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libgbqv.so"
 GBQV_OK = 0
 ERRORS = {1: "argument", 2: "qubit", 3: "cuda", 4: "allocation", 5: "kind", 6: "timeout"}
 C64, C128 = 0, 1
-STATEVECTOR, DENSITY_MATRIX = 0, 1
+STATEVECTOR, DENSITY_MATRIX, UNITARY = 0, 1, 2
 
 
 class GBQVError(RuntimeError):

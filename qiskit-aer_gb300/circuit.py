@@ -263,6 +263,10 @@ class QuantumCircuit:
         self.data.append(Instruction("save", "density_matrix", [], data=label))
         return self
 
+    def save_unitary(self, label="unitary"):
+        self.data.append(Instruction("save", "unitary", [], data=label))
+        return self
+
     def save_probabilities(self, qubits=None, label="probabilities"):
         q = list(range(self.num_qubits)) if qubits is None else [int(x) for x in qubits]
         self.data.append(Instruction("save", "probabilities", q, data=label))

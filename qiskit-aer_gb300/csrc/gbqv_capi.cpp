@@ -270,8 +270,9 @@ extern "C" int gbqv_create(int num_qubits, int precision, int kind, gbqv_handle 
     REQUIRE(out, GBQV_ERR_ARG, "null output handle");
     *out = nullptr;
     REQUIRE(precision == GBQV_C64 || precision == GBQV_C128, GBQV_ERR_ARG, "precision must be GBQV_C64 or GBQV_C128");
-    REQUIRE(kind == GBQV_STATEVECTOR || kind == GBQV_DENSITY_MATRIX, GBQV_ERR_ARG, "unknown state kind");
-    const int nvec = kind == GBQV_DENSITY_MATRIX ? 2 * num_qubits : num_qubits;
+    REQUIRE(kind == GBQV_STATEVECTOR || kind == GBQV_DENSITY_MATRIX || kind == GBQV_UNITARY, GBQV_ERR_ARG,
+            "unknown state kind");
+    const int nvec = kind == GBQV_STATEVECTOR ? num_qubits : 2 * num_qubits;
     REQUIRE(num_qubits >= 1 && nvec <= kMaxQubits, GBQV_ERR_ARG,
             "number of qubits out of range: " + std::to_string(num_qubits));
     int ndev = 0;
@@ -283,6 +284,7 @@ extern "C" int gbqv_create(int num_qubits, int precision, int kind, gbqv_handle 
     d.n = nvec;
     d.dbl = precision == GBQV_C128;
     d.density = kind == GBQV_DENSITY_MATRIX;
+    d.unitary = kind == GBQV_UNITARY;
     cuda_check(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking), "stream creation");
     const size_t bytes = d.amps() * d.amp_bytes();
     cudaError_t e = cudaMalloc(&d.state, bytes);
@@ -294,7 +296,10 @@ extern "C" int gbqv_create(int num_qubits, int precision, int kind, gbqv_handle 
       throw Error(GBQV_ERR_ALLOC, "cannot allocate " + std::to_string(bytes) + " bytes of device memory (" +
                                       std::to_string(free_b) + " free)");
     }
-    launch_set_basis(d, 0, cd(1.0, 0.0));
+    if (d.unitary)
+      launch_set_identity(d);
+    else
+      launch_set_basis(d, 0, cd(1.0, 0.0));
     *out = s.release();
   });
 }
@@ -343,7 +348,13 @@ extern "C" int gbqv_zero(gbqv_handle h) {
 }
 
 extern "C" int gbqv_initialize(gbqv_handle h) {
-  return guard(h, [&] { need_handle(h); launch_set_basis(h->dev, 0, cd(1.0, 0.0)); });
+  return guard(h, [&] {
+    need_handle(h);
+    if (h->dev.unitary)
+      launch_set_identity(h->dev);
+    else
+      launch_set_basis(h->dev, 0, cd(1.0, 0.0));
+  });
 }
 
 namespace {

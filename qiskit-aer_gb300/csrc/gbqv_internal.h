@@ -46,6 +46,7 @@ struct Device {
   int nq = 0;           // logical qubits
   bool dbl = true;      // complex128 (true) or complex64 (false)
   bool density = false;
+  bool unitary = false;     // UnitaryMatrix: 2 nq vector qubits, identity at initialisation
   int blocking = 1;         // 0 one kernel per op, 1 register-tile runs, 2 shared-memory runs
   int tensor_c128 = 1;      // complex128 dense k = 4, 5: 0 FP64 cores, 1 tensor (tcgen05 for k = 4), 2 mma.sync only
   int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up
@@ -85,6 +86,7 @@ void launch_pauli(Device &dev, uint64_t x_mask, uint64_t z_mask, uint64_t x_max,
 void launch_dm_y(Device &dev, uint64_t q);
 void launch_scale(Device &dev, cd s);
 void launch_set_basis(Device &dev, uint64_t index, cd value); // zero + one entry
+void launch_set_identity(Device &dev);                         // unitary: vec(I) over 2 nq qubits
 // complex64 states: state[offset, +count) <- narrow(src) / dst <- widen(state[offset, +count));
 // src and dst are device buffers of complex128
 void launch_narrow(Device &dev, const void *src, uint64_t offset, uint64_t count);

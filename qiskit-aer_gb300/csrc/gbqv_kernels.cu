@@ -650,6 +650,20 @@ __global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, i
   if (threadIdx.x == 0) partials[((size_t)term * nseg + seg) * bps + slice] = acc;
 }
 
+// UnitaryMatrix::initialize (unitarymatrix.hpp:236-247): entry (i, j) at
+// i + 2^nq j is 1 on the diagonal.
+template <typename T>
+__global__ void k_set_identity(T *__restrict__ psi, int nq, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t low = (1ULL << nq) - 1;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    T z;
+    z.x = (i & low) == (i >> nq) ? 1 : 0;
+    z.y = 0;
+    psi[i] = z;
+  }
+}
+
 template <typename T>
 __global__ void k_set_basis_seg(T *__restrict__ psi, int sb, uint64_t nvalid, uint64_t count) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -1038,6 +1052,15 @@ void reduce_expval_segments(Device &dev, const std::vector<PauliTerm> &terms, in
     check_launch("segmented expval kernel");
   }
   finish(dev, (int)values, bps);
+}
+
+void launch_set_identity(Device &dev) {
+  const int grid = grid_for(dev.amps(), 256);
+  if (dev.dbl)
+    k_set_identity<double2><<<grid, 256, 0, dev.stream>>>(st<double2>(dev), dev.nq, dev.amps());
+  else
+    k_set_identity<float2><<<grid, 256, 0, dev.stream>>>(st<float2>(dev), dev.nq, dev.amps());
+  check_launch("initialize kernel");
 }
 
 void launch_set_basis_segments(Device &dev, int state_bits, uint64_t count) {

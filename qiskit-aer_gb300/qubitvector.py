@@ -323,3 +323,25 @@ class DensityMatrix(QubitVector):
         z = A.c128()
         self._c(self._L.gbqv_dm_trace(self._h, C.byref(z)))
         return complex(z.re, z.im)
+
+
+class UnitaryMatrix(QubitVector):
+    """QV::UnitaryMatrix (src/simulators/unitary/unitarymatrix.hpp): the
+    2^n x 2^n matrix of the unitary method, stored column-major over 2n vector
+    qubits and resident on the GPU; starts as the identity, and gates on
+    qubits 0..n-1 multiply it from the left."""
+
+    _kind = A.UNITARY
+
+    def initialize_from_matrix(self, mat) -> None:
+        m = np.asarray(mat, dtype=np.complex128)
+        d = 1 << self._nq
+        if m.shape != (d, d):
+            raise ValueError("Unitary::State::initialize: initial state does not match qubit number")
+        super().initialize_from_vector(m.reshape(-1, order="F"))
+
+    def copy_to_matrix(self) -> np.ndarray:
+        d = 1 << self._nq
+        return self.copy_to_vector().reshape(d, d, order="F")
+
+    move_to_matrix = copy_to_matrix

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _capi as A
 from .circuit import Instruction, NativeCircuit, QuantumCircuit
-from .qubitvector import DensityMatrix, QubitVector
+from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
 
 
 def discrete_draw(probs, u: float) -> int:
@@ -63,9 +63,12 @@ class Result:
     def get_statevector(self, i=0):
         return self.results[i]["data"]["statevector"]
 
+    def get_unitary(self, i=0):
+        return self.results[i]["data"]["unitary"]
+
 
 class AerSimulator:
-    METHODS = ("statevector", "density_matrix")
+    METHODS = ("statevector", "density_matrix", "unitary")
 
     def __init__(self, method: str = "statevector", device: str = "GPU", precision: str = "double",
                  noise_model=None, fusion_enable: bool = True, fusion_max_qubit: int | None = None,
@@ -97,6 +100,8 @@ class AerSimulator:
         cfg.enable = int(o["fusion_enable"])
         if o["fusion_max_qubit"] is not None:
             cfg.max_qubit = int(o["fusion_max_qubit"])
+        if self.method == "unitary":
+            cfg.threshold //= 2  # Executor::transpile_fusion, Method::unitary (circuit_executor.hpp:1259-1262)
         if o["fusion_threshold"] is not None:
             cfg.threshold = int(o["fusion_threshold"])
         cfg.cost_factor = float(o["fusion_cost_factor"])
@@ -280,8 +285,10 @@ class AerSimulator:
     def _run_one(self, circuit: QuantumCircuit, shots: int, seed: int):
         if self.method == "statevector" and circuit.needs_shots("statevector"):
             return self._run_shots(circuit, shots, seed)
+        if self.method == "unitary":
+            self._check_unitary_circuit(circuit)
         segments, meas, saves, meta = self.compile(circuit)
-        cls = DensityMatrix if self.method == "density_matrix" else QubitVector
+        cls = {"density_matrix": DensityMatrix, "unitary": UnitaryMatrix}.get(self.method, QubitVector)
         data = {}
         with cls(circuit.num_qubits, self.precision) as st:
             if not self.options["blocking_enable"]:
@@ -394,8 +401,23 @@ class AerSimulator:
         vals, cnt = np.unique(memory, return_counts=True)
         return {format(int(v), f"0{num_clbits}b"): int(n) for v, n in zip(vals, cnt)}
 
+    def _check_unitary_circuit(self, circuit: QuantumCircuit):
+        """The unitary method's op set (QubitUnitary::StateOpSet,
+        unitary_state.hpp:35-54): gates, unitary / diagonal matrices,
+        barriers, save_unitary."""
+        if self.noise_model is not None and not self.noise_model.is_ideal():
+            raise ValueError("the unitary method does not support noise")
+        for ins in circuit.data:
+            if ins.kind in ("gate", "unitary", "diagonal", "barrier"):
+                continue
+            if ins.kind == "save" and ins.name == "unitary":
+                continue
+            raise ValueError(f"QubitUnitary::State::invalid instruction '{ins.name}'.")
+
     def _save(self, st, ins, data):
-        if ins.name == "statevector":
+        if ins.name == "unitary":
+            data[ins.data] = st.copy_to_matrix()
+        elif ins.name == "statevector":
             data[ins.data] = st.copy_to_vector()
         elif ins.name == "density_matrix":
             data[ins.data] = st.copy_to_matrix()

@@ -118,3 +118,19 @@ def test_estimator_pub_coercion_and_broadcast_shapes():
         pr.coerce_parameter_values(np.zeros((3, 3)), qc)
     with pytest.raises(ValueError):
         pr.coerce_parameter_values(None, qc)
+
+
+def test_unitary_method_host_rules():
+    """The unitary method halves the fusion threshold
+    (Executor::transpile_fusion, circuit_executor.hpp:1259-1262) and accepts
+    only its op set (unitary_state.hpp:35-54)."""
+    P = pkg()
+    sv = P.AerSimulator().fusion_config()
+    un = P.AerSimulator(method="unitary").fusion_config()
+    assert (sv.threshold, un.threshold, un.max_qubit) == (14, 7, 5)
+    sim = P.AerSimulator(method="unitary")
+    sim._check_unitary_circuit(P.QuantumCircuit(2).h(0).cx(0, 1).unitary(np.eye(2), [1]).save_unitary())
+    for bad in (P.QuantumCircuit(2).measure(0, 0), P.QuantumCircuit(2).reset(0),
+                P.QuantumCircuit(2).h(0).save_statevector()):
+        with pytest.raises(ValueError, match="invalid instruction"):
+            sim._check_unitary_circuit(bad)
