@@ -45,7 +45,11 @@ class QubitVector {
   QubitVector(QubitVector &&o) noexcept : h_(std::exchange(o.h_, nullptr)), n_(o.n_) {}
   ~QubitVector() { gbqv_destroy(h_); }
 
-  static std::string name() { return Kind == GBQV_STATEVECTOR ? "statevector_gb300" : "density_matrix_gb300"; }
+  static std::string name() {
+    return Kind == GBQV_STATEVECTOR ? "statevector_gb300"
+           : Kind == GBQV_UNITARY   ? "unitary_gb300"
+                                    : "density_matrix_gb300";
+  }
 
   // ---- utility (qubitvector.hpp:913-1110) ----
   void set_num_qubits(size_t num_qubits) {
@@ -166,5 +170,19 @@ class QubitVector {
 
 template <typename data_t = double>
 using DensityMatrix = QubitVector<data_t, GBQV_DENSITY_MATRIX>;
+
+// QV::UnitaryMatrix<data_t> (unitarymatrix.hpp): the unit of the unitary
+// method; the QubitVector members act on the 2n-qubit vec(U), and
+// initialize() sets the identity.
+template <typename data_t = double>
+class UnitaryMatrix : public QubitVector<data_t, GBQV_UNITARY> {
+ public:
+  using QubitVector<data_t, GBQV_UNITARY>::QubitVector;
+  uint_t rows() const { return 1ULL << this->num_qubits(); }
+  // column-major, as Utils::vectorize_matrix
+  void initialize_from_matrix(const cvector_t &mat) { this->initialize_from_vector(mat); }
+  cvector_t copy_to_matrix() const { return this->copy_to_vector(); }
+  cvector_t move_to_matrix() { return this->copy_to_vector(); }
+};
 
 }  // namespace gbqv_aer
