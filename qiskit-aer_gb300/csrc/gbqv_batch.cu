@@ -152,11 +152,14 @@ __device__ void tile_gate(T *tile, int m, const GateDev &g, int a, int b, bool i
   }
 }
 
-// Im <lam| P |psi> over a tile for the generator of a rotation gate on local bit a.
+// This thread's part of Im <lam| P |psi> over a tile for the generator of a
+// rotation gate on local bit a (summed in the data precision: at most 2^m /
+// blockDim terms per thread; the caller accumulates in double).
 template <typename T>
 __device__ double tile_generator(const T *lam, const T *psi, int m, int kind, int a) {
+  using R = decltype(T::x);
   const uint32_t L = 1u << m, bit = 1u << a;
-  double acc = 0.0;
+  R acc = 0;
   for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) {
     const T lv = lam[l];
     T pv;
@@ -172,9 +175,9 @@ __device__ double tile_generator(const T *lam, const T *psi, int m, int kind, in
       pv.y = (decltype(pv.y))(-sg * (double)v.x);
     }
     // Im(conj(lv) * pv)
-    acc += (double)lv.x * (double)pv.y - (double)lv.y * (double)pv.x;
+    acc += lv.x * pv.y - lv.y * pv.x;
   }
-  return acc;
+  return (double)acc;
 }
 
 template <typename T, int M>
@@ -192,7 +195,11 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
   uint64_t *pd_lo = reinterpret_cast<uint64_t *>(tl + (1u << M));
   uint64_t *pd_hi = pd_lo + 64;
   __shared__ double red[32];
-  __shared__ double gacc[kBatchMaxRunOps];
+  // per run: its gates with their tile-local bits, and per-warp sums of the
+  // generator inner products (reduced over warps once per run)
+  __shared__ GateDev s_g[kBatchMaxRunOps];
+  __shared__ uint8_t s_a[kBatchMaxRunOps], s_b[kBatchMaxRunOps];
+  __shared__ double gacc[kBatchMaxRunOps][kBatchThreads / 32];
   __shared__ int s_idx;
   __shared__ int s_T[64];
   for (;;) {
@@ -294,7 +301,20 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           for (int q = 0; q < I.n; ++q)
             if ((R.tmask >> q) & 1) s_T[j++] = q;
         }
-        if (threadIdx.x < kBatchMaxRunOps) gacc[threadIdx.x] = 0.0;
+        for (int i = threadIdx.x; i < kBatchMaxRunOps * (kBatchThreads / 32); i += blockDim.x)
+          gacc[i / (kBatchThreads / 32)][i % (kBatchThreads / 32)] = 0.0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < R.count; k += blockDim.x) {
+          const GateDev g = gates[I.op_off + R.first + k];
+          int a = 0, b = 0;
+          for (int j = 0; j < __popcll(R.tmask); ++j) {
+            if (s_T[j] == g.q0) a = j;
+            if (s_T[j] == g.q1) b = j;
+          }
+          s_g[k] = g;
+          s_a[k] = (uint8_t)a;
+          s_b[k] = (uint8_t)b;
+        }
         __syncthreads();
         const int m = __popcll(R.tmask);
         const int lo_bits = min(m, 6), hi_bits = m - lo_bits;
@@ -329,16 +349,12 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           __syncthreads();
           for (int k = 0; k < R.count; ++k) {
             const int oi = dir == 0 ? k : R.count - 1 - k;
-            const GateDev g = gates[I.op_off + R.first + oi];
-            int a = 0, b = 0;
-            for (int j = 0; j < m; ++j) {
-              if (s_T[j] == g.q0) a = j;
-              if (s_T[j] == g.q1) b = j;
-            }
+            const GateDev &g = s_g[oi];
+            const int a = s_a[oi], b = s_b[oi];
             if (dir == 1 && g.param >= 0) {
-              const double part = bsum(tile_generator(tl, tp, m, g.kind, a), red);
-              if (threadIdx.x == 0) gacc[oi] += part;
-              __syncthreads();
+              double part = tile_generator(tl, tp, m, g.kind, a);
+              for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+              if ((threadIdx.x & 31) == 0) gacc[oi][threadIdx.x >> 5] += part;
             }
             tile_gate(tp, m, g, a, b, dir == 1);
             if (dir == 1) tile_gate(tl, m, g, a, b, true);
@@ -353,8 +369,11 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
         }
         if (dir == 1 && threadIdx.x == 0)
           for (int k = 0; k < R.count; ++k) {
-            const GateDev g = gates[I.op_off + R.first + k];
-            if (g.param >= 0) grads[I.grad_off + g.param] += gacc[k];
+            const GateDev &g = s_g[k];
+            if (g.param < 0) continue;
+            double sum = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += gacc[k][w];
+            grads[I.grad_off + g.param] += sum;
           }
         __syncthreads();
       }
