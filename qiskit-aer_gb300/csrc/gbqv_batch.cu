@@ -101,19 +101,24 @@ __device__ __forceinline__ uint32_t ins1(uint32_t i, int q) {
 }
 
 // Apply gate g (or its inverse) to a tile; a, b are the local positions.
-template <typename T>
-__device__ void tile_gate(T *tile, int m, const GateDev &g, int a, int b, bool inverse) {
-  const uint32_t L = 1u << m;
+// MT > 0: the tile has MT qubits (compile-time trip counts, fully unrolled
+// loops so that the shared-memory accesses of a thread overlap); MT = 0: m.
+template <typename T, int MT>
+__device__ __forceinline__ void tile_gate(T *tile, int m, const GateDev &g, int a, int b, bool inverse) {
+  const uint32_t L = MT ? (1u << MT) : (1u << m);
+  constexpr int kU = MT ? 16 : 1;
   if (g.kind == B_RZ) {
     // diag(e^{-i t/2}, e^{i t/2}); inverse conjugates
     const double sg = inverse ? -1.0 : 1.0;
     const T d0 = cplx<T>(g.c, -sg * g.s), d1 = cplx<T>(g.c, sg * g.s);
-    for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) tile[l] = cmul(tile[l], (l >> a) & 1 ? d1 : d0);
+#pragma unroll kU
+    for (uint32_t l = threadIdx.x; l < L; l += kBatchThreads) tile[l] = cmul(tile[l], (l >> a) & 1 ? d1 : d0);
     return;
   }
   if (g.kind == B_CX || g.kind == B_CZ) {
     const int lo = min(a, b), hi = max(a, b);
-    for (uint32_t p = threadIdx.x; p < (L >> 2); p += blockDim.x) {
+#pragma unroll kU
+    for (uint32_t p = threadIdx.x; p < (L >> 2); p += kBatchThreads) {
       const uint32_t base = ins1(ins1(p, lo), hi) | (1u << a);  // control set
       const uint32_t i1 = base | (1u << b);
       if (g.kind == B_CX) {
@@ -141,7 +146,8 @@ __device__ void tile_gate(T *tile, int m, const GateDev &g, int a, int b, bool i
     const double h = 0.70710678118654752440;
     m00 = cplx<T>(h, 0); m01 = cplx<T>(h, 0); m10 = cplx<T>(h, 0); m11 = cplx<T>(-h, 0);
   }
-  for (uint32_t p = threadIdx.x; p < (L >> 1); p += blockDim.x) {
+#pragma unroll kU
+  for (uint32_t p = threadIdx.x; p < (L >> 1); p += kBatchThreads) {
     const uint32_t i0 = ins1(p, a), i1 = i0 | (1u << a);
     const T x0 = tile[i0], x1 = tile[i1];
     T y0 = cmul(m00, x0), y1 = cmul(m10, x0);
@@ -155,12 +161,14 @@ __device__ void tile_gate(T *tile, int m, const GateDev &g, int a, int b, bool i
 // This thread's part of Im <lam| P |psi> over a tile for the generator of a
 // rotation gate on local bit a (summed in the data precision: at most 2^m /
 // blockDim terms per thread; the caller accumulates in double).
-template <typename T>
-__device__ double tile_generator(const T *lam, const T *psi, int m, int kind, int a) {
+template <typename T, int MT>
+__device__ __forceinline__ double tile_generator(const T *lam, const T *psi, int m, int kind, int a) {
   using R = decltype(T::x);
-  const uint32_t L = 1u << m, bit = 1u << a;
+  const uint32_t L = MT ? (1u << MT) : (1u << m), bit = 1u << a;
+  constexpr int kU = MT ? 16 : 1;
   R acc = 0;
-  for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) {
+#pragma unroll kU
+  for (uint32_t l = threadIdx.x; l < L; l += kBatchThreads) {
     const T lv = lam[l];
     T pv;
     if (kind == B_RZ) {
@@ -170,9 +178,9 @@ __device__ double tile_generator(const T *lam, const T *psi, int m, int kind, in
       pv = psi[l ^ bit];
     } else {  // Y = -i X Z in the (x, z) form: phase -i, sign (-1)^{bit of l}
       const T v = psi[l ^ bit];
-      const double sg = (l & bit) ? -1.0 : 1.0;
-      pv.x = (decltype(pv.x))(sg * (double)v.y);   // -i * v = (v.y, -v.x)
-      pv.y = (decltype(pv.y))(-sg * (double)v.x);
+      const R sg = (l & bit) ? R(-1) : R(1);
+      pv.x = sg * v.y;   // -i * v = (v.y, -v.x)
+      pv.y = -sg * v.x;
     }
     // Im(conj(lv) * pv)
     acc += lv.x * pv.y - lv.y * pv.x;
@@ -230,7 +238,10 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           double sacc = 0.0;
           for (uint64_t j = threadIdx.x & 31; j < (1ULL << bb); j += 32) {
             const T a = psi[(b << bb) + j];
-            sacc += (double)a.x * a.x + (double)a.y * a.y;
+            if constexpr (sizeof(T) == 8)
+              sacc += (double)(a.x * a.x + a.y * a.y);
+            else
+              sacc += (double)a.x * a.x + (double)a.y * a.y;
           }
           for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
           if ((threadIdx.x & 31) == 0) cdf[b] = sacc;
@@ -253,39 +264,65 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
             const uint64_t b0 = lo << bb;
             bool found = false;
             for (uint64_t j0 = 0; j0 < (1ULL << bb) && !found; j0 += 32) {
-              double v = 0.0;
-              if (j0 + lane < (1ULL << bb)) {
-                const T a = psi[b0 + j0 + lane];
-                v = (double)a.x * a.x + (double)a.y * a.y;
+              unsigned msk;
+              if constexpr (sizeof(T) == 8) {
+                // complex64: the 32 probabilities and their prefix sums in
+                // float, compared with the remaining mass r - p of the
+                // block (one double subtraction per 32 amplitudes, not one
+                // per amplitude: the FP64 pipe is narrow)
+                float v = 0.0f;
+                if (j0 + lane < (1ULL << bb)) {
+                  const T a = psi[b0 + j0 + lane];
+                  v = a.x * a.x + a.y * a.y;
+                }
+                for (int o = 1; o < 32; o <<= 1) {
+                  const float u = __shfl_up_sync(0xffffffffu, v, o);
+                  if (lane >= o) v += u;
+                }
+                const float rem = (float)(r - p);
+                msk = __ballot_sync(0xffffffffu, (j0 + lane < (1ULL << bb)) && (rem < v));
+                p += (double)__shfl_sync(0xffffffffu, v, 31);
+              } else {
+                double v = 0.0;
+                if (j0 + lane < (1ULL << bb)) {
+                  const T a = psi[b0 + j0 + lane];
+                  v = (double)a.x * a.x + (double)a.y * a.y;
+                }
+                for (int o = 1; o < 32; o <<= 1) {
+                  const double u = __shfl_up_sync(0xffffffffu, v, o);
+                  if (lane >= o) v += u;
+                }
+                msk = __ballot_sync(0xffffffffu, (j0 + lane < (1ULL << bb)) && (r < p + v));
+                p += __shfl_sync(0xffffffffu, v, 31);
               }
-              for (int o = 1; o < 32; o <<= 1) {
-                const double u = __shfl_up_sync(0xffffffffu, v, o);
-                if (lane >= o) v += u;
-              }
-              const unsigned msk = __ballot_sync(0xffffffffu, (j0 + lane < (1ULL << bb)) && (r < p + v));
               if (msk) { res = b0 + j0 + (__ffs(msk) - 1); found = true; }
-              p += __shfl_sync(0xffffffffu, v, 31);
             }
             if (!found) res = b0 + (1ULL << bb) - 1;
           }
           if (lane == 0) samples[I.smp_off + sh] = res;
         }
         __syncthreads();
-        // lambda = H psi and <H> = Re <psi|lambda>
+        // lambda = H psi and <H> = Re <psi|lambda>: lambda in the data
+        // precision (complex64 sums its terms in float: the FP64 pipe is
+        // far narrower), <H> accumulated in double
+        using Rt = decltype(T::x);
         double e_acc = 0.0;
         for (uint64_t i = threadIdx.x; i < N; i += blockDim.x) {
-          double ar = 0.0, ai = 0.0;
+          Rt ar = 0, ai = 0;
           for (int t = 0; t < I.nterms; ++t) {
             const TermDevB h = terms[I.term_off + t];
             const T a = psi[i ^ h.x_mask];
-            double cr = h.re, ci = h.im;
+            Rt cr = (Rt)h.re, ci = (Rt)h.im;
             if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
-            ar += cr * (double)a.x - ci * (double)a.y;
-            ai += cr * (double)a.y + ci * (double)a.x;
+            ar += cr * a.x - ci * a.y;
+            ai += cr * a.y + ci * a.x;
           }
           const T p = psi[i];
-          e_acc += (double)p.x * ar + (double)p.y * ai;
-          lam[i] = cplx<T>(ar, ai);
+          e_acc += (double)(p.x * ar + p.y * ai);
+          T l;
+          l.x = ar;
+          l.y = ai;
+          lam[i] = l;
         }
         const double e = bsum(e_acc, red);
         if (threadIdx.x == 0) energy[idx] = e;
@@ -341,10 +378,28 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
               base |= (tt & 1) << q;
               tt >>= 1;
             }
-          for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) {
-            const uint64_t gi = base | pd_lo[l & 63] | pd_hi[l >> 6];
-            tp[l] = psi[gi];
-            if (dir == 1) tl[l] = lam[gi];
+          if (m == M) {  // every load of the thread issued before the first store
+            constexpr int kPer = (1 << M) / kBatchThreads;
+            T vp[kPer], vl[kPer];
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+              const uint32_t l = threadIdx.x + j * kBatchThreads;
+              const uint64_t gi = base | pd_lo[l & 63] | pd_hi[l >> 6];
+              vp[j] = psi[gi];
+              if (dir == 1) vl[j] = lam[gi];
+            }
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+              const uint32_t l = threadIdx.x + j * kBatchThreads;
+              tp[l] = vp[j];
+              if (dir == 1) tl[l] = vl[j];
+            }
+          } else {
+            for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) {
+              const uint64_t gi = base | pd_lo[l & 63] | pd_hi[l >> 6];
+              tp[l] = psi[gi];
+              if (dir == 1) tl[l] = lam[gi];
+            }
           }
           __syncthreads();
           for (int k = 0; k < R.count; ++k) {
@@ -352,15 +407,22 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
             const GateDev &g = s_g[oi];
             const int a = s_a[oi], b = s_b[oi];
             if (dir == 1 && g.param >= 0) {
-              double part = tile_generator(tl, tp, m, g.kind, a);
+              double part = m == M ? tile_generator<T, M>(tl, tp, m, g.kind, a)
+                                   : tile_generator<T, 0>(tl, tp, m, g.kind, a);
               for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
               if ((threadIdx.x & 31) == 0) gacc[oi][threadIdx.x >> 5] += part;
             }
-            tile_gate(tp, m, g, a, b, dir == 1);
-            if (dir == 1) tile_gate(tl, m, g, a, b, true);
+            if (m == M) {
+              tile_gate<T, M>(tp, m, g, a, b, dir == 1);
+              if (dir == 1) tile_gate<T, M>(tl, m, g, a, b, true);
+            } else {
+              tile_gate<T, 0>(tp, m, g, a, b, dir == 1);
+              if (dir == 1) tile_gate<T, 0>(tl, m, g, a, b, true);
+            }
             __syncthreads();
           }
-          for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) {
+#pragma unroll 8
+          for (uint32_t l = threadIdx.x; l < L; l += kBatchThreads) {
             const uint64_t gi = base | pd_lo[l & 63] | pd_hi[l >> 6];
             psi[gi] = tp[l];
             if (dir == 1) lam[gi] = tl[l];
