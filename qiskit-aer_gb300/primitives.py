@@ -199,12 +199,14 @@ class EstimatorV2:
         circ = circuit.copy()
         params = circ.parameters
         param_shape = values.shape[:-1] if values is not None else ()
-        param_indices = np.fromiter(np.ndindex(param_shape), dtype=object).reshape(param_shape) \
-            if param_shape else np.empty((), dtype=object)
-        if not param_shape:
-            param_indices[()] = ()
-        bc_param_ind, bc_obs = np.broadcast_arrays(param_indices, observables)
-        paulis = sorted({lab for d in observables.reshape(-1) for lab in d})
+        # position of each parameter set in the flattened binding list
+        # (the reference's param_indices / flat_indices, as integers)
+        param_pos = np.arange(int(np.prod(param_shape, dtype=np.int64))).reshape(param_shape)
+        obs_flat = observables.reshape(-1)
+        obs_id = np.arange(obs_flat.size).reshape(observables.shape)
+        bc_pos, bc_oid = np.broadcast_arrays(param_pos, obs_id)
+        paulis = sorted({lab for d in obs_flat for lab in d})
+        col = {lab: i for i, lab in enumerate(paulis)}
         n = circ.num_qubits
         for lab in paulis:
             circ.save_expectation_value([(1.0, lab, list(range(n)))], label=lab)
@@ -215,13 +217,16 @@ class EstimatorV2:
             result = self._backend.run(circ, parameter_binds=binds, **run_options)
         else:
             result = self._backend.run(circ, **run_options)
-        position = {idx: i for i, idx in enumerate(param_indices.reshape(-1))}
-        evs = np.zeros(bc_param_ind.shape, dtype=float)
-        stds = np.full(bc_param_ind.shape, precision)
-        for index in np.ndindex(*bc_param_ind.shape):
-            data = result.data(position[bc_param_ind[index]] if params else 0)
-            for lab, coeff in bc_obs[index].items():
-                evs[index] += np.real(data[lab] * coeff)
+        # E[binding, pauli] and the observables' coefficients C[observable, pauli]
+        nexp = len(result.results) if params else 1
+        E = np.array([[result.data(j)[lab] for lab in paulis] for j in range(nexp)]).reshape(nexp, len(paulis))
+        Cm = np.zeros((obs_flat.size, len(paulis)), dtype=complex)
+        for i, d in enumerate(obs_flat):
+            for lab, coeff in d.items():
+                Cm[i, col[lab]] += coeff
+        rows = E[bc_pos.reshape(-1) if params else np.zeros(bc_pos.size, dtype=np.int64)]
+        evs = np.real(np.sum(rows * Cm[bc_oid.reshape(-1)], axis=-1)).reshape(bc_pos.shape).astype(float)
+        stds = np.full(bc_pos.shape, precision)
         if precision > 0:
             rng = np.random.default_rng(self._options.run_options.get("seed_simulator"))
             evs = rng.normal(evs, precision, evs.shape)
