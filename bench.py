@@ -271,21 +271,34 @@ def bench_qv(args, torch, P):
         psi0[0] = 1.0
         sim = P.AerSimulator(precision=args.precision, blocking_enable=not args.no_blocking)
 
+        parts = np.zeros(4)
+
         def e2e_step():
+            t = [time.perf_counter()]
             segs, _, _, _ = sim.compile(qc)        # Fusion pass on the host
-            st.initialize_from_vector(psi0)        # H2D
+            t.append(time.perf_counter())
+            st.initialize_from_vector(psi0)        # H2D (returns when the copy is done)
+            t.append(time.perf_counter())
             A_check(L, L.gbqv_execute(st.handle, segs[0][1].handle), st)
+            st.synchronize()
+            t.append(time.perf_counter())
             st.probabilities(list(range(8)))       # D2H of a marginal
+            t.append(time.perf_counter())
+            parts[:] += np.diff(t)
 
         e2e_step()                                 # warm-up: staging buffers, first use of psi0's pages
         st.synchronize()
+        parts[:] = 0
         t1 = time.perf_counter()
         for _ in range(max(1, args.steps)):
             e2e_step()
         st.synchronize()
         te = (time.perf_counter() - t1) / max(1, args.steps)
+        parts /= max(1, args.steps)
         e2e = {"value": round(nops * pass_bytes / te / 1e9, 3), "unit": "GB/s", "ms_per_step": round(te * 1e3, 2),
-               "h2d_bytes_per_step": int(psi0.nbytes), "d2h_bytes_per_step": 8 * 256}
+               "h2d_bytes_per_step": int(psi0.nbytes), "d2h_bytes_per_step": 8 * 256,
+               "breakdown_ms": {k: round(float(v) * 1e3, 2) for k, v in
+                                zip(("fusion", "upload", "execute", "readback"), parts)}}
         del psi0, psi0_t
     st.close()
     base = None

@@ -358,17 +358,39 @@ extern "C" int gbqv_initialize(gbqv_handle h) {
 }
 
 namespace {
-// complex64 states move through a device staging slice of kChunk complex128
-// values (256 MB): copy engine for the host <-> device leg, a kernel for the
-// precision change.  One stream orders each copy after the kernel that used
-// the slice before it.
+// complex64 states from / to pageable host memory move through a device
+// staging slice of kChunk complex128 values (256 MB): copy engine for the
+// host <-> device leg, a kernel for the precision change.  One stream orders
+// each copy after the kernel that used the slice before it.
 constexpr uint64_t kChunk = 1ULL << 24;
 
+// The device address of page-locked (pinned or registered) host memory, or
+// nullptr for ordinary pageable memory.  A kernel reads or writes pinned
+// host memory directly over the CPU-GPU link at the link's rate.
+const void *pinned_device_view(const void *host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 void upload(Device &d, const cd *src, uint64_t offset, uint64_t count) {
+  if (d.dbl && count >= (1ULL << 20)) {
+    if (const void *dv = pinned_device_view(src)) {  // SMs pull the pinned pages at the link's rate
+      launch_copy_in(d, dv, offset, count);
+      return;
+    }
+  }
   if (d.dbl) {
     cuda_check(cudaMemcpyAsync(reinterpret_cast<cd *>(d.state) + offset, src, count * sizeof(cd),
                                cudaMemcpyHostToDevice, d.stream),
                "state upload");
+    return;
+  }
+  if (const void *dv = pinned_device_view(src)) {  // one pass: read the host data, write complex64
+    launch_narrow(d, dv, offset, count);
     return;
   }
   void *stage = grow(d.aux2, d.aux2_cap, std::min(count, kChunk) * sizeof(cd));
@@ -414,6 +436,11 @@ extern "C" int gbqv_copy_to_host(gbqv_handle h, gbqv_c128 *out, uint64_t len) {
     REQUIRE(len == d.amps(), GBQV_ERR_ARG, "copy_to_host: length must equal the number of stored amplitudes");
     if (d.dbl) {
       cuda_check(cudaMemcpyAsync(out, d.state, len * sizeof(cd), cudaMemcpyDeviceToHost, d.stream), "state download");
+      sync(d);
+      return;
+    }
+    if (const void *dv = pinned_device_view(out)) {
+      launch_widen(d, 0, len, const_cast<void *>(dv));
       sync(d);
       return;
     }

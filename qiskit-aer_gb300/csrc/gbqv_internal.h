@@ -90,6 +90,7 @@ void launch_set_identity(Device &dev);                         // unitary: vec(I
 // complex64 states: state[offset, +count) <- narrow(src) / dst <- widen(state[offset, +count));
 // src and dst are device buffers of complex128
 void launch_narrow(Device &dev, const void *src, uint64_t offset, uint64_t count);
+void launch_copy_in(Device &dev, const void *src, uint64_t offset, uint64_t count);  // complex128 states
 void launch_widen(Device &dev, uint64_t offset, uint64_t count, void *dst);
 
 // Reductions: write results into dev.results[0..count) (device), async.

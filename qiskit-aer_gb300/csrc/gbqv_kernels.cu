@@ -501,6 +501,10 @@ __global__ void k_narrow(const double2 *__restrict__ src, float2 *__restrict__ d
     dst[i] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
   }
 }
+__global__ void k_copy_c128(const double2 *__restrict__ src, double2 *__restrict__ dst, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) dst[i] = src[i];
+}
 __global__ void k_widen(const float2 *__restrict__ src, double2 *__restrict__ dst, uint64_t count) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
@@ -980,6 +984,12 @@ void launch_narrow(Device &dev, const void *src, uint64_t offset, uint64_t count
   k_narrow<<<grid_for(count, 256), 256, 0, dev.stream>>>(static_cast<const double2 *>(src),
                                                           st<float2>(dev) + offset, count);
   check_launch("state narrowing kernel");
+}
+
+void launch_copy_in(Device &dev, const void *src, uint64_t offset, uint64_t count) {
+  k_copy_c128<<<grid_for(count, 256), 256, 0, dev.stream>>>(static_cast<const double2 *>(src),
+                                                             st<double2>(dev) + offset, count);
+  check_launch("state copy kernel");
 }
 
 void launch_widen(Device &dev, uint64_t offset, uint64_t count, void *dst) {

@@ -57,3 +57,29 @@ def test_c128_round_trip_exact_and_pure_state_dm():
             rho = np.outer(phi, phi.conj())
             want = rho if precision == "double" else rho.astype(np.complex64).astype(np.complex128)
             np.testing.assert_allclose(dm.copy_to_matrix(), want, rtol=0, atol=1e-15)
+
+
+def test_c64_download_into_pinned_memory():
+    torch = pytest.importorskip("torch")
+    P = pkg()
+    n = 21
+    rng = np.random.default_rng(12)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    out = torch.zeros(1 << n, dtype=torch.complex128, pin_memory=True)
+    with P.QubitVector(n, "single") as qv:
+        qv.initialize_from_vector(psi)
+        P._capi.check(P.lib().gbqv_copy_to_host(qv.handle, P._capi.C.c_void_p(out.data_ptr()), 1 << n), qv.handle)
+    np.testing.assert_array_equal(out.numpy(), psi.astype(np.complex64).astype(np.complex128))
+
+
+def test_c128_upload_from_pinned_memory_is_exact():
+    torch = pytest.importorskip("torch")
+    P = pkg()
+    n = 21
+    t = torch.zeros(1 << n, dtype=torch.complex128, pin_memory=True)
+    psi = t.numpy()
+    rng = np.random.default_rng(13)
+    psi[:] = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    with P.QubitVector(n, "double") as qv:
+        qv.initialize_from_vector(psi)
+        np.testing.assert_array_equal(qv.copy_to_vector(), psi)
