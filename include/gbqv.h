@@ -341,6 +341,12 @@ int gbqv_execute_bound(gbqv_handle h, gbqv_circuit_t c, uint64_t first, uint64_t
  * (QubitVector::expval_pauli per state, qubitvector.hpp:2299-2347). */
 int gbqv_expval_pauli_segments(gbqv_handle h, int state_qubits, uint64_t nseg, int nterms, const uint64_t *qubits,
                                const int *offsets, const char *const *labels, double *out);
+/* QubitVector::sample_measure (qubitvector.hpp:2148-2228) on states first ..
+ * first + nseg - 1 of such a stack, each exactly as a state of its own:
+ * state first + s draws with rnds[s * shots .. (s + 1) * shots) into
+ * out[s * shots ..] (indices within the state). */
+int gbqv_sample_measure_segments(gbqv_handle h, int state_qubits, uint64_t first, uint64_t nseg,
+                                 const double *rnds, uint64_t shots, uint64_t *out);
 
 /* Adjoint-method gradient of E(theta) = <psi(theta)|H|psi(theta)>, psi =
  * c applied to |0...0>.  No counterpart in the reference (Aer has no gradient

@@ -18,10 +18,10 @@ from .noise import (NoiseModel, QuantumError, amplitude_damping_error, depolariz
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
 from .simulator import AerSimulator, Result, uniforms
 from . import adjoint, batched
-from .primitives import EstimatorV2
+from .primitives import EstimatorV2, SamplerV2
 
 __all__ = [
-    "AerSimulator", "adjoint", "batched", "DensityMatrix", "EstimatorV2", "GBQVError", "NativeCircuit", "NoiseModel",
+    "AerSimulator", "adjoint", "batched", "DensityMatrix", "EstimatorV2", "SamplerV2", "GBQVError", "NativeCircuit", "NoiseModel",
     "Parameter", "ParameterExpression", "QuantumCircuit",
     "QuantumError", "QubitVector", "Result", "UnitaryMatrix", "amplitude_damping_error", "depolarizing_error", "lib",
     "phase_amplitude_damping_error", "uniforms",

@@ -117,6 +117,7 @@ _SIGS = {
     "gbqv_execute_bound": (C.c_int, [H, H, C.c_uint64, C.c_uint64]),
     "gbqv_expval_pauli_segments": (C.c_int, [H, C.c_int, C.c_uint64, C.c_int, u64p, C.POINTER(C.c_int),
                                              C.POINTER(C.c_char_p), dp]),
+    "gbqv_sample_measure_segments": (C.c_int, [H, C.c_int, C.c_uint64, C.c_uint64, dp, C.c_uint64, u64p]),
     "gbqv_set_blocking": (C.c_int, [H, C.c_int]),
     "gbqv_set_tensor_c128": (C.c_int, [H, C.c_int]),
     "gbqv_batch_create": (C.c_int, [C.c_int, C.POINTER(H)]),

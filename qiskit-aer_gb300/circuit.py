@@ -150,6 +150,7 @@ class QuantumCircuit:
         self.num_clbits = int(num_clbits)
         self.name = name
         self.metadata = dict(metadata or {})
+        self.creg_name = "c"  # the classical register's name ("meas" after measure_all, as qiskit names it)
         self.data: list[Instruction] = []
 
     # ---- generic ----
@@ -175,6 +176,7 @@ class QuantumCircuit:
 
     def copy(self) -> "QuantumCircuit":
         out = QuantumCircuit(self.num_qubits, self.num_clbits, self.name, self.metadata)
+        out.creg_name = self.creg_name
         out.data = [Instruction(i.kind, i.name, list(i.qubits), list(i.params), i.data, list(i.clbits), i.condition)
                     for i in self.data]
         return out
@@ -226,6 +228,8 @@ class QuantumCircuit:
         return self
 
     def measure_all(self):
+        if self.num_clbits == 0:
+            self.creg_name = "meas"
         return self.measure(list(range(self.num_qubits)), list(range(self.num_qubits)))
 
     def c_if(self, clbits, value: int):

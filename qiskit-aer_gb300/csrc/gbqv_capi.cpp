@@ -684,6 +684,29 @@ extern "C" int gbqv_sample_measure(gbqv_handle h, const double *rnds, uint64_t s
   });
 }
 
+extern "C" int gbqv_sample_measure_segments(gbqv_handle h, int state_qubits, uint64_t first, uint64_t nseg,
+                                            const double *rnds, uint64_t shots, uint64_t *out) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    REQUIRE(!d.density && !d.unitary, GBQV_ERR_KIND, "sample_measure_segments: statevector stacks only");
+    REQUIRE(state_qubits >= 1 && state_qubits <= d.n && first + nseg <= (d.amps() >> state_qubits), GBQV_ERR_ARG,
+            "sample_measure_segments: the states do not fit the handle's vector");
+    if (shots == 0 || nseg == 0) return;
+    REQUIRE(rnds && out, GBQV_ERR_ARG, "null shot buffers");
+    const uint64_t total = shots * nseg;
+    grow(reinterpret_cast<void *&>(h->io), h->io_cap, total * 16);
+    double *d_r = reinterpret_cast<double *>(h->io);
+    uint64_t *d_o = h->io + total;
+    cuda_check(cudaMemcpyAsync(d_r, rnds, total * sizeof(double), cudaMemcpyHostToDevice, d.stream),
+               "uniform upload");
+    for (uint64_t s = 0; s < nseg; ++s)  // each state sampled exactly as a state of its own
+      sample_measure(d, d_r + s * shots, shots, d_o + s * shots, (first + s) << state_qubits, state_qubits);
+    cuda_check(cudaMemcpyAsync(out, d_o, total * sizeof(uint64_t), cudaMemcpyDeviceToHost, d.stream), "sample copy");
+    sync(d);
+  });
+}
+
 extern "C" int gbqv_expval_pauli(gbqv_handle h, const uint64_t *qubits, int nq, const char *label,
                                  gbqv_c128 initial_phase, double *out) {
   return guard(h, [&] {

@@ -104,8 +104,11 @@ void reduce_probabilities(Device &dev, const reg_t &qubits);     // 2^k values
 void reduce_dm_trace(Device &dev);                               // 2 values
 // Probabilities of every basis state into a device buffer of 2^nq doubles.
 void probabilities_all(Device &dev, double *d_out);
-// Sampling: rnds/out are device buffers of `shots` entries.
-void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out);
+// Sampling: rnds/out are device buffers of `shots` entries.  amp_offset /
+// nbits (>= 0) sample the 2^nbits-amplitude statevector starting at that
+// amplitude (one state of a stack) instead of the whole state.
+void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out, uint64_t amp_offset = 0,
+                    int nbits = -1);
 
 // Adjoint gradients: out = sum_t c_t P_t src (one pass), and
 // <lam|P|psi> into dev.results[2*slot .. 2*slot+1] (re, im).

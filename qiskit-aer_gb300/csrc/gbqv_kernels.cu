@@ -1156,8 +1156,9 @@ void probabilities_all(Device &dev, double *d_out) {
   check_launch("probabilities kernel");
 }
 
-void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out) {
-  const int n = sample_bits(dev);
+void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out, uint64_t amp_offset,
+                    int nbits) {
+  const int n = nbits >= 0 ? nbits : sample_bits(dev);
   const int bb = std::min(n, kSampleBlockBits);
   const uint64_t nblocks = 1ULL << (n - bb);
   const uint64_t nchunks = (nblocks + 1023) / 1024;
@@ -1167,9 +1168,9 @@ void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t 
   const uint64_t ds = diag_stride(dev);
   const int g1 = grid_for(nblocks * 32, 256);
   if (dev.dbl)
-    k_block_sums<double2><<<g1, 256, 0, dev.stream>>>(st<double2>(dev), nblocks, bb, ds, cdf);
+    k_block_sums<double2><<<g1, 256, 0, dev.stream>>>(st<double2>(dev) + amp_offset, nblocks, bb, ds, cdf);
   else
-    k_block_sums<float2><<<g1, 256, 0, dev.stream>>>(st<float2>(dev), nblocks, bb, ds, cdf);
+    k_block_sums<float2><<<g1, 256, 0, dev.stream>>>(st<float2>(dev) + amp_offset, nblocks, bb, ds, cdf);
   check_launch("sampling block sums");
   k_scan_chunks<<<(unsigned)nchunks, 1024, 0, dev.stream>>>(cdf, nblocks, tot);
   check_launch("sampling prefix");
@@ -1179,9 +1180,11 @@ void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t 
   check_launch("sampling prefix");
   const int g2 = grid_for(shots * 32, 256, 16);
   if (dev.dbl)
-    k_sample<double2><<<g2, 256, 0, dev.stream>>>(st<double2>(dev), n, cdf, nblocks, bb, ds, d_rnds, shots, d_out);
+    k_sample<double2><<<g2, 256, 0, dev.stream>>>(st<double2>(dev) + amp_offset, n, cdf, nblocks, bb, ds, d_rnds,
+                                                  shots, d_out);
   else
-    k_sample<float2><<<g2, 256, 0, dev.stream>>>(st<float2>(dev), n, cdf, nblocks, bb, ds, d_rnds, shots, d_out);
+    k_sample<float2><<<g2, 256, 0, dev.stream>>>(st<float2>(dev) + amp_offset, n, cdf, nblocks, bb, ds, d_rnds,
+                                                 shots, d_out);
   check_launch("sampling search");
 }
 

@@ -233,3 +233,136 @@ class EstimatorV2:
         return PubResult(DataBin(evs=evs, stds=stds, shape=evs.shape),
                          metadata={"target_precision": precision, "circuit_metadata": circuit.metadata,
                                    "simulator_metadata": result.metadata(0) if result.results else {}})
+
+
+# ---------------------------------------------------------------------------
+# SamplerV2 (qiskit_aer/primitives/sampler_v2.py): shots of (parameterised)
+# circuits, returned per classical register as bit arrays of the pub's shape.
+# ---------------------------------------------------------------------------
+class BitArray:
+    """Shots of one classical register: `values` holds each shot's register
+    value, shape pub_shape + (shots,); `array` is the packed big-endian byte
+    form of qiskit's BitArray."""
+
+    def __init__(self, values: np.ndarray, num_bits: int):
+        self._values = np.asarray(values, dtype=np.uint64)
+        self.num_bits = int(num_bits)
+
+    @property
+    def shape(self):
+        return self._values.shape[:-1]
+
+    @property
+    def num_shots(self) -> int:
+        return self._values.shape[-1]
+
+    @property
+    def array(self) -> np.ndarray:
+        nbytes = max(1, (self.num_bits + 7) // 8)
+        out = np.zeros(self._values.shape + (nbytes,), dtype=np.uint8)
+        for b in range(nbytes):
+            out[..., nbytes - 1 - b] = ((self._values >> np.uint64(8 * b)) & np.uint64(0xFF)).astype(np.uint8)
+        return out
+
+    def _sel(self, loc):
+        v = self._values if loc is None else self._values[loc]
+        return v.reshape(-1)
+
+    def get_int_counts(self, loc=None) -> dict:
+        vals, cnt = np.unique(self._sel(loc), return_counts=True)
+        return {int(v): int(c) for v, c in zip(vals, cnt)}
+
+    def get_counts(self, loc=None) -> dict:
+        return {format(v, f"0{self.num_bits}b"): c for v, c in self.get_int_counts(loc).items()}
+
+    def get_bitstrings(self, loc=None) -> list:
+        return [format(int(v), f"0{self.num_bits}b") for v in self._sel(loc)]
+
+
+class SamplerPubResult(PubResult):
+    def join_data(self):
+        return next(iter(v for k, v in vars(self.data).items() if k not in ("_fields", "shape")))
+
+
+class SamplerV2:
+    """Samples of circuits with their final measurements (sampler_v2.py:53-228):
+    pubs with the same shot count run as one job with their parameter
+    bindings, `seed` as seed_simulator, per-shot memory turned into bit
+    arrays."""
+
+    def __init__(self, *, default_shots: int = 1024, seed: int | None = None, options: dict | None = None):
+        self._default_shots = int(default_shots)
+        self._seed = seed
+        opts = dict(options or {})
+        self._options = Options(backend_options=opts.get("backend_options", {}),
+                                run_options=opts.get("run_options", {}))
+        self._backend = AerSimulator(**self._options.backend_options)
+
+    @property
+    def default_shots(self) -> int:
+        return self._default_shots
+
+    @property
+    def seed(self):
+        return self._seed
+
+    @property
+    def options(self) -> Options:
+        return self._options
+
+    def run(self, pubs, *, shots: int | None = None) -> PrimitiveJob:
+        if shots is None:
+            shots = self._default_shots
+        coerced = []
+        for pub in pubs:
+            if isinstance(pub, QuantumCircuit):
+                pub = (pub,)
+            circuit = pub[0]
+            values = pub[1] if len(pub) > 1 else None
+            s = pub[2] if len(pub) > 2 and pub[2] is not None else shots
+            if int(s) < 1:
+                raise ValueError("shots must be positive")
+            coerced.append((circuit, coerce_parameter_values(values, circuit), int(s)))
+        job = PrimitiveJob(self._run, coerced)
+        job._submit()
+        return job
+
+    def _run(self, pubs) -> PrimitiveResult:
+        by_shots: dict = {}
+        for i, pub in enumerate(pubs):
+            by_shots.setdefault(pub[2], []).append(i)
+        results = [None] * len(pubs)
+        for shots, idx in by_shots.items():
+            for i, r in zip(idx, self._run_pubs([pubs[i] for i in idx], shots)):
+                results[i] = r
+        return PrimitiveResult(results, metadata={"version": 2})
+
+    def _run_pubs(self, pubs, shots: int):
+        circuits, binds, shapes = [], [], []
+        for circuit, values, _ in pubs:
+            params = circuit.parameters
+            shape = values.shape[:-1] if values is not None else ()
+            flat = values.reshape(-1, len(params)) if values is not None else np.zeros((1, 0))
+            circuits.append(circuit)
+            binds.append({p: flat[:, i] for i, p in enumerate(params)} if params else {})
+            shapes.append(shape)
+        run_options = {k: v for k, v in self._options.run_options.items()
+                       if k not in ("shots", "parameter_binds", "memory", "seed_simulator")}
+        result = self._backend.run(circuits, shots=shots, seed_simulator=self._seed, parameter_binds=binds,
+                                   memory=True, **run_options)
+        out, k = [], 0
+        for (circuit, _, _), shape in zip(pubs, shapes):
+            size = int(np.prod(shape, dtype=np.int64))
+            vals = np.zeros((size, shots), dtype=np.uint64)
+            for j in range(size):
+                mem = result.data(k + j).get("memory")
+                if mem:
+                    vals[j] = [int(x, 16) for x in mem]
+            k += size
+            bits = BitArray(vals.reshape(tuple(shape) + (shots,)), circuit.num_clbits)
+            out.append(SamplerPubResult(DataBin(**{circuit.creg_name: bits, "shape": tuple(shape)}),
+                                        metadata={"shots": shots, "circuit_metadata": circuit.metadata,
+                                                  "simulator_metadata": result.metadata(0) if result.results
+                                                  else {}}))
+        return out
+

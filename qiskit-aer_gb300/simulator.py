@@ -54,6 +54,9 @@ class Result:
     def get_counts(self, i=0):
         return self.results[i]["counts"]
 
+    def get_memory(self, i=0):
+        return self.results[i]["data"]["memory"]
+
     def data(self, i=0):
         return self.results[i]["data"]
 
@@ -157,11 +160,15 @@ class AerSimulator:
                 meta["fusion"]["method"] = method_name
         return segments, meas, saves, meta
 
-    def run(self, circuits, shots: int = 1024, seed_simulator: int | None = None, parameter_binds=None, **_):
+    _want_memory = False
+
+    def run(self, circuits, shots: int = 1024, seed_simulator: int | None = None, parameter_binds=None,
+            memory: bool = False, **_):
         """parameter_binds: one dict {Parameter: values} per circuit (AerBackend.run,
         qiskit_aer/backends/aerbackend.py:146-185); a parameterised circuit
         becomes one experiment per binding, in order, and experiment k of the
         job gets seed seed_simulator + 2113 * k (controller_execute.hpp:188-210)."""
+        self._want_memory = bool(memory)
         single = isinstance(circuits, QuantumCircuit)
         if single:
             circuits = [circuits]
@@ -220,14 +227,13 @@ class AerSimulator:
     def _bound_batchable(self, circuit: QuantumCircuit) -> bool:
         """Bindings run together on one stack of states when the circuit is a
         unitary statevector circuit whose saves (expectation values,
-        statevectors) all sit at its end."""
+        statevectors) and measurements all sit at its end; each binding's
+        shots are then drawn from its own state of the stack."""
         if self.method != "statevector" or (self.noise_model is not None and not self.noise_model.is_ideal()):
             return False
         if circuit.needs_shots("statevector"):
             return False
         body, meas, saves = circuit.split_final()
-        if meas:
-            return False
         if any(ins.kind not in ("gate", "unitary", "diagonal", "barrier") for ins in body):
             return False
         return all(pos == len(body) and ins.name in ("expval", "statevector") for pos, ins in saves)
@@ -243,7 +249,10 @@ class AerSimulator:
         and each chunk of bindings runs on one stack of states
         (gbqv_execute_bound); expectation values are reduced per state."""
         n = circuit.num_qubits
-        body, _, saves = circuit.split_final()
+        body, meas, saves = circuit.split_final()
+        mq = [q for m in meas for q in m.qubits]
+        mc = [c for m in meas for c in m.clbits]
+        counts = [None] * nbind
         nc = NativeCircuit(n, body)
         nc.bind(binds, nbind)
         data = [{} for _ in range(nbind)]
@@ -259,6 +268,17 @@ class AerSimulator:
                         st.close()
                     st, st_bits = QubitVector(n + b, self.precision), b
                 A.check(L.gbqv_execute_bound(st.handle, nc.handle, first, cnt), st.handle)
+                if meas and shots > 0:
+                    # every binding draws from its own RngEngine stream, seed_simulator + 2113 k
+                    rnds = np.ascontiguousarray(np.concatenate([uniforms(seeds[first + j], shots) for j in range(cnt)]))
+                    smp = np.empty(cnt * shots, dtype=np.uint64)
+                    A.check(L.gbqv_sample_measure_segments(st.handle, n, 0, cnt, rnds.ctypes.data_as(A.dp), shots,
+                                                           smp.ctypes.data_as(A.u64p)), st.handle)
+                    for j in range(cnt):
+                        sj = smp[j * shots:(j + 1) * shots]
+                        counts[first + j] = self._counts(sj, mq, mc, circuit.num_clbits)
+                        if self._want_memory:
+                            data[first + j]["memory"] = self._memory(self._memory_values(sj, mq, mc))
                 for _, ins in saves:
                     if ins.name == "statevector":
                         vec = st.copy_to_vector()
@@ -279,8 +299,8 @@ class AerSimulator:
                 st.close()
         meta = {"fusion": {"enabled": False}, "parameter_binding": {"batched": True, "bindings": nbind,
                                                                    "stack_qubits": n + max(st_bits, 0)}}
-        return [{"counts": None, "data": data[j], "metadata": dict(meta), "seed_simulator": seeds[j], "shots": shots}
-                for j in range(nbind)]
+        return [{"counts": counts[j], "data": data[j], "metadata": dict(meta), "seed_simulator": seeds[j],
+                 "shots": shots} for j in range(nbind)]
 
     def _run_one(self, circuit: QuantumCircuit, shots: int, seed: int):
         if self.method == "statevector" and circuit.needs_shots("statevector"):
@@ -307,6 +327,8 @@ class AerSimulator:
                 rnds = uniforms(seed, shots)
                 samples = st.sample_measure(rnds)
                 counts = self._counts(samples, qubits, clbits, circuit.num_clbits)
+                if self._want_memory:
+                    data["memory"] = self._memory(self._memory_values(samples, qubits, clbits))
             st.synchronize()
         return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
 
@@ -394,12 +416,23 @@ class AerSimulator:
                 st.apply_matrix(qubits, perm)
 
     @staticmethod
-    def _counts(samples, qubits, clbits, num_clbits):
+    def _memory_values(samples, qubits, clbits):
+        """Classical memory per shot (measured qubit q -> clbit c)."""
         memory = np.zeros(samples.size, dtype=np.uint64)
         for q, c in zip(qubits, clbits):
             memory |= ((samples >> np.uint64(q)) & np.uint64(1)) << np.uint64(c)
-        vals, cnt = np.unique(memory, return_counts=True)
+        return memory
+
+    @classmethod
+    def _counts(cls, samples, qubits, clbits, num_clbits):
+        vals, cnt = np.unique(cls._memory_values(samples, qubits, clbits), return_counts=True)
         return {format(int(v), f"0{num_clbits}b"): int(n) for v, n in zip(vals, cnt)}
+
+    @staticmethod
+    def _memory(values):
+        """Per-shot memory in the reference's hex form (ExperimentResult
+        memory, one "0x..." string per shot in draw order)."""
+        return [hex(int(v)) for v in values]
 
     def _check_unitary_circuit(self, circuit: QuantumCircuit):
         """The unitary method's op set (QubitUnitary::StateOpSet,

@@ -169,16 +169,43 @@ def test_padding_states_stay_zero_and_binding_offset():
         np.testing.assert_allclose(stack[j << n:(j + 1) << n], o.data, atol=1e-13)
 
 
-def test_measured_circuit_runs_binding_by_binding():
+@pytest.mark.parametrize("n", [3, 12])
+def test_measured_bound_circuit_samples_each_state_as_its_own(n):
+    """Shots of a bound circuit come from each binding's own state of the
+    stack with its own seed: counts and per-shot memory equal the circuit
+    bound and run alone."""
     P = pkg()
     a, b = P.Parameter("a"), P.Parameter("b")
-    qc = P.QuantumCircuit(3).ry(a, 0).cx(0, 1).rx(b, 2).measure_all()
-    binds = {a: [0.3, 1.9], b: [2.2, -0.4]}
-    res = P.AerSimulator().run(qc, shots=500, parameter_binds=[binds], seed_simulator=21)
-    for j in range(2):
+    qc = P.QuantumCircuit(n).ry(a, 0).cx(0, 1).rx(b, n - 1)
+    for q in range(2, n, 3):
+        qc.h(q)
+    qc.measure_all()
+    binds = {a: [0.3, 1.9, -2.2], b: [2.2, -0.4, 0.9]}
+    res = P.AerSimulator().run(qc, shots=500, parameter_binds=[binds], seed_simulator=21, memory=True)
+    assert res.metadata(0)["parameter_binding"]["batched"]
+    for j in range(3):
         one = P.AerSimulator().run(qc.assign_parameters({a: binds[a][j], b: binds[b][j]}), shots=500,
-                                   seed_simulator=21 + 2113 * j)
+                                   seed_simulator=21 + 2113 * j, memory=True)
         assert res.get_counts(j) == one.get_counts()
+        assert res.get_memory(j) == one.get_memory()
+        assert len(res.get_memory(j)) == 500
+
+
+def test_sampler_v2_shapes_and_counts():
+    P = pkg()
+    a = P.Parameter("a")
+    qc = P.QuantumCircuit(2).ry(a, 0).cx(0, 1).measure_all()
+    vals = np.linspace(0.2, 2.8, 6).reshape(2, 3, 1)
+    res = P.SamplerV2(seed=7).run([(qc, vals), (P.QuantumCircuit(1).h(0).measure_all(),)], shots=300).result()
+    bits = res[0].data.meas
+    assert bits.shape == (2, 3) and bits.num_shots == 300 and bits.num_bits == 2
+    assert bits.array.shape == (2, 3, 300, 1)
+    for k, idx in enumerate(np.ndindex(2, 3)):
+        want = P.AerSimulator().run(qc.assign_parameters([vals[idx][0]]), shots=300,
+                                    seed_simulator=7 + 2113 * k).get_counts()
+        assert bits.get_counts(idx) == want
+        assert set(bits.get_counts(idx)) <= {"00", "11"}
+    assert sum(res[1].data.meas.get_counts().values()) == 300
 
 
 def test_unbound_parameters_are_an_error():

@@ -134,3 +134,17 @@ def test_unitary_method_host_rules():
                 P.QuantumCircuit(2).h(0).save_statevector()):
         with pytest.raises(ValueError, match="invalid instruction"):
             sim._check_unitary_circuit(bad)
+
+
+def test_bit_array_packing_and_counts():
+    P = pkg()
+    import importlib
+    pr = importlib.import_module(P.__name__ + ".primitives")
+    vals = np.array([[0b1011, 0b0001, 0b1011], [0x1FF, 0, 1]], dtype=np.uint64)
+    b = pr.BitArray(vals, 9)
+    assert b.shape == (2,) and b.num_shots == 3
+    np.testing.assert_array_equal(b.array[0, 0], [0x00, 0x0B])      # big-endian bytes
+    np.testing.assert_array_equal(b.array[1, 0], [0x01, 0xFF])
+    assert b.get_counts(0) == {"000001011": 2, "000000001": 1}
+    assert b.get_bitstrings(1) == ["111111111", "000000000", "000000001"]
+    assert sum(b.get_int_counts().values()) == 6
