@@ -51,6 +51,11 @@ class Result:
         self.results = results
         self.time_taken = time_taken
 
+    def result(self):
+        """The job's result: run() completes before it returns, so the
+        AerJob-style `backend.run(...).result()` chain is this object."""
+        return self
+
     def get_counts(self, i=0):
         return self.results[i]["counts"]
 
