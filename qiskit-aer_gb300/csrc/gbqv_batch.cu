@@ -103,25 +103,34 @@ __device__ __forceinline__ uint32_t ins1(uint32_t i, int q) {
 // Apply gate g (or its inverse) to a tile; a, b are the local positions.
 // MT > 0: the tile has MT qubits (compile-time trip counts, fully unrolled
 // loops so that the shared-memory accesses of a thread overlap); MT = 0: m.
+// gc, gs: cos(theta/2), sin(theta/2) of a rotation in the data precision
+// (converted once per run: conversions and products in double would run on
+// the narrow FP64 pipe for every tile).
 template <typename T, int MT>
-__device__ __forceinline__ void tile_gate(T *tile, int m, const GateDev &g, int a, int b, bool inverse) {
+__device__ __forceinline__ void tile_gate(T *tile, int m, int kind, decltype(T::x) gc, decltype(T::x) gs, int a,
+                                          int b, bool inverse) {
+  using R = decltype(T::x);
   const uint32_t L = MT ? (1u << MT) : (1u << m);
   constexpr int kU = MT ? 16 : 1;
-  if (g.kind == B_RZ) {
+  if (kind == B_RZ) {
     // diag(e^{-i t/2}, e^{i t/2}); inverse conjugates
-    const double sg = inverse ? -1.0 : 1.0;
-    const T d0 = cplx<T>(g.c, -sg * g.s), d1 = cplx<T>(g.c, sg * g.s);
+    const R s1 = inverse ? -gs : gs;
+    T d0, d1;
+    d0.x = gc;
+    d0.y = -s1;
+    d1.x = gc;
+    d1.y = s1;
 #pragma unroll kU
     for (uint32_t l = threadIdx.x; l < L; l += kBatchThreads) tile[l] = cmul(tile[l], (l >> a) & 1 ? d1 : d0);
     return;
   }
-  if (g.kind == B_CX || g.kind == B_CZ) {
+  if (kind == B_CX || kind == B_CZ) {
     const int lo = min(a, b), hi = max(a, b);
 #pragma unroll kU
     for (uint32_t p = threadIdx.x; p < (L >> 2); p += kBatchThreads) {
       const uint32_t base = ins1(ins1(p, lo), hi) | (1u << a);  // control set
       const uint32_t i1 = base | (1u << b);
-      if (g.kind == B_CX) {
+      if (kind == B_CX) {
         const T t0 = tile[base];
         tile[base] = tile[i1];
         tile[i1] = t0;
@@ -136,15 +145,14 @@ __device__ __forceinline__ void tile_gate(T *tile, int m, const GateDev &g, int 
   }
   // 2x2 matrices: RX, RY, H
   T m00, m01, m10, m11;
-  if (g.kind == B_RY) {
-    const double s = inverse ? -g.s : g.s;
-    m00 = cplx<T>(g.c, 0); m01 = cplx<T>(-s, 0); m10 = cplx<T>(s, 0); m11 = cplx<T>(g.c, 0);
-  } else if (g.kind == B_RX) {
-    const double s = inverse ? -g.s : g.s;
-    m00 = cplx<T>(g.c, 0); m01 = cplx<T>(0, -s); m10 = cplx<T>(0, -s); m11 = cplx<T>(g.c, 0);
+  const R zero = 0, s1 = inverse ? -gs : gs;
+  if (kind == B_RY) {
+    m00.x = gc; m00.y = zero; m01.x = -s1; m01.y = zero; m10.x = s1; m10.y = zero; m11.x = gc; m11.y = zero;
+  } else if (kind == B_RX) {
+    m00.x = gc; m00.y = zero; m01.x = zero; m01.y = -s1; m10.x = zero; m10.y = -s1; m11.x = gc; m11.y = zero;
   } else {  // H
-    const double h = 0.70710678118654752440;
-    m00 = cplx<T>(h, 0); m01 = cplx<T>(h, 0); m10 = cplx<T>(h, 0); m11 = cplx<T>(-h, 0);
+    const R h = (R)0.70710678118654752440;
+    m00.x = h; m00.y = zero; m01.x = h; m01.y = zero; m10.x = h; m10.y = zero; m11.x = -h; m11.y = zero;
   }
 #pragma unroll kU
   for (uint32_t p = threadIdx.x; p < (L >> 1); p += kBatchThreads) {
@@ -159,10 +167,11 @@ __device__ __forceinline__ void tile_gate(T *tile, int m, const GateDev &g, int 
 }
 
 // This thread's part of Im <lam| P |psi> over a tile for the generator of a
-// rotation gate on local bit a (summed in the data precision: at most 2^m /
-// blockDim terms per thread; the caller accumulates in double).
+// rotation gate on local bit a, summed in the data precision (at most 2^m /
+// blockDim terms per thread; the caller sums the warp and then accumulates
+// in double).
 template <typename T, int MT>
-__device__ __forceinline__ double tile_generator(const T *lam, const T *psi, int m, int kind, int a) {
+__device__ __forceinline__ decltype(T::x) tile_generator(const T *lam, const T *psi, int m, int kind, int a) {
   using R = decltype(T::x);
   const uint32_t L = MT ? (1u << MT) : (1u << m), bit = 1u << a;
   constexpr int kU = MT ? 16 : 1;
@@ -185,7 +194,7 @@ __device__ __forceinline__ double tile_generator(const T *lam, const T *psi, int
     // Im(conj(lv) * pv)
     acc += lv.x * pv.y - lv.y * pv.x;
   }
-  return (double)acc;
+  return acc;
 }
 
 template <typename T, int M>
@@ -207,6 +216,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
   // generator inner products (reduced over warps once per run)
   __shared__ GateDev s_g[kBatchMaxRunOps];
   __shared__ uint8_t s_a[kBatchMaxRunOps], s_b[kBatchMaxRunOps];
+  __shared__ decltype(T::x) s_c[kBatchMaxRunOps], s_s[kBatchMaxRunOps];
   __shared__ double gacc[kBatchMaxRunOps][kBatchThreads / 32];
   __shared__ int s_idx;
   __shared__ int s_T[64];
@@ -351,6 +361,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           s_g[k] = g;
           s_a[k] = (uint8_t)a;
           s_b[k] = (uint8_t)b;
+          s_c[k] = (decltype(T::x))g.c;
+          s_s[k] = (decltype(T::x))g.s;
         }
         __syncthreads();
         const int m = __popcll(R.tmask);
@@ -407,17 +419,20 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
             const GateDev &g = s_g[oi];
             const int a = s_a[oi], b = s_b[oi];
             if (dir == 1 && g.param >= 0) {
-              double part = m == M ? tile_generator<T, M>(tl, tp, m, g.kind, a)
-                                   : tile_generator<T, 0>(tl, tp, m, g.kind, a);
+              // the warp's sum in the data precision (32 terms), then into the
+              // double accumulator of the warp
+              auto part = m == M ? tile_generator<T, M>(tl, tp, m, g.kind, a)
+                                 : tile_generator<T, 0>(tl, tp, m, g.kind, a);
               for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-              if ((threadIdx.x & 31) == 0) gacc[oi][threadIdx.x >> 5] += part;
+              if ((threadIdx.x & 31) == 0) gacc[oi][threadIdx.x >> 5] += (double)part;
             }
+            const auto gc = s_c[oi], gs = s_s[oi];
             if (m == M) {
-              tile_gate<T, M>(tp, m, g, a, b, dir == 1);
-              if (dir == 1) tile_gate<T, M>(tl, m, g, a, b, true);
+              tile_gate<T, M>(tp, m, g.kind, gc, gs, a, b, dir == 1);
+              if (dir == 1) tile_gate<T, M>(tl, m, g.kind, gc, gs, a, b, true);
             } else {
-              tile_gate<T, 0>(tp, m, g, a, b, dir == 1);
-              if (dir == 1) tile_gate<T, 0>(tl, m, g, a, b, true);
+              tile_gate<T, 0>(tp, m, g.kind, gc, gs, a, b, dir == 1);
+              if (dir == 1) tile_gate<T, 0>(tl, m, g.kind, gc, gs, a, b, true);
             }
             __syncthreads();
           }
