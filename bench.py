@@ -446,7 +446,8 @@ def bench_batch(args, torch, P):
     gradient and shots per instance in one graph-captured persistent launch,
     next to one instance per launch (the per-instance engine) on a sample."""
     B, adj = P.batched, P.adjoint
-    insts = B.config5_instances(args.instances, seed=args.seed)
+    insts = B.config5_instances(args.instances, seed=args.seed, qmin=args.batch_qmin, qmax=args.batch_qmax,
+                                dmin=args.batch_dmin, dmax=args.batch_dmax)
     b = B.Batch(args.precision)
     for inst in insts:
         b.add(inst["n"], inst["gates"], inst["theta"], inst["terms"], inst["coeffs"], inst["shots"], inst["seed"])
@@ -485,7 +486,8 @@ def bench_batch(args, torch, P):
             "one_instance_per_launch_s_estimated": round(est_single, 2),
             "one_instance_per_launch_measured": f"{len(sample)} instances in {t_single:.2f} s",
             "speedup_vs_per_launch": round(est_single / (ms / 1e3), 2),
-            "config": {"workload": f"{len(insts)} instances, 12-22 qubits, depth 4-16, 20-60 Paulis, 4096 shots",
+            "config": {"workload": f"{len(insts)} instances, {args.batch_qmin}-{args.batch_qmax} qubits, depth "
+                                   f"{args.batch_dmin}-{args.batch_dmax}, 20-60 Paulis, 4096 shots",
                        "instances": len(insts)}, "clocks": clk}
 
 
@@ -653,6 +655,10 @@ def main():
     ap.add_argument("--est-bindings", type=int, default=1024)
     ap.add_argument("--per-binding-sample", type=int, default=8)
     ap.add_argument("--instances", type=int, default=2048)
+    ap.add_argument("--batch-qmin", type=int, default=12)
+    ap.add_argument("--batch-qmax", type=int, default=22)
+    ap.add_argument("--batch-dmin", type=int, default=4)
+    ap.add_argument("--batch-dmax", type=int, default=16)
     ap.add_argument("--per-launch-sample", type=int, default=24)
     ap.add_argument("--precision", default="double", choices=["double", "single"])
     ap.add_argument("--qubits", type=int, default=30)
