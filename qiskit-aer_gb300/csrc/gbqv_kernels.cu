@@ -566,7 +566,12 @@ __global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n
   const TermDev t = terms[blockIdx.y];
   using R = decltype(T::x);
   const R pr = (R)t.ph_re, pi = (R)t.ph_im;
+  // complex64: short sums in float before the double accumulator (one FP64
+  // add per 8 amplitudes instead of one per amplitude)
+  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
   double acc = 0.0;
+  R part = 0;
+  int cnt = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   if (!t.x_mask) {
     const uint64_t count = 1ULL << n;
@@ -575,7 +580,8 @@ __global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n
       // real(phase * a * conj(a)) = Re(phase) * |a|^2 in the data precision
       R v = pr * (a.x * a.x + a.y * a.y);
       if (t.z_mask && (__popcll(i & t.z_mask) & 1)) v = -v;
-      acc += (double)v;
+      part += v;
+      if (++cnt == kChunk) { acc += (double)part; part = 0; cnt = 0; }
     }
   } else {
     const uint64_t count = 1ULL << (n - 1);
@@ -592,10 +598,11 @@ __global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n
       R v1 = pr * zr + pi * zi;
       if (t.z_mask && (__popcll(i0 & t.z_mask) & 1)) v0 = -v0;
       if (t.z_mask && (__popcll(i1 & t.z_mask) & 1)) v1 = -v1;
-      acc += (double)v0;
-      acc += (double)v1;
+      part += v0 + v1;
+      if (++cnt == kChunk) { acc += (double)part; part = 0; cnt = 0; }
     }
   }
+  acc += (double)part;
   acc = block_sum(acc);
   if (threadIdx.x == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = acc;
 }
@@ -1499,16 +1506,24 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_ham_apply(const T *__restrict__ psi, T *__restrict__ out, uint64_t count,
                                                    const HamTermDev *__restrict__ terms, int nterms) {
   using R = decltype(T::x);
+  // complex64: the products and short sums (8 terms) in float, then into the
+  // double sums; complex128: everything in double
+  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
     double ar = 0.0, ai = 0.0;
-    for (int t = 0; t < nterms; ++t) {
-      const HamTermDev h = terms[t];
-      const T a = psi[i ^ h.x_mask];
-      double cr = h.re, ci = h.im;
-      if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
-      ar += cr * (double)a.x - ci * (double)a.y;
-      ai += cr * (double)a.y + ci * (double)a.x;
+    for (int t0 = 0; t0 < nterms; t0 += kChunk) {
+      R sr = 0, si = 0;
+      for (int t = t0; t < min(nterms, t0 + kChunk); ++t) {
+        const HamTermDev h = terms[t];
+        const T a = psi[i ^ h.x_mask];
+        R cr = (R)h.re, ci = (R)h.im;
+        if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
+        sr += cr * a.x - ci * a.y;
+        si += cr * a.y + ci * a.x;
+      }
+      ar += (double)sr;
+      ai += (double)si;
     }
     T o;
     o.x = (R)ar;
@@ -1522,17 +1537,32 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_pauli_inner(const T *__restrict__ lam, const T *__restrict__ psi, uint64_t count,
                                                      uint64_t x_mask, uint64_t z_mask, double ph_re, double ph_im,
                                                      double *__restrict__ partials) {
+  using R = decltype(T::x);
+  // complex64: products and short sums (8 amplitudes) in float, then into
+  // the double sums; complex128: everything in double
+  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
   double re = 0.0, im = 0.0;
+  R sr = 0, si = 0;
+  int cnt = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
     const T l = lam[i], a = psi[i ^ x_mask];
     // conj(l) * a
-    double zr = (double)l.x * a.x + (double)l.y * a.y;
-    double zi = (double)l.x * a.y - (double)l.y * a.x;
+    R zr = l.x * a.x + l.y * a.y;
+    R zi = l.x * a.y - l.y * a.x;
     if (__popcll(i & z_mask) & 1) { zr = -zr; zi = -zi; }
-    re += zr;
-    im += zi;
+    sr += zr;
+    si += zi;
+    if (++cnt == kChunk) {
+      re += (double)sr;
+      im += (double)si;
+      sr = 0;
+      si = 0;
+      cnt = 0;
+    }
   }
+  re += (double)sr;
+  im += (double)si;
   // times the phase
   const double pr = re * ph_re - im * ph_im, pi = re * ph_im + im * ph_re;
   const double r = block_sum(pr);
