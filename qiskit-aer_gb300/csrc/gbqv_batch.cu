@@ -218,6 +218,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
   __shared__ uint8_t s_a[kBatchMaxRunOps], s_b[kBatchMaxRunOps];
   __shared__ decltype(T::x) s_c[kBatchMaxRunOps], s_s[kBatchMaxRunOps];
   __shared__ double gacc[kBatchMaxRunOps][kBatchThreads / 32];
+  __shared__ decltype(T::x) gaccf[kBatchMaxRunOps][kBatchThreads / 32];  // this tile group's sums, data precision
   __shared__ int s_idx;
   __shared__ int s_T[64];
   for (;;) {
@@ -271,15 +272,15 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           uint64_t res = N - 1;
           if (lo < nb) {
             double p = lo ? cdf[lo - 1] : 0.0;
+            float rem = (float)(r - p);  // complex64: the block's remaining mass, walked in float
             const uint64_t b0 = lo << bb;
             bool found = false;
             for (uint64_t j0 = 0; j0 < (1ULL << bb) && !found; j0 += 32) {
               unsigned msk;
               if constexpr (sizeof(T) == 8) {
                 // complex64: the 32 probabilities and their prefix sums in
-                // float, compared with the remaining mass r - p of the
-                // block (one double subtraction per 32 amplitudes, not one
-                // per amplitude: the FP64 pipe is narrow)
+                // float, compared with the block's remaining mass (converted
+                // once per shot; the FP64 pipe is narrow)
                 float v = 0.0f;
                 if (j0 + lane < (1ULL << bb)) {
                   const T a = psi[b0 + j0 + lane];
@@ -289,9 +290,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
                   const float u = __shfl_up_sync(0xffffffffu, v, o);
                   if (lane >= o) v += u;
                 }
-                const float rem = (float)(r - p);
                 msk = __ballot_sync(0xffffffffu, (j0 + lane < (1ULL << bb)) && (rem < v));
-                p += (double)__shfl_sync(0xffffffffu, v, 31);
+                rem -= __shfl_sync(0xffffffffu, v, 31);
               } else {
                 double v = 0.0;
                 if (j0 + lane < (1ULL << bb)) {
@@ -348,8 +348,10 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           for (int q = 0; q < I.n; ++q)
             if ((R.tmask >> q) & 1) s_T[j++] = q;
         }
-        for (int i = threadIdx.x; i < kBatchMaxRunOps * (kBatchThreads / 32); i += blockDim.x)
+        for (int i = threadIdx.x; i < kBatchMaxRunOps * (kBatchThreads / 32); i += blockDim.x) {
           gacc[i / (kBatchThreads / 32)][i % (kBatchThreads / 32)] = 0.0;
+          gaccf[i / (kBatchThreads / 32)][i % (kBatchThreads / 32)] = 0;
+        }
         __syncthreads();
         for (int k = threadIdx.x; k < R.count; k += blockDim.x) {
           const GateDev g = gates[I.op_off + R.first + k];
@@ -424,7 +426,15 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
               auto part = m == M ? tile_generator<T, M>(tl, tp, m, g.kind, a)
                                  : tile_generator<T, 0>(tl, tp, m, g.kind, a);
               for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-              if ((threadIdx.x & 31) == 0) gacc[oi][threadIdx.x >> 5] += (double)part;
+              if ((threadIdx.x & 31) == 0) {
+                // 16 tiles' warp sums in the data precision, then into double
+                auto &f = gaccf[oi][threadIdx.x >> 5];
+                f += part;
+                if ((t & 15) == 15) {
+                  gacc[oi][threadIdx.x >> 5] += (double)f;
+                  f = 0;
+                }
+              }
             }
             const auto gc = s_c[oi], gs = s_s[oi];
             if (m == M) {
@@ -449,7 +459,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
             const GateDev &g = s_g[k];
             if (g.param < 0) continue;
             double sum = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += gacc[k][w];
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += gacc[k][w] + (double)gaccf[k][w];
             grads[I.grad_off + g.param] += sum;
           }
         __syncthreads();
