@@ -381,6 +381,12 @@ int gbqv_batch_add(gbqv_batch_t b, int num_qubits, int ngates, const int *kinds,
                    const int *param_of_gate, const double *params, int nparams, int nterms, const uint64_t *tq,
                    const int *toffsets, const char *const *labels, const double *coeffs, uint64_t shots,
                    uint64_t seed, int *index);
+/* Teams: the costliest instances (at most max_team_instances <= 64, cost =
+ * gates x 2^qubits at least min_cost_fraction of the largest, spanning two or
+ * more tiles) run on two CTAs each, splitting every run's tiles and meeting at
+ * a bounded barrier after each run (GBQV_ERR_TIMEOUT if one gives up).  Set
+ * before the first gbqv_batch_run; default 64 and 0.5. */
+int gbqv_batch_set_teams(gbqv_batch_t b, int max_team_instances, double min_cost_fraction);
 /* Run every instance in one persistent kernel launch (captured once as a CUDA
  * graph and replayed on later calls): forward pass, `shots` samples of the
  * final state, E = <H>, and with want_grad the adjoint gradient dE/dparams.

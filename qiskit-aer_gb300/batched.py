@@ -55,6 +55,11 @@ class Batch:
         self.instances.append((num_qubits, len(params), int(shots)))
         return idx.value
 
+    def set_teams(self, max_team_instances: int = 64, min_cost_fraction: float = 0.5) -> None:
+        """Two CTAs for each of the costliest instances (gbqv_batch_set_teams);
+        call before the first run."""
+        A.check(self._L.gbqv_batch_set_teams(self._h, int(max_team_instances), float(min_cost_fraction)))
+
     def run(self, want_grad: bool = True) -> float:
         ms = C.c_double()
         A.check(self._L.gbqv_batch_run(self._h, int(want_grad), C.byref(ms)))

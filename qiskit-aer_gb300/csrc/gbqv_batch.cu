@@ -53,6 +53,7 @@ struct TermDevB {
 
 struct InstDev {
   int n, nops, nruns, nterms, nparams;
+  int team;  // CTAs sharing the instance (1: one CTA); members split every run's tiles
   int op_off, run_off, term_off, grad_off;
   uint64_t psi_off, lam_off;  // element offsets in the arena
   uint64_t shots, rnd_off, smp_off;
@@ -205,7 +206,9 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
                                                          const double *__restrict__ rnds, uint64_t *__restrict__ samples,
                                                          double *__restrict__ energy, double *__restrict__ grads,
                                                          unsigned long long *__restrict__ t_start,
-                                                         unsigned long long *__restrict__ t_end, int *queue, int want_grad) {
+                                                         unsigned long long *__restrict__ t_end, int *queue, int want_grad,
+                                                         const int2 *__restrict__ items, int nitems,
+                                                         unsigned *__restrict__ team_bar, int *__restrict__ team_err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *tp = reinterpret_cast<T *>(smem_raw);
   T *tl = tp + (1u << M);
@@ -219,16 +222,51 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
   __shared__ decltype(T::x) s_c[kBatchMaxRunOps], s_s[kBatchMaxRunOps];
   __shared__ double gacc[kBatchMaxRunOps][kBatchThreads / 32];
   __shared__ decltype(T::x) gaccf[kBatchMaxRunOps][kBatchThreads / 32];  // this tile group's sums, data precision
-  __shared__ int s_idx;
+  __shared__ int s_idx, s_member, s_abort;
+  __shared__ unsigned s_nsync;
   __shared__ int s_T[64];
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) s_idx = atomicAdd(queue, 1);
+    if (threadIdx.x == 0) {
+      const int q = atomicAdd(queue, 1);
+      s_idx = q < nitems ? items[q].x : ninst;
+      s_member = q < nitems ? items[q].y : 0;
+      s_nsync = 0;
+      s_abort = 0;
+    }
     __syncthreads();
     const int idx = s_idx;
     if (idx >= ninst) break;
+    const int member = s_member;
     const InstDev I = insts[idx];
-    if (threadIdx.x == 0) {
+    const int TM = I.team;
+    // Barrier of the instance's team (its members are consecutive queue
+    // items, taken at about the same time): every member arrives, then all
+    // go on.  Bounded: after 2 s, or when another CTA gave up, the team's
+    // CTAs raise *team_err and leave the kernel; the host reports it.
+    auto team_sync = [&]() -> bool {
+      __syncthreads();
+      if (TM == 1) return true;
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&team_bar[idx], 1u);
+        const unsigned target = (unsigned)TM * (++s_nsync);
+        unsigned long long t0, t1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+        int bad = 0;
+        while (atomicAdd(&team_bar[idx], 0u) < target) {
+          __nanosleep(256);
+          if (*(volatile int *)team_err) { bad = 1; break; }
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+          if (t1 - t0 > 2000000000ULL) { atomicExch(team_err, 1); bad = 1; break; }
+        }
+        __threadfence();
+        s_abort = bad;
+      }
+      __syncthreads();
+      return !s_abort;
+    };
+    if (threadIdx.x == 0 && member == 0) {
       unsigned long long t;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
       t_start[idx] = t;
@@ -236,8 +274,10 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
     T *psi = arena + I.psi_off;
     T *lam = arena + I.lam_off;
     const uint64_t N = 1ULL << I.n;
-    for (uint64_t i = threadIdx.x; i < N; i += blockDim.x) psi[i] = cplx<T>(i == 0 ? 1.0 : 0.0, 0.0);
-    __syncthreads();
+    const uint64_t tstride = (uint64_t)blockDim.x * TM;  // thread stride over the team
+    const uint64_t tbase = (uint64_t)member * blockDim.x + threadIdx.x;
+    for (uint64_t i = tbase; i < N; i += tstride) psi[i] = cplx<T>(i == 0 ? 1.0 : 0.0, 0.0);
+    if (!team_sync()) return;
     // ---------------- runs: forward (dir = 0) and backward (dir = 1) ----------------
     for (int dir = 0; dir < 2; ++dir) {
       if (dir == 1) {
@@ -245,7 +285,9 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
         const int bb = min(I.n, kSampleBits);
         const uint64_t nb = N >> bb;
         double *cdf = reinterpret_cast<double *>(lam);  // lam is free until H psi
-        for (uint64_t b = threadIdx.x >> 5; b < nb; b += blockDim.x >> 5) {
+        const uint64_t wbase = (uint64_t)member * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        const uint64_t wstride = (uint64_t)(blockDim.x >> 5) * TM;  // warp stride over the team
+        for (uint64_t b = wbase; b < nb; b += wstride) {
           double sacc = 0.0;
           for (uint64_t j = threadIdx.x & 31; j < (1ULL << bb); j += 32) {
             const T a = psi[(b << bb) + j];
@@ -257,12 +299,12 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
           if ((threadIdx.x & 31) == 0) cdf[b] = sacc;
         }
-        __syncthreads();
-        if (threadIdx.x == 0)
+        if (!team_sync()) return;
+        if (threadIdx.x == 0 && member == 0)
           for (uint64_t b = 1; b < nb; ++b) cdf[b] += cdf[b - 1];
-        __syncthreads();
+        if (!team_sync()) return;
         const int lane = threadIdx.x & 31;
-        for (uint64_t sh = threadIdx.x >> 5; sh < I.shots; sh += blockDim.x >> 5) {
+        for (uint64_t sh = wbase; sh < I.shots; sh += wstride) {
           const double r = rnds[I.rnd_off + sh];
           uint64_t lo = 0, hi = nb;
           while (lo < hi) {
@@ -311,13 +353,13 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           }
           if (lane == 0) samples[I.smp_off + sh] = res;
         }
-        __syncthreads();
+        if (!team_sync()) return;  // the CDF (in lambda's space) is read until here
         // lambda = H psi and <H> = Re <psi|lambda>: lambda in the data
         // precision (complex64 sums its terms in float: the FP64 pipe is
         // far narrower), <H> accumulated in double
         using Rt = decltype(T::x);
         double e_acc = 0.0;
-        for (uint64_t i = threadIdx.x; i < N; i += blockDim.x) {
+        for (uint64_t i = tbase; i < N; i += tstride) {
           Rt ar = 0, ai = 0;
           for (int t = 0; t < I.nterms; ++t) {
             const TermDevB h = terms[I.term_off + t];
@@ -335,9 +377,15 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           lam[i] = l;
         }
         const double e = bsum(e_acc, red);
-        if (threadIdx.x == 0) energy[idx] = e;
-        for (int pi = threadIdx.x; pi < I.nparams; pi += blockDim.x) grads[I.grad_off + pi] = 0.0;
-        __syncthreads();
+        if (threadIdx.x == 0) {
+          if (TM == 1)
+            energy[idx] = e;
+          else
+            atomicAdd(&energy[idx], e);  // zeroed before the launch
+        }
+        if (TM == 1)
+          for (int pi = threadIdx.x; pi < I.nparams; pi += blockDim.x) grads[I.grad_off + pi] = 0.0;
+        if (!team_sync()) return;
         if (!want_grad) break;
       }
       for (int rr = 0; rr < I.nruns; ++rr) {
@@ -384,7 +432,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
         __syncthreads();
         const uint64_t ntiles = 1ULL << (I.n - m);
         const uint32_t L = 1u << m;
-        for (uint64_t t = 0; t < ntiles; ++t) {
+        uint64_t lt = 0;  // tiles this CTA has processed in the run
+        for (uint64_t t = member; t < ntiles; t += TM, ++lt) {
           // deposit the tile id into the bits outside the tile
           uint64_t base = 0, tt = t;
           for (int q = 0; q < I.n && tt; ++q)
@@ -430,7 +479,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
                 // 16 tiles' warp sums in the data precision, then into double
                 auto &f = gaccf[oi][threadIdx.x >> 5];
                 f += part;
-                if ((t & 15) == 15) {
+                if ((lt & 15) == 15) {
                   gacc[oi][threadIdx.x >> 5] += (double)f;
                   f = 0;
                 }
@@ -460,12 +509,15 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
             if (g.param < 0) continue;
             double sum = 0.0;
             for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += gacc[k][w] + (double)gaccf[k][w];
-            grads[I.grad_off + g.param] += sum;
+            if (TM == 1)
+              grads[I.grad_off + g.param] += sum;
+            else
+              atomicAdd(&grads[I.grad_off + g.param], sum);  // zeroed before the launch
           }
-        __syncthreads();
+        if (!team_sync()) return;
       }
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && member == 0) {
       unsigned long long t;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
       t_end[idx] = t;
@@ -505,6 +557,12 @@ struct gbqv_batch {
   cudaGraph_t graph_def = nullptr;
   bool built = false;
   std::string err;
+  // teams: the costliest instances (up to team_max instances whose cost is
+  // at least team_frac of the largest) run on two CTAs each
+  int team_max = 64;
+  double team_frac = 0.5;
+  void *team_blob = nullptr;  // queue items (int2), per-instance barrier counters, error word
+  int nitems = 0;
 };
 
 namespace {
@@ -587,10 +645,22 @@ extern "C" int gbqv_batch_destroy(gbqv_batch_t b) {
   if (b->graph_def) cudaGraphDestroy(b->graph_def);
   if (b->arena) cudaFree(b->arena);
   if (b->dev_blob) cudaFree(b->dev_blob);
+  if (b->team_blob) cudaFree(b->team_blob);
   if (b->stream) cudaStreamDestroy(b->stream);
   cudaGetLastError();
   delete b;
   return GBQV_OK;
+}
+
+extern "C" int gbqv_batch_set_teams(gbqv_batch_t b, int max_team_instances, double min_cost_fraction) {
+  return bguard([&] {
+    if (!b) throw Error(GBQV_ERR_ARG, "null batch");
+    if (b->built) throw Error(GBQV_ERR_ARG, "teams are fixed once the batch has run");
+    if (max_team_instances < 0 || max_team_instances > 64 || !(min_cost_fraction >= 0.0))
+      throw Error(GBQV_ERR_ARG, "team settings out of range (at most 64 team instances)");
+    b->team_max = max_team_instances;
+    b->team_frac = min_cost_fraction;
+  });
 }
 
 extern "C" int gbqv_batch_add(gbqv_batch_t b, int num_qubits, int ngates, const int *kinds, const uint64_t *qubits,
@@ -646,10 +716,26 @@ void batch_build(gbqv_batch *b) {
   const size_t ninst = b->inst.size();
   if (!ninst) throw Error(GBQV_ERR_ARG, "empty batch");
   cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
-  // largest instances first
+  // costliest instances first (gates x amplitudes), so the long ones start early
+  auto cost = [&](size_t i) { return (double)std::max<size_t>(b->inst[i].gates.size(), 1) * std::ldexp(1.0, b->inst[i].n); };
   std::vector<size_t> order(ninst);
   for (size_t i = 0; i < ninst; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t c) { return b->inst[a].n > b->inst[c].n; });
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t c) { return cost(a) > cost(c); });
+  // teams of two CTAs for the costliest instances that span at least two tiles
+  const int tile_bits = b->dbl ? 11 : 12;
+  std::vector<int> team(ninst, 1);
+  int nteams = 0;
+  for (size_t k = 0; k < ninst && nteams < b->team_max; ++k) {
+    const size_t i = order[k];
+    if (cost(i) < b->team_frac * cost(order[0])) break;
+    if (b->inst[i].n <= tile_bits) continue;
+    team[k] = 2;
+    ++nteams;
+  }
+  std::vector<int2> items;
+  for (size_t k = 0; k < ninst; ++k)
+    for (int m = 0; m < team[k]; ++m) items.push_back(make_int2((int)k, m));
+  b->nitems = (int)items.size();
   std::vector<InstDev> idev(ninst);
   std::vector<GateDev> gates;
   std::vector<RunDev> runs;
@@ -665,6 +751,7 @@ void batch_build(gbqv_batch *b) {
     BatchInstHost &h = b->inst[i];
     InstDev &d = idev[k];
     d.n = h.n;
+    d.team = team[k];
     d.nops = (int)h.gates.size();
     d.nruns = (int)h.runs.size();
     d.nterms = (int)h.terms.size();
@@ -722,6 +809,11 @@ void batch_build(gbqv_batch *b) {
   b->t0.assign(ninst, 0);
   b->t1.assign(ninst, 0);
   b->order = order;
+  // team buffers: items, one barrier counter per instance, the error word
+  const size_t s_items = (sizeof(int2) * items.size() + 255) & ~size_t(255);
+  cuda_check(cudaMalloc(&b->team_blob, s_items + sizeof(unsigned) * ninst + 256), "batch team buffers");
+  cuda_check(cudaMemcpy(b->team_blob, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice),
+             "batch upload");
   b->built = true;
 }
 
@@ -735,6 +827,7 @@ struct BatchLayout {
   double *energy, *grads;
   unsigned long long *t0, *t1;
   int *queue;
+  size_t ngrad;
 };
 
 BatchLayout layout(gbqv_batch *b, size_t ngates, size_t nruns, size_t nterms, size_t nrnds, size_t nsmp, size_t ngrad) {
@@ -753,6 +846,7 @@ BatchLayout layout(gbqv_batch *b, size_t ngates, size_t nruns, size_t nterms, si
   L.t0 = reinterpret_cast<unsigned long long *>(p); p += al(sizeof(unsigned long long) * ninst);
   L.t1 = reinterpret_cast<unsigned long long *>(p); p += al(sizeof(unsigned long long) * ninst);
   L.queue = reinterpret_cast<int *>(p);
+  L.ngrad = ngrad;
   return L;
 }
 
@@ -766,12 +860,31 @@ void launch_batch(gbqv_batch *b, const BatchLayout &L, int want_grad) {
   }
   int per_sm = 1;
   cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<T, M>, kBatchThreads, smem), "occupancy");
-  const int grid = (int)std::min<size_t>(b->inst.size(), (size_t)152 * std::max(per_sm, 1));
+  // every CTA resident at once (a team member waits for its partner, the next queue item)
+  const int grid = (int)std::min<size_t>((size_t)b->nitems, (size_t)sm_count() * std::max(per_sm, 1));
+  const size_t ninst = b->inst.size();
+  char *tb = static_cast<char *>(b->team_blob);
+  const size_t s_items = (sizeof(int2) * b->nitems + 255) & ~size_t(255);
+  unsigned *bar = reinterpret_cast<unsigned *>(tb + s_items);
+  int *err = reinterpret_cast<int *>(tb + s_items + sizeof(unsigned) * ninst);
   cuda_check(cudaMemsetAsync(L.queue, 0, sizeof(int), b->stream), "queue reset");
-  k_batch<T, M><<<grid, kBatchThreads, smem, b->stream>>>(L.inst, (int)b->inst.size(), L.gates, L.runs, L.terms,
+  cuda_check(cudaMemsetAsync(bar, 0, sizeof(unsigned) * ninst + sizeof(int), b->stream), "team reset");
+  cuda_check(cudaMemsetAsync(L.energy, 0, sizeof(double) * ninst, b->stream), "energy reset");
+  if (L.ngrad) cuda_check(cudaMemsetAsync(L.grads, 0, sizeof(double) * L.ngrad, b->stream), "gradient reset");
+  k_batch<T, M><<<grid, kBatchThreads, smem, b->stream>>>(L.inst, (int)ninst, L.gates, L.runs, L.terms,
                                                           static_cast<T *>(b->arena), L.rnds, L.samples, L.energy,
-                                                          L.grads, L.t0, L.t1, L.queue, want_grad);
+                                                          L.grads, L.t0, L.t1, L.queue, want_grad,
+                                                          reinterpret_cast<const int2 *>(tb), b->nitems, bar, err);
   cuda_check(cudaGetLastError(), "batch kernel");
+}
+
+int team_error(gbqv_batch *b) {
+  const size_t s_items = (sizeof(int2) * b->nitems + 255) & ~size_t(255);
+  int e = 0;
+  cuda_check(cudaMemcpy(&e, static_cast<char *>(b->team_blob) + s_items + sizeof(unsigned) * b->inst.size(),
+                        sizeof(int), cudaMemcpyDeviceToHost),
+             "team status");
+  return e;
 }
 
 }  // namespace
@@ -811,6 +924,7 @@ extern "C" int gbqv_batch_run(gbqv_batch_t b, int want_grad, double *elapsed_ms)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (elapsed_ms) *elapsed_ms = ms;
+    if (team_error(b)) throw Error(GBQV_ERR_TIMEOUT, "a team barrier of the batched kernel gave up after 2 s");
     // results back, in instance order
     const size_t ninst = b->inst.size();
     std::vector<double> energy(ninst);

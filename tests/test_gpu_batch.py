@@ -57,3 +57,26 @@ def test_batch_matches_single_instance_engine(precision, tol, gtol):
     b.run(want_grad=True)
     assert b.result(0)[0] == e0
     b.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("double", 1e-12), ("single", 2e-5)])
+def test_teams_match_single_cta_instances(precision, tol):
+    """Instances run by two-CTA teams (tiles split, a barrier after each run,
+    energy and gradient partial sums added atomically) give the results of
+    the same instances on one CTA each; the shots are identical."""
+    P = pkg()
+    B = P.batched
+    insts = B.config5_instances(12, seed=9, qmin=11, qmax=15, dmin=2, dmax=5, tmin=5, tmax=15, shots=256)
+    out = []
+    for teams in (0, 64):
+        b = B.Batch(precision)
+        b.set_teams(teams, 0.0)
+        for inst in insts:
+            b.add(inst["n"], inst["gates"], inst["theta"], inst["terms"], inst["coeffs"], inst["shots"], inst["seed"])
+        b.run(want_grad=True)
+        out.append([b.result(i) for i in range(len(insts))])
+        b.close()
+    for (e0, g0, s0, _), (e1, g1, s1, _) in zip(*out):
+        assert abs(e0 - e1) < tol * max(1.0, abs(e0))
+        np.testing.assert_allclose(g1, g0, atol=tol * 10)
+        np.testing.assert_array_equal(s1, s0)
