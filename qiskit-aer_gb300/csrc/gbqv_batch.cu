@@ -144,24 +144,42 @@ __device__ __forceinline__ void tile_gate(T *tile, int m, int kind, decltype(T::
     }
     return;
   }
-  // 2x2 matrices: RX, RY, H
-  T m00, m01, m10, m11;
-  const R zero = 0, s1 = inverse ? -gs : gs;
+  // 2x2 matrices with real (RY, H) or real-diagonal / imaginary off-diagonal
+  // (RX) entries: the zero parts of the complex products are left out (half
+  // the multiply-adds; at complex128 these run on the narrow FP64 pipe)
+  const R s1 = inverse ? -gs : gs;
+  if (kind == B_RX) {
+    // [[c, -i s], [-i s, c]]: y0 = c x0 - i s x1, y1 = -i s x0 + c x1
+#pragma unroll kU
+    for (uint32_t p = threadIdx.x; p < (L >> 1); p += kBatchThreads) {
+      const uint32_t i0 = ins1(p, a), i1 = i0 | (1u << a);
+      const T x0 = tile[i0], x1 = tile[i1];
+      T y0, y1;
+      y0.x = fma(s1, x1.y, gc * x0.x);
+      y0.y = fma(-s1, x1.x, gc * x0.y);
+      y1.x = fma(s1, x0.y, gc * x1.x);
+      y1.y = fma(-s1, x0.x, gc * x1.y);
+      tile[i0] = y0;
+      tile[i1] = y1;
+    }
+    return;
+  }
+  R m00, m01, m10, m11;  // RY [[c, -s], [s, c]], H [[h, h], [h, -h]]
   if (kind == B_RY) {
-    m00.x = gc; m00.y = zero; m01.x = -s1; m01.y = zero; m10.x = s1; m10.y = zero; m11.x = gc; m11.y = zero;
-  } else if (kind == B_RX) {
-    m00.x = gc; m00.y = zero; m01.x = zero; m01.y = -s1; m10.x = zero; m10.y = -s1; m11.x = gc; m11.y = zero;
-  } else {  // H
+    m00 = gc; m01 = -s1; m10 = s1; m11 = gc;
+  } else {
     const R h = (R)0.70710678118654752440;
-    m00.x = h; m00.y = zero; m01.x = h; m01.y = zero; m10.x = h; m10.y = zero; m11.x = -h; m11.y = zero;
+    m00 = h; m01 = h; m10 = h; m11 = -h;
   }
 #pragma unroll kU
   for (uint32_t p = threadIdx.x; p < (L >> 1); p += kBatchThreads) {
     const uint32_t i0 = ins1(p, a), i1 = i0 | (1u << a);
     const T x0 = tile[i0], x1 = tile[i1];
-    T y0 = cmul(m00, x0), y1 = cmul(m10, x0);
-    cfma(y0, m01, x1);
-    cfma(y1, m11, x1);
+    T y0, y1;
+    y0.x = fma(m01, x1.x, m00 * x0.x);
+    y0.y = fma(m01, x1.y, m00 * x0.y);
+    y1.x = fma(m11, x1.x, m10 * x0.x);
+    y1.y = fma(m11, x1.y, m10 * x0.y);
     tile[i0] = y0;
     tile[i1] = y1;
   }
