@@ -94,6 +94,10 @@ int gbqv_device_count(void);
  * over std::mt19937_64.  These are the draws State::sample_measure consumes
  * (statevector_state.hpp:1016-1027); needs no GPU. */
 int gbqv_uniforms(uint64_t seed, uint64_t count, double *out);
+/* count draws of each of the streams seed0, seed0 + 1, .., seed0 + nstreams - 1
+ * (mod 2^64) into out[s * count + i]: the per-shot streams of a circuit run
+ * shot by shot (shot i seeded seed + i, circuit_executor.hpp:880-940). */
+int gbqv_uniforms_streams(uint64_t seed0, uint64_t nstreams, uint64_t count, double *out);
 
 /* ------------------------------------------------------------------ */
 /* State lifetime — QubitVector(num_qubits) / set_num_qubits           */
@@ -347,6 +351,44 @@ int gbqv_expval_pauli_segments(gbqv_handle h, int state_qubits, uint64_t nseg, i
  * out[s * shots ..] (indices within the state). */
 int gbqv_sample_measure_segments(gbqv_handle h, int state_qubits, uint64_t first, uint64_t nseg,
                                  const double *rnds, uint64_t shots, uint64_t *out);
+
+/* Batched shots of a circuit that cannot be measure-sampled (mid-circuit
+ * measurements, resets, classically conditioned ops): shot s of a group is
+ * state s of such a stack, the work QubitVectorThrust's batched-shots hooks
+ * do (apply_batched_measure / apply_batched_reset,
+ * src/simulators/statevector/qubitvector_thrust.hpp:2251-2448, conditions
+ * through set_batched_system_conditional, :2568).  The classical memory and
+ * each shot's RNG stay with the caller.
+ *
+ * initialize_segments: states 0..count-1 to |0...0>, the rest zero.
+ * execute_segments: the unitary ops of c (n qubits, n <= the handle's) on
+ *   every state of the stack at once (no size match needed).
+ * probabilities_segments: out[s * 2^k + v] = the probability of outcome v
+ *   (bit j on qubits[j], k <= state_qubits) in state s
+ *   (QubitVector::probabilities, qubitvector.hpp:2089-2143, per state).
+ * draw_segments: for registers of k >= 10 qubits, the probabilities and
+ *   each state's outcome drawn on the device (RngEngine::rand_int,
+ *   rng.hpp:94-96, with the uniform u[s]; u[s] < 0 draws nothing and gives
+ *   outcome 0xffffffff): outcome[s] and its probability prob[s].  Parallel
+ *   sums: an outcome can differ from the sequential draw only when u[s] lies
+ *   within a few ulps of a cumulative boundary.
+ * collapse_segments: State::measure_reset_update (statevector_state.hpp:
+ *   936-1011) per state: the amplitude of outcome meas_state[s] times
+ *   scale[s] (1/sqrt(p)) moves to outcome final_state[s] (the measured value
+ *   for a measurement, 0 for a reset), the others become 0;
+ *   meas_state[s] = 0xffffffff leaves state s untouched.
+ * apply_matrix_segments: a k <= 4 qubit matrix (column-major) on the states
+ *   whose mask[s] is non-zero (a classically conditioned gate). */
+int gbqv_initialize_segments(gbqv_handle h, int state_qubits, uint64_t count);
+int gbqv_execute_segments(gbqv_handle h, gbqv_circuit_t c);
+int gbqv_probabilities_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                                double *out);
+int gbqv_draw_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                       const double *u, uint32_t *outcome, double *prob);
+int gbqv_collapse_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                           const uint32_t *meas_state, const uint32_t *final_state, const double *scale);
+int gbqv_apply_matrix_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                               const gbqv_c128 *mat, const uint8_t *mask);
 
 /* Adjoint-method gradient of E(theta) = <psi(theta)|H|psi(theta)>, psi =
  * c applied to |0...0>.  No counterpart in the reference (Aer has no gradient

@@ -88,6 +88,12 @@ def uniforms(seed: int, count: int) -> np.ndarray:
     return out
 
 
+def _narrow(qubits) -> None:
+    """The C restatement keeps per-group index tables of 2^10 entries."""
+    if len(qubits) > 10:
+        raise ValueError("the oracle applies matrices of at most 10 qubits")
+
+
 class OracleQV:
     """QubitVector<double> restated in C, on a numpy complex128 buffer."""
 
@@ -106,11 +112,13 @@ class OracleQV:
         return self.data.ctypes.data_as(_vp)
 
     def apply_matrix(self, qubits, mat):
+        _narrow(qubits)
         q, qp = _u64(qubits)
         m, mp = _c128(np.asarray(mat).reshape(-1, order="F") if np.ndim(mat) == 2 else mat)
         self.lib.orc_apply_matrix(self._p, C.c_int(self.n), qp, C.c_int(len(q)), mp)
 
     def apply_diagonal_matrix(self, qubits, diag):
+        _narrow(qubits)
         q, qp = _u64(qubits)
         d, dp = _c128(diag)
         self.lib.orc_apply_diagonal(self._p, C.c_int(self.n), qp, C.c_int(len(q)), dp)
@@ -158,6 +166,7 @@ class OracleQV:
             raise ValueError(f"invalid Pauli {label!r}")
 
     def apply_permutation_matrix(self, qubits, pairs):
+        _narrow(qubits)
         q, qp = _u64(qubits)
         p, pp = _u64(np.asarray(pairs).reshape(-1))
         self.lib.orc_apply_permutation(self._p, C.c_int(self.n), qp, C.c_int(len(q)), pp,

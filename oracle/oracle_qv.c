@@ -491,6 +491,17 @@ void orc_probabilities(const cplx *sv, int n, const uint64_t *qubits, int k, dou
   const uint64_t DIM = 1ULL << k;
   const int64_t END = (int64_t)(1ULL << (n - k));
   for (uint64_t m = 0; m < DIM; ++m) out[m] = 0.0;
+  if (k > 10) {
+    /* registers wider than the per-thread tables below: one sequential
+       pass, each amplitude added to its outcome's entry */
+    const uint64_t N = 1ULL << n;
+    for (uint64_t j = 0; j < N; ++j) {
+      uint64_t m = 0;
+      for (int b = 0; b < k; ++b) m |= ((j >> qubits[b]) & 1ULL) << b;
+      out[m] += creal(sv[j] * conj(sv[j]));
+    }
+    return;
+  }
 #pragma omp parallel OMP_IF(n)
   {
     double priv[1024];

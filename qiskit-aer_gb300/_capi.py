@@ -48,6 +48,7 @@ _SIGS = {
     "gbqv_last_error": (C.c_char_p, [H]),
     "gbqv_device_count": (C.c_int, []),
     "gbqv_uniforms": (C.c_int, [C.c_uint64, C.c_uint64, dp]),
+    "gbqv_uniforms_streams": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint64, dp]),
     "gbqv_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(H)]),
     "gbqv_destroy": (C.c_int, [H]),
     "gbqv_num_qubits": (C.c_int, [H, C.POINTER(C.c_int)]),
@@ -118,6 +119,12 @@ _SIGS = {
     "gbqv_expval_pauli_segments": (C.c_int, [H, C.c_int, C.c_uint64, C.c_int, u64p, C.POINTER(C.c_int),
                                              C.POINTER(C.c_char_p), dp]),
     "gbqv_sample_measure_segments": (C.c_int, [H, C.c_int, C.c_uint64, C.c_uint64, dp, C.c_uint64, u64p]),
+    "gbqv_initialize_segments": (C.c_int, [H, C.c_int, C.c_uint64]),
+    "gbqv_execute_segments": (C.c_int, [H, H]),
+    "gbqv_probabilities_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, dp]),
+    "gbqv_draw_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, dp, vp, dp]),
+    "gbqv_collapse_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, vp, vp, dp]),
+    "gbqv_apply_matrix_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, vp, vp]),
     "gbqv_set_blocking": (C.c_int, [H, C.c_int]),
     "gbqv_set_tensor_c128": (C.c_int, [H, C.c_int]),
     "gbqv_batch_create": (C.c_int, [C.c_int, C.POINTER(H)]),

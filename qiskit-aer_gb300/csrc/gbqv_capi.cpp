@@ -263,6 +263,17 @@ extern "C" int gbqv_uniforms(uint64_t seed, uint64_t count, double *out) {
   });
 }
 
+extern "C" int gbqv_uniforms_streams(uint64_t seed0, uint64_t nstreams, uint64_t count, double *out) {
+  return guard(nullptr, [&] {
+    REQUIRE(out || nstreams * count == 0, GBQV_ERR_ARG, "null output");
+    for (uint64_t s = 0; s < nstreams; ++s) {
+      std::mt19937_64 rng(seed0 + s);
+      std::uniform_real_distribution<double> dist(0.0, 1.0);
+      for (uint64_t i = 0; i < count; ++i) out[s * count + i] = dist(rng);
+    }
+  });
+}
+
 // ============================== lifetime ==============================
 
 extern "C" int gbqv_create(int num_qubits, int precision, int kind, gbqv_handle *out) {
@@ -775,6 +786,83 @@ extern "C" int gbqv_expval_pauli_segments(gbqv_handle h, int state_qubits, uint6
       read_results(d, vals.data(), vals.size());
       std::copy(vals.begin(), vals.end(), out + (size_t)t0 * nseg);
     }
+  });
+}
+
+// ============================== batched shots ==============================
+
+namespace {
+void check_stack(const Device &d, int state_qubits, uint64_t nseg, const char *what) {
+  REQUIRE(!d.density && !d.unitary, GBQV_ERR_KIND, std::string(what) + ": statevector stacks only");
+  REQUIRE(state_qubits >= 1 && state_qubits <= d.n && nseg >= 1 && nseg <= (d.amps() >> state_qubits), GBQV_ERR_ARG,
+          std::string(what) + ": the states do not fit the handle's vector");
+}
+}  // namespace
+
+extern "C" int gbqv_initialize_segments(gbqv_handle h, int state_qubits, uint64_t count) {
+  return guard(h, [&] {
+    need_handle(h);
+    check_stack(h->dev, state_qubits, std::max<uint64_t>(count, 1), "initialize_segments");
+    launch_set_basis_segments(h->dev, state_qubits, count);
+  });
+}
+
+extern "C" int gbqv_probabilities_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits,
+                                           int k, double *out) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    check_stack(d, state_qubits, nseg, "probabilities_segments");
+    reg_t q = check_qubits(qubits, k, state_qubits, "probabilities_segments");
+    REQUIRE(k <= seg_max_measure_qubits() && out, GBQV_ERR_ARG, "probabilities_segments: 1..30 qubits, an output");
+    reduce_probabilities_segments(d, q, state_qubits, nseg);
+    read_results(d, out, nseg << k);
+  });
+}
+
+extern "C" int gbqv_draw_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                                  const double *u, uint32_t *outcome, double *prob) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    check_stack(d, state_qubits, nseg, "draw_segments");
+    reg_t q = check_qubits(qubits, k, state_qubits, "draw_segments");
+    REQUIRE(k >= 10 && k <= seg_max_measure_qubits() && u && outcome && prob, GBQV_ERR_ARG,
+            "draw_segments: 10..30 qubits, uniforms and two outputs");
+    for (uint64_t s = 0; s < nseg; ++s)
+      REQUIRE(u[s] < 1.0, GBQV_ERR_ARG, "draw_segments: uniforms must lie below 1");
+    draw_segments(d, q, state_qubits, nseg, u, outcome, prob);
+    check_tc_status(d);
+  });
+}
+
+extern "C" int gbqv_collapse_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                                      const uint32_t *meas_state, const uint32_t *final_state, const double *scale) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    check_stack(d, state_qubits, nseg, "collapse_segments");
+    reg_t q = check_qubits(qubits, k, state_qubits, "collapse_segments");
+    REQUIRE(k <= seg_max_measure_qubits() && meas_state && final_state && scale, GBQV_ERR_ARG,
+            "collapse_segments: 1..30 qubits and three per-state arrays");
+    const uint32_t D = 1u << k;
+    for (uint64_t s = 0; s < nseg; ++s)
+      REQUIRE(meas_state[s] == 0xffffffffu || (meas_state[s] < D && final_state[s] < D), GBQV_ERR_ARG,
+              "collapse_segments: outcome of state " + std::to_string(s) + " out of range");
+    launch_collapse_segments(d, q, state_qubits, nseg, meas_state, final_state, scale);
+  });
+}
+
+extern "C" int gbqv_apply_matrix_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits,
+                                          int k, const gbqv_c128 *mat, const uint8_t *mask) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    check_stack(d, state_qubits, nseg, "apply_matrix_segments");
+    reg_t q = check_qubits(qubits, k, state_qubits, "apply_matrix_segments");
+    REQUIRE(k <= seg_max_matrix_qubits() && mat && mask, GBQV_ERR_ARG,
+            "apply_matrix_segments: 1..4 qubits, a matrix and a mask");
+    launch_matrix_segments(d, q, state_qubits, nseg, reinterpret_cast<const cd *>(mat), mask);
   });
 }
 

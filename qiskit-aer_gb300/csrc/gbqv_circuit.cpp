@@ -1465,6 +1465,27 @@ extern "C" int gbqv_execute(gbqv_handle h, gbqv_circuit_t c) {
       h);
 }
 
+extern "C" int gbqv_execute_segments(gbqv_handle h, gbqv_circuit_t c) {
+  return guard(
+      [&] {
+        REQUIRE(h && c, GBQV_ERR_ARG, "null argument");
+        REQUIRE(c->nbind == 0, GBQV_ERR_ARG, "the circuit has parameter bindings: run it with gbqv_execute_bound");
+        Device &d = device_of(h);
+        REQUIRE(!d.density && !d.unitary, GBQV_ERR_KIND, "execute_segments: statevector stacks only");
+        REQUIRE(c->num_qubits <= d.n, GBQV_ERR_ARG,
+                "circuit has " + std::to_string(c->num_qubits) + " qubits, the stacked states have " +
+                    std::to_string(d.n));
+        for (const Op &op : c->ops)
+          REQUIRE(op.type != GBQV_OP_RESET && op.type != GBQV_OP_KRAUS && op.type != GBQV_OP_SUPEROP, GBQV_ERR_KIND,
+                  "op '" + op.name + "' acts on the whole vector: execute_segments runs unitary ops");
+        if (d.blocking)
+          execute_blocked(d, c->ops);
+        else
+          for (const Op &op : c->ops) exec_op(d, op);
+      },
+      h);
+}
+
 // ============================== adjoint gradients ==============================
 // No reference counterpart (Aer has no gradient code).  E(theta) =
 // <psi|H|psi> with psi = U_L...U_1|0>; for a gate U = exp(-i theta P / 2)

@@ -197,4 +197,16 @@ void launch_set_basis_segments(Device &dev, int state_bits, uint64_t count);
 // of 2^state_bits-amplitude states, into dev.results[t * nseg + s].
 void reduce_expval_segments(Device &dev, const std::vector<PauliTerm> &terms, int state_bits, uint64_t nseg);
 
+// batched shots (gbqv_shots.cu): per-state probabilities (nseg 2^k values
+// in dev.results), collapse and a masked matrix over a stack of states
+int seg_max_measure_qubits();
+int seg_max_matrix_qubits();
+void reduce_probabilities_segments(Device &dev, const reg_t &qubits, int state_bits, uint64_t nseg);
+void launch_collapse_segments(Device &dev, const reg_t &qubits, int state_bits, uint64_t nseg, const uint32_t *meas,
+                              const uint32_t *fin, const double *scale);
+void launch_matrix_segments(Device &dev, const reg_t &qubits, int state_bits, uint64_t nseg, const cd *mat,
+                            const uint8_t *mask);
+void draw_segments(Device &dev, const reg_t &qubits, int state_bits, uint64_t nseg, const double *u,
+                   uint32_t *outcome, double *prob);
+
 }  // namespace gbqv

@@ -39,6 +39,18 @@ def discrete_draw(probs, u: float) -> int:
     return int(np.searchsorted(cp, u, side="left"))
 
 
+def discrete_draws(probs: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """discrete_draw for each row of probs with its own uniform: the same
+    sequential sums per row, so every row gives discrete_draw's index."""
+    p = np.asarray(probs, dtype=np.float64)
+    if p.shape[0] == 0:
+        return np.zeros(0, dtype=np.int64)
+    total = np.add.accumulate(p, axis=1)[:, -1]
+    cp = np.add.accumulate(p / total[:, None], axis=1)
+    cp[:, -1] = 1.0
+    return np.sum(cp < np.asarray(u, dtype=np.float64)[:, None], axis=1).astype(np.int64)
+
+
 def uniforms(seed: int, count: int) -> np.ndarray:
     """RngEngine::rand(0,1) stream for `seed` (std::mt19937_64)."""
     out = np.empty(int(count), dtype=np.float64)
@@ -337,14 +349,25 @@ class AerSimulator:
             st.synchronize()
         return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
 
+    # shots per stacked group and the largest stack (qubits of the circuit +
+    # shot bits), about 4 GB of complex128 amplitudes
+    SHOT_GROUP_BITS = 16
+    SHOT_STACK_QUBITS = 28
+    HOST_DRAW_QUBITS = 10  # wider registers are drawn on the device
+
     def _run_shots(self, circuit: QuantumCircuit, shots: int, seed: int):
-        """A circuit that cannot be measure-sampled, one shot at a time
-        (CircuitExecutor::run_circuit_shots, circuit_executor.hpp:880-940):
-        shot i starts from |0...0> with RngEngine seed + i; unitary stretches
-        between measurements, resets and conditional ops are fused once and
-        executed per shot; measure and reset draw one outcome each
-        (State::sample_measure_with_prob) and collapse the state
-        (State::measure_reset_update, statevector_state.hpp:936-1011)."""
+        """A circuit that cannot be measure-sampled (CircuitExecutor::
+        run_circuit_shots, circuit_executor.hpp:880-940): shot i starts from
+        |0...0> with RngEngine seed + i; unitary stretches between
+        measurements, resets and conditional ops are fused once; measure and
+        reset draw one outcome each (State::sample_measure_with_prob) and
+        collapse the state (State::measure_reset_update,
+        statevector_state.hpp:936-1011).  Shots run in groups, one stacked
+        state per shot (the reference's batched shots on a GPU,
+        QubitVectorThrust::apply_batched_measure / apply_batched_reset,
+        qubitvector_thrust.hpp:2251-2448): each stretch runs once over the
+        whole group, each measurement is one probability pass, a host draw
+        per shot from its own stream and one collapse pass."""
         if self.noise_model is not None and not self.noise_model.is_ideal():
             raise NotImplementedError("noise on a statevector needs per-shot noise sampling; use density_matrix")
         cfg = self.fusion_config()
@@ -372,9 +395,128 @@ class AerSimulator:
             elif ins.kind != "barrier":
                 stretch.append(ins)
         flush()
+        meta = {"fusion": {"enabled": bool(cfg.enable)}, "shot_branching": False, "measure_sampling": False}
+        matrices = self._conditioned_matrices(items)
+        if matrices is not None and circuit.num_clbits <= 63:
+            memory = self._shots_batched(circuit.num_qubits, items, matrices, shots, seed)
+            meta["batched_shots_optimization"] = True  # batch_shots_executor.hpp:373
+        else:
+            memory = self._shots_serial(circuit.num_qubits, items, shots, seed)
+        data = {}
+        if self._want_memory and circuit.num_clbits:
+            data["memory"] = self._memory(memory)
+        counts = None
+        if circuit.num_clbits:
+            counts = {}
+            for v in memory:
+                key = format(int(v), f"0{circuit.num_clbits}b")
+                counts[key] = counts.get(key, 0) + 1
+        return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
+
+    @staticmethod
+    def _conditioned_matrices(items):
+        """The matrix of every classically conditioned op, for applying it to
+        the shots whose condition holds; None when an item needs the one-shot
+        path (a conditioned op on more than 4 qubits)."""
+        out = {}
+        for idx, (kind, obj, cond) in enumerate(items):
+            if kind in ("measure", "reset"):
+                continue
+            if cond is None:
+                continue
+            ops = obj.ops()
+            if len(ops) != 1 or not 1 <= len(ops[0][2]) <= 4 or ops[0][0] not in (0, 1, 2):
+                return None
+            m = obj.op_matrix(0)
+            if ops[0][0] == 2:
+                m = np.diag(m).reshape(-1, order="F")
+            out[idx] = (ops[0][2], np.ascontiguousarray(m, dtype=np.complex128))
+        return out
+
+    def _shots_batched(self, n, items, matrices, shots, seed):
+        L = A.lib()
         ndraw = sum(1 for kind, _, _ in items if kind in ("measure", "reset"))
-        counts: dict[str, int] = {}
-        with QubitVector(circuit.num_qubits, self.precision) as st:
+        # a group's outcome probabilities (group x 2^k doubles): below 32 MB on
+        # the host (registers of <= 10 qubits, drawn there), 1 GB on the device
+        ks = [len(obj.qubits) for kind, obj, _ in items if kind in ("measure", "reset")]
+        k_host = max([k for k in ks if k <= self.HOST_DRAW_QUBITS], default=0)
+        k_dev = max([k for k in ks if k > self.HOST_DRAW_QUBITS], default=0)
+        b = max(0, min((int(shots) - 1).bit_length(), self.SHOT_GROUP_BITS, self.SHOT_STACK_QUBITS - n,
+                       22 - k_host, 27 - k_dev))
+        group = 1 << b
+        out = np.zeros(shots, dtype=np.uint64)
+        with QubitVector(n + b, self.precision) as st:
+            h = st.handle
+            if not self.options["blocking_enable"]:
+                A.check(L.gbqv_set_blocking(h, 0))
+            for g0 in range(0, shots, group):
+                cnt = min(group, shots - g0)
+                u = np.empty((cnt, ndraw), dtype=np.float64)
+                if ndraw:
+                    A.check(L.gbqv_uniforms_streams((seed + g0) & (2**64 - 1), cnt, ndraw, u.ctypes.data_as(A.dp)))
+                used = np.zeros(cnt, dtype=np.int64)
+                memory = np.zeros(cnt, dtype=np.uint64)
+                A.check(L.gbqv_initialize_segments(h, n, cnt), h)
+                for idx, (kind, obj, cond) in enumerate(items):
+                    active = np.ones(cnt, dtype=bool)
+                    if cond is not None:
+                        cbits, value = cond
+                        for i, c in enumerate(cbits):
+                            active &= ((memory >> np.uint64(c)) & np.uint64(1)) == ((value >> i) & 1)
+                        if not active.any():
+                            continue
+                    if kind == "ops":
+                        if active.all():
+                            A.check(L.gbqv_execute_segments(h, obj.handle), h)
+                        else:
+                            qubits, mat = matrices[idx]
+                            mask = active.astype(np.uint8)
+                            A.check(L.gbqv_apply_matrix_segments(h, n, cnt, (C.c_uint64 * len(qubits))(*qubits),
+                                                                 len(qubits), mat.ctypes.data_as(A.vp),
+                                                                 mask.ctypes.data_as(A.vp)), h)
+                        continue
+                    qubits = obj.qubits
+                    k = len(qubits)
+                    qarr = (C.c_uint64 * k)(*qubits)
+                    rows = np.nonzero(active)[0]
+                    if k <= self.HOST_DRAW_QUBITS:
+                        probs = np.empty((cnt, 1 << k), dtype=np.float64)
+                        A.check(L.gbqv_probabilities_segments(h, n, cnt, qarr, k, probs.ctypes.data_as(A.dp)), h)
+                        outcome = discrete_draws(probs[rows], u[rows, used[rows]])
+                        p_out = probs[rows, outcome]
+                    else:
+                        ur = np.full(cnt, -1.0)
+                        ur[rows] = u[rows, used[rows]]
+                        drawn = np.empty(cnt, dtype=np.uint32)
+                        pd = np.empty(cnt, dtype=np.float64)
+                        A.check(L.gbqv_draw_segments(h, n, cnt, qarr, k, ur.ctypes.data_as(A.dp),
+                                                     drawn.ctypes.data_as(A.vp), pd.ctypes.data_as(A.dp)), h)
+                        outcome, p_out = drawn[rows].astype(np.int64), pd[rows]
+                    used[rows] += 1
+                    meas = np.full(cnt, 0xFFFFFFFF, dtype=np.uint32)
+                    meas[rows] = outcome
+                    final = meas.copy()
+                    if kind == "reset":
+                        final[rows] = 0
+                    scale = np.zeros(cnt, dtype=np.float64)
+                    scale[rows] = 1.0 / np.sqrt(p_out)
+                    A.check(L.gbqv_collapse_segments(h, n, cnt, qarr, k, meas.ctypes.data_as(A.vp),
+                                                     final.ctypes.data_as(A.vp), scale.ctypes.data_as(A.dp)), h)
+                    if kind == "measure":
+                        o = outcome.astype(np.uint64)
+                        for i, c in enumerate(obj.clbits):
+                            bit = np.uint64(1) << np.uint64(c)
+                            memory[rows] = (memory[rows] & ~bit) | (((o >> np.uint64(i)) & np.uint64(1)) << np.uint64(c))
+                out[g0:g0 + cnt] = memory
+            st.synchronize()
+        return out
+
+    def _shots_serial(self, n, items, shots, seed):
+        """One state, one shot at a time (classical memory wider than 63
+        bits, or a conditioned op beyond the stacked kernels)."""
+        ndraw = sum(1 for kind, _, _ in items if kind in ("measure", "reset"))
+        out = []
+        with QubitVector(n, self.precision) as st:
             for shot in range(shots):
                 u = uniforms(seed + shot, ndraw) if ndraw else np.empty(0)
                 used, memory = 0, 0
@@ -395,13 +537,9 @@ class AerSimulator:
                     if kind == "measure":
                         for i, c in enumerate(obj.clbits):
                             memory = (memory & ~(1 << c)) | (((outcome >> i) & 1) << c)
-                key = format(memory, f"0{circuit.num_clbits}b") if circuit.num_clbits else ""
-                counts[key] = counts.get(key, 0) + 1
+                out.append(memory)
             st.synchronize()
-        return {"counts": counts if circuit.num_clbits else None, "data": {},
-                "metadata": {"fusion": {"enabled": bool(cfg.enable)}, "shot_branching": False,
-                             "measure_sampling": False},
-                "seed_simulator": seed, "shots": shots}
+        return out
 
     @staticmethod
     def _collapse(st, qubits, meas_state: int, final_state: int, prob: float):

@@ -43,3 +43,28 @@ def test_needs_shots_rules():
     assert P.QuantumCircuit(2, 1).h(0).reset(0).needs_shots("statevector")
     assert not P.QuantumCircuit(2, 1).h(0).reset(0).needs_shots("density_matrix")
     assert P.QuantumCircuit(2, 1).measure(0, 0).x(1).c_if(0, 1).needs_shots()
+
+
+def test_row_draws_equal_one_draw_per_row():
+    """The stacked-shot path draws every shot's outcome at once; each row must
+    give discrete_draw's index for its own uniform (same sequential sums)."""
+    P = pkg()
+    rng = np.random.default_rng(11)
+    for d in (2, 4, 8, 32):
+        probs = rng.random((300, d)) ** 3
+        probs[::7, 0] = 0.0
+        probs /= probs.sum(axis=1, keepdims=True) * (1 + 1e-15 * rng.standard_normal((300, 1)))
+        u = rng.random(300)
+        u[:5] = [0.0, 1 - 2 ** -53, probs[5, 0], 0.5, 1e-300]
+        got = P.simulator.discrete_draws(probs, u)
+        want = [P.simulator.discrete_draw(p, x) for p, x in zip(probs, u)]
+        np.testing.assert_array_equal(got, want)
+    assert P.simulator.discrete_draws(np.zeros((0, 2)), np.zeros(0)).shape == (0,)
+
+
+def test_uniform_streams_are_per_shot_seeds():
+    P = pkg()
+    out = np.empty((5, 7))
+    P._capi.check(P.lib().gbqv_uniforms_streams(2**64 - 2, 5, 7, out.ctypes.data_as(P._capi.dp)))
+    for s in range(5):
+        np.testing.assert_array_equal(out[s], P.uniforms((2**64 - 2 + s) % 2**64, 7))
