@@ -31,7 +31,9 @@ damping superoperators, 50 Pauli expectation values), ``sample``
 uneven instances of 12-22 qubits with gradients and 4,096 shots each in one
 graph-captured persistent launch, next to one instance per launch),
 ``estimator`` (EstimatorV2 job: a parameterised 20-qubit ansatz with 1,024
-parameter sets run on one stack of states, 50 observables).
+parameter sets run on one stack of states, 50 observables), ``shots``
+(a 16-qubit circuit with mid-circuit measurements, conditioned gates and
+resets: 4,096 shots, each running the circuit, stacked as states).
 
 ``--impl reference`` times the reference's CPU algorithm on the same
 workload (the oracle port: the reference's own build exists only where its
@@ -491,6 +493,60 @@ def bench_batch(args, torch, P):
                        "instances": len(insts)}, "clocks": clk}
 
 
+def dynamic_circuit(P, n, rounds, seed):
+    """Brickwork Haar SU(4) layers; after each round a measurement, an X
+    conditioned on it and a reset; at the end every qubit measured."""
+    rng = np.random.default_rng(seed)
+    qc = P.QuantumCircuit(n, rounds + n)
+    for r in range(rounds):
+        for start in (0, 1):
+            for q in range(start, n - 1, 2):
+                qc.unitary(haar_su4(rng), [q, q + 1])
+        qc.measure(r % n, r)
+        qc.x((r + 1) % n).c_if(r, 1)
+        qc.reset([r % n])
+    qc.measure(list(range(n)), list(range(rounds, rounds + n)))
+    return qc
+
+
+def bench_shots(args, torch, P):
+    """Circuits that cannot be measure-sampled (mid-circuit measurement,
+    conditioned gates, resets): every shot runs the circuit, shots stacked
+    as states through AerSimulator.run; next to one shot at a time on one
+    state (a sample, registers of <= 10 qubits only)."""
+    qc = dynamic_circuit(P, args.shots_qubits, args.shots_rounds, args.seed)
+    sim = P.AerSimulator(precision=args.precision)
+    for _ in range(max(1, args.warmup)):
+        sim.run(qc, shots=min(args.shots, 256), seed_simulator=args.seed)
+    clocks = ClockSampler().start()
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        counts = sim.run(qc, shots=args.shots, seed_simulator=args.seed + i).get_counts()
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    t = float(np.median(times))
+    line = {"metric": "shots/s (mid-circuit measurement, reset, conditions)", "value": round(args.shots / t, 1),
+            "unit": "shots/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t * 1e3, 2), "dtype": "c128" if args.precision == "double" else "c64",
+            "data": "synthetic", "outcomes": len(counts),
+            "config": {"workload": f"{args.shots_qubits}q, {args.shots_rounds} rounds of 2 SU(4) layers + measure, "
+                                   f"conditioned X, reset; final measure of every qubit; {args.shots} shots",
+                       "qubits": args.shots_qubits, "shots": args.shots}, "clocks": clk}
+    if args.shots_qubits <= 10:
+        one = P.AerSimulator(precision=args.precision)
+        one._conditioned_matrices = lambda items: None   # the one-state loop
+        ns = min(args.shots, 256)
+        t0 = time.perf_counter()
+        ref = one.run(qc, shots=ns, seed_simulator=args.seed).get_counts()
+        t1 = time.perf_counter() - t0
+        same = sim.run(qc, shots=ns, seed_simulator=args.seed).get_counts() == ref
+        line["one_shot_at_a_time_shots_per_s"] = round(ns / t1, 1)
+        line["speedup_vs_one_shot_at_a_time"] = round((args.shots / t) / (ns / t1), 1)
+        line["same_counts_on_sample"] = same
+    return line
+
+
 def hea_bound_circuit(P, n, layers):
     """RY(theta) and RZ(theta) on every qubit, then a CX ladder, per layer;
     one Parameter per rotation (the adjoint workload's ansatz, parameterised)."""
@@ -649,7 +705,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="qv", choices=["qv", "adjoint", "dm", "sample", "batch", "estimator"])
+    ap.add_argument("--workload", default="qv",
+                    choices=["qv", "adjoint", "dm", "sample", "batch", "estimator", "shots"])
+    ap.add_argument("--shots-qubits", type=int, default=16)
+    ap.add_argument("--shots-rounds", type=int, default=8)
+    ap.add_argument("--shots", type=int, default=4096)
     ap.add_argument("--est-qubits", type=int, default=20)
     ap.add_argument("--est-layers", type=int, default=8)
     ap.add_argument("--est-bindings", type=int, default=1024)
@@ -682,7 +742,7 @@ def main():
     P = entry.load_package()
     P.build()
     fn = {"qv": bench_qv, "adjoint": bench_adjoint, "dm": bench_dm, "sample": bench_sample,
-          "batch": bench_batch, "estimator": bench_estimator}[args.workload]
+          "batch": bench_batch, "estimator": bench_estimator, "shots": bench_shots}[args.workload]
     line = fn(args, torch, P)
     if int(os.environ.get("RANK", "0")) == 0:
         print(json.dumps(line))

@@ -433,16 +433,21 @@ class AerSimulator:
             out[idx] = (ops[0][2], np.ascontiguousarray(m, dtype=np.complex128))
         return out
 
+    def _shot_group_bits(self, n: int, shots: int, ks) -> int:
+        """log2 of the shots stacked per group: enough for every shot (up to
+        2^SHOT_GROUP_BITS), a stack of at most SHOT_STACK_QUBITS qubits, and a
+        group's outcome probabilities (group x 2^k doubles) below 32 MB on the
+        host (registers drawn there) and 1 GB on the device (wider ones)."""
+        k_host = max([k for k in ks if k <= self.HOST_DRAW_QUBITS], default=0)
+        k_dev = max([k for k in ks if k > self.HOST_DRAW_QUBITS], default=0)
+        return max(0, min((int(shots) - 1).bit_length(), self.SHOT_GROUP_BITS, self.SHOT_STACK_QUBITS - n,
+                          22 - k_host, 27 - k_dev))
+
     def _shots_batched(self, n, items, matrices, shots, seed):
         L = A.lib()
         ndraw = sum(1 for kind, _, _ in items if kind in ("measure", "reset"))
-        # a group's outcome probabilities (group x 2^k doubles): below 32 MB on
-        # the host (registers of <= 10 qubits, drawn there), 1 GB on the device
         ks = [len(obj.qubits) for kind, obj, _ in items if kind in ("measure", "reset")]
-        k_host = max([k for k in ks if k <= self.HOST_DRAW_QUBITS], default=0)
-        k_dev = max([k for k in ks if k > self.HOST_DRAW_QUBITS], default=0)
-        b = max(0, min((int(shots) - 1).bit_length(), self.SHOT_GROUP_BITS, self.SHOT_STACK_QUBITS - n,
-                       22 - k_host, 27 - k_dev))
+        b = self._shot_group_bits(n, shots, ks)
         group = 1 << b
         out = np.zeros(shots, dtype=np.uint64)
         with QubitVector(n + b, self.precision) as st:

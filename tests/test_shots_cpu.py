@@ -68,3 +68,40 @@ def test_uniform_streams_are_per_shot_seeds():
     P._capi.check(P.lib().gbqv_uniforms_streams(2**64 - 2, 5, 7, out.ctypes.data_as(P._capi.dp)))
     for s in range(5):
         np.testing.assert_array_equal(out[s], P.uniforms((2**64 - 2 + s) % 2**64, 7))
+
+
+def test_stacked_shot_group_sizes():
+    P = pkg()
+    sim = P.AerSimulator()
+    g = sim._shot_group_bits
+    assert g(10, 1, [1]) == 0                 # one shot: one state
+    assert g(10, 50, [1]) == 6                # 64 states hold 50 shots
+    assert g(10, 10**6, [1]) == 16            # at most 2^16 shots per group
+    assert g(20, 10**6, [1]) == 8             # stack of at most 28 qubits
+    assert g(12, 10**6, [10]) == 12           # 2^12 x 2^10 host probabilities
+    assert g(16, 10**6, [3, 16]) == 11        # 2^11 x 2^16 device probabilities
+    assert g(30, 4096, [30]) == 0
+
+
+def test_conditioned_ops_become_matrices():
+    """Conditioned gates, matrices and diagonals of up to 4 qubits are applied
+    to the shots whose condition holds as one matrix; wider ones need the
+    one-state loop."""
+    P = pkg()
+    items = []
+    qc = P.QuantumCircuit(5, 2).measure(0, 0)
+    nc_x = P.NativeCircuit(5, P.QuantumCircuit(5).x(3).data)
+    d = np.exp(1j * np.arange(4))
+    nc_d = P.NativeCircuit(5, P.QuantumCircuit(5).diagonal(d, [1, 4]).data)
+    items = [("measure", qc.data[0], None), ("ops", nc_x, ([0], 1)), ("ops", nc_d, ([0], 0)),
+             ("ops", nc_x, None)]
+    mats = P.AerSimulator._conditioned_matrices(items)
+    assert set(mats) == {1, 2}
+    q, m = mats[1]
+    assert q == [3]
+    np.testing.assert_array_equal(m.reshape(2, 2, order="F"), [[0, 1], [1, 0]])
+    q, m = mats[2]
+    assert q == [1, 4]
+    np.testing.assert_array_equal(m.reshape(4, 4, order="F"), np.diag(d))
+    wide = P.NativeCircuit(5, P.QuantumCircuit(5).unitary(np.eye(32), [0, 1, 2, 3, 4]).data)
+    assert P.AerSimulator._conditioned_matrices([("ops", wide, ([0], 1))]) is None
