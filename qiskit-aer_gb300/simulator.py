@@ -322,6 +322,8 @@ class AerSimulator:
     def _run_one(self, circuit: QuantumCircuit, shots: int, seed: int):
         if self.method == "statevector" and circuit.needs_shots("statevector"):
             return self._run_shots(circuit, shots, seed)
+        if self.method == "density_matrix" and circuit.needs_shots("density_matrix"):
+            return self._run_shots_dm(circuit, shots, seed)
         if self.method == "unitary":
             self._check_unitary_circuit(circuit)
         segments, meas, saves, meta = self.compile(circuit)
@@ -545,6 +547,81 @@ class AerSimulator:
                 out.append(memory)
             st.synchronize()
         return out
+
+    def _run_shots_dm(self, circuit: QuantumCircuit, shots: int, seed: int):
+        """The density-matrix method on a circuit that cannot be
+        measure-sampled: every shot runs the circuit on one density matrix
+        (CircuitExecutor::run_circuit_shots, seed + i per shot).  Noise stays
+        superoperators inserted after each gate (under the gate's condition),
+        resets are the reset channel, and a measurement draws one outcome and
+        projects, D rho D^dag with D = diag(1/sqrt(p) at the outcome)
+        (DensityMatrix::State::measure_reset_update,
+        densitymatrix_state.hpp:949-990)."""
+        items, stretch = [], []
+        fused = {"enabled": False}
+
+        def flush():
+            if stretch:
+                body = self._with_noise(list(stretch))
+                kinds = {i.kind for i in body}
+                cfg = self.fusion_config(has_superop="superop" in kinds, has_kraus="kraus" in kinds)
+                fused["enabled"] |= bool(cfg.enable)
+                nc = NativeCircuit(circuit.num_qubits, body)
+                nc.fuse(cfg)
+                items.append(("ops", nc, None))
+                stretch.clear()
+
+        for ins in circuit.data:
+            if ins.kind == "save":
+                raise NotImplementedError("save instructions in a circuit run shot by shot")
+            if ins.kind == "measure":
+                flush()
+                items.append(("measure", ins, ins.condition))
+            elif ins.condition is not None:
+                flush()
+                plain = Instruction(ins.kind, ins.name, ins.qubits, ins.params, ins.data, ins.clbits)
+                items.append(("ops", NativeCircuit(circuit.num_qubits, self._with_noise([plain])), ins.condition))
+            elif ins.kind != "barrier":
+                stretch.append(ins)
+        flush()
+        ndraw = sum(1 for kind, _, _ in items if kind == "measure")
+        memories = []
+        with DensityMatrix(circuit.num_qubits, self.precision) as st:
+            if not self.options["blocking_enable"]:
+                A.check(st._L.gbqv_set_blocking(st.handle, 0))
+            for shot in range(shots):
+                u = uniforms(seed + shot, ndraw) if ndraw else np.empty(0)
+                used, memory = 0, 0
+                st.initialize()
+                for kind, obj, cond in items:
+                    if cond is not None:
+                        cbits, value = cond
+                        if any(((memory >> c) & 1) != ((value >> i) & 1) for i, c in enumerate(cbits)):
+                            continue
+                    if kind == "ops":
+                        A.check(st._L.gbqv_execute(st.handle, obj.handle), st.handle)
+                        continue
+                    probs = st.probabilities(obj.qubits)
+                    outcome = discrete_draw(probs, u[used])
+                    used += 1
+                    diag = np.zeros(1 << len(obj.qubits), dtype=complex)
+                    diag[outcome] = 1.0 / np.sqrt(probs[outcome])
+                    st.apply_diagonal_unitary_matrix(obj.qubits, diag)
+                    for i, c in enumerate(obj.clbits):
+                        memory = (memory & ~(1 << c)) | (((outcome >> i) & 1) << c)
+                memories.append(memory)
+            st.synchronize()
+        data = {}
+        if self._want_memory and circuit.num_clbits:
+            data["memory"] = self._memory(memories)
+        counts = None
+        if circuit.num_clbits:
+            counts = {}
+            for v in memories:
+                key = format(int(v), f"0{circuit.num_clbits}b")
+                counts[key] = counts.get(key, 0) + 1
+        meta = {"fusion": fused, "shot_branching": False, "measure_sampling": False}
+        return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
 
     @staticmethod
     def _collapse(st, qubits, meas_state: int, final_state: int, prob: float):

@@ -282,3 +282,72 @@ def test_wide_mid_circuit_register_matches_oracle():
     qc.measure(list(range(n)), list(range(n, 2 * n)))
     got = P.AerSimulator().run(qc, shots=40, seed_simulator=99).get_counts()
     assert got == oracle_counts(P, qc, 40, 99)
+
+
+def _measured_feedback(P, n, rng, gate_set="unitary"):
+    """Mid-circuit measurements and conditioned gates, no reset."""
+    qc = P.QuantumCircuit(n, 2 * n)
+    for r in range(3):
+        for q in range(n):
+            qc.u3(*rng.uniform(0, 2 * np.pi, 3), q)
+        for q in range(r % 2, n - 1, 2):
+            qc.cx(q, q + 1)
+        qc.measure([r % n, (r + 2) % n], [2 * r, 2 * r + 1])
+        qc.u3(*rng.uniform(0, 2 * np.pi, 3), (r + 1) % n).c_if([2 * r], 1)
+        qc.cx((r + 1) % n, (r + 3) % n).c_if([2 * r, 2 * r + 1], 2)
+    qc.measure(list(range(n)), list(range(n, 2 * n)))
+    return qc
+
+
+def test_density_matrix_shots_equal_statevector_shots_when_ideal():
+    """Without noise the density-matrix method's shots draw from the same
+    probabilities with the same per-shot uniforms: identical counts."""
+    P = pkg()
+    qc = _measured_feedback(P, 4, np.random.default_rng(12))
+    dm = P.AerSimulator(method="density_matrix").run(qc, shots=60, seed_simulator=8, memory=True)
+    sv = P.AerSimulator().run(qc, shots=60, seed_simulator=8, memory=True)
+    assert dm.get_memory() == sv.get_memory()
+
+
+def test_noisy_density_matrix_shots_match_oracle():
+    P = pkg()
+    n = 4
+    e1 = P.depolarizing_error(0.05, 1).compose(P.amplitude_damping_error(0.1))
+    nm = P.NoiseModel()
+    nm.add_all_qubit_quantum_error(e1, ["u3"])
+    nm.add_all_qubit_quantum_error(e1.tensor(e1), ["cx"])
+    qc = _measured_feedback(P, n, np.random.default_rng(13))
+    sim = P.AerSimulator(method="density_matrix", noise_model=nm)
+    got = sim.run(qc, shots=40, seed_simulator=4).get_counts()
+    ndraw = sum(1 for ins in qc.data if ins.kind == "measure")
+    want = {}
+    for shot in range(40):
+        o = O.OracleDM(n)
+        u = P.uniforms(4 + shot, ndraw)
+        used, mem = 0, 0
+        for ins in qc.data:
+            if ins.condition is not None:
+                cb, val = ins.condition
+                if any(((mem >> c) & 1) != ((val >> i) & 1) for i, c in enumerate(cb)):
+                    continue
+            if ins.kind == "measure":
+                probs = o.probabilities(ins.qubits)
+                k = P.simulator.discrete_draw(probs, u[used])
+                used += 1
+                diag = np.zeros(1 << len(ins.qubits), dtype=complex)
+                diag[k] = 1 / np.sqrt(probs[k])
+                o.apply_diagonal_unitary_matrix(ins.qubits, diag)
+                for i, c in enumerate(ins.clbits):
+                    mem = (mem & ~(1 << c)) | (((k >> i) & 1) << c)
+                continue
+            plain = P.circuit.Instruction(ins.kind, ins.name, ins.qubits, ins.params, ins.data, ins.clbits)
+            for op in sim._with_noise([plain]):
+                if op.kind == "superop":
+                    o.apply_superop_matrix(op.qubits, op.data)
+                elif op.name == "u3":
+                    o.apply_unitary_matrix(op.qubits, O.u3(*op.params))
+                else:
+                    o.apply_cnot(*op.qubits)
+        key = format(mem, f"0{2 * n}b")
+        want[key] = want.get(key, 0) + 1
+    assert got == want
