@@ -13,8 +13,9 @@ Package layout:
 """
 from ._capi import GBQVError, lib
 from .circuit import NativeCircuit, Parameter, ParameterExpression, QuantumCircuit
-from .noise import (NoiseModel, QuantumError, amplitude_damping_error, depolarizing_error,
-                    phase_amplitude_damping_error)
+from .noise import (NoiseModel, QuantumError, amplitude_damping_error, coherent_unitary_error,
+                    depolarizing_error, kraus_error, mixed_unitary_error, pauli_error, phase_amplitude_damping_error,
+                    phase_damping_error, reset_error, thermal_relaxation_error)
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
 from .simulator import AerSimulator, Result, uniforms
 from . import adjoint, batched
@@ -24,7 +25,8 @@ __all__ = [
     "AerSimulator", "adjoint", "batched", "DensityMatrix", "EstimatorV2", "SamplerV2", "GBQVError", "NativeCircuit", "NoiseModel",
     "Parameter", "ParameterExpression", "QuantumCircuit",
     "QuantumError", "QubitVector", "Result", "UnitaryMatrix", "amplitude_damping_error", "depolarizing_error", "lib",
-    "phase_amplitude_damping_error", "uniforms",
+    "phase_amplitude_damping_error", "uniforms", "coherent_unitary_error", "kraus_error", "mixed_unitary_error",
+    "pauli_error", "phase_damping_error", "reset_error", "thermal_relaxation_error",
 ]
 
 

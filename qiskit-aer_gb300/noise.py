@@ -1,14 +1,19 @@
 """Noise channels as superoperators, in the vec(rho) layout the engine uses.
 
-``depolarizing_error`` and ``amplitude_damping_error`` follow
-qiskit_aer/noise/errors/standard_errors.py:170-219 and 351-462; a
-``QuantumError`` is carried as its superoperator S (4^k x 4^k,
-S = sum conj(K) (x) K over its Kraus / Pauli terms), which is how the
-reference applies errors under the density-matrix method
-(src/noise/quantum_error.hpp:177-183, 493-509).  ``NoiseModel`` inserts the
-error after every gate of the listed names, as
-``NoiseModel::sample_noise(..., Method::superop)`` does
-(src/noise/noise_model.hpp:274, 434-450).
+The standard errors follow qiskit_aer/noise/errors/standard_errors.py
+(kraus_error :32, mixed_unitary_error :59, coherent_unitary_error :110,
+pauli_error :123, depolarizing_error :170-219, reset_error :222,
+thermal_relaxation_error :257, phase_amplitude_damping_error /
+amplitude_damping_error / phase_damping_error :351-520); a ``QuantumError``
+is carried as its superoperator S (4^k x 4^k, S = sum conj(K) (x) K over its
+Kraus / Pauli / unitary terms), which is how the reference applies errors
+under the density-matrix method (src/noise/quantum_error.hpp:177-183,
+493-509).  ``NoiseModel`` inserts the error after every gate of the listed
+names, as ``NoiseModel::sample_noise(..., Method::superop)`` does
+(src/noise/noise_model.hpp:274, 434-450): an error given for the gate's
+exact qubits (``add_quantum_error``) in place of the all-qubit one
+(``NoiseModel::sample_local_quantum_noise``, noise_model.hpp:710-780);
+errors added twice for the same key are composed (noise_model.py:669-806).
 """
 from __future__ import annotations
 
@@ -36,6 +41,9 @@ def kraus_superop(kraus) -> np.ndarray:
     return sum(np.kron(np.conj(k), k) for k in kraus)
 
 
+ATOL = 1e-8  # the reference's QuantumError tolerance (TolerancesMixin)
+
+
 class QuantumError:
     """A k-qubit channel held as its superoperator (column-major meaning:
     vec(rho') = S vec(rho), vec index = row + 2^k col)."""
@@ -43,6 +51,15 @@ class QuantumError:
     def __init__(self, superop: np.ndarray, num_qubits: int):
         self.superop = np.asarray(superop, dtype=complex)
         self.num_qubits = num_qubits
+
+    def ideal(self) -> bool:
+        """The identity channel (a global phase included), which a noise
+        model does not add (noise_model.py:669-700)."""
+        return bool(np.max(np.abs(self.superop - np.eye(self.superop.shape[0]))) <= 1e-12)
+
+    def expand(self, other: "QuantumError") -> "QuantumError":
+        """other (x) self, with self on the lower qubits (QuantumError.expand)."""
+        return other.tensor(self)
 
     @classmethod
     def from_kraus(cls, kraus):
@@ -70,6 +87,127 @@ class QuantumError:
         return self.superop
 
 
+def _check_probs(probs) -> None:
+    probs = [float(p) for p in probs]
+    if any(p < -ATOL for p in probs):
+        raise ValueError("Probabilities are invalid.")
+    if not np.isclose(sum(probs) - 1, 0, atol=ATOL):
+        raise ValueError(f"Probabilities are not normalized: {sum(probs)} != 1")
+
+
+def _as_square(m) -> tuple[np.ndarray, int]:
+    m = np.asarray(m, dtype=complex)
+    k = int(round(np.log2(m.shape[0]))) if m.ndim == 2 and m.shape[0] else -1
+    if m.ndim != 2 or m.shape[0] != m.shape[1] or k < 1 or m.shape[0] != 1 << k:
+        raise ValueError("A matrix in the error is not a square matrix of qubits.")
+    return m, k
+
+
+def kraus_error(noise_ops, canonical_kraus: bool = False) -> QuantumError:
+    """A channel from Kraus matrices (trace preserving within ATOL)."""
+    if not isinstance(noise_ops, (list, tuple)) or not noise_ops:
+        raise ValueError("Invalid Kraus error input.")
+    mats = [_as_square(k) for k in noise_ops]
+    if len({k for _, k in mats}) != 1:
+        raise ValueError("Kraus matrices of different sizes.")
+    ks = [m for m, _ in mats]
+    if not np.allclose(sum(m.conj().T @ m for m in ks), np.eye(ks[0].shape[0]), atol=ATOL):
+        raise ValueError("Input Kraus matrices are not a CPTP channel.")
+    return QuantumError(kraus_superop(ks), mats[0][1])
+
+
+def mixed_unitary_error(noise_ops) -> QuantumError:
+    """sum_j p_j U_j rho U_j^dag from pairs (U_j, p_j)."""
+    ops = list(noise_ops) if isinstance(noise_ops, (list, tuple, zip)) else None
+    if not ops:
+        raise ValueError("Input noise ops is not a list." if ops is None else "Input noise list is empty.")
+    mats = [(_as_square(u), p) for u, p in ops]
+    k = mats[0][0][1]
+    for (u, ku), _ in mats:
+        if ku != k:
+            raise ValueError("Input matrices different size.")
+        if not np.allclose(u.conj().T @ u, np.eye(u.shape[0]), atol=ATOL):
+            raise ValueError("Input matrix is not unitary.")
+    _check_probs([p for _, p in mats])
+    return QuantumError(sum(float(p) * np.kron(u.conj(), u) for (u, _), p in mats), k)
+
+
+def coherent_unitary_error(unitary) -> QuantumError:
+    return mixed_unitary_error([(unitary, 1)])
+
+
+def pauli_error(noise_ops) -> QuantumError:
+    """A Pauli mixture from pairs (label, p); labels read as qiskit's Pauli
+    strings (the rightmost character on qubit 0)."""
+    ops = list(noise_ops) if isinstance(noise_ops, (list, tuple, zip)) else None
+    if not ops:
+        raise ValueError("Input noise ops is not a list." if ops is None else "Input noise list is empty.")
+    labels = [str(lab).upper() for lab, _ in ops]
+    if any(not lab or set(lab) - set("IXYZ") for lab in labels):
+        raise ValueError(f"Invalid Pauli input operator: {labels}")
+    if len({len(lab) for lab in labels}) != 1:
+        raise ValueError("Pauli's are not all of the same length.")
+    probs = [float(p) for _, p in ops]
+    _check_probs(probs)
+    sup = 0
+    for lab, p in zip(labels, probs):
+        m = _kron_all([_P[c] for c in lab])
+        sup = sup + p * np.kron(m.conj(), m)
+    return QuantumError(sup, len(labels[0]))
+
+
+_RESET0 = kraus_superop([np.array([[1, 0], [0, 0]], dtype=complex), np.array([[0, 1], [0, 0]], dtype=complex)])
+_X = np.kron(_P["X"].conj(), _P["X"])
+_Z = np.kron(_P["Z"].conj(), _P["Z"])
+
+
+def reset_error(prob0: float, prob1: float = 0.0) -> QuantumError:
+    """E(rho) = (1 - p0 - p1) rho + Tr[rho] (p0 |0><0| + p1 |1><1|)."""
+    if prob0 < 0 or prob1 < 0 or prob0 > 1 or prob1 > 1 or prob0 + prob1 > 1:
+        raise ValueError("Invalid reset probabilities.")
+    return QuantumError((1 - prob0 - prob1) * np.eye(4) + prob0 * _RESET0 + prob1 * (_X @ _RESET0), 1)
+
+
+def thermal_relaxation_error(t1: float, t2: float, time: float, excited_state_population: float = 0.0) -> QuantumError:
+    """T1 relaxation towards the equilibrium populations (p0, p1) and T2
+    dephasing over `time`.  For T2 <= T1 the reference builds it as a mixture
+    of I, Z, reset to |0> and reset to |1>; for T1 < T2 <= 2 T1 from its Choi
+    matrix; both are the channel rho00' = (1 - p1 r) rho00 + p0 r rho11,
+    rho11' = p1 r rho00 + (1 - p0 r) rho11, rho01' = e^(-time/T2) rho01 with
+    r = 1 - e^(-time/T1).  The mixture is built here for T2 <= T1, the Choi
+    matrix's superoperator otherwise."""
+    if excited_state_population < 0:
+        raise ValueError(f"Invalid excited state population ({excited_state_population} < 0).")
+    if excited_state_population > 1:
+        raise ValueError(f"Invalid excited state population ({excited_state_population} > 1).")
+    if time < 0:
+        raise ValueError(f"Invalid gate_time ({time} < 0)")
+    if t1 <= 0:
+        raise ValueError("Invalid T_1 relaxation time parameter: T_1 <= 0.")
+    if t2 <= 0:
+        raise ValueError("Invalid T_2 relaxation time parameter: T_2 <= 0.")
+    if t2 - 2 * t1 > 0:
+        raise ValueError("Invalid T_2 relaxation time parameter: T_2 greater than 2 * T_1.")
+    rate1, p_reset = (0.0, 0.0) if t1 == np.inf else (1 / t1, 1 - np.exp(-time / t1))
+    rate2, exp_t2 = (0.0, 1.0) if t2 == np.inf else (1 / t2, np.exp(-time / t2))
+    p1 = excited_state_population
+    p0 = 1 - p1
+    if t2 > t1:
+        sup = np.zeros((4, 4), dtype=complex)  # vec index row + 2 col
+        sup[0, 0], sup[0, 3] = 1 - p1 * p_reset, p0 * p_reset
+        sup[3, 0], sup[3, 3] = p1 * p_reset, 1 - p0 * p_reset
+        sup[1, 1] = sup[2, 2] = exp_t2
+        return QuantumError(sup, 1)
+    p_reset0, p_reset1 = p_reset * p0, p_reset * p1
+    p_z = (1 - p_reset) * (1 - np.exp(-time * (rate2 - rate1))) / 2
+    p_id = 1 - p_z - p_reset0 - p_reset1
+    return QuantumError(p_id * np.eye(4) + p_z * _Z + p_reset0 * _RESET0 + p_reset1 * (_X @ _RESET0), 1)
+
+
+def phase_damping_error(param_phase: float, canonical_kraus: bool = True) -> QuantumError:
+    return phase_amplitude_damping_error(0.0, param_phase, 0.0)
+
+
 def depolarizing_error(param: float, num_qubits: int) -> QuantumError:
     terms = 4 ** num_qubits
     max_param = terms / (terms - 1)
@@ -83,11 +221,13 @@ def depolarizing_error(param: float, num_qubits: int) -> QuantumError:
     return QuantumError(sup, num_qubits)
 
 
-def amplitude_damping_error(param_amp: float, excited_state_population: float = 0.0) -> QuantumError:
+def amplitude_damping_error(param_amp: float, excited_state_population: float = 0.0,
+                            canonical_kraus: bool = True) -> QuantumError:
     return phase_amplitude_damping_error(param_amp, 0.0, excited_state_population)
 
 
-def phase_amplitude_damping_error(param_amp, param_phase, excited_state_population=0.0) -> QuantumError:
+def phase_amplitude_damping_error(param_amp, param_phase, excited_state_population=0.0,
+                                  canonical_kraus: bool = True) -> QuantumError:
     if param_amp < 0 or param_phase < 0 or param_amp + param_phase > 1:
         raise ValueError("Invalid amplitude and phase damping parameters")
     c0 = np.sqrt(1 - excited_state_population)
@@ -108,13 +248,48 @@ def phase_amplitude_damping_error(param_amp, param_phase, excited_state_populati
 class NoiseModel:
     def __init__(self):
         self._all_qubit = {}   # gate name -> QuantumError
+        self._local = {}       # gate name -> {qubit tuple: QuantumError}
 
-    def add_all_qubit_quantum_error(self, error: QuantumError, instructions):
-        for name in ([instructions] if isinstance(instructions, str) else instructions):
-            self._all_qubit[name] = error
+    @staticmethod
+    def _names(instructions):
+        return [instructions] if isinstance(instructions, str) else list(instructions)
 
-    def error_for(self, name: str):
+    def add_all_qubit_quantum_error(self, error: QuantumError, instructions, warnings: bool = True):
+        """An error after every listed gate; a second error for the same gate
+        is composed after the first; an ideal error is not added."""
+        if error.ideal():
+            return
+        for name in self._names(instructions):
+            old = self._all_qubit.get(name)
+            self._all_qubit[name] = error if old is None else old.compose(error)
+
+    def add_quantum_error(self, error: QuantumError, instructions, qubits, warnings: bool = True):
+        """An error after the listed gates on exactly these qubits (in this
+        order), used there in place of the all-qubit error."""
+        if error.ideal():
+            return
+        qubits = tuple(int(q) for q in qubits)
+        if error.num_qubits != len(qubits):
+            raise ValueError(f"Number of qubits ({len(qubits)}) does not match  the error size ({error.num_qubits})")
+        for name in self._names(instructions):
+            table = self._local.setdefault(name, {})
+            old = table.get(qubits)
+            table[qubits] = error if old is None else old.compose(error)
+
+    def error_for(self, name: str, qubits=None):
+        if qubits is not None:
+            local = self._local.get(name, {}).get(tuple(int(q) for q in qubits))
+            if local is not None:
+                return local
         return self._all_qubit.get(name)
 
+    @property
+    def noise_instructions(self) -> list:
+        return sorted(set(self._all_qubit) | set(self._local))
+
+    @property
+    def noise_qubits(self) -> list:
+        return sorted({q for table in self._local.values() for key in table for q in key})
+
     def is_ideal(self) -> bool:
-        return not self._all_qubit
+        return not self._all_qubit and not self._local

@@ -140,7 +140,7 @@ class AerSimulator:
             new_index.append(len(out))
             out.append(ins)
             if ins.kind == "gate":
-                err = self.noise_model.error_for(ins.name)
+                err = self.noise_model.error_for(ins.name, ins.qubits)
                 if err is not None:
                     if err.num_qubits != len(ins.qubits):
                         raise ValueError(f"error on '{ins.name}' acts on {err.num_qubits} qubits")

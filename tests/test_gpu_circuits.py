@@ -89,3 +89,39 @@ def test_noisy_density_matrix_vs_oracle():
     np.testing.assert_allclose(rho.reshape(-1, order="F"), o.data, atol=1e-12)
     want = sum(c * o.expval_pauli(q, lab) for c, lab, q in terms)
     assert abs(res.data()["expectation_value"] - want) < 1e-12
+
+
+def test_density_matrix_with_relaxation_and_local_errors_vs_oracle():
+    """Thermal relaxation on every u3, a Pauli + reset error on the u3 of
+    qubit 2 in its place, a two-qubit error on cx(0, 1) only and relaxation
+    on both qubits of every other cx: the density matrix after fusion of
+    gates and superoperators equals the oracle applying each gate and its
+    error in turn."""
+    P = pkg()
+    n = 5
+    rng = np.random.default_rng(44)
+    t = P.thermal_relaxation_error(50.0, 70.0, 1.5, 0.05)
+    nm = P.NoiseModel()
+    nm.add_all_qubit_quantum_error(t, ["u3"])
+    nm.add_quantum_error(P.pauli_error([("X", 0.02), ("Z", 0.03), ("I", 0.95)]).compose(P.reset_error(0.01, 0.02)),
+                         "u3", [2])
+    nm.add_all_qubit_quantum_error(t.tensor(P.thermal_relaxation_error(40.0, 30.0, 3.0)), ["cx"])
+    nm.add_quantum_error(P.depolarizing_error(0.04, 2), "cx", [0, 1])
+    qc = P.QuantumCircuit(n)
+    for _ in range(4):
+        for q in range(n):
+            qc.u3(*rng.uniform(0, 2 * np.pi, 3), q)
+        qc.cx(0, 1).cx(2, 3).cx(1, 4).cx(4, 0)
+    qc.save_density_matrix()
+    sim = P.AerSimulator(method="density_matrix", noise_model=nm, fusion_threshold=2)
+    rho = sim.run(qc).data()["density_matrix"]
+    o = O.OracleDM(n)
+    for ins in sim._with_noise(qc.split_final()[0]):
+        if ins.kind == "gate" and ins.name == "u3":
+            o.apply_unitary_matrix(ins.qubits, O.u3(*ins.params))
+        elif ins.kind == "gate" and ins.name == "cx":
+            o.apply_cnot(*ins.qubits)
+        elif ins.kind == "superop":
+            o.apply_superop_matrix(ins.qubits, ins.data)
+    np.testing.assert_allclose(rho.reshape(-1, order="F"), o.data, atol=1e-12)
+    assert abs(np.trace(rho) - 1) < 1e-12

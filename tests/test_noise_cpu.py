@@ -1,0 +1,154 @@
+"""The standard noise channels (qiskit_aer/noise/errors/standard_errors.py)
+as superoperators, and NoiseModel's error lookup (noise_model.py:669-806,
+NoiseModel::sample_local_quantum_noise, noise_model.hpp:710-780).  No GPU:
+the channels are checked by their action on random density matrices, by
+trace preservation and complete positivity, and against the reference's own
+constructions (the thermal-relaxation Choi matrix, the Pauli mixture of the
+depolarizing channel)."""
+import numpy as np
+import pytest
+
+from _pkg import pkg
+
+X = np.array([[0, 1], [1, 0]], dtype=complex)
+Z = np.diag([1.0, -1.0]).astype(complex)
+
+
+def act(err, rho):
+    d = rho.shape[0]
+    return (err.superop @ rho.reshape(-1, order="F")).reshape(d, d, order="F")
+
+
+def random_rho(rng, d):
+    a = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    r = a @ a.conj().T
+    return r / np.trace(r)
+
+
+def choi_of(err):
+    """Choi matrix sum_ij |i><j| (x) E(|i><j|) (rows (i, a), columns (j, b))."""
+    d = 1 << err.num_qubits
+    out = np.zeros((d * d, d * d), dtype=complex)
+    for i in range(d):
+        for j in range(d):
+            e = np.zeros((d, d), dtype=complex)
+            e[i, j] = 1
+            out += np.kron(e, act(err, e))
+    return out
+
+
+def is_cptp(err):
+    d = 1 << err.num_qubits
+    c = choi_of(err)
+    tp = all(abs(np.trace(act(err, np.outer(np.eye(d)[i], np.eye(d)[j]))) - (i == j)) < 1e-12
+             for i in range(d) for j in range(d))
+    return tp and np.min(np.linalg.eigvalsh((c + c.conj().T) / 2)) > -1e-12
+
+
+@pytest.mark.parametrize("t1,t2,time,pop", [(50.0, 30.0, 2.0, 0.0), (50.0, 30.0, 2.0, 0.2), (40.0, 70.0, 3.0, 0.0),
+                                            (40.0, 80.0, 5.0, 0.3), (np.inf, np.inf, 1.0, 0.0),
+                                            (30.0, 60.0, 0.0, 0.1)])
+def test_thermal_relaxation(t1, t2, time, pop):
+    P = pkg()
+    err = P.thermal_relaxation_error(t1, t2, time, pop)
+    assert err.num_qubits == 1 and is_cptp(err)
+    r = 0.0 if t1 == np.inf else 1 - np.exp(-time / t1)
+    e2 = 1.0 if t2 == np.inf else np.exp(-time / t2)
+    rho = random_rho(np.random.default_rng(1), 2)
+    out = act(err, rho)
+    p0, p1 = 1 - pop, pop
+    np.testing.assert_allclose(out[0, 0], (1 - p1 * r) * rho[0, 0] + p0 * r * rho[1, 1], atol=1e-14)
+    np.testing.assert_allclose(out[1, 1], p1 * r * rho[0, 0] + (1 - p0 * r) * rho[1, 1], atol=1e-14)
+    np.testing.assert_allclose(out[0, 1], e2 * rho[0, 1], atol=1e-14)
+    # the reference's Choi matrix of the T2 > T1 branch, standard_errors.py:320-330
+    choi = np.array([[1 - p1 * r, 0, 0, e2], [0, p1 * r, 0, 0], [0, 0, p0 * r, 0], [e2, 0, 0, 1 - p0 * r]])
+    np.testing.assert_allclose(choi_of(err), choi, atol=1e-14)
+
+
+def test_thermal_relaxation_errors():
+    P = pkg()
+    for args, msg in [((0, 1, 1), "T_1"), ((1, 0, 1), "T_2"), ((1, 3, 1), "greater than 2"), ((1, 1, -1), "gate_time"),
+                      ((1, 1, 1, 1.5), "excited")]:
+        with pytest.raises(ValueError, match=msg):
+            P.thermal_relaxation_error(*args)
+
+
+def test_reset_error_action():
+    P = pkg()
+    rho = random_rho(np.random.default_rng(2), 2)
+    err = P.reset_error(0.2, 0.1)
+    want = 0.7 * rho + np.trace(rho) * np.diag([0.2, 0.1])
+    np.testing.assert_allclose(act(err, rho), want, atol=1e-15)
+    assert is_cptp(err)
+    with pytest.raises(ValueError):
+        P.reset_error(0.7, 0.5)
+
+
+def test_pauli_error_labels_and_depolarizing():
+    P = pkg()
+    rho = random_rho(np.random.default_rng(3), 4)
+    err = P.pauli_error([("XZ", 0.3), ("II", 0.7)])
+    m = np.kron(X, Z)  # X on qubit 1, Z on qubit 0 (qiskit's label order)
+    np.testing.assert_allclose(act(err, rho), 0.7 * rho + 0.3 * m @ rho @ m.conj().T, atol=1e-15)
+    dep = P.depolarizing_error(0.12, 1)
+    mix = P.pauli_error([("I", 1 - 0.12 * 3 / 4), ("X", 0.03), ("Y", 0.03), ("Z", 0.03)])
+    np.testing.assert_allclose(dep.superop, mix.superop, atol=1e-15)
+    with pytest.raises(ValueError, match="normalized"):
+        P.pauli_error([("X", 0.5)])
+    with pytest.raises(ValueError, match="same length"):
+        P.pauli_error([("X", 0.5), ("XX", 0.5)])
+    with pytest.raises(ValueError, match="Invalid Pauli"):
+        P.pauli_error([("Q", 1.0)])
+
+
+def test_unitary_and_kraus_errors():
+    P = pkg()
+    rng = np.random.default_rng(4)
+    q, _ = np.linalg.qr(rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)))
+    rho = random_rho(rng, 4)
+    err = P.mixed_unitary_error([(q, 0.25), (np.eye(4), 0.75)])
+    np.testing.assert_allclose(act(err, rho), 0.25 * q @ rho @ q.conj().T + 0.75 * rho, atol=1e-14)
+    coh = P.coherent_unitary_error(q)
+    np.testing.assert_allclose(act(coh, rho), q @ rho @ q.conj().T, atol=1e-14)
+    with pytest.raises(ValueError, match="not unitary"):
+        P.mixed_unitary_error([(np.diag([1.0, 2.0]), 1.0)])
+    with pytest.raises(ValueError, match="different size"):
+        P.mixed_unitary_error([(np.eye(2), 0.5), (np.eye(4), 0.5)])
+    g = 0.3
+    k = [np.array([[1, 0], [0, np.sqrt(1 - g)]]), np.array([[0, np.sqrt(g)], [0, 0]])]
+    np.testing.assert_allclose(P.kraus_error(k).superop, P.amplitude_damping_error(g).superop, atol=1e-15)
+    with pytest.raises(ValueError, match="CPTP"):
+        P.kraus_error([np.eye(2) * 2])
+    pd = P.phase_damping_error(0.4)
+    r1 = random_rho(rng, 2)
+    np.testing.assert_allclose(act(pd, r1), [[r1[0, 0], np.sqrt(0.6) * r1[0, 1]], [np.sqrt(0.6) * r1[1, 0], r1[1, 1]]],
+                               atol=1e-15)
+
+
+def test_noise_model_lookup_and_composition():
+    P = pkg()
+    nm = P.NoiseModel()
+    assert nm.is_ideal()
+    nm.add_all_qubit_quantum_error(P.depolarizing_error(0.0, 1), ["x"])    # ideal: not added
+    assert nm.is_ideal()
+    a, b = P.depolarizing_error(0.1, 1), P.amplitude_damping_error(0.2)
+    nm.add_all_qubit_quantum_error(a, ["x", "sx"])
+    nm.add_all_qubit_quantum_error(b, "x")                                   # composed after a
+    np.testing.assert_allclose(nm.error_for("x", [3]).superop, b.superop @ a.superop, atol=1e-15)
+    assert nm.error_for("sx", [0]) is a
+    loc = P.thermal_relaxation_error(30.0, 20.0, 1.0)
+    nm.add_quantum_error(loc, "x", [2])
+    assert nm.error_for("x", [2]) is loc                                      # in place of the all-qubit error
+    assert nm.error_for("x", [1]).superop is not loc.superop
+    two = P.depolarizing_error(0.05, 2)
+    nm.add_quantum_error(two, ["cx"], [0, 1])
+    assert nm.error_for("cx", [0, 1]) is two and nm.error_for("cx", [1, 0]) is None
+    assert nm.noise_instructions == ["cx", "sx", "x"] and nm.noise_qubits == [0, 1, 2]
+    with pytest.raises(ValueError, match="does not match"):
+        nm.add_quantum_error(two, "cx", [0])
+
+
+def test_expand_is_tensor_swapped():
+    P = pkg()
+    a, b = P.amplitude_damping_error(0.3), P.phase_damping_error(0.2)
+    np.testing.assert_allclose(a.expand(b).superop, b.tensor(a).superop, atol=0)
