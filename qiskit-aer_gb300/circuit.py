@@ -2,9 +2,12 @@
 assemble into the engine's op list the way ``aer_compiler._assemble_op``
 (qiskit_aer/backends/aer_compiler.py:875-1020) assembles qiskit instructions
 into AerCircuit ops: named gates, ``unitary``, ``diagonal``, ``superop``,
-``kraus``, ``reset``, ``barrier``, final ``measure`` and the save
-instructions ``save_statevector`` / ``save_density_matrix`` /
-``save_probabilities`` / ``save_expectation_value``.
+``kraus``, ``reset``, ``barrier``, ``measure`` and the save instructions
+``save_statevector`` / ``save_statevector_dict`` / ``save_density_matrix``
+/ ``save_unitary`` / ``save_probabilities`` / ``save_probabilities_dict`` /
+``save_amplitudes`` / ``save_amplitudes_squared`` /
+``save_expectation_value`` / ``save_expectation_value_variance``
+(qiskit_aer/library/save_instructions/).
 """
 from __future__ import annotations
 
@@ -282,6 +285,33 @@ class QuantumCircuit:
         self.data.append(Instruction("save", "expval", [], data=(label, list(terms))))
         return self
 
+    def save_expectation_value_variance(self, terms, label="expectation_value_variance"):
+        """[<O>, <O^2> - <O>^2] (SaveExpectationValueVariance,
+        save_expectation_value.py:100-135)."""
+        self.data.append(Instruction("save", "expval_var", [], data=(label, list(terms))))
+        return self
+
+    def save_amplitudes(self, params, label="amplitudes"):
+        """Amplitudes of the listed basis states (statevector method,
+        State::apply_save_amplitudes, statevector_state.hpp:654-679)."""
+        self.data.append(Instruction("save", "amplitudes", [], data=(label, [int(i) for i in params])))
+        return self
+
+    def save_amplitudes_squared(self, params, label="amplitudes_squared"):
+        self.data.append(Instruction("save", "amplitudes_squared", [], data=(label, [int(i) for i in params])))
+        return self
+
+    def save_probabilities_dict(self, qubits=None, label="probabilities_dict"):
+        """Probabilities as {hex outcome: p}, entries above the chop threshold
+        (save_probs_ket, statevector_state.hpp:575-588)."""
+        q = list(range(self.num_qubits)) if qubits is None else [int(x) for x in qubits]
+        self.data.append(Instruction("save", "probabilities_dict", q, data=label))
+        return self
+
+    def save_statevector_dict(self, label="statevector_dict"):
+        self.data.append(Instruction("save", "statevector_dict", [], data=label))
+        return self
+
     # ---- standard gates (names of the reference gate sets) ----
     def _g(name, nq, npar=0):
         def f(self, *args):
@@ -324,6 +354,64 @@ class QuantumCircuit:
                     raise ValueError("only final measurements are supported (no mid-circuit measure)")
                 body.append(ins)
         return body, meas, saves
+
+
+_PAULI_PRODUCT = {("X", "Y"): (1j, "Z"), ("Y", "Z"): (1j, "X"), ("Z", "X"): (1j, "Y"),
+                  ("Y", "X"): (-1j, "Z"), ("Z", "Y"): (-1j, "X"), ("X", "Z"): (-1j, "Y")}
+
+
+def _pauli_of(label: str, qubits) -> dict:
+    """{qubit: 'X'|'Y'|'Z'} of a label read right to left onto qubits."""
+    out = {}
+    for j, q in enumerate(qubits):
+        c = label[len(label) - 1 - j].upper()
+        if c not in "IXYZ":
+            raise ValueError(f"invalid Pauli label {label!r}")
+        if c != "I":
+            out[int(q)] = c
+    return out
+
+
+def _pauli_product(a: dict, b: dict):
+    phase, out = 1 + 0j, dict(a)
+    for q, pb in b.items():
+        pa = out.get(q)
+        if pa is None:
+            out[q] = pb
+        elif pa == pb:
+            del out[q]
+        else:
+            ph, pc = _PAULI_PRODUCT[(pa, pb)]
+            phase *= ph
+            out[q] = pc
+    return phase, out
+
+
+def expval_params(terms, variance: bool = False):
+    """The reference's expectation-value parameters (_expval_params,
+    save_expectation_value.py:139-168): one entry per distinct Pauli, in
+    first-seen order, with the sum of the real parts of its coefficients in
+    O and, for the variance, in O.O (the Pauli products of every ordered pair
+    of terms, phases folded into the coefficients).  Returns
+    [((qubits, label), c_O, c_OO)] with label over the sorted qubits."""
+    ops = [(complex(c), _pauli_of(lab, q)) for c, lab, q in terms]
+    params = {}
+    for c, d in ops:
+        key = tuple(sorted(d.items()))
+        c1, c2 = params.get(key, (0.0, 0.0))
+        params[key] = (c1 + c.real, c2)
+    if variance:
+        for ca, da in ops:
+            for cb, db in ops:
+                ph, d = _pauli_product(da, db)
+                key = tuple(sorted(d.items()))
+                c1, c2 = params.get(key, (0.0, 0.0))
+                params[key] = (c1, c2 + (ca * cb * ph).real)
+    out = []
+    for key, (c1, c2) in params.items():
+        qubits = [q for q, _ in key]
+        out.append(((qubits, "".join(p for _, p in reversed(key))), c1, c2))
+    return out
 
 
 class NativeCircuit:

@@ -21,7 +21,7 @@ import time
 import numpy as np
 
 from . import _capi as A
-from .circuit import Instruction, NativeCircuit, QuantumCircuit
+from .circuit import Instruction, NativeCircuit, QuantumCircuit, expval_params
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
 
 
@@ -37,6 +37,19 @@ def discrete_draw(probs, u: float) -> int:
     cp = np.add.accumulate(p / total)
     cp[-1] = 1.0
     return int(np.searchsorted(cp, u, side="left"))
+
+
+def ket_dict(values, epsilon: float) -> dict:
+    """Utils::vec2ket(values, epsilon, 16) (framework/utils.hpp:963-990):
+    each value chopped (real and imaginary parts below epsilon in magnitude
+    set to 0, utils.hpp:909-934), kept when its magnitude then exceeds
+    epsilon, keyed by its index as "0x..." hex without leading zeros."""
+    v = np.asarray(values)
+    if np.iscomplexobj(v):
+        v = np.where(np.abs(v.real) < epsilon, 0.0, v.real) + 1j * np.where(np.abs(v.imag) < epsilon, 0.0, v.imag)
+    else:
+        v = np.where(np.abs(v) < epsilon, 0.0, v)
+    return {hex(int(k)): v[k].item() for k in np.nonzero(np.abs(v) > epsilon)[0]}
 
 
 def discrete_draws(probs: np.ndarray, u: np.ndarray) -> np.ndarray:
@@ -303,12 +316,13 @@ class AerSimulator:
                             data[first + j][ins.data] = vec[j << n:(j + 1) << n].copy()
                         continue
                     label, terms = ins.data
-                    vals = st.expval_pauli_segments(n, cnt, [(q, lab) for _, lab, q in terms])
-                    coeffs = np.array([complex(c) for c, _, _ in terms])
-                    re = coeffs.real @ vals
-                    im = coeffs.imag @ vals
+                    params = expval_params(terms)
+                    vals = st.expval_pauli_segments(n, cnt, [ql for ql, _, _ in params])
+                    total = np.zeros(cnt)
+                    for (_, c1, _), v in zip(params, vals):  # in parameter order, per binding
+                        total += c1 * v
                     for j in range(cnt):
-                        data[first + j][label] = float(re[j]) if not np.any(coeffs.imag) else complex(re[j], im[j])
+                        data[first + j][label] = float(total[j])
             if st is not None:
                 st.synchronize()
         finally:
@@ -353,6 +367,7 @@ class AerSimulator:
 
     # shots per stacked group and the largest stack (qubits of the circuit +
     # shot bits), about 4 GB of complex128 amplitudes
+    CHOP_THRESHOLD = 1e-8  # Config::chop_threshold (framework/config.hpp:125)
     SHOT_GROUP_BITS = 16
     SHOT_STACK_QUBITS = 28
     HOST_DRAW_QUBITS = 10  # wider registers are drawn on the device
@@ -681,11 +696,38 @@ class AerSimulator:
             data[ins.data] = st.copy_to_matrix()
         elif ins.name == "probabilities":
             data[ins.data] = st.probabilities(ins.qubits)
-        elif ins.name == "expval":
+        elif ins.name in ("expval", "expval_var"):
+            # Base::apply_save_expval (state.hpp:416-447) over the reference's
+            # parameters: real coefficients of O (and of O.O for the variance)
             label, terms = ins.data
-            pairs = [(q, lab) for _, lab, q in terms]
-            coeffs = [complex(c).real for c, _, _ in terms]
-            vals, total = st.expval_pauli_many(pairs, coeffs)
-            # Base::apply_save_expval adds the imaginary part of complex coefficients too
-            imag = sum(complex(c).imag * v for (c, _, _), v in zip(terms, vals))
-            data[label] = total if imag == 0 else complex(total, imag)
+            if not terms:
+                raise ValueError("Invalid save expval instruction (Pauli components are empty).")
+            variance = ins.name == "expval_var"
+            params = expval_params(terms, variance)
+            vals, _ = st.expval_pauli_many([ql for ql, _, _ in params])
+            expval, sq = 0.0, 0.0
+            for (_, c1, c2), v in zip(params, vals):
+                expval += c1 * float(v)
+                if variance:
+                    sq += c2 * float(v)
+            data[label] = [expval, sq - expval * expval] if variance else expval
+        elif ins.name in ("amplitudes", "amplitudes_squared"):
+            label, idx = ins.data
+            if not idx:
+                raise ValueError("Invalid save_amplitudes instructions (empty params).")
+            if ins.name == "amplitudes":
+                if isinstance(st, (DensityMatrix, UnitaryMatrix)):
+                    raise ValueError("save_amplitudes needs the statevector method")
+                vec = st.copy_to_vector()
+                data[label] = np.array([vec[i] for i in idx], dtype=complex)
+            else:
+                probs = st.probabilities()
+                data[label] = np.array([probs[i] for i in idx], dtype=np.float64)
+        elif ins.name == "probabilities_dict":
+            probs = st.probabilities(ins.qubits)
+            data[ins.data] = ket_dict(probs, self.CHOP_THRESHOLD)
+        elif ins.name == "statevector_dict":
+            if isinstance(st, (DensityMatrix, UnitaryMatrix)):
+                raise ValueError("save_statevector_dict needs the statevector method")
+            vec = st.copy_to_vector()
+            data[ins.data] = ket_dict(vec, self.CHOP_THRESHOLD)
