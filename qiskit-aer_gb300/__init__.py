@@ -13,7 +13,7 @@ Package layout:
 """
 from ._capi import GBQVError, lib
 from .circuit import NativeCircuit, Parameter, ParameterExpression, QuantumCircuit
-from .noise import (NoiseModel, QuantumError, amplitude_damping_error, coherent_unitary_error,
+from .noise import (NoiseModel, QuantumError, ReadoutError, amplitude_damping_error, coherent_unitary_error,
                     depolarizing_error, kraus_error, mixed_unitary_error, pauli_error, phase_amplitude_damping_error,
                     phase_damping_error, reset_error, thermal_relaxation_error)
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
@@ -26,7 +26,7 @@ __all__ = [
     "Parameter", "ParameterExpression", "QuantumCircuit",
     "QuantumError", "QubitVector", "Result", "UnitaryMatrix", "amplitude_damping_error", "depolarizing_error", "lib",
     "phase_amplitude_damping_error", "uniforms", "coherent_unitary_error", "kraus_error", "mixed_unitary_error",
-    "pauli_error", "phase_damping_error", "reset_error", "thermal_relaxation_error",
+    "pauli_error", "phase_damping_error", "reset_error", "thermal_relaxation_error", "ReadoutError",
 ]
 
 

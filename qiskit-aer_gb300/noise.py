@@ -245,10 +245,100 @@ def phase_amplitude_damping_error(param_amp, param_phase, excited_state_populati
     return QuantumError.from_kraus(ops)
 
 
+class ReadoutError:
+    """Classical readout error of k qubits: probabilities[a][m] = P(read m |
+    actual a), outcome index bit j on the error's qubit j
+    (qiskit_aer/noise/errors/readout_error.py:36-110, checks :254-282)."""
+
+    def __init__(self, probabilities, atol: float = ATOL):
+        if probabilities is None or len(probabilities) == 0:
+            raise ValueError("Input probabilities: empty.")
+        rows = [np.asarray(r, dtype=np.float64) for r in probabilities]
+        n_out = len(rows[0])
+        k = int(np.log2(n_out)) if n_out else 0
+        if n_out == 0 or 2 ** k != n_out:
+            raise ValueError(f"Invalid probabilities: length {n_out} != 2**{k}")
+        if len(rows) != n_out:
+            raise ValueError("Invalid probabilities.")
+        for r in rows:
+            if len(r) != n_out:
+                raise ValueError("Invalid probabilities: vectors are different lengths.")
+            if abs(r.sum() - 1) > atol:
+                raise ValueError(f"Invalid probabilities: sum({list(r)})= {r.sum()} is not 1.")
+            if np.any(r < 0):
+                raise ValueError(f"Invalid probabilities: {list(r)} contains a negative probability.")
+        self.probabilities = np.array(rows)
+        self.number_of_qubits = k
+
+    def ideal(self) -> bool:
+        return round(float(np.linalg.norm(self.probabilities - np.eye(self.probabilities.shape[0]))), 12) == 0
+
+
+def apply_readout(memory: int, bits, probs: np.ndarray, u: float) -> int:
+    """ClassicalRegister::apply_roerror (framework/creg.hpp:230-262) on an
+    integer classical memory: the actual value of `bits` (bit j of the value
+    on bits[j]) picks the row of probs, one draw with uniform u
+    (RngEngine::rand_int) gives the value read, written back to `bits`."""
+    from .simulator import discrete_draw
+    actual = 0
+    for j, b in enumerate(bits):
+        actual |= ((memory >> b) & 1) << j
+    read = discrete_draw(probs[actual], u)
+    for j, b in enumerate(bits):
+        memory = (memory & ~(1 << b)) | (((read >> j) & 1) << b)
+    return memory
+
+
 class NoiseModel:
     def __init__(self):
         self._all_qubit = {}   # gate name -> QuantumError
         self._local = {}       # gate name -> {qubit tuple: QuantumError}
+        self._readout_default = None   # single-qubit ReadoutError for every measured qubit
+        self._readout_local = {}       # qubit tuple -> ReadoutError
+
+    def add_all_qubit_readout_error(self, error, warnings: bool = True):
+        """A single-qubit readout error on every measured qubit without one of
+        its own; a second call replaces the first (noise_model.py:808-856)."""
+        error = error if isinstance(error, ReadoutError) else ReadoutError(error)
+        if error.ideal():
+            return
+        if error.number_of_qubits != 1:
+            raise ValueError("All-qubit readout errors must defined as single-qubit errors.")
+        self._readout_default = error
+
+    def add_readout_error(self, error, qubits, warnings: bool = True):
+        """A readout error on exactly these qubits (noise_model.py:858-920)."""
+        error = error if isinstance(error, ReadoutError) else ReadoutError(error)
+        if error.ideal():
+            return
+        qubits = tuple(int(q) for q in qubits)
+        if error.number_of_qubits != len(qubits):
+            raise ValueError(f"Number of qubits ({len(qubits)}) does not match the readout error size "
+                             f"({error.number_of_qubits})")
+        self._readout_local[qubits] = error
+
+    def readout_ops(self, qubits, clbits) -> list:
+        """The readout errors after a measurement of qubits into clbits, as
+        (clbits, probabilities) in the order they apply
+        (NoiseModel::sample_readout_noise, noise_model.hpp): one error over
+        the whole measurement when one is given for exactly its qubits, else
+        per qubit its own error or the all-qubit one."""
+        qubits = [int(q) for q in qubits]
+        exact = self._readout_local.get(tuple(qubits))
+        if exact is not None:
+            return [(list(clbits), exact.probabilities)]
+        out = []
+        for q, c in zip(qubits, clbits):
+            e = self._readout_local.get((q,), self._readout_default)
+            if e is not None:
+                out.append(([int(c)], e.probabilities))
+        return out
+
+    def has_readout_errors(self) -> bool:
+        return self._readout_default is not None or bool(self._readout_local)
+
+    def has_quantum_errors(self) -> bool:
+        return bool(self._all_qubit) or bool(self._local)
 
     @staticmethod
     def _names(instructions):
@@ -285,11 +375,13 @@ class NoiseModel:
 
     @property
     def noise_instructions(self) -> list:
-        return sorted(set(self._all_qubit) | set(self._local))
+        names = set(self._all_qubit) | set(self._local)
+        return sorted(names | ({"measure"} if self.has_readout_errors() else set()))
 
     @property
     def noise_qubits(self) -> list:
-        return sorted({q for table in self._local.values() for key in table for q in key})
+        qs = {q for table in self._local.values() for key in table for q in key}
+        return sorted(qs | {q for key in self._readout_local for q in key})
 
     def is_ideal(self) -> bool:
-        return not self._all_qubit and not self._local
+        return not self.has_quantum_errors() and not self.has_readout_errors()

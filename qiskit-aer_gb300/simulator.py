@@ -22,6 +22,7 @@ import numpy as np
 
 from . import _capi as A
 from .circuit import Instruction, NativeCircuit, QuantumCircuit, expval_params
+from .noise import apply_readout
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
 
 
@@ -144,7 +145,7 @@ class AerSimulator:
     def _with_noise(self, body, positions=None):
         """Insert the noise model's superoperators after each matching gate.
         `positions` (op indices into `body`) are mapped to the new list."""
-        if self.noise_model is None or self.noise_model.is_ideal():
+        if self.noise_model is None or not self.noise_model.has_quantum_errors():
             return (body, list(positions)) if positions is not None else body
         if self.method != "density_matrix":
             raise ValueError("noise is supported with method='density_matrix' (superoperator noise)")
@@ -357,11 +358,18 @@ class AerSimulator:
             if meas:
                 qubits = [q for m in meas for q in m.qubits]
                 clbits = [c for m in meas for c in m.clbits]
-                rnds = uniforms(seed, shots)
-                samples = st.sample_measure(rnds)
-                counts = self._counts(samples, qubits, clbits, circuit.num_clbits)
-                if self._want_memory:
-                    data["memory"] = self._memory(self._memory_values(samples, qubits, clbits))
+                ro = self._readout_ops(meas)
+                stream = uniforms(seed, shots * (1 + len(ro)))
+                samples = st.sample_measure(stream[:shots])
+                if ro:
+                    mem = self._readout_sampled(self._memory_values(samples, qubits, clbits), ro, stream[shots:])
+                    counts = self._counts_of(mem, circuit.num_clbits)
+                    if self._want_memory:
+                        data["memory"] = self._memory(mem)
+                else:
+                    counts = self._counts(samples, qubits, clbits, circuit.num_clbits)
+                    if self._want_memory:
+                        data["memory"] = self._memory(self._memory_values(samples, qubits, clbits))
             st.synchronize()
         return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
 
@@ -385,7 +393,7 @@ class AerSimulator:
         qubitvector_thrust.hpp:2251-2448): each stretch runs once over the
         whole group, each measurement is one probability pass, a host draw
         per shot from its own stream and one collapse pass."""
-        if self.noise_model is not None and not self.noise_model.is_ideal():
+        if self.noise_model is not None and self.noise_model.has_quantum_errors():
             raise NotImplementedError("noise on a statevector needs per-shot noise sampling; use density_matrix")
         cfg = self.fusion_config()
         items, stretch = [], []
@@ -460,9 +468,15 @@ class AerSimulator:
         return max(0, min((int(shots) - 1).bit_length(), self.SHOT_GROUP_BITS, self.SHOT_STACK_QUBITS - n,
                           22 - k_host, 27 - k_dev))
 
+    def _draws_per_shot(self, items) -> int:
+        """Uniforms one shot consumes at most: one per measure / reset, one
+        per readout error after a measurement."""
+        return sum(1 + (len(self._readout_ops([obj])) if kind == "measure" else 0)
+                   for kind, obj, _ in items if kind in ("measure", "reset"))
+
     def _shots_batched(self, n, items, matrices, shots, seed):
         L = A.lib()
-        ndraw = sum(1 for kind, _, _ in items if kind in ("measure", "reset"))
+        ndraw = self._draws_per_shot(items)
         ks = [len(obj.qubits) for kind, obj, _ in items if kind in ("measure", "reset")]
         b = self._shot_group_bits(n, shots, ks)
         group = 1 << b
@@ -529,6 +543,17 @@ class AerSimulator:
                         for i, c in enumerate(obj.clbits):
                             bit = np.uint64(1) << np.uint64(c)
                             memory[rows] = (memory[rows] & ~bit) | (((o >> np.uint64(i)) & np.uint64(1)) << np.uint64(c))
+                        for bits, probs in self._readout_ops([obj]):   # ClassicalRegister::apply_roerror per shot
+                            mem = memory[rows]
+                            actual = np.zeros(rows.size, dtype=np.int64)
+                            for j, b in enumerate(bits):
+                                actual |= ((mem >> np.uint64(b)) & np.uint64(1)).astype(np.int64) << j
+                            read = discrete_draws(probs[actual], u[rows, used[rows]]).astype(np.uint64)
+                            used[rows] += 1
+                            for j, b in enumerate(bits):
+                                bit = np.uint64(1) << np.uint64(b)
+                                mem = (mem & ~bit) | (((read >> np.uint64(j)) & np.uint64(1)) << np.uint64(b))
+                            memory[rows] = mem
                 out[g0:g0 + cnt] = memory
             st.synchronize()
         return out
@@ -536,7 +561,7 @@ class AerSimulator:
     def _shots_serial(self, n, items, shots, seed):
         """One state, one shot at a time (classical memory wider than 63
         bits, or a conditioned op beyond the stacked kernels)."""
-        ndraw = sum(1 for kind, _, _ in items if kind in ("measure", "reset"))
+        ndraw = self._draws_per_shot(items)
         out = []
         with QubitVector(n, self.precision) as st:
             for shot in range(shots):
@@ -559,6 +584,9 @@ class AerSimulator:
                     if kind == "measure":
                         for i, c in enumerate(obj.clbits):
                             memory = (memory & ~(1 << c)) | (((outcome >> i) & 1) << c)
+                        for bits, rp in self._readout_ops([obj]):
+                            memory = apply_readout(memory, bits, rp, u[used])
+                            used += 1
                 out.append(memory)
             st.synchronize()
         return out
@@ -599,7 +627,7 @@ class AerSimulator:
             elif ins.kind != "barrier":
                 stretch.append(ins)
         flush()
-        ndraw = sum(1 for kind, _, _ in items if kind == "measure")
+        ndraw = self._draws_per_shot(items)
         memories = []
         with DensityMatrix(circuit.num_qubits, self.precision) as st:
             if not self.options["blocking_enable"]:
@@ -624,6 +652,9 @@ class AerSimulator:
                     st.apply_diagonal_unitary_matrix(obj.qubits, diag)
                     for i, c in enumerate(obj.clbits):
                         memory = (memory & ~(1 << c)) | (((outcome >> i) & 1) << c)
+                    for bits, rp in self._readout_ops([obj]):
+                        memory = apply_readout(memory, bits, rp, u[used])
+                        used += 1
                 memories.append(memory)
             st.synchronize()
         data = {}
@@ -654,6 +685,36 @@ class AerSimulator:
                 perm = np.eye(dim, dtype=complex)
                 perm[[final_state, meas_state]] = perm[[meas_state, final_state]]
                 st.apply_matrix(qubits, perm)
+
+    def _readout_ops(self, meas) -> list:
+        """Readout errors after the measurements, in order: (clbits, probs)."""
+        if self.noise_model is None or not self.noise_model.has_readout_errors():
+            return []
+        return [op for m in meas for op in self.noise_model.readout_ops(m.qubits, m.clbits)]
+
+    @staticmethod
+    def _readout_sampled(memory, ro, u) -> list:
+        """Executor::measure_sampler with readout errors
+        (circuit_executor.hpp:1097-1121): after the samples have taken the
+        stream's first `shots` draws, the samples are walked from the last to
+        the first, each readout error drawing the stream's next uniform; the
+        memories come out in that order."""
+        out, k = [], 0
+        for i in range(len(memory) - 1, -1, -1):
+            m = int(memory[i])
+            for bits, probs in ro:
+                m = apply_readout(m, bits, probs, float(u[k]))
+                k += 1
+            out.append(m)
+        return out
+
+    @staticmethod
+    def _counts_of(memory, num_clbits: int) -> dict:
+        counts = {}
+        for v in memory:
+            key = format(int(v), f"0{num_clbits}b")
+            counts[key] = counts.get(key, 0) + 1
+        return counts
 
     @staticmethod
     def _memory_values(samples, qubits, clbits):

@@ -351,3 +351,31 @@ def test_noisy_density_matrix_shots_match_oracle():
         key = format(mem, f"0{2 * n}b")
         want[key] = want.get(key, 0) + 1
     assert got == want
+
+
+@pytest.mark.parametrize("method", ["statevector", "density_matrix"])
+def test_readout_errors_deterministic(method):
+    """Readout errors with 0/1 probabilities: sampled final measurements, a
+    two-qubit error on exactly the measured qubits, and a readout error
+    ahead of a classical condition in a circuit run shot by shot."""
+    P = pkg()
+    always0 = P.ReadoutError([[1, 0], [1, 0]])
+    flip = P.ReadoutError([[0, 1], [1, 0]])
+    nm = P.NoiseModel()
+    nm.add_all_qubit_readout_error(flip)
+    nm.add_readout_error(always0, [0])
+    qc = P.QuantumCircuit(3, 3).x(0).measure([0, 1, 2], [0, 1, 2])
+    res = P.AerSimulator(method=method, noise_model=nm).run(qc, shots=50, seed_simulator=1, memory=True)
+    assert res.get_counts() == {"110": 50}           # qubit 0 reads 0, qubits 1 and 2 read 1
+    assert res.get_memory() == ["0x6"] * 50
+    nm2 = P.NoiseModel()
+    nm2.add_readout_error(P.ReadoutError(np.eye(4)[[3, 2, 1, 0]]), [0, 1])   # reads a ^ 3
+    qc2 = P.QuantumCircuit(2, 2).x(0).measure([0, 1], [0, 1])
+    assert P.AerSimulator(method=method, noise_model=nm2).run(qc2, shots=20, seed_simulator=2).get_counts() == {"10": 20}
+    nm3 = P.NoiseModel()
+    nm3.add_readout_error(always0, [0])
+    qc3 = P.QuantumCircuit(2, 2).x(0).measure(0, 0)
+    qc3.x(1).c_if(0, 1)
+    qc3.measure(1, 1)
+    assert P.AerSimulator(method=method).run(qc3, shots=30, seed_simulator=3).get_counts() == {"11": 30}
+    assert P.AerSimulator(method=method, noise_model=nm3).run(qc3, shots=30, seed_simulator=3).get_counts() == {"00": 30}

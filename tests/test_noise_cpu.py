@@ -152,3 +152,76 @@ def test_expand_is_tensor_swapped():
     P = pkg()
     a, b = P.amplitude_damping_error(0.3), P.phase_damping_error(0.2)
     np.testing.assert_allclose(a.expand(b).superop, b.tensor(a).superop, atol=0)
+
+
+def roerror_reference(creg: str, memory_bits, probs, u, P):
+    """ClassicalRegister::apply_roerror restated on the reference's string
+    register (creg[size - 1 - bit] holds bit `bit`)."""
+    creg = list(creg)
+    mem_str = "".join(creg[len(creg) - 1 - b] for b in reversed(memory_bits))
+    outcome = P.simulator.discrete_draw(probs[int(mem_str, 2)], u)
+    noise = format(outcome, f"0{len(memory_bits)}b")
+    for pos, b in enumerate(memory_bits):
+        creg[len(creg) - 1 - b] = noise[len(noise) - 1 - pos]
+    return "".join(creg)
+
+
+def test_readout_error_checks_and_lookup():
+    P = pkg()
+    with pytest.raises(ValueError, match="is not 1"):
+        P.ReadoutError([[0.9, 0.2], [0.1, 0.9]])
+    with pytest.raises(ValueError, match="2\\*\\*"):
+        P.ReadoutError([[0.5, 0.3, 0.2], [0.5, 0.3, 0.2], [0.5, 0.3, 0.2]])
+    assert P.ReadoutError([[1, 0], [0, 1]]).ideal()
+    nm = P.NoiseModel()
+    nm.add_all_qubit_readout_error(P.ReadoutError([[1, 0], [0, 1]]))   # ideal: not added
+    assert nm.is_ideal()
+    d = P.ReadoutError([[0.9, 0.1], [0.2, 0.8]])
+    loc = P.ReadoutError([[0.7, 0.3], [0.4, 0.6]])
+    two = P.ReadoutError(np.eye(4)[[1, 0, 3, 2]])
+    nm.add_all_qubit_readout_error(d)
+    nm.add_readout_error(loc, [2])
+    nm.add_readout_error(two, [0, 1])
+    assert nm.has_readout_errors() and not nm.has_quantum_errors() and not nm.is_ideal()
+    ops = nm.readout_ops([0, 1], [5, 6])                 # exactly the 2-qubit error's qubits
+    assert len(ops) == 1 and ops[0][0] == [5, 6] and ops[0][1] is two.probabilities
+    ops = nm.readout_ops([1, 2, 3], [0, 1, 2])           # per qubit: default, local, default
+    assert [b for b, _ in ops] == [[0], [1], [2]]
+    assert ops[1][1] is loc.probabilities and ops[0][1] is d.probabilities
+    with pytest.raises(ValueError, match="single-qubit"):
+        nm.add_all_qubit_readout_error(two)
+    assert nm.noise_instructions == ["measure"]
+
+
+def test_apply_readout_matches_string_register():
+    P = pkg()
+    rng = np.random.default_rng(7)
+    probs2 = rng.random((4, 4))
+    probs2 /= probs2.sum(axis=1, keepdims=True)
+    for _ in range(200):
+        mem = int(rng.integers(0, 1 << 6))
+        bits = [int(x) for x in rng.choice(6, 2, replace=False)]
+        u = float(rng.random())
+        got = P.noise.apply_readout(mem, bits, probs2, u)
+        want = roerror_reference(format(mem, "06b"), bits, probs2, u, P)
+        assert format(got, "06b") == want
+
+
+def test_sampled_readout_walks_samples_backwards():
+    """measure_sampler: samples take the stream's first draws, then the
+    readout draws go from the last sample to the first."""
+    P = pkg()
+    rng = np.random.default_rng(8)
+    probs = np.array([[0.6, 0.4], [0.3, 0.7]])
+    ro = [([0], probs), ([2], probs)]
+    mem = rng.integers(0, 8, size=5).astype(np.uint64)
+    u = rng.random(10)
+    got = P.AerSimulator._readout_sampled(mem, ro, u)
+    want, k = [], 0
+    for i in reversed(range(5)):
+        m = int(mem[i])
+        for bits, p in ro:
+            m = int(roerror_reference(format(m, "03b"), bits, p, u[k], P), 2)
+            k += 1
+        want.append(m)
+    assert got == want
