@@ -10,6 +10,7 @@ Package layout:
   noise.py        noise channels as superoperators
   simulator.py    AerSimulator-shaped run() with fusion, sampling, saves
   adjoint.py      adjoint-method gradients behind torch.autograd
+  autotune.py     schedule autotuner (execution form, batch team split)
 """
 from ._capi import GBQVError, lib
 from .circuit import NativeCircuit, Parameter, ParameterExpression, QuantumCircuit
@@ -18,11 +19,11 @@ from .noise import (NoiseModel, QuantumError, ReadoutError, amplitude_damping_er
                     phase_damping_error, reset_error, thermal_relaxation_error)
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
 from .simulator import AerSimulator, Result, uniforms
-from . import adjoint, batched
+from . import adjoint, autotune, batched
 from .primitives import EstimatorV2, SamplerV2
 
 __all__ = [
-    "AerSimulator", "adjoint", "batched", "DensityMatrix", "EstimatorV2", "SamplerV2", "GBQVError", "NativeCircuit", "NoiseModel",
+    "AerSimulator", "adjoint", "autotune", "batched", "DensityMatrix", "EstimatorV2", "SamplerV2", "GBQVError", "NativeCircuit", "NoiseModel",
     "Parameter", "ParameterExpression", "QuantumCircuit",
     "QuantumError", "QubitVector", "Result", "UnitaryMatrix", "amplitude_damping_error", "depolarizing_error", "lib",
     "phase_amplitude_damping_error", "uniforms", "coherent_unitary_error", "kraus_error", "mixed_unitary_error",

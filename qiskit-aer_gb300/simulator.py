@@ -21,6 +21,7 @@ import time
 import numpy as np
 
 from . import _capi as A
+from .autotune import Autotuner, default_tuner, tune_execute
 from .circuit import Instruction, NativeCircuit, QuantumCircuit, expval_params
 from .noise import apply_readout
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
@@ -107,7 +108,8 @@ class AerSimulator:
     def __init__(self, method: str = "statevector", device: str = "GPU", precision: str = "double",
                  noise_model=None, fusion_enable: bool = True, fusion_max_qubit: int | None = None,
                  fusion_threshold: int | None = None, fusion_cost_factor: float = 1.8,
-                 fusion_avx2_costs: bool = True, blocking_enable: bool = True, seed_simulator: int | None = None):
+                 fusion_avx2_costs: bool = True, blocking_enable: bool = True, seed_simulator: int | None = None,
+                 autotune: bool = False, autotune_cache: str | None = None):
         if method not in self.METHODS:
             raise ValueError(f"method must be one of {self.METHODS}")
         if device != "GPU":
@@ -118,7 +120,16 @@ class AerSimulator:
         self.options = dict(fusion_enable=fusion_enable, fusion_max_qubit=fusion_max_qubit,
                             fusion_threshold=fusion_threshold, fusion_cost_factor=fusion_cost_factor,
                             fusion_avx2_costs=fusion_avx2_costs, blocking_enable=blocking_enable,
-                            seed_simulator=seed_simulator)
+                            seed_simulator=seed_simulator, autotune=autotune, autotune_cache=autotune_cache)
+        self._tuner = None
+
+    def tuner(self) -> Autotuner:
+        """The schedule autotuner of this simulator: its own cache file when
+        autotune_cache is given, else the process-wide tuner."""
+        if self._tuner is None:
+            path = self.options["autotune_cache"]
+            self._tuner = Autotuner(path) if path else default_tuner()
+        return self._tuner
 
     # ---- fusion configuration ----
     def fusion_config(self, has_superop=False, has_kraus=False) -> A.FusionConfig:
@@ -347,6 +358,8 @@ class AerSimulator:
         with cls(circuit.num_qubits, self.precision) as st:
             if not self.options["blocking_enable"]:
                 A.check(st._L.gbqv_set_blocking(st.handle, 0))
+            elif self.options["autotune"] and self.method == "statevector":
+                meta["autotune"] = {"blocking": tune_execute(st, [nc for _, nc in segments], self.tuner())}
             save_iter = iter(saves)
             pending = next(save_iter, None)
             for bound, nc in segments:
