@@ -345,8 +345,9 @@ class NoiseModel:
         return [instructions] if isinstance(instructions, str) else list(instructions)
 
     def add_all_qubit_quantum_error(self, error: QuantumError, instructions, warnings: bool = True):
-        """An error after every listed gate; a second error for the same gate
-        is composed after the first; an ideal error is not added."""
+        """An error after every listed gate or reset, or before every
+        measure; a second error for the same instruction is composed after
+        the first; an ideal error is not added."""
         if error.ideal():
             return
         for name in self._names(instructions):
@@ -354,8 +355,9 @@ class NoiseModel:
             self._all_qubit[name] = error if old is None else old.compose(error)
 
     def add_quantum_error(self, error: QuantumError, instructions, qubits, warnings: bool = True):
-        """An error after the listed gates on exactly these qubits (in this
-        order), used there in place of the all-qubit error."""
+        """An error on the listed instructions on exactly these qubits (in
+        this order), used there in place of the all-qubit error: after a gate
+        or reset, before a measure."""
         if error.ideal():
             return
         qubits = tuple(int(q) for q in qubits)
@@ -372,6 +374,28 @@ class NoiseModel:
             if local is not None:
                 return local
         return self._all_qubit.get(name)
+
+    def op_errors(self, name: str, qubits) -> list:
+        """[(qubits, QuantumError)] an instruction gets
+        (NoiseModel::sample_local_quantum_noise, noise_model.hpp:726-781).
+        A gate gets the error for exactly its qubits, else the all-qubit
+        one.  A measure or reset without an error for exactly its qubits gets,
+        per qubit, that qubit's own error or the all-qubit one, because
+        measure and reset act on any number of qubits while their errors are
+        usually single-qubit."""
+        qubits = [int(q) for q in qubits]
+        if name not in ("measure", "reset"):
+            err = self.error_for(name, qubits)
+            return [] if err is None else [(qubits, err)]
+        exact = self._local.get(name, {}).get(tuple(qubits))
+        if exact is not None:
+            return [(qubits, exact)]
+        out = []
+        for q in qubits:
+            err = self.error_for(name, [q])
+            if err is not None:
+                out.append(([q], err))
+        return out
 
     @property
     def noise_instructions(self) -> list:

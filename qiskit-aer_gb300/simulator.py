@@ -153,9 +153,23 @@ class AerSimulator:
         cfg.avx2_costs = int(o["fusion_avx2_costs"])
         return cfg
 
+    def _noise_ops(self, name, qubits) -> list:
+        """The noise model's errors on one instruction as superop
+        instructions (NoiseModel::op_errors)."""
+        if self.noise_model is None or not self.noise_model.has_quantum_errors():
+            return []
+        out = []
+        for q, err in self.noise_model.op_errors(name, qubits):
+            if err.num_qubits != len(q):
+                raise ValueError(f"error on '{name}' acts on {err.num_qubits} qubits, the instruction on {len(q)}")
+            out.append(Instruction("superop", "superop", list(q), data=err.superop))
+        return out
+
     def _with_noise(self, body, positions=None):
-        """Insert the noise model's superoperators after each matching gate.
-        `positions` (op indices into `body`) are mapped to the new list."""
+        """Insert the noise model's superoperators: after each matching gate
+        or reset, before each measure (the reference sets measure errors to
+        act before the op, noise_model.hpp:1075-1085).  `positions` (op
+        indices into `body`) are mapped to the new list."""
         if self.noise_model is None or not self.noise_model.has_quantum_errors():
             return (body, list(positions)) if positions is not None else body
         if self.method != "density_matrix":
@@ -163,13 +177,15 @@ class AerSimulator:
         out, new_index = [], []
         for ins in body:
             new_index.append(len(out))
+            if ins.kind == "measure":
+                out.extend(self._noise_ops("measure", ins.qubits))
+                out.append(ins)
+                continue
             out.append(ins)
             if ins.kind == "gate":
-                err = self.noise_model.error_for(ins.name, ins.qubits)
-                if err is not None:
-                    if err.num_qubits != len(ins.qubits):
-                        raise ValueError(f"error on '{ins.name}' acts on {err.num_qubits} qubits")
-                    out.append(Instruction("superop", "superop", list(ins.qubits), data=err.superop))
+                out.extend(self._noise_ops(ins.name, ins.qubits))
+            elif ins.kind == "reset":
+                out.extend(self._noise_ops("reset", ins.qubits))
         if positions is None:
             return out
         new_index.append(len(out))
@@ -181,6 +197,8 @@ class AerSimulator:
         body, meas, saves = circuit.split_final()
         body, pos = self._with_noise(body, [p for p, _ in saves])
         saves = [(p, ins) for p, (_, ins) in zip(pos, saves)]
+        # errors on the final measurements act before them: after every op and save
+        body = body + [e for m in meas for e in self._noise_ops("measure", m.qubits)]
         kinds = {i.kind for i in body}
         cfg = self.fusion_config(has_superop="superop" in kinds, has_kraus="kraus" in kinds)
         meta = {"fusion": {"enabled": bool(cfg.enable)}}
@@ -632,6 +650,9 @@ class AerSimulator:
                 raise NotImplementedError("save instructions in a circuit run shot by shot")
             if ins.kind == "measure":
                 flush()
+                errs = self._noise_ops("measure", ins.qubits)
+                if errs:  # measure errors act before the measurement, under its condition
+                    items.append(("ops", NativeCircuit(circuit.num_qubits, errs), ins.condition))
                 items.append(("measure", ins, ins.condition))
             elif ins.condition is not None:
                 flush()
