@@ -450,7 +450,13 @@ def bench_batch(args, torch, P):
     B, adj = P.batched, P.adjoint
     insts = B.config5_instances(args.instances, seed=args.seed, qmin=args.batch_qmin, qmax=args.batch_qmax,
                                 dmin=args.batch_dmin, dmax=args.batch_dmax)
+    tuned = None
+    if args.autotune:  # team split picked by timing the whole batch under each candidate (untimed here)
+        T = P.autotune
+        tuned = T.tune_batch(insts, args.precision, True, T.Autotuner(warmup=1, repeats=1))
     b = B.Batch(args.precision)
+    if tuned is not None:
+        b.set_teams(*tuned)
     for inst in insts:
         b.add(inst["n"], inst["gates"], inst["theta"], inst["terms"], inst["coeffs"], inst["shots"], inst["seed"])
     for _ in range(max(1, args.warmup)):
@@ -490,7 +496,8 @@ def bench_batch(args, torch, P):
             "speedup_vs_per_launch": round(est_single / (ms / 1e3), 2),
             "config": {"workload": f"{len(insts)} instances, {args.batch_qmin}-{args.batch_qmax} qubits, depth "
                                    f"{args.batch_dmin}-{args.batch_dmax}, 20-60 Paulis, 4096 shots",
-                       "instances": len(insts)}, "clocks": clk}
+                       "instances": len(insts),
+                       "teams": list(tuned) if tuned is not None else "default (64, 0.5)"}, "clocks": clk}
 
 
 def dynamic_circuit(P, n, rounds, seed):
@@ -728,6 +735,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-blocking", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="batch workload: pick the two-CTA team split by timing the candidates first")
     ap.add_argument("--no-variants", action="store_true", help="skip the complex64 run of the default workload")
     args = ap.parse_args()
     if args.impl == "reference":
