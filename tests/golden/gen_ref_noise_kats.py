@@ -4,14 +4,17 @@ noise models.
 test/terra/reference/ref_pauli_noise.py, ref_reset_noise.py and
 ref_kraus_noise.py pair small circuits (gates, reset, final measurements)
 with noise models: Pauli, reset and amplitude-damping errors on gates, on
-reset and on measure.  They also give the exact outcome distributions as
-counts of a number of shots.  They need qiskit's circuit builder and
-qiskit_aer's noise module; neither is importable here.  This script puts
-recording stand-ins for both in sys.modules, imports the three files from
-the reference tree and writes, per case: the circuit (instruction kind,
+reset and on measure.  ref_readout_noise.py does the same with readout
+errors, on single measurements and on one 2-qubit measurement.  All four
+files give the exact outcome distributions as counts of a number of shots.
+They need qiskit's circuit builder and qiskit_aer's noise module; neither
+is importable here.  This script puts recording stand-ins for both in
+sys.modules, imports the four files from the reference tree and writes,
+per case: the circuit (instruction kind,
 name, qubits, parameters, classical bits), the noise model as the list of
-add_*_quantum_error calls with the error constructor and its arguments, and
-the target probabilities (counts / shots).
+add_*_quantum_error calls with the error constructor and its arguments
+(readout cases: the add_*_readout_error calls with their matrices), and the
+target probabilities (counts / shots).
 
 Usage:  python tests/golden/gen_ref_noise_kats.py [reference test dir]
 (default: the reference checkout's test/terra/reference folder).
@@ -30,6 +33,7 @@ DEFAULT_DIR = Path("/root/reference/test/terra/reference")
 SETS = (("ref_pauli_noise", "pauli_gate_error"), ("ref_pauli_noise", "pauli_measure_error"),
         ("ref_pauli_noise", "pauli_reset_error"), ("ref_reset_noise", "reset_gate_error"),
         ("ref_kraus_noise", "kraus_gate_error"))
+READOUT_SETS = (("ref_readout_noise", "readout_error"),)
 SHOTS = 4096
 
 
@@ -92,6 +96,22 @@ class QuantumCircuit:
     def x(self, q):
         return self._one_qubit("gate", "x", q)
 
+    def h(self, q):
+        return self._one_qubit("gate", "h", q)
+
+    def cx(self, c, t):
+        for a, b in zip(self._bits(c, self.qoff), self._bits(t, self.qoff)):
+            self.ops.append(["gate", "cx", [a, b], [], []])
+        return self
+
+    def append(self, instruction, qargs, cargs=()):
+        if instruction.name != "measure":
+            raise AssertionError(f"unexpected instruction {instruction.name}")
+        # one measure over all of its qubits (a multi-qubit measurement)
+        self.ops.append(["measure", "measure", self._bits(list(qargs), self.qoff), [],
+                         self._bits(list(cargs), self.coff)])
+        return self
+
     def id(self, q):
         return self._one_qubit("gate", "id", q)
 
@@ -124,9 +144,20 @@ def _ctor(fn):
     return lambda *args, **kw: _ErrorSpec(fn, args, kw)
 
 
+class Instruction:
+    def __init__(self, name, num_qubits, num_clbits, params):
+        self.name, self.num_qubits, self.num_clbits, self.params = name, num_qubits, num_clbits, params
+
+
 class NoiseModel:
     def __init__(self, *args, **kw):
         self.calls = []
+
+    def add_readout_error(self, error, qubits, warnings=True):
+        self.calls.append({"call": "add_readout_error", "matrix": _plain(error), "qubits": [int(q) for q in qubits]})
+
+    def add_all_qubit_readout_error(self, error, warnings=True):
+        self.calls.append({"call": "add_all_qubit_readout_error", "matrix": _plain(error)})
 
     def add_all_qubit_quantum_error(self, error, instructions, warnings=True):
         names = [instructions] if isinstance(instructions, str) else list(instructions)
@@ -154,6 +185,7 @@ def _install_stubs():
 
     module("qiskit", QuantumRegister=QuantumRegister, ClassicalRegister=ClassicalRegister,
            QuantumCircuit=QuantumCircuit)
+    module("qiskit.circuit", Instruction=Instruction)
     errors = dict(QuantumError=_ErrorSpec, PauliError=_ctor("PauliError"))
     std = {f: _ctor(f) for f in ("pauli_error", "reset_error", "amplitude_damping_error", "depolarizing_error",
                                  "kraus_error", "thermal_relaxation_error")}
@@ -176,19 +208,19 @@ def _load(path: Path):
 
 def main(ref_dir: Path = DEFAULT_DIR):
     _install_stubs()
-    cases = []
-    for fname, stem in SETS:
+    cases, readout_cases = [], []
+    for fname, stem in SETS + READOUT_SETS:
         m = _load(ref_dir / f"{fname}.py")
         circuits = getattr(m, f"{stem}_circuits")()
         models = getattr(m, f"{stem}_noise_models")()
         counts = getattr(m, f"{stem}_counts")(SHOTS)
         # paired by position, as the reference's tests zip them
         for i, (qc, nm, ct) in enumerate(zip(circuits, models, counts)):
-            cases.append({"source": f"{fname}.py:{stem}", "index": i, "num_qubits": qc.num_qubits,
+            (readout_cases if (fname, stem) in READOUT_SETS else cases).append({"source": f"{fname}.py:{stem}", "index": i, "num_qubits": qc.num_qubits,
                           "num_clbits": qc.num_clbits, "ops": qc.ops, "noise": nm.calls,
                           "probabilities": {str(int(k, 16)): v / SHOTS for k, v in ct.items()}})
-    OUT.write_text(json.dumps({"shots": SHOTS, "cases": cases}, indent=0))
-    print(f"{len(cases)} cases -> {OUT}")
+    OUT.write_text(json.dumps({"shots": SHOTS, "cases": cases, "readout_cases": readout_cases}, indent=0))
+    print(f"{len(cases)} + {len(readout_cases)} readout cases -> {OUT}")
 
 
 if __name__ == "__main__":

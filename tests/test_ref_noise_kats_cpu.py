@@ -2,7 +2,8 @@
 (test/terra/reference/ref_pauli_noise.py, ref_reset_noise.py,
 ref_kraus_noise.py; recorded in tests/golden/ref_noise_kats.json by
 gen_ref_noise_kats.py): Pauli, reset and amplitude-damping errors on gates,
-on reset and on measure.
+on reset and on measure; readout errors on single and 2-qubit measurements
+(ref_readout_noise.py).
 
 Each noise model is rebuilt through this package's noise API, and each
 circuit is compiled by AerSimulator(method='density_matrix'): error
@@ -20,7 +21,9 @@ import pytest
 from _pkg import pkg
 from oracle import oracle as O
 
-NOISE_KATS = json.loads((Path(__file__).parent / "golden" / "ref_noise_kats.json").read_text())["cases"]
+_FIXTURE = json.loads((Path(__file__).parent / "golden" / "ref_noise_kats.json").read_text())
+NOISE_KATS = _FIXTURE["cases"]
+READOUT_KATS = _FIXTURE["readout_cases"]
 
 
 def noise_model_of(P, calls):
@@ -158,3 +161,62 @@ def test_final_measure_errors_come_after_saves():
     segments, _, _, _ = P.AerSimulator(method="density_matrix", noise_model=nm2, fusion_enable=False).compile(
         P.QuantumCircuit(2, 2).h(0).measure([0, 1], [0, 1]))
     assert [[t for t, _, _ in nc.ops()] for _, nc in segments] == [[0, 3]]
+
+
+def readout_model_of(P, calls):
+    nm = P.NoiseModel()
+    for c in calls:
+        if c["call"] == "add_readout_error":
+            nm.add_readout_error(P.ReadoutError(c["matrix"]), c["qubits"])
+        else:
+            nm.add_all_qubit_readout_error(P.ReadoutError(c["matrix"]))
+    return nm
+
+
+def ideal_memory(P, qc):
+    """Distribution of the classical memory of the ideal circuit (oracle)."""
+    sim = P.AerSimulator(method="statevector", fusion_enable=False)
+    segments, meas, _, _ = sim.compile(qc)
+    o = O.OracleQV(qc.num_qubits)
+    for _, nc in segments:
+        for i, (t, _, q) in enumerate(nc.ops()):
+            o.apply_matrix(q, nc.op_matrix(i))
+    qubits = [q for m in meas for q in m.qubits]
+    clbits = [c for m in meas for c in m.clbits]
+    out = np.zeros(1 << qc.num_clbits)
+    for idx, v in enumerate(o.probabilities(qubits)):
+        out[sum(((idx >> j) & 1) << c for j, c in enumerate(clbits))] += v
+    return out, meas
+
+
+@pytest.mark.parametrize("case", READOUT_KATS, ids=kat_id)
+def test_reference_readout_kat(case):
+    """The readout errors the simulator applies after the final measurements
+    (which errors, over which classical bits, with which matrices), composed
+    exactly over the ideal distribution, give the reference's target; the
+    per-shot draws of the sampled path converge to it (200,000 shots)."""
+    P = pkg()
+    qc = circuit_of(P, case)
+    sim = P.AerSimulator(noise_model=readout_model_of(P, case["noise"]))
+    dist, meas = ideal_memory(P, qc)
+    ro = sim._readout_ops(meas)
+    assert ro
+    exact = dist.copy()
+    for bits, probs in ro:
+        nxt = np.zeros_like(exact)
+        for m, p in enumerate(exact):
+            actual = sum(((m >> b) & 1) << j for j, b in enumerate(bits))
+            cleared = m & ~sum(1 << b for b in bits)
+            for read, q in enumerate(probs[actual]):
+                nxt[cleared | sum(((read >> j) & 1) << b for j, b in enumerate(bits))] += p * q
+        exact = nxt
+    want = np.zeros(1 << case["num_clbits"])
+    for k, v in case["probabilities"].items():
+        want[int(k)] = v
+    np.testing.assert_allclose(exact, want, atol=1e-12)
+    shots = 200_000
+    rng = np.random.default_rng(5)
+    memory = rng.choice(dist.size, size=shots, p=dist)
+    read = np.asarray(sim._readout_sampled(memory, ro, rng.random(shots * len(ro))))
+    freq = np.bincount(read, minlength=want.size) / shots
+    assert np.all(np.abs(freq - want) <= 5 * np.sqrt(want * (1 - want) / shots) + 1e-12)
