@@ -7,9 +7,10 @@ with noise models: Pauli, reset and amplitude-damping errors on gates, on
 reset and on measure.  ref_readout_noise.py does the same with readout
 errors, on single measurements and on one 2-qubit measurement.  All four
 files give the exact outcome distributions as counts of a number of shots.
+ref_reset.py adds reset circuits, noiseless, with their distributions.
 They need qiskit's circuit builder and qiskit_aer's noise module; neither
 is importable here.  This script puts recording stand-ins for both in
-sys.modules, imports the four files from the reference tree and writes,
+sys.modules, imports the five files from the reference tree and writes,
 per case: the circuit (instruction kind,
 name, qubits, parameters, classical bits), the noise model as the list of
 add_*_quantum_error calls with the error constructor and its arguments
@@ -34,6 +35,12 @@ SETS = (("ref_pauli_noise", "pauli_gate_error"), ("ref_pauli_noise", "pauli_meas
         ("ref_pauli_noise", "pauli_reset_error"), ("ref_reset_noise", "reset_gate_error"),
         ("ref_kraus_noise", "kraus_gate_error"))
 READOUT_SETS = (("ref_readout_noise", "readout_error"),)
+# ref_reset.py: (circuits function, counts function), circuits that end in
+# their only measurements (reset_circuits_repeated measures mid-circuit and is left out)
+RESET_SETS = (("reset_circuits_deterministic", "reset_counts_deterministic"),
+              ("reset_circuits_nondeterministic", "reset_counts_nondeterministic"),
+              ("reset_circuits_sampling_optimization", "reset_counts_sampling_optimization"),
+              ("reset_circuits_with_entangled_and_moving_qubits", "reset_counts_with_entangled_and_moving_qubits"))
 SHOTS = 4096
 
 
@@ -219,8 +226,16 @@ def main(ref_dir: Path = DEFAULT_DIR):
             (readout_cases if (fname, stem) in READOUT_SETS else cases).append({"source": f"{fname}.py:{stem}", "index": i, "num_qubits": qc.num_qubits,
                           "num_clbits": qc.num_clbits, "ops": qc.ops, "noise": nm.calls,
                           "probabilities": {str(int(k, 16)): v / SHOTS for k, v in ct.items()}})
-    OUT.write_text(json.dumps({"shots": SHOTS, "cases": cases, "readout_cases": readout_cases}, indent=0))
-    print(f"{len(cases)} + {len(readout_cases)} readout cases -> {OUT}")
+    reset_cases = []
+    m = _load(ref_dir / "ref_reset.py")
+    for circ_fn, count_fn in RESET_SETS:
+        for i, (qc, ct) in enumerate(zip(getattr(m, circ_fn)(), getattr(m, count_fn)(SHOTS))):
+            reset_cases.append({"source": f"ref_reset.py:{circ_fn}", "index": i, "num_qubits": qc.num_qubits,
+                                "num_clbits": qc.num_clbits, "ops": qc.ops, "noise": [],
+                                "probabilities": {str(int(k, 16)): v / SHOTS for k, v in ct.items()}})
+    OUT.write_text(json.dumps({"shots": SHOTS, "cases": cases, "readout_cases": readout_cases,
+                               "reset_cases": reset_cases}, indent=0))
+    print(f"{len(cases)} + {len(readout_cases)} readout + {len(reset_cases)} reset cases -> {OUT}")
 
 
 if __name__ == "__main__":

@@ -4,16 +4,18 @@ ref_1q_clifford.py, ref_2q_clifford.py, ref_non_clifford.py and
 ref_rotation.py): the statevector method's final state and outcome
 probabilities, and the unitary method's matrix, against the reference's
 targets including the global phase.  Noise (tests/golden/
-ref_noise_kats.json, from ref_pauli_noise.py, ref_reset_noise.py and
-ref_kraus_noise.py): the density-matrix method's sampled counts equal the
-oracle's density matrix sampled with the same uniforms, and that matrix
-gives the reference's target distribution (tests/test_ref_noise_kats_cpu.py)."""
+ref_noise_kats.json, from ref_pauli_noise.py, ref_reset_noise.py,
+ref_kraus_noise.py, and ref_reset.py's noiseless resets): the density-matrix
+method's sampled counts equal the oracle's density matrix sampled with the
+same uniforms, and that matrix gives the reference's target distribution
+(tests/test_ref_noise_kats_cpu.py)."""
 import numpy as np
 import pytest
 
 from _pkg import pkg
 from test_ref_kats_cpu import KATS, cplx
-from test_ref_noise_kats_cpu import NOISE_KATS, circuit_of as noisy_circuit_of, kat_id, noise_model_of, oracle_state
+from test_ref_noise_kats_cpu import (NOISE_KATS, RESET_KATS, circuit_of as noisy_circuit_of, kat_id, noise_model_of,
+                                     oracle_state)
 
 pytestmark = pytest.mark.gpu
 
@@ -59,7 +61,7 @@ def test_unitary_method_reference_kats():
     assert checked >= 90
 
 
-@pytest.mark.parametrize("case", NOISE_KATS, ids=kat_id)
+@pytest.mark.parametrize("case", NOISE_KATS + RESET_KATS, ids=kat_id)
 def test_density_matrix_reference_noise_kats(case):
     P = pkg()
     sim = P.AerSimulator(method="density_matrix", noise_model=noise_model_of(P, case["noise"]))

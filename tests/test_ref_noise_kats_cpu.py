@@ -3,7 +3,7 @@
 ref_kraus_noise.py; recorded in tests/golden/ref_noise_kats.json by
 gen_ref_noise_kats.py): Pauli, reset and amplitude-damping errors on gates,
 on reset and on measure; readout errors on single and 2-qubit measurements
-(ref_readout_noise.py).
+(ref_readout_noise.py); noiseless resets of entangled qubits (ref_reset.py).
 
 Each noise model is rebuilt through this package's noise API, and each
 circuit is compiled by AerSimulator(method='density_matrix'): error
@@ -24,6 +24,7 @@ from oracle import oracle as O
 _FIXTURE = json.loads((Path(__file__).parent / "golden" / "ref_noise_kats.json").read_text())
 NOISE_KATS = _FIXTURE["cases"]
 READOUT_KATS = _FIXTURE["readout_cases"]
+RESET_KATS = _FIXTURE["reset_cases"]
 
 
 def noise_model_of(P, calls):
@@ -97,7 +98,7 @@ def test_fixture_covers_gate_measure_and_reset_errors():
 
 
 @pytest.mark.parametrize("fusion", [None, 1], ids=["unfused", "fused"])
-@pytest.mark.parametrize("case", NOISE_KATS, ids=kat_id)
+@pytest.mark.parametrize("case", NOISE_KATS + RESET_KATS, ids=kat_id)
 def test_reference_noise_kat(case, fusion):
     P = pkg()
     nm = noise_model_of(P, case["noise"])
