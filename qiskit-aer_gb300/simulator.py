@@ -123,6 +123,53 @@ class AerSimulator:
                             seed_simulator=seed_simulator, autotune=autotune, autotune_cache=autotune_cache)
         self._tuner = None
 
+    # ---- options (AerBackend.set_option / set_options, aerbackend.py:623-658;
+    # AerSimulator.set_option, available_methods / available_devices,
+    # aer_simulator.py:877-935) ----
+    _DEFAULTS = dict(method="statevector", device="GPU", precision="double", noise_model=None, fusion_enable=True,
+                     fusion_max_qubit=None, fusion_threshold=None, fusion_cost_factor=1.8, fusion_avx2_costs=True,
+                     blocking_enable=True, seed_simulator=None, autotune=False, autotune_cache=None)
+
+    @property
+    def name(self) -> str:
+        return f"aer_simulator_{self.method}_gpu"
+
+    def available_methods(self) -> list:
+        return list(self.METHODS)
+
+    def available_devices(self) -> list:
+        return ["GPU"]
+
+    def set_option(self, key: str, value) -> None:
+        """Set one option; None restores its default.  Unknown keys and
+        methods, devices or precisions this engine does not have are errors
+        (the reference's AerError messages, as ValueError)."""
+        if key not in self._DEFAULTS:
+            raise ValueError(f"Invalid option {key}")
+        if value is None:
+            value = self._DEFAULTS[key]
+        if key == "method":
+            if value not in self.METHODS:
+                raise ValueError(f"Invalid simulation method {value}. Available methods are: {self.available_methods()}")
+            self.method = value
+        elif key == "device":
+            if value != "GPU":
+                raise ValueError("this engine runs on the GPU only (device='GPU')")
+        elif key == "precision":
+            if value not in ("double", "single"):
+                raise ValueError(f"Invalid precision {value}: 'double' or 'single'")
+            self.precision = value
+        elif key == "noise_model":
+            self.noise_model = value
+        else:
+            self.options[key] = value
+            if key == "autotune_cache":
+                self._tuner = None
+
+    def set_options(self, **fields) -> None:
+        for key, value in fields.items():
+            self.set_option(key, value)
+
     def tuner(self) -> Autotuner:
         """The schedule autotuner of this simulator: its own cache file when
         autotune_cache is given, else the process-wide tuner."""
