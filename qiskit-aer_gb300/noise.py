@@ -289,8 +289,23 @@ def apply_readout(memory: int, bits, probs: np.ndarray, u: float) -> int:
     return memory
 
 
+# Standard instructions of fixed size, for the error-size check of
+# NoiseModel._check_number_of_qubits (qiskit_aer/noise/noise_model.py:128-173, 1082-1107)
+_1Q_INSTRUCTIONS = frozenset(["u1", "u2", "u3", "u", "p", "r", "rx", "ry", "rz", "id", "x", "y", "z", "h", "s", "sdg",
+                              "sx", "sxdg", "t", "tdg"])
+_2Q_INSTRUCTIONS = frozenset(["swap", "cx", "cy", "cz", "csx", "cp", "cu", "cu1", "cu2", "cu3", "rxx", "ryy", "rzz",
+                              "rzx", "ecr"])
+_3Q_INSTRUCTIONS = frozenset(["ccx", "cswap"])
+# gates the simulator takes as they are: a noisy one among them joins basis_gates
+_SIMULATOR_GATES = _1Q_INSTRUCTIONS | _2Q_INSTRUCTIONS | _3Q_INSTRUCTIONS | frozenset(
+    ["ccz", "crx", "cry", "crz", "csxdg", "mcx", "mcy", "mcz", "mcp", "mcphase", "mcr", "mcrx", "mcry", "mcrz",
+     "mcu", "mcu1", "mcu2", "mcu3", "mcswap", "mcsx", "mcsxdg", "delay", "pauli", "unitary", "diagonal"])
+
+
 class NoiseModel:
-    def __init__(self):
+    def __init__(self, basis_gates=None):
+        # basis gates for compiling to the noise model (noise_model.py:193-199)
+        self._basis_gates = set(["id", "rz", "sx", "cx"] if basis_gates is None else basis_gates)
         self._all_qubit = {}   # gate name -> QuantumError
         self._local = {}       # gate name -> {qubit tuple: QuantumError}
         self._readout_default = None   # single-qubit ReadoutError for every measured qubit
@@ -334,6 +349,28 @@ class NoiseModel:
                 out.append(([int(c)], e.probabilities))
         return out
 
+    @property
+    def basis_gates(self) -> list:
+        return sorted(self._basis_gates)
+
+    def add_basis_gates(self, instructions) -> None:
+        """Add instructions to basis_gates: those the simulator takes as
+        gates (not measure, reset, kraus, superop; noise_model.py:652-667)."""
+        for name in self._names(instructions):
+            if name in _SIMULATOR_GATES:
+                self._basis_gates.add(name)
+
+    def reset(self) -> None:
+        """Remove every error and restore the default basis gates."""
+        self.__init__()
+
+    @staticmethod
+    def _check_number_of_qubits(error, name: str) -> None:
+        for size, names in ((1, _1Q_INSTRUCTIONS), (2, _2Q_INSTRUCTIONS), (3, _3Q_INSTRUCTIONS)):
+            if name in names and error.num_qubits != size:
+                raise ValueError(f"{error.num_qubits} qubit QuantumError cannot be applied to {size} qubit "
+                                 f'instruction "{name}".')
+
     def has_readout_errors(self) -> bool:
         return self._readout_default is not None or bool(self._readout_local)
 
@@ -351,8 +388,10 @@ class NoiseModel:
         if error.ideal():
             return
         for name in self._names(instructions):
+            self._check_number_of_qubits(error, name)
             old = self._all_qubit.get(name)
             self._all_qubit[name] = error if old is None else old.compose(error)
+            self.add_basis_gates(name)
 
     def add_quantum_error(self, error: QuantumError, instructions, qubits, warnings: bool = True):
         """An error on the listed instructions on exactly these qubits (in
@@ -364,9 +403,11 @@ class NoiseModel:
         if error.num_qubits != len(qubits):
             raise ValueError(f"Number of qubits ({len(qubits)}) does not match  the error size ({error.num_qubits})")
         for name in self._names(instructions):
+            self._check_number_of_qubits(error, name)
             table = self._local.setdefault(name, {})
             old = table.get(qubits)
             table[qubits] = error if old is None else old.compose(error)
+            self.add_basis_gates(name)
 
     def error_for(self, name: str, qubits=None):
         if qubits is not None:

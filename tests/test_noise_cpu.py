@@ -225,3 +225,24 @@ def test_sampled_readout_walks_samples_backwards():
             k += 1
         want.append(m)
     assert got == want
+
+
+def test_basis_gates_reset_and_error_sizes():
+    """NoiseModel.basis_gates / add_basis_gates / reset and the size check of
+    errors on standard instructions (qiskit_aer/noise/noise_model.py:193-199,
+    648-667, 1082-1107)."""
+    P = pkg()
+    nm = P.NoiseModel()
+    assert nm.basis_gates == ["cx", "id", "rz", "sx"]
+    nm.add_all_qubit_quantum_error(P.depolarizing_error(0.1, 1), ["u3", "measure"])
+    nm.add_quantum_error(P.depolarizing_error(0.1, 2), "ecr", [0, 1])
+    nm.add_quantum_error(P.depolarizing_error(0.1, 1), "my_label", [0])
+    assert nm.basis_gates == ["cx", "ecr", "id", "rz", "sx", "u3"]
+    assert nm.noise_instructions == ["ecr", "measure", "my_label", "u3"]
+    with pytest.raises(ValueError, match='1 qubit QuantumError cannot be applied to 2 qubit instruction "cx"'):
+        nm.add_all_qubit_quantum_error(P.depolarizing_error(0.1, 1), "cx")
+    with pytest.raises(ValueError, match='2 qubit QuantumError cannot be applied to 1 qubit instruction "x"'):
+        nm.add_quantum_error(P.depolarizing_error(0.1, 2), "x", [0, 1])
+    nm.reset()
+    assert nm.is_ideal() and nm.basis_gates == ["cx", "id", "rz", "sx"]
+    assert P.NoiseModel(basis_gates=["u", "cz"]).basis_gates == ["cz", "u"]
