@@ -273,6 +273,54 @@ class ReadoutError:
     def ideal(self) -> bool:
         return round(float(np.linalg.norm(self.probabilities - np.eye(self.probabilities.shape[0]))), 12) == 0
 
+    # ---- algebra, as the reference's ReadoutError (readout_error.py:156-330):
+    # rows are the actual outcome, columns the value read ----
+    def copy(self) -> "ReadoutError":
+        return ReadoutError(self.probabilities.copy())
+
+    def to_dict(self) -> dict:
+        return {"type": "roerror", "operations": ["measure"], "probabilities": self.probabilities.tolist()}
+
+    @staticmethod
+    def _other(other) -> "ReadoutError":
+        return other if isinstance(other, ReadoutError) else ReadoutError(other)
+
+    def _matmul(self, other, left_multiply: bool = False) -> "ReadoutError":
+        other = self._other(other)
+        if self.number_of_qubits != other.number_of_qubits:
+            raise ValueError("other must have same number of qubits.")
+        a, b = (other, self) if left_multiply else (self, other)
+        return ReadoutError(a.probabilities @ b.probabilities)
+
+    def compose(self, other, front: bool = False) -> "ReadoutError":
+        """other * self (the reference's order); front=True gives self * other."""
+        return self._matmul(other) if front else self._matmul(other, left_multiply=True)
+
+    def dot(self, other) -> "ReadoutError":
+        return self._matmul(other)
+
+    def power(self, n: int) -> "ReadoutError":
+        if not isinstance(n, int) or n < 1:
+            raise ValueError("Can only power with positive integer powers.")
+        ret = self.copy()
+        for _ in range(1, n):
+            ret = ret.compose(self)
+        return ret
+
+    def tensor(self, other) -> "ReadoutError":
+        """self (x) other: other acts on the lower bits of the outcome."""
+        return ReadoutError(np.kron(self.probabilities, self._other(other).probabilities))
+
+    def expand(self, other) -> "ReadoutError":
+        return ReadoutError(np.kron(self._other(other).probabilities, self.probabilities))
+
+    def __matmul__(self, other):
+        return self.compose(other)
+
+    def __eq__(self, other) -> bool:
+        return (isinstance(other, ReadoutError) and self.probabilities.shape == other.probabilities.shape
+                and np.allclose(self.probabilities, other.probabilities, atol=ATOL))
+
 
 def apply_readout(memory: int, bits, probs: np.ndarray, u: float) -> int:
     """ClassicalRegister::apply_roerror (framework/creg.hpp:230-262) on an

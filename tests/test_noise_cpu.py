@@ -246,3 +246,39 @@ def test_basis_gates_reset_and_error_sizes():
     nm.reset()
     assert nm.is_ideal() and nm.basis_gates == ["cx", "id", "rz", "sx"]
     assert P.NoiseModel(basis_gates=["u", "cz"]).basis_gates == ["cz", "u"]
+
+
+def test_readout_error_algebra():
+    """ReadoutError compose / dot / power / tensor / expand / to_dict as the
+    reference's (qiskit_aer/noise/errors/readout_error.py:156-330): compose
+    multiplies other * self, dot self * other, tensor self (x) other."""
+    P = pkg()
+    a = P.ReadoutError([[0.9, 0.1], [0.3, 0.7]])
+    b = P.ReadoutError([[0.8, 0.2], [0.4, 0.6]])
+    np.testing.assert_allclose(a.compose(b).probabilities, b.probabilities @ a.probabilities)
+    np.testing.assert_allclose(a.compose(b, front=True).probabilities, a.probabilities @ b.probabilities)
+    np.testing.assert_allclose(a.dot(b).probabilities, a.probabilities @ b.probabilities)
+    np.testing.assert_allclose((a @ b).probabilities, a.compose(b).probabilities)
+    np.testing.assert_allclose(a.power(3).probabilities, np.linalg.matrix_power(a.probabilities, 3))
+    ab = a.tensor(b)
+    assert ab.number_of_qubits == 2
+    np.testing.assert_allclose(ab.probabilities, np.kron(a.probabilities, b.probabilities))
+    np.testing.assert_allclose(a.expand(b).probabilities, np.kron(b.probabilities, a.probabilities))
+    assert a.to_dict() == {"type": "roerror", "operations": ["measure"], "probabilities": [[0.9, 0.1], [0.3, 0.7]]}
+    assert a.copy() == a and a != b
+    with pytest.raises(ValueError, match="same number of qubits"):
+        a.compose(ab)
+    with pytest.raises(ValueError, match="positive integer"):
+        a.power(0)
+    # a tensor-product error on a 2-qubit measurement acts like the two
+    # single-qubit errors: b on the first measured bit, a on the second
+    nm2, nm1 = P.NoiseModel(), P.NoiseModel()
+    nm2.add_readout_error(ab, [0, 1])
+    nm1.add_readout_error(b, [0])
+    nm1.add_readout_error(a, [1])
+    (bits, probs), = nm2.readout_ops([0, 1], [0, 1])
+    ops1 = nm1.readout_ops([0, 1], [0, 1])
+    for actual in range(4):
+        for read in range(4):
+            p1 = np.prod([ops1[j][1][(actual >> j) & 1][(read >> j) & 1] for j in range(2)])
+            assert abs(probs[actual][read] - p1) < 1e-15
