@@ -135,7 +135,7 @@ def _param(x):
 
 @dataclass
 class Instruction:
-    kind: str                      # "gate" | "unitary" | "diagonal" | "superop" | "kraus" | "reset" | "barrier" | "measure" | "save"
+    kind: str                      # "gate" | "unitary" | "diagonal" | "superop" | "kraus" | "reset" | "barrier" | "measure" | "save" | "set"
     name: str
     qubits: list
     params: list = field(default_factory=list)
@@ -256,11 +256,41 @@ class QuantumCircuit:
                 return True
             if ins.kind == "measure":
                 seen_measure = True
-            elif ins.kind not in ("save", "barrier") and seen_measure:
+            elif ins.kind not in ("save", "barrier") and seen_measure:  # a set after a measure too
                 return True
             if method == "statevector" and ins.kind in ("reset", "kraus"):
                 return True
         return False
+
+    # ---- set instructions (qiskit_aer/library/set_instructions: SetStatevector,
+    # SetDensityMatrix, SetUnitary; applied as the state's initialize_from_vector /
+    # initialize_from_matrix, statevector_state.hpp:538-540,
+    # densitymatrix_state.hpp:456-461) ----
+    def set_statevector(self, state):
+        v = np.asarray(state, dtype=complex).reshape(-1)
+        if v.size != 1 << self.num_qubits:
+            raise ValueError("The size of the statevector for the set_statevector instruction must be equal to "
+                             "the number of qubits")
+        self.data.append(Instruction("set", "statevector", list(range(self.num_qubits)), data=v))
+        return self
+
+    def set_density_matrix(self, state):
+        m = np.asarray(state, dtype=complex)
+        d = 1 << self.num_qubits
+        if m.shape != (d, d):
+            raise ValueError("The size of the density matrix for the set_density_matrix instruction must be "
+                             "equal to the number of qubits")
+        self.data.append(Instruction("set", "density_matrix", list(range(self.num_qubits)), data=m))
+        return self
+
+    def set_unitary(self, state):
+        m = np.asarray(state, dtype=complex)
+        d = 1 << self.num_qubits
+        if m.shape != (d, d):
+            raise ValueError("The size of the unitary matrix for the set_unitary instruction must be equal to "
+                             "the number of qubits")
+        self.data.append(Instruction("set", "unitary", list(range(self.num_qubits)), data=m))
+        return self
 
     def save_statevector(self, label="statevector"):
         self.data.append(Instruction("save", "statevector", [], data=label))
@@ -341,13 +371,16 @@ class QuantumCircuit:
     # ---- assembly ----
     def split_final(self):
         """Ops before the first measurement / save, the trailing measures, and
-        the saves (a sampleable circuit: measures only at the end,
-        Executor::check_measure_sampling_opt)."""
+        the saves and set instructions in circuit order, each with the
+        number of body ops before it (a sampleable circuit: measures only at
+        the end, Executor::check_measure_sampling_opt)."""
         body, meas, saves = [], [], []
         for ins in self.data:
             if ins.kind == "measure":
                 meas.append(ins)
-            elif ins.kind == "save":
+            elif ins.kind in ("save", "set"):
+                if ins.kind == "set" and meas:
+                    raise ValueError("only final measurements are supported (no mid-circuit measure)")
                 saves.append((len(body), ins))
             else:
                 if meas:

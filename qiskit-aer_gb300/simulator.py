@@ -343,7 +343,8 @@ class AerSimulator:
         body, meas, saves = circuit.split_final()
         if any(ins.kind not in ("gate", "unitary", "diagonal", "barrier") for ins in body):
             return False
-        return all(pos == len(body) and ins.name in ("expval", "statevector") for pos, ins in saves)
+        return all(pos == len(body) and ins.kind == "save" and ins.name in ("expval", "statevector")
+                   for pos, ins in saves)
 
     # largest stack of bound states held at once: 2^31 amplitudes (34 GB at complex128)
     MAX_STACK_QUBITS = 31
@@ -428,7 +429,8 @@ class AerSimulator:
             save_iter = iter(saves)
             pending = next(save_iter, None)
             for bound, nc in segments:
-                A.check(st._L.gbqv_execute(st.handle, nc.handle), st.handle)
+                if nc.num_ops():  # a save or set before any op leaves an empty segment
+                    A.check(st._L.gbqv_execute(st.handle, nc.handle), st.handle)
                 while pending is not None and pending[0] == bound:
                     self._save(st, pending[1], data)
                     pending = next(save_iter, None)
@@ -484,8 +486,8 @@ class AerSimulator:
                 stretch.clear()
 
         for ins in circuit.data:
-            if ins.kind == "save":
-                raise NotImplementedError("save instructions in a circuit run shot by shot")
+            if ins.kind in ("save", "set"):
+                raise NotImplementedError(f"{ins.kind} instructions in a circuit run shot by shot")
             if ins.kind == "kraus":
                 raise NotImplementedError("Kraus channels on a statevector need per-shot noise sampling")
             if ins.kind in ("measure", "reset"):
@@ -693,8 +695,8 @@ class AerSimulator:
                 stretch.clear()
 
         for ins in circuit.data:
-            if ins.kind == "save":
-                raise NotImplementedError("save instructions in a circuit run shot by shot")
+            if ins.kind in ("save", "set"):
+                raise NotImplementedError(f"{ins.kind} instructions in a circuit run shot by shot")
             if ins.kind == "measure":
                 flush()
                 errs = self._noise_ops("measure", ins.qubits)
@@ -825,12 +827,30 @@ class AerSimulator:
         for ins in circuit.data:
             if ins.kind in ("gate", "unitary", "diagonal", "barrier"):
                 continue
-            if ins.kind == "save" and ins.name == "unitary":
+            if ins.kind in ("save", "set") and ins.name == "unitary":
                 continue
             raise ValueError(f"QubitUnitary::State::invalid instruction '{ins.name}'.")
 
+    def _set_state(self, st, ins):
+        """A set instruction: the state becomes the given one.  The
+        density-matrix method takes a statevector as the pure state
+        |v><v| (DensityMatrix::initialize_from_vector) or a density matrix;
+        the unitary method a unitary; the statevector method a statevector."""
+        allowed = {"statevector": ("statevector",), "density_matrix": ("statevector", "density_matrix"),
+                   "unitary": ("unitary",)}[self.method]
+        if ins.name not in allowed:
+            raise ValueError(f"set_{ins.name} is not supported by the {self.method} method")
+        if ins.name == "statevector" and self.method == "density_matrix":
+            st.initialize_from_matrix(np.outer(ins.data, np.conj(ins.data)))
+        elif ins.name == "statevector":
+            st.initialize_from_vector(ins.data)
+        else:
+            st.initialize_from_matrix(ins.data)
+
     def _save(self, st, ins, data):
-        if ins.name == "unitary":
+        if ins.kind == "set":
+            self._set_state(st, ins)
+        elif ins.name == "unitary":
             data[ins.data] = st.copy_to_matrix()
         elif ins.name == "statevector":
             data[ins.data] = st.copy_to_vector()
