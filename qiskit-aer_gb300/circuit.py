@@ -292,6 +292,14 @@ class QuantumCircuit:
         self.data.append(Instruction("set", "unitary", list(range(self.num_qubits)), data=m))
         return self
 
+    def save_state(self, label=None):
+        """The method's own state (SaveState, qiskit_aer/library/save_instructions/
+        save_state.py): the statevector, density matrix or unitary, saved
+        under the method's name unless a label is given
+        (statevector_state.hpp:597-615)."""
+        self.data.append(Instruction("save", "state", [], data="_method_" if label is None else label))
+        return self
+
     def save_statevector(self, label="statevector"):
         self.data.append(Instruction("save", "statevector", [], data=label))
         return self

@@ -827,7 +827,7 @@ class AerSimulator:
         for ins in circuit.data:
             if ins.kind in ("gate", "unitary", "diagonal", "barrier"):
                 continue
-            if ins.kind in ("save", "set") and ins.name == "unitary":
+            if ins.kind in ("save", "set") and ins.name == "unitary" or ins.kind == "save" and ins.name == "state":
                 continue
             raise ValueError(f"QubitUnitary::State::invalid instruction '{ins.name}'.")
 
@@ -850,6 +850,9 @@ class AerSimulator:
     def _save(self, st, ins, data):
         if ins.kind == "set":
             self._set_state(st, ins)
+        elif ins.name == "state":
+            key = self.method if ins.data == "_method_" else ins.data
+            data[key] = st.copy_to_vector() if self.method == "statevector" else st.copy_to_matrix()
         elif ins.name == "unitary":
             data[ins.data] = st.copy_to_matrix()
         elif ins.name == "statevector":

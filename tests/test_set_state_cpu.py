@@ -82,3 +82,25 @@ def test_each_method_initialises_its_state():
     assert st.calls[0][0] == "matrix"
     with pytest.raises(ValueError, match="not supported by the unitary method"):
         sim._save(FakeState(), ins, {})
+
+
+class FakeCopies:
+    def copy_to_vector(self):
+        return "vector"
+
+    def copy_to_matrix(self):
+        return "matrix"
+
+
+def test_save_state_key_and_form_per_method():
+    """save_state saves the method's own state under the method's name
+    (statevector_state.hpp:597-615, densitymatrix_state.hpp:562), or under
+    its label."""
+    P = pkg()
+    qc = P.QuantumCircuit(1).save_state().save_state("mine")
+    for method, form in (("statevector", "vector"), ("density_matrix", "matrix"), ("unitary", "matrix")):
+        sim, data = P.AerSimulator(method=method), {}
+        for ins in qc.data:
+            sim._save(FakeCopies(), ins, data)
+        assert data == {method: form, "mine": form}
+    P.AerSimulator(method="unitary")._check_unitary_circuit(qc)
