@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import time
+import warnings
 
 import numpy as np
 
@@ -270,11 +271,31 @@ class AerSimulator:
     _want_memory = False
 
     def run(self, circuits, shots: int = 1024, seed_simulator: int | None = None, parameter_binds=None,
-            memory: bool = False, **_):
+            memory: bool = False, **run_options):
         """parameter_binds: one dict {Parameter: values} per circuit (AerBackend.run,
         qiskit_aer/backends/aerbackend.py:146-185); a parameterised circuit
         becomes one experiment per binding, in order, and experiment k of the
-        job gets seed seed_simulator + 2113 * k (controller_execute.hpp:188-210)."""
+        job gets seed seed_simulator + 2113 * k (controller_execute.hpp:188-210).
+        Other keyword options (method, noise_model, precision, fusion_*, ...)
+        override the simulator's options for this call only, as the
+        reference's run_options do; options this engine does not have are
+        ignored with a warning."""
+        unknown = sorted(k for k in run_options if k not in self._DEFAULTS)
+        if unknown:
+            warnings.warn(f"run options not used by this engine: {', '.join(unknown)}", stacklevel=2)
+        run_options = {k: v for k, v in run_options.items() if k in self._DEFAULTS}
+        if not run_options:
+            return self._run(circuits, shots, seed_simulator, parameter_binds, memory)
+        saved = {"method": self.method, "precision": self.precision, "noise_model": self.noise_model,
+                 "options": dict(self.options), "tuner": self._tuner}
+        try:
+            self.set_options(**run_options)
+            return self._run(circuits, shots, seed_simulator, parameter_binds, memory)
+        finally:
+            self.method, self.precision, self.noise_model = saved["method"], saved["precision"], saved["noise_model"]
+            self.options, self._tuner = saved["options"], saved["tuner"]
+
+    def _run(self, circuits, shots, seed_simulator, parameter_binds, memory):
         self._want_memory = bool(memory)
         single = isinstance(circuits, QuantumCircuit)
         if single:

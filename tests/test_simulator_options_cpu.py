@@ -49,3 +49,37 @@ def test_autotune_cache_option_replaces_the_tuner(tmp_path):
     first = sim.tuner()
     sim.set_options(autotune_cache=str(tmp_path / "t.json"))
     assert sim.tuner() is not first and sim.tuner().path == str(tmp_path / "t.json")
+
+
+def test_run_options_apply_to_one_call_only():
+    """Keyword options of run() override the simulator's options for that
+    call (AerBackend.run's run_options, aerbackend.py:146-185) and are
+    restored afterwards, also when the run fails; unknown ones are ignored
+    with a warning."""
+    P = pkg()
+    sim = P.AerSimulator()
+    nm = P.NoiseModel()
+    seen = []
+
+    def fake_run(circuits, shots, seed, binds, memory):
+        seen.append((sim.method, sim.precision, sim.noise_model, sim.options["fusion_threshold"], shots))
+        if shots == 13:
+            raise RuntimeError("boom")
+        return "result"
+
+    sim._run = fake_run
+    qc = P.QuantumCircuit(1)
+    assert sim.run(qc, shots=7, method="density_matrix", precision="single", noise_model=nm,
+                   fusion_threshold=2) == "result"
+    assert seen[-1] == ("density_matrix", "single", nm, 2, 7)
+    assert (sim.method, sim.precision, sim.noise_model, sim.options["fusion_threshold"]) == (
+        "statevector", "double", None, None)
+    with pytest.raises(RuntimeError):
+        sim.run(qc, shots=13, method="unitary")
+    assert sim.method == "statevector"
+    with pytest.warns(UserWarning, match="blocking_qubits"):
+        sim.run(qc, shots=1, blocking_qubits=20)
+    assert seen[-1][0] == "statevector"
+    with pytest.raises(ValueError, match="Invalid simulation method"):
+        sim.run(qc, method="mps")
+    assert sim.method == "statevector"
