@@ -20,8 +20,16 @@ same circuit under ``variants``.
            traffic = DRAM bytes per launch from an ncu capture of the same
            kernel on a 26-qubit state, scaled by 16 (traffic grows with the
            state)
+  parity   after the timed region: |0> through the fused circuit and back
+           through every op's inverse at the full size (max amplitude error,
+           reduced on the GPU), and the same circuit family at 26 qubits
+           against the complex128 oracle applying every unfused SU(4)
   cpu_baseline  the oracle (C restatement of Aer's QubitVector + OpenMP) on
-           the host cores, over a bounded sample of the same fused ops
+           the host cores, a bounded sample of the same fused ops applied to
+           the same 2^30-amplitude complex128 state in host memory
+  variants the complex64 run of the same circuit; the adjoint gradient of the
+           26-qubit, 624-parameter ansatz (complex128 and complex64) against
+           parameter shift on the same GPU; the 14-qubit noisy density matrix
 
 Other workloads (--workload): ``adjoint`` (26-qubit hardware-efficient
 ansatz, 624 parameters, 200 Pauli terms: adjoint gradient vs parameter
@@ -37,7 +45,9 @@ resets: 4,096 shots, each running the circuit, stacked as states).
 
 ``--impl reference`` times the reference's CPU algorithm on the same
 workload (the oracle port: the reference's own build exists only where its
-sources do, not on the GPU host), all host threads, bounded per step.
+sources do, not on the GPU host), all host threads, bounded per step: the
+same 30-qubit complex128 state in host memory and the same fused ops, read
+from the file build() writes, so that the arm maps no engine library.
 States of 2^26 amplitudes and more exceed L2 (129 MB), so no flush is needed.
 """
 from __future__ import annotations
@@ -146,30 +156,34 @@ class Timer:
         self.ms = self.e0.elapsed_time(self.e1)
 
 
-def cpu_baseline(fused_ops, n_small, budget_s=12.0):
-    """Oracle (C restatement of Aer's QubitVector, OpenMP on all host cores) on
-    a bounded sample: the workload's fused ops on a 2^n_small complex128 state."""
+def oracle_sample(fused_ops, n, budget_s=12.0, max_ops=None):
+    """The oracle (C restatement of Aer's QubitVector::apply_matrix, OpenMP on
+    every host core) applying the workload's fused ops, in order, to a
+    2^n-amplitude complex128 state on the host: a bounded sample (one untimed
+    op first touches the state's pages).  Returns (GB/s, ops, seconds, threads)."""
     from oracle import oracle as O
 
     O.build()
     threads = os.cpu_count() or 1
     O.set_threads(threads, 14)
-    o = O.OracleQV(n_small)
+    o = O.OracleQV(n)
+    o.apply_matrix(*fused_ops[0])
     t0 = time.perf_counter()
     done = 0
-    for q, m in fused_ops:
-        qq = [x % n_small for x in q]
-        if len(set(qq)) != len(qq):
-            continue
-        o.apply_matrix(qq, m)
+    while time.perf_counter() - t0 < budget_s and (max_ops is None or done < max_ops):
+        q, m = fused_ops[(1 + done) % len(fused_ops)]
+        o.apply_matrix(q, m)
         done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
     dt = time.perf_counter() - t0
-    gbs = done * 2 * (1 << n_small) * 16 / dt / 1e9
+    del o
+    return done * 2 * (1 << n) * 16 / dt / 1e9, done, dt, threads
+
+
+def cpu_baseline(fused_ops, n, budget_s=12.0):
+    gbs, done, dt, threads = oracle_sample(fused_ops, n, budget_s)
     return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": f"{done} fused ops of the workload on a {n_small}-qubit complex128 state "
-                      f"({(1 << n_small) * 16 / 1e9:.2f} GB), {dt:.1f} s wall, OpenMP {threads} threads"}
+            "sample": f"{done} fused ops of the workload on the {n}-qubit complex128 state "
+                      f"({(1 << n) * 16 / 1e9:.2f} GB in host memory), {dt:.1f} s wall, OpenMP {threads} threads"}
 
 
 def fused_ops_of(P, args):
@@ -179,24 +193,148 @@ def fused_ops_of(P, args):
     return qc, nc, [(q, nc.op_matrix(i)) for i, (_, _, q) in enumerate(nc.ops())]
 
 
+def qv_config(args, nops):
+    """The workload description both arms print (identical by construction)."""
+    return {"workload": f"QV {args.qubits}q x {args.layers} layers (Haar SU(4) per pair), Aer fusion max 5",
+            "qubits": args.qubits, "layers": args.layers, "seed": args.seed, "fused_ops": nops,
+            "l2": "state larger than L2, no flush" if (16 << args.qubits) > 129e6 else "state fits L2, no flush"}
+
+
+def ops_file(qubits, layers, seed):
+    return ROOT / "_build" / "bench_ops" / f"qv_{qubits}q_{layers}l_seed{seed}_fused.npz"
+
+
+def export_fused_ops(P=None, qubits=30, layers=30, seed=2024):
+    """Writes the fused op list of the QV workload (Aer's Fusion, max 5 qubits)
+    to a numpy file, so that the reference arm reads its input with numpy
+    alone and never maps the engine's library."""
+    P = P or entry.load_package()
+    args = argparse.Namespace(qubits=qubits, layers=layers, seed=seed, precision="double")
+    _, _, fused = fused_ops_of(P, args)
+    path = ops_file(qubits, layers, seed)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    np.savez(str(path) + ".tmp.npz", k=np.array([len(q) for q, _ in fused], dtype=np.int32),
+             qubits=np.concatenate([np.asarray(q, dtype=np.uint64) for q, _ in fused]),
+             mats=np.concatenate([np.asarray(m, dtype=np.complex128).reshape(-1) for _, m in fused]))
+    os.replace(str(path) + ".tmp.npz", path)
+    return path
+
+
+def load_fused_ops(path):
+    d = np.load(path)
+    out, qo, mo = [], 0, 0
+    for k in d["k"]:
+        k = int(k)
+        dim = 1 << k
+        out.append(([int(x) for x in d["qubits"][qo:qo + k]], d["mats"][mo:mo + dim * dim].reshape(dim, dim)))
+        qo += k
+        mo += dim * dim
+    return out
+
+
 def run_reference_arm(args):
+    """The reference's CPU algorithm (the oracle port of QubitVector::apply_matrix,
+    every host thread) on the same 30-qubit state and the same fused ops, read
+    from the file build() writes; each step a bounded sample of the circuit's
+    ops (--ref-ops-per-step, continuing through the list)."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
-    P = entry.load_package()
-    _, _, fused = fused_ops_of(P, args)
-    n_small = min(args.qubits, 26)
+    path = ops_file(args.qubits, args.layers, args.seed)
+    if not path.exists():
+        # the fused list is written by build(); make it in a child process so
+        # this process maps no engine library
+        subprocess.run([sys.executable, "-c", "import bench; bench.export_fused_ops("
+                        f"qubits={args.qubits}, layers={args.layers}, seed={args.seed})"], cwd=ROOT, check=True)
+    fused = load_fused_ops(path)
+    from oracle import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads, 14)
+    n = args.qubits
+    o = O.OracleQV(n)
+    pos = [0]
+
+    def step():
+        for _ in range(args.ref_ops_per_step):
+            q, m = fused[pos[0] % len(fused)]
+            o.apply_matrix(q, m)
+            pos[0] += 1
+
     for _ in range(args.warmup):
-        cpu_baseline(fused[:2], n_small, budget_s=2.0)
-    vals = [cpu_baseline(fused, n_small, budget_s=8.0) for _ in range(args.steps)]
-    v = float(np.median([x["value"] for x in vals]))
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    nops = args.steps * args.ref_ops_per_step
+    v = round(nops * 2 * (1 << n) * 16 / dt / 1e9, 3)
     print(json.dumps({
         "metric": "fused-gate GB/s", "value": v, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "dtype": "c128", "data": "synthetic",
-        "config": {"workload": f"QV {args.qubits}q x {args.layers} layers, Aer fusion max 5",
-                   "qubits": args.qubits, "layers": args.layers},
-        "cpu_baseline": {**vals[-1], "value": v},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": qv_config(args, len(fused)),
+        "cpu_baseline": {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.ref_ops_per_step} fused ops per step of the workload's {len(fused)}, "
+                                   f"applied in circuit order to the {n}-qubit complex128 state "
+                                   f"({(1 << n) * 16 / 1e9:.1f} GB in host memory), {nops} ops timed in "
+                                   f"{dt:.1f} s, OpenMP {threads} threads"},
         "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+class _DeviceArray:
+    """A device buffer the engine owns, described to torch without a copy."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def roundtrip_err(torch, P, st, nc, fused):
+    """Full-size check: |0> through the fused circuit and then through the
+    inverse of every fused op (U^dagger, in reverse order) must return to |0>;
+    max |amplitude - delta_0| over the 2^n amplitudes, reduced on the GPU."""
+    L = P.lib()
+    st.initialize()
+    A_check(L, L.gbqv_execute(st.handle, nc.handle), st)
+    for q, m in reversed(fused):
+        st.apply_matrix(q, np.conj(np.asarray(m)).T)
+    st.synchronize()
+    typestr = "<c16" if st.precision == "double" else "<c8"
+    t = torch.as_tensor(_DeviceArray(st.device_pointer(), 1 << st.num_qubits(), typestr), device="cuda")
+    err = max(abs(complex(t[0].item()) - 1.0), float(t[1:].abs().max().item()))
+    del t
+    torch.cuda.empty_cache()
+    return err
+
+
+_ORACLE_STATES = {}
+
+
+def err_vs_oracle(P, args, n):
+    """The QV family at n qubits (same layers and seed) through the engine
+    (fused, the headline's kernels), against the oracle applying every unfused
+    SU(4) in complex128: max |amplitude difference|."""
+    from oracle import oracle as O
+
+    qc = qv_circuit(P, n, args.layers, args.seed)
+    key = (n, args.layers, args.seed)
+    if key not in _ORACLE_STATES:
+        O.build()
+        O.set_threads(os.cpu_count() or 1, 14)
+        o = O.OracleQV(n)
+        for ins in qc.data:
+            o.apply_matrix(ins.qubits, ins.data)
+        _ORACLE_STATES[key] = o.data.copy()
+        del o
+    segs, _, _, _ = P.AerSimulator(precision=args.precision).compile(qc)
+    L = P.lib()
+    st = P.QubitVector(n, args.precision)
+    st.initialize()
+    A_check(L, L.gbqv_execute(st.handle, segs[0][1].handle), st)
+    sv = st.copy_to_vector()
+    st.close()
+    return float(np.max(np.abs(sv - _ORACLE_STATES[key])))
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from
@@ -302,30 +440,75 @@ def bench_qv(args, torch, P):
                "breakdown_ms": {k: round(float(v) * 1e3, 2) for k, v in
                                 zip(("fusion", "upload", "execute", "readback"), parts)}}
         del psi0, psi0_t
+    # parity at the full size (inverse round trip, on the device) and against
+    # the oracle at the largest size it finishes in seconds
+    checks = None
+    if not args.no_checks:
+        checks = {"roundtrip_max_abs_err": roundtrip_err(torch, P, st, nc, fused),
+                  "roundtrip": f"|0> through the {nops} fused ops and their inverses at {args.qubits} qubits, "
+                               "max |amp - delta_0| over every amplitude"}
     st.close()
+    if not args.no_checks:
+        n_or = min(args.qubits, args.oracle_qubits)
+        checks["err_vs_oracle"] = err_vs_oracle(P, args, n_or)
+        checks["oracle"] = (f"QV {n_or}q x {args.layers} layers (seed {args.seed}) through the engine, "
+                            "max |amp - oracle| against the complex128 oracle applying every unfused SU(4)")
     base = None
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
-        base = cpu_baseline(fused, min(args.qubits, 26))
+        base = cpu_baseline(fused, args.qubits)
     variants = None
     if args.precision == "double" and not args.no_variants:
         v64 = argparse.Namespace(**{**vars(args), "precision": "single", "no_cpu_baseline": True,
                                     "no_variants": True, "steps": max(2, args.steps), "warmup": 3})
         r = bench_qv(v64, torch, P)
-        variants = {"c64": {k: r[k] for k in ("value", "unit", "ms_per_step", "gpu_launches", "roofline", "e2e")}}
+        variants = {"c64": {k: r[k] for k in ("value", "unit", "ms_per_step", "gpu_launches", "roofline", "e2e",
+                                              "parity")}}
+        for prec in ("double", "single"):
+            va = argparse.Namespace(**{**vars(args), "precision": prec, "qubits": 26, "steps": 2, "warmup": 1})
+            r = bench_adjoint(va, torch, P)
+            variants["adjoint_" + ("c128" if prec == "double" else "c64")] = {
+                k: r[k] for k in ("value", "unit", "adjoint_s", "param_shift_s_extrapolated", "param_shift_measured",
+                                  "rel_err_vs_param_shift", "energy_err_vs_oracle", "config")}
+        vd = argparse.Namespace(**{**vars(args), "precision": "double", "steps": 3, "warmup": 1})
+        r = bench_dm(vd, torch, P)
+        variants["dm14_c128"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "fused_ops",
+                                                   "expval_50_terms_ms", "config")}
     return {"metric": "fused-gate GB/s", "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
-            "config": {"workload": f"QV {args.qubits}q x {args.layers} layers (Haar SU(4) per pair), Aer fusion max 5",
-                       "qubits": args.qubits, "layers": args.layers, "fused_ops": nops,
-                       "l2": "state larger than L2, no flush", "blocking": not args.no_blocking},
+            "config": qv_config(args, nops), "engine": {"blocking": not args.no_blocking},
             "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clk,
-            "variants": variants}
+            "parity": checks, "variants": variants}
 
 
 def A_check(L, rc, st):
     if rc != 0:
         raise RuntimeError(L.gbqv_last_error(st.handle).decode())
+
+
+_ORACLE_ENERGY = {}
+
+
+def oracle_energy(ans, theta, ham, key):
+    """<H> of the ansatz state from the complex128 oracle (every gate applied
+    one by one, then each Pauli term's expectation value)."""
+    if key not in _ORACLE_ENERGY:
+        from oracle import oracle as O
+
+        O.build()
+        O.set_threads(os.cpu_count() or 1, 14)
+        o = O.OracleQV(ans.num_qubits)
+        axis = {"rx": 0, "ry": 1, "rz": 2}
+        for ins in ans.instructions(theta):
+            if ins.name in axis:
+                o.apply_rotation(ins.qubits, axis[ins.name], ins.params[0])
+            elif ins.name == "cx":
+                o.apply_mcx(ins.qubits)
+            else:
+                raise ValueError(f"oracle_energy: gate {ins.name} is not in the ansatz family")
+        _ORACLE_ENERGY[key] = sum(c * o.expval_pauli(q, lab) for (q, lab), c in zip(ham.terms, ham.coeffs))
+    return _ORACLE_ENERGY[key]
 
 
 def bench_adjoint(args, torch, P):
@@ -356,12 +539,15 @@ def bench_adjoint(args, torch, P):
     ps_v = np.array([ps[i] for i in idx])
     rel = float(np.linalg.norm(g[idx] - ps_v) / np.linalg.norm(ps_v))
     eng.close()
+    e_err = None
+    if not args.no_checks:
+        e_err = abs(e - oracle_energy(ans, theta, ham, (n, args.seed)))
     return {"metric": "adjoint-grad time vs param-shift", "value": round(t_ps / t_adj, 2), "unit": "x faster",
             "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
             "adjoint_s": round(t_adj, 4), "param_shift_s_extrapolated": round(t_ps, 2),
             "param_shift_measured": f"{len(idx)} params x 2 evaluations in {t_ps_sub:.2f} s",
-            "rel_err_vs_param_shift": rel, "energy": e,
+            "rel_err_vs_param_shift": rel, "energy": e, "energy_err_vs_oracle": e_err,
             "config": {"workload": f"HEA {n}q x {layers} layers, {ans.num_params} params, 200 Pauli terms",
                        "qubits": n}, "clocks": clk}
 
@@ -737,7 +923,13 @@ def main():
     ap.add_argument("--no-blocking", action="store_true")
     ap.add_argument("--autotune", action="store_true",
                     help="batch workload: pick the two-CTA team split by timing the candidates first")
-    ap.add_argument("--no-variants", action="store_true", help="skip the complex64 run of the default workload")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the complex64, adjoint and density-matrix runs of the default workload")
+    ap.add_argument("--no-checks", action="store_true", help="skip the parity checks of the default workload")
+    ap.add_argument("--oracle-qubits", type=int, default=26,
+                    help="state size of the default workload's comparison with the oracle")
+    ap.add_argument("--ref-ops-per-step", type=int, default=2,
+                    help="reference arm: fused ops of the 30-qubit circuit applied per step")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)

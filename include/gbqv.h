@@ -214,8 +214,10 @@ int gbqv_expval_pauli_many(gbqv_handle h, int nterms, const uint64_t *qubits,
  * default stream) and the call returns once out / *total are written.  More
  * than 64 terms is GBQV_ERR_ARG.  The first call on a device looks up the
  * array's address (cudaGetSymbolAddress) with that device current: make it
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU race; serialise them. */
+ * before any stream capture.  The address is kept for the life of the
+ * process; after a reset of the device (cudaDeviceReset) do not call this
+ * entry point on that device again.  offsets[0] must be 0.  All calls share
+ * the array: calls whose work overlaps on the GPU race; serialise them. */
 int gbqv_expval_pauli_many_noalloc(const void *state, int num_qubits, int precision, int nterms,
                                    const uint64_t *qubits, const int *offsets, const char *const *labels,
                                    const double *coeffs, void *stream, double *out, double *total);

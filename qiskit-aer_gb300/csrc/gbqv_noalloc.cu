@@ -115,7 +115,11 @@ std::mutex g_noalloc_mu;
 double *g_noalloc_ptr[64] = {nullptr};
 
 // Device address of the static array on the current device (resolved once
-// per device, with that device current).
+// per device, with that device current).  The address is cached for the
+// life of the process: after cudaDeviceReset (or any reset of the device's
+// primary context) the module is loaded again and the array may move, so a
+// process that resets a device must not call the allocation-free entry point
+// on that device afterwards.
 double *noalloc_scratch() {
   int dev = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -148,6 +152,7 @@ extern "C" int gbqv_expval_pauli_many_noalloc(const void *state, int num_qubits,
                                     std::to_string(kNoAllocDoubles * sizeof(double)) + " bytes); got " +
                                     std::to_string(nterms));
     if (!offsets || !labels) throw Error(GBQV_ERR_ARG, "null term arrays");
+    if (offsets[0] != 0) throw Error(GBQV_ERR_ARG, "bad term offsets: offsets[0] must be 0");
     NoAllocTerms terms{};
     for (int t = 0; t < nterms; ++t) {
       const int k = offsets[t + 1] - offsets[t];

@@ -1,6 +1,6 @@
 """Batched uneven instances in one persistent launch (gbqv_batch_*): per
-instance <H> and the adjoint gradient against the single-instance adjoint
-engine, and the sampled shots bit-exact against the oracle for the same
+instance <H> against the oracle and the single-instance adjoint engine, the
+adjoint gradient against the single-instance engine, and the sampled shots bit-exact against the oracle for the same
 RngEngine seed.  Instances span 3..13 qubits so that some fit one tile and
 some need several tiles per run."""
 import numpy as np
@@ -19,6 +19,21 @@ def _engine_ansatz(adj, inst):
         q = [q0, q1] if k in (3, 4) else [q0]
         gates.append((kinds[k], q, p if p >= 0 else None, None))
     return adj.Ansatz(inst["n"], gates)
+
+
+def _oracle_state(inst):
+    """The instance's ansatz applied gate by gate by the oracle (complex128)."""
+    o = O.OracleQV(inst["n"])
+    for k, q0, q1, p in inst["gates"]:
+        if k in (0, 1, 2):
+            o.apply_rotation([q0], k, inst["theta"][p])
+        elif k == 3:
+            o.apply_mcx([q0, q1])
+        elif k == 4:
+            o.apply_mcphase([q0, q1], -1.0)
+        elif k == 5:
+            o.apply_mcu([q0], O.u4(np.pi / 2, 0, np.pi, 0))
+    return o
 
 
 @pytest.mark.parametrize("precision,tol,gtol", [("double", 1e-11, 1e-9), ("single", 2e-4, 2e-3)])
@@ -41,15 +56,10 @@ def test_batch_matches_single_instance_engine(precision, tol, gtol):
         assert abs(e - e_ref) < tol * max(1, abs(e_ref)), (i, e, e_ref)
         np.testing.assert_allclose(g, g_ref, atol=gtol)
         assert lat > 0
+        o = _oracle_state(inst)
+        e_or = sum(c * o.expval_pauli(q, lab) for (q, lab), c in zip(inst["terms"], inst["coeffs"]))
+        assert abs(e - e_or) < tol * max(1, abs(e_or)), (i, e, e_or)
         if precision == "double":
-            o = O.OracleQV(inst["n"])
-            for k, q0, q1, p in inst["gates"]:
-                if k == 1:
-                    o.apply_rotation([q0], 1, inst["theta"][p])
-                elif k == 2:
-                    o.apply_rotation([q0], 2, inst["theta"][p])
-                elif k == 3:
-                    o.apply_mcx([q0, q1])
             want = o.sample_measure(O.uniforms(inst["seed"], inst["shots"]))
             np.testing.assert_array_equal(s, want)
     # a second run replays the captured graph and gives the same results

@@ -4,8 +4,8 @@ allocator owns the GPU's memory, or a loop that must not pay cudaMalloc's
 synchronisation).  Its partial sums live in a static __device__ array
 instead of cudaMalloc'd scratch.  Checked against gbqv_expval_pauli_many on
 the same state, on two calls in a row with different terms (the array keeps
-the previous call's contents), within the tolerance of the other expval
-tests.  This file sorts last so a failure here comes after every other test.
+the previous call's contents), and against the oracle's expval_pauli, within
+the tolerance of the other expval tests.  This file sorts last so a failure here comes after every other test.
 """
 import ctypes as C
 
@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 from _pkg import pkg
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -26,7 +27,7 @@ def _terms(rng, n, count):
     return out
 
 
-def _noalloc(qv, terms, coeffs, precision):
+def _noalloc(qv, terms, coeffs, precision, offset_shift=0):
     P = pkg()
     L = P.lib()
     qs, offs, labels = [], [0], []
@@ -34,6 +35,7 @@ def _noalloc(qv, terms, coeffs, precision):
         qs.extend(q)
         offs.append(len(qs))
         labels.append(lab.encode())
+    offs = [o + offset_shift for o in offs]
     qa = np.ascontiguousarray(np.asarray(qs, dtype=np.uint64))
     oa = (C.c_int * len(offs))(*offs)
     la = (C.c_char_p * len(labels))(*labels)
@@ -65,6 +67,9 @@ def test_noalloc_matches_expval_many_twice(precision, tol):
             want, want_total = qv.expval_pauli_many(terms, coeffs)
             np.testing.assert_allclose(got, want, atol=tol, rtol=0)
             assert abs(got_total - want_total) < tol * 10
+            # and directly against the oracle's expval_pauli on the same state
+            o = O.OracleQV(n, data=psi)
+            np.testing.assert_allclose(got, [o.expval_pauli(q, lab) for q, lab in terms], atol=tol, rtol=0)
 
 
 def test_noalloc_rejects_too_many_terms():
@@ -75,3 +80,15 @@ def test_noalloc_rejects_too_many_terms():
         with pytest.raises(P.GBQVError) as e:
             _noalloc(qv, _terms(rng, 8, 65), np.ones(65), "double")
         assert e.value.code == 1 and "terms per call" in str(e.value)
+
+
+def test_noalloc_rejects_nonzero_first_offset():
+    """offsets[0] must be 0: a negative start would read before the caller's
+    qubit array."""
+    P = pkg()
+    rng = np.random.default_rng(2)
+    with P.QubitVector(8) as qv:
+        qv.initialize()
+        with pytest.raises(P.GBQVError) as e:
+            _noalloc(qv, _terms(rng, 8, 3), np.ones(3), "double", offset_shift=-1)
+        assert e.value.code == 1 and "offsets[0]" in str(e.value)
