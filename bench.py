@@ -226,7 +226,9 @@ def load_fused_ops(path):
     for k in d["k"]:
         k = int(k)
         dim = 1 << k
-        out.append(([int(x) for x in d["qubits"][qo:qo + k]], d["mats"][mo:mo + dim * dim].reshape(dim, dim)))
+        # stored as the engine's column-major vector; the 2-D matrix is U itself
+        out.append(([int(x) for x in d["qubits"][qo:qo + k]],
+                     d["mats"][mo:mo + dim * dim].reshape(dim, dim, order="F")))
         qo += k
         mo += dim * dim
     return out
@@ -298,7 +300,9 @@ def roundtrip_err(torch, P, st, nc, fused):
     st.initialize()
     A_check(L, L.gbqv_execute(st.handle, nc.handle), st)
     for q, m in reversed(fused):
-        st.apply_matrix(q, np.conj(np.asarray(m)).T)
+        dim = 1 << len(q)
+        u = np.asarray(m).reshape(dim, dim, order="F") if np.ndim(m) == 1 else np.asarray(m)
+        st.apply_matrix(q, u.conj().T)
     st.synchronize()
     typestr = "<c16" if st.precision == "double" else "<c8"
     t = torch.as_tensor(_DeviceArray(st.device_pointer(), 1 << st.num_qubits(), typestr), device="cuda")

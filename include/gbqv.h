@@ -145,7 +145,7 @@ int gbqv_inner_product(gbqv_handle h, gbqv_c128 *out);
 /* ------------------------------------------------------------------ */
 
 /* QubitVector::apply_matrix (qubitvector.hpp:1298-1303, transformer.hpp:89-232):
- * dense 2^k x 2^k column-major matrix, 1 <= k <= 10. */
+ * dense 2^k x 2^k column-major matrix, 1 <= k <= 13. */
 int gbqv_apply_matrix(gbqv_handle h, const uint64_t *qubits, int k, const gbqv_c128 *mat);
 /* QubitVector::apply_diagonal_matrix (qubitvector.hpp:1342-1347,
  * transformer.hpp:234-372): diag has 2^k entries, 1 <= k <= 20. */
@@ -181,12 +181,19 @@ int gbqv_apply_multi_swaps(gbqv_handle h, const uint64_t *qubits, int nq);
 /* QubitVector::norm (qubitvector.hpp:1878-1886); for a density matrix this is
  * the squared Frobenius norm of the stored vector, as in the reference. */
 int gbqv_norm(gbqv_handle h, double *out);
-/* QubitVector::norm(qubits, mat) (qubitvector.hpp:1888-2082): ||M psi||^2. */
+/* QubitVector::norm(qubits, mat) (qubitvector.hpp:1888-2082): ||M psi||^2,
+ * 1 <= k <= 13; the state is left as it is. */
 int gbqv_norm_matrix(gbqv_handle h, const uint64_t *qubits, int k, const gbqv_c128 *mat, double *out);
 /* QubitVector::probabilities() / probabilities(qubits)
  * (qubitvector.hpp:2089-2143); DensityMatrix uses the diagonal
- * (densitymatrix.hpp:516-520).  k == 0 means all qubits (out has 2^n). */
+ * (densitymatrix.hpp:516-520).  k == 0 means all qubits (out has 2^n);
+ * otherwise out has 2^k entries for any 1 <= k <= n, outcome bit j = qubit
+ * qubits[j]. */
 int gbqv_probabilities(gbqv_handle h, const uint64_t *qubits, int k, double *out);
+/* QubitVector::probability(outcome) (qubitvector.hpp:302, |psi_k|^2) and
+ * DensityMatrix::probability (densitymatrix.hpp:530-534, Re rho[k, k]):
+ * reads the one entry back. */
+int gbqv_probability(gbqv_handle h, uint64_t outcome, double *out);
 /* QubitVector::sample_measure (qubitvector.hpp:2148-2228): for each uniform
  * r in [0,1) the first basis index whose cumulative probability exceeds r. */
 int gbqv_sample_measure(gbqv_handle h, const double *rnds, uint64_t shots, uint64_t *out);

@@ -6,11 +6,25 @@
 // Statevector::State<statevec_t> / DensityMatrix::State<densmat_t>
 // (statevector_state.hpp:100-101); errors surface as std::runtime_error /
 // std::invalid_argument like the reference's.  Only the types Aer already
-// uses appear here (std::vector, std::complex, std::string).
+// uses appear here (std::vector, std::complex, std::string, std::map);
+// members whose arguments are Aer's own types (Operations::Op, RngEngine,
+// AER::Vector) are templates, so the header compiles on its own and accepts
+// Aer's types unchanged.
+//
+// Besides the gates and reductions, the class carries every configuration
+// and chunk hook that the States and executors call on their register
+// (qubitvector.hpp:100-170, 420-462; qubitvector_thrust.hpp:57-560).  The
+// engine is one state on one GPU: OpenMP, chunk and batching knobs are kept
+// and reported back (the CPU QubitVector also ignores most of them), a
+// multi-chunk set-up is refused, and batched-shot hooks report "no batch"
+// (enable_batch() is false), so Aer's executors take their per-state path;
+// batched work goes through gbqv_execute_bound / gbqv_execute_segments.
 #pragma once
 
 #include <complex>
 #include <cstdint>
+#include <cstdio>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -42,7 +56,11 @@ class QubitVector {
   explicit QubitVector(size_t num_qubits) { set_num_qubits(num_qubits); }
   QubitVector(const QubitVector &) = delete;
   QubitVector &operator=(const QubitVector &) = delete;
-  QubitVector(QubitVector &&o) noexcept : h_(std::exchange(o.h_, nullptr)), n_(o.n_) {}
+  QubitVector(QubitVector &&o) noexcept
+      : h_(std::exchange(o.h_, nullptr)), n_(o.n_), omp_threads_(o.omp_threads_), omp_threshold_(o.omp_threshold_),
+        chunk_index_(o.chunk_index_), json_chop_threshold_(o.json_chop_threshold_),
+        sample_index_size_(o.sample_index_size_), max_matrix_bits_(o.max_matrix_bits_),
+        max_sampling_shots_(o.max_sampling_shots_), target_gpus_(std::move(o.target_gpus_)) {}
   ~QubitVector() { gbqv_destroy(h_); }
 
   static std::string name() {
@@ -140,6 +158,120 @@ class QubitVector {
     return v;
   }
 
+  // QubitVector::probability(outcome) (qubitvector.hpp:302); DensityMatrix:
+  // the diagonal entry (densitymatrix.hpp:530-534)
+  double probability(uint_t outcome) const {
+    double v;
+    check(gbqv_probability(h_, outcome, &v), h_);
+    return v;
+  }
+  // QubitVector::norm_diagonal (qubitvector.hpp:388-393): ||D psi||^2
+  double norm_diagonal(uint_t qubit, const cvector_t &diag) const { return norm_diagonal(reg_t{qubit}, diag); }
+  double norm_diagonal(const reg_t &q, const cvector_t &diag) const {
+    const size_t D = 1ULL << q.size();
+    if (diag.size() != D) throw std::invalid_argument("norm_diagonal: diagonal length must be 2^k");
+    cvector_t mat(D * D, 0.0);
+    for (size_t j = 0; j < D; ++j) mat[j + D * j] = diag[j];
+    return norm(q, mat);
+  }
+
+  // ---- state set-up (qubitvector.hpp:143-145, 195-206, 856-899) ----
+  // initialize_component: the qubits were reset to |0>; amplitude j of each
+  // group becomes state[j] times the group's |0> amplitude, i.e. the matrix
+  // whose first column is `state` and whose other columns are zero.
+  void initialize_component(const reg_t &q, const cvector_t &state) {
+    const size_t D = 1ULL << q.size();
+    if (state.size() != D) throw std::invalid_argument("initialize_component: state length must be 2^k");
+    cvector_t mat(D * D, 0.0);
+    for (size_t j = 0; j < D; ++j) mat[j] = state[j];
+    apply_matrix(q, mat);
+  }
+  template <typename T>
+  void initialize_from_data(const std::complex<T> *data, size_t num_states) {
+    if (num_states != size()) throw std::runtime_error("initialize_from_data: length does not match the state");
+    cvector_t v(data, data + num_states);
+    initialize_from_vector(v);
+  }
+  // AER::Vector (data(), size()) or std::vector of std::complex<T>, consumed
+  template <class Vec>
+  void move_from_vector(Vec &&vec) { initialize_from_data(vec.data(), vec.size()); }
+  cvector_t vector() const { return copy_to_vector(); }
+  // Utils::vec2ket(data, size, epsilon, 16): entries whose chopped magnitude
+  // exceeds epsilon, keyed by the basis index in "0x" lowercase hex
+  std::map<std::string, complex_t> vector_ket(double epsilon = 0) const {
+    const cvector_t v = copy_to_vector();
+    std::map<std::string, complex_t> out;
+    auto chop = [epsilon](double x) { return std::abs(x) < epsilon ? 0.0 : x; };
+    for (size_t k = 0; k < v.size(); ++k) {
+      const complex_t z{chop(v[k].real()), chop(v[k].imag())};
+      if (std::abs(z) > epsilon) {
+        char key[24];
+        std::snprintf(key, sizeof key, "0x%llx", (unsigned long long)k);
+        out.emplace(key, z);
+      }
+    }
+    return out;
+  }
+  // Statevector::State::required_memory_mb (qubitvector.hpp:110): the state
+  // itself; per-handle scratch grows on demand
+  size_t required_memory_mb(uint_t num_qubits) const {
+    const uint_t vq = Kind == GBQV_STATEVECTOR ? num_qubits : 2 * num_qubits;
+    return (size_t)((sizeof(std::complex<data_t>) << vq) >> 20);
+  }
+  void synchronize() { check(gbqv_synchronize(h_), h_); }
+
+  // ---- configuration hooks (qubitvector.hpp:147-170, 420-462) ----
+  void set_omp_threads(int n) {
+    if (n > 0) omp_threads_ = (uint_t)n;
+  }
+  uint_t get_omp_threads() { return omp_threads_; }
+  void set_omp_threshold(int n) {
+    if (n > 0) omp_threshold_ = (uint_t)n;
+  }
+  uint_t get_omp_threshold() { return omp_threshold_; }
+  void set_json_chop_threshold(double t) { json_chop_threshold_ = t; }
+  double get_json_chop_threshold() { return json_chop_threshold_; }
+  void set_sample_measure_index_size(int n) { sample_index_size_ = n; }
+  int get_sample_measure_index_size() { return sample_index_size_; }
+  void set_max_matrix_bits(int64_t bits) { max_matrix_bits_ = bits; }
+  void set_max_sampling_shots(int64_t shots) { max_sampling_shots_ = shots; }
+  void set_num_threads_per_group(int) {}
+  // cuStateVec is not used by this engine (qubitvector_thrust.hpp:90)
+  void cuStateVec_enable(bool flg) {
+    if (flg) throw std::invalid_argument("cuStateVec is not available in the GB300 engine");
+  }
+  // the engine runs on the current CUDA device; the list is kept
+  void set_target_gpus(reg_t &t) { target_gpus_ = t; }
+  const reg_t &target_gpus() const { return target_gpus_; }
+
+  // ---- chunk and batch hooks (qubitvector.hpp:147-170, 322-362) ----
+  uint_t chunk_setup(int chunk_bits, int num_qubits, uint_t chunk_index, uint_t num_local_chunks) {
+    if (chunk_bits != num_qubits)
+      throw std::runtime_error("the GB300 engine holds the whole state on one GPU: no multi-chunk set-up");
+    chunk_index_ = chunk_index;
+    return num_local_chunks;
+  }
+  uint_t chunk_setup(QubitVector &, const uint_t chunk_index) {
+    chunk_index_ = chunk_index;
+    return 0;
+  }
+  uint_t chunk_index() { return chunk_index_; }
+  bool top_of_group() { return true; }
+  bool fetch_chunk() const { return true; }
+  void release_chunk(bool = true) const {}
+  void enter_register_blocking(const reg_t &) {}
+  void leave_register_blocking() {}
+  bool support_global_indexing() { return false; }
+  bool enable_batch(bool) const { return false; }
+  bool batched_optimization_supported() { return false; }
+  template <class... Args>
+  void initialize_creg(Args &&...) {}
+  template <class Op>
+  void apply_bfunc(const Op &) {}
+  void set_conditional(int64_t) {}
+  template <class Op, class Rngs>
+  void apply_roerror(const Op &, Rngs &) {}
+
   // ---- density matrix (densitymatrix.hpp:265-542) ----
   void apply_superop_matrix(const reg_t &q, const cvector_t &mat) {
     check(gbqv_dm_apply_superop_matrix(h_, q.data(), (int)q.size(), c(mat)), h_);
@@ -166,6 +298,11 @@ class QubitVector {
  private:
   gbqv_handle h_ = nullptr;
   size_t n_ = 0;
+  uint_t omp_threads_ = 1, omp_threshold_ = 14, chunk_index_ = 0;
+  double json_chop_threshold_ = 0;
+  int sample_index_size_ = 10;
+  int64_t max_matrix_bits_ = 0, max_sampling_shots_ = 0;
+  reg_t target_gpus_;
 };
 
 template <typename data_t = double>

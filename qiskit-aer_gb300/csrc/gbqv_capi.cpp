@@ -174,7 +174,7 @@ void apply_matrix_impl(Device &dev, const reg_t &q, const cd *mat) {
       return;
     }
   }
-  REQUIRE((int)q.size() <= kMaxDenseK, GBQV_ERR_ARG, "apply_matrix supports at most 10 qubits");
+  REQUIRE((int)q.size() <= kMaxDenseK, GBQV_ERR_ARG, "apply_matrix supports at most 13 qubits");
   if (tensor_dense_available(dev, (int)q.size())) {
     launch_dense_tensor(dev, q, mat);
     return;
@@ -615,7 +615,7 @@ extern "C" int gbqv_apply_multiplexer(gbqv_handle h, const uint64_t *controls, i
     reg_t all(targets, targets + nt);
     all.insert(all.end(), controls, controls + nc);
     reg_t q = check_qubits(all.data(), nt + nc, h->dev.n, "apply_multiplexer");
-    REQUIRE(nt >= 1 && nt + nc <= kMaxDenseK, GBQV_ERR_ARG, "apply_multiplexer supports at most 10 qubits");
+    REQUIRE(nt >= 1 && nt + nc <= kMaxDenseK, GBQV_ERR_ARG, "apply_multiplexer supports at most 13 qubits");
     // Block-diagonal expansion of the stacked matrix (qubitvector.hpp:1316-1331):
     // full[i + b*cols, j + b*cols] = mat[i + b*cols + DIM*j].
     const uint64_t DIM = 1ULL << (nt + nc), cols = 1ULL << nt, blocks = 1ULL << nc;
@@ -652,7 +652,7 @@ extern "C" int gbqv_norm_matrix(gbqv_handle h, const uint64_t *qubits, int k, co
   return guard(h, [&] {
     need_handle(h);
     reg_t q = check_qubits(qubits, k, h->dev.n, "norm");
-    REQUIRE(k <= kMaxDenseParamK, GBQV_ERR_ARG, "norm(qubits, mat) supports at most 5 qubits");
+    REQUIRE(k <= kMaxDenseK, GBQV_ERR_ARG, "norm(qubits, mat) supports at most 13 qubits");
     reduce_norm_matrix(h->dev, q, as_cd(mat));
     read_results(h->dev, out, 1);
   });
@@ -676,6 +676,36 @@ extern "C" int gbqv_probabilities(gbqv_handle h, const uint64_t *qubits, int k, 
     reg_t q = check_qubits(qubits, k, limit, "probabilities");
     reduce_probabilities(d, q);
     read_results(d, out, 1ULL << k);
+  });
+}
+
+extern "C" int gbqv_probability(gbqv_handle h, uint64_t outcome, double *out) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    REQUIRE(out, GBQV_ERR_ARG, "null output");
+    const int limit = d.density ? d.nq : d.n;
+    REQUIRE(limit >= 64 || outcome < (1ULL << limit), GBQV_ERR_QUBIT, "outcome out of range");
+    // the amplitude (or diagonal entry rho[k, k] of vec(rho)) is read back alone
+    const uint64_t idx = d.density ? outcome * ((1ULL << d.nq) + 1) : outcome;
+    const size_t amp = d.dbl ? 16 : 8;
+    unsigned char buf[16] = {0};
+    cuda_check(cudaMemcpyAsync(buf, static_cast<const unsigned char *>(d.state) + idx * amp, amp,
+                               cudaMemcpyDeviceToHost, d.stream),
+               "probability copy");
+    sync(d);
+    double re, im;
+    if (d.dbl) {
+      std::memcpy(&re, buf, 8);
+      std::memcpy(&im, buf + 8, 8);
+    } else {
+      float r, i;
+      std::memcpy(&r, buf, 4);
+      std::memcpy(&i, buf + 4, 4);
+      re = r;
+      im = i;
+    }
+    *out = d.density ? re : re * re + im * im;
   });
 }
 
@@ -881,7 +911,7 @@ extern "C" int gbqv_dm_apply_superop_matrix(gbqv_handle h, const uint64_t *qubit
     need_handle(h);
     require_density(h->dev, "apply_superop_matrix");
     reg_t q = check_qubits(qubits, k, h->dev.nq, "apply_superop_matrix");
-    REQUIRE(2 * k <= kMaxDenseK && mat, GBQV_ERR_ARG, "apply_superop_matrix supports at most 5 qubits");
+    REQUIRE(2 * k <= 10 && mat, GBQV_ERR_ARG, "apply_superop_matrix supports at most 5 qubits");
     apply_matrix_impl(h->dev, superop_qubits(h->dev, q), as_cd(mat));
   });
 }
@@ -902,7 +932,7 @@ namespace gbqv {
 void dm_unitary(Device &d, const reg_t &q, const cd *mat) {
   const size_t k = q.size(), dim = 1ULL << k;
   if (k > 4) {
-    REQUIRE(k <= (size_t)kMaxDenseK, GBQV_ERR_ARG, "apply_unitary_matrix supports at most 10 qubits");
+    REQUIRE(k <= (size_t)kMaxDenseK, GBQV_ERR_ARG, "apply_unitary_matrix supports at most 13 qubits");
     apply_matrix_impl(d, q, mat);
     std::vector<cd> c(mat, mat + dim * dim);
     for (auto &z : c) z = std::conj(z);
@@ -1012,7 +1042,7 @@ extern "C" int gbqv_dm_apply_reset(gbqv_handle h, const uint64_t *qubits, int k)
     need_handle(h);
     require_density(h->dev, "apply_reset");
     reg_t q = check_qubits(qubits, k, h->dev.nq, "apply_reset");
-    REQUIRE(2 * k <= kMaxDenseK, GBQV_ERR_ARG, "apply_reset supports at most 5 qubits");
+    REQUIRE(2 * k <= 10, GBQV_ERR_ARG, "apply_reset supports at most 5 qubits");
     apply_matrix_impl(h->dev, superop_qubits(h->dev, q), gates::reset_superop(k).data());
   });
 }

@@ -695,7 +695,7 @@ extern "C" int gbqv_circuit_superop(gbqv_circuit_t c, const uint64_t *qubits, in
     op.type = GBQV_OP_SUPEROP;
     op.name = "superop";
     op.qubits = check_q(c, qubits, k);
-    REQUIRE(mat && 2 * k <= kMaxDenseK, GBQV_ERR_ARG, "bad superoperator");
+    REQUIRE(mat && 2 * k <= 10, GBQV_ERR_ARG, "bad superoperator");
     const cd *m = reinterpret_cast<const cd *>(mat);
     op.mat.assign(m, m + (1ULL << (4 * k)));
     c->ops.push_back(std::move(op));
@@ -709,7 +709,7 @@ extern "C" int gbqv_circuit_kraus(gbqv_circuit_t c, const uint64_t *qubits, int 
     op.type = GBQV_OP_KRAUS;
     op.name = "kraus";
     op.qubits = check_q(c, qubits, k);
-    REQUIRE(mats && nk >= 1 && 2 * k <= kMaxDenseK, GBQV_ERR_ARG, "bad Kraus set");
+    REQUIRE(mats && nk >= 1 && 2 * k <= 10, GBQV_ERR_ARG, "bad Kraus set");
     const cd *m = reinterpret_cast<const cd *>(mats);
     const size_t sz = 1ULL << (2 * k);
     for (int i = 0; i < nk; ++i) op.kraus.emplace_back(m + i * sz, m + (i + 1) * sz);

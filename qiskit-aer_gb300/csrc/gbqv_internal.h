@@ -31,7 +31,7 @@ uint64_t launch_count();
 // Limits of the kernels.
 constexpr int kMaxQubits = 40;         // 2^40 c64 = 8 TB: capped by memory anyway
 constexpr int kMaxDenseParamK = 5;     // dense k <= 5: matrix passed as kernel parameter
-constexpr int kMaxDenseK = 10;         // dense k <= 10: matrix in device memory
+constexpr int kMaxDenseK = 13;         // dense k <= 13: matrix in device memory, group in smem
 constexpr int kMaxDiagK = 10;          // diagonal entries passed as kernel parameter
 constexpr int kMaxPermPairs = 1024;
 constexpr int kReduceBlocks = 152 * 4; // 4 CTAs per SM on a GB300

@@ -169,17 +169,21 @@ __global__ void __launch_bounds__(256) k_dense(T *__restrict__ psi, const __grid
   }
 }
 
-// Dense k-qubit matrix, 6 <= k <= 10: one CTA per group, the group staged in
-// shared memory, the matrix read from device memory (L2 resident); thread r
-// computes output row r.  MatrixMultNxN (chunk/thrust_kernels.hpp:900-933).
-template <typename T>
+// Dense k-qubit matrix, 6 <= k <= 13: one CTA per group, the group staged in
+// shared memory, the matrix read from device memory (L2 resident up to
+// k = 11 at complex128); thread r computes output rows r, r + blockDim.x, ...
+// MatrixMultNxN (chunk/thrust_kernels.hpp:900-933).  NORM: ||M psi||^2
+// (QubitVector::norm(qubits, mat), qubitvector.hpp:1878-2082) into one FP64
+// partial per CTA, the state left as it is.
+template <typename T, bool NORM>
 __global__ void k_dense_big(T *__restrict__ psi, const T *__restrict__ mat, int k, uint64_t ngroups,
-                            const uint64_t *__restrict__ meta) {
+                            const uint64_t *__restrict__ meta, double *__restrict__ partials) {
   extern __shared__ unsigned char smem_raw[];
   T *cache = reinterpret_cast<T *>(smem_raw);
   const int D = 1 << k;
   const uint64_t *offs = meta;
   const uint64_t *lowmask = meta + D;
+  double nacc = 0.0;
   for (uint64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
     const uint64_t base = insert_zeros(g, lowmask, k);
     for (int a = threadIdx.x; a < D; a += blockDim.x) cache[a] = psi[base + offs[a]];
@@ -189,9 +193,23 @@ __global__ void k_dense_big(T *__restrict__ psi, const T *__restrict__ mat, int 
       acc.x = 0;
       acc.y = 0;
       for (int c = 0; c < D; ++c) cfma(acc, mat[r + (uint64_t)D * c], cache[c]);
-      psi[base + offs[r]] = acc;
+      if (NORM)
+        nacc += (double)acc.x * (double)acc.x + (double)acc.y * (double)acc.y;
+      else
+        psi[base + offs[r]] = acc;
     }
     __syncthreads();
+  }
+  if (NORM) {
+    for (int o = 16; o > 0; o >>= 1) nacc += __shfl_xor_sync(0xffffffffu, nacc, o);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nacc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    }
   }
 }
 
@@ -225,8 +243,10 @@ void dense_any(Device &dev, const reg_t &qubits, const cd *mat, bool norm) {
     case 5: return dense_small<T, 5>(dev, qubits, mat, norm);
     default: break;
   }
-  if (norm) throw Error(1, "norm(qubits, mat) supports at most 5 qubits");
   const int D = 1 << k;
+  const size_t smem = sizeof(T) * (size_t)D;
+  if (k > kMaxDenseK || smem > 227 * 1024)
+    throw Error(1, "dense matrix supports at most " + std::to_string(kMaxDenseK) + " qubits");
   // matrix + offsets + masks in one device buffer
   const size_t mat_bytes = sizeof(T) * (size_t)D * D;
   const size_t meta_bytes = sizeof(uint64_t) * (D + k);
@@ -243,10 +263,20 @@ void dense_any(Device &dev, const reg_t &qubits, const cd *mat, bool norm) {
   // only once the source has been consumed, so hm/meta may go out of scope.
   const uint64_t ngroups = dev.amps() >> k;
   const int threads = std::min(D, 1024);
-  const int grid = (int)std::min<uint64_t>(ngroups, 152ULL * 16);
-  k_dense_big<T><<<grid, threads, sizeof(T) * D, dev.stream>>>(reinterpret_cast<T *>(dev.state),
-                                                                 reinterpret_cast<const T *>(dev.mat), k, ngroups,
-                                                                 d_meta);
+  // norm: one partial per CTA, at most kReduceBlocks of them
+  const int grid = (int)std::min<uint64_t>(ngroups, norm ? (uint64_t)kReduceBlocks : 152ULL * 16);
+  auto kern = norm ? k_dense_big<T, true> : k_dense_big<T, false>;
+  if (smem > 48 * 1024)
+    cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "dense matrix kernel attribute");
+  kern<<<grid, threads, smem, dev.stream>>>(reinterpret_cast<T *>(dev.state), reinterpret_cast<const T *>(dev.mat), k,
+                                            ngroups, d_meta, dev.partials);
+  if (norm) {
+    // partials past the last CTA are zero for finish()'s fixed block count
+    if (grid < kReduceBlocks)
+      cuda_check(cudaMemsetAsync(dev.partials + grid, 0, sizeof(double) * (kReduceBlocks - grid), dev.stream),
+                 "norm partials");
+  }
   check_launch("dense matrix kernel (k > 5)");
 }
 
@@ -792,6 +822,52 @@ __global__ void __launch_bounds__(256) k_probs(const T *__restrict__ psi, const 
   }
 }
 
+// Marginals over more than 10 qubits (probabilities(qubits),
+// qubitvector.hpp:2106-2143, any k): one thread per outcome v and slice of
+// the groups; outcome bit j sits at amplitude bit q[j], the group index
+// fills the other bits in ascending order.  Slice s of outcome v sums groups
+// s, s + bps, ... and writes partials[v * bps + s]; a second kernel adds the
+// slices in order (deterministic).
+struct ProbWide {
+  uint8_t q[kMaxQubits];     // outcome bit j -> amplitude bit q[j]
+  uint8_t free[kMaxQubits];  // group bit i -> amplitude bit free[i]
+  int k, nfree;
+  uint64_t diag_stride;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_probs_wide(const T *__restrict__ psi, const __grid_constant__ ProbWide w,
+                                                    int bps, double *__restrict__ partials) {
+  const uint64_t D = 1ULL << w.k;
+  const uint64_t v = (uint64_t)(blockIdx.x / bps) * blockDim.x + threadIdx.x;
+  const uint32_t slice = blockIdx.x % bps;
+  if (v >= D) return;
+  uint64_t off = 0;
+  for (int j = 0; j < w.k; ++j) off |= ((v >> j) & 1ULL) << w.q[j];
+  const uint64_t ngroups = 1ULL << w.nfree;
+  double acc = 0.0;
+  for (uint64_t g = slice; g < ngroups; g += bps) {
+    uint64_t idx = off;
+    for (int i = 0; i < w.nfree; ++i) idx |= ((g >> i) & 1ULL) << w.free[i];
+    if (w.diag_stride) {
+      acc += (double)psi[idx * w.diag_stride].x;
+    } else {
+      const T a = psi[idx];
+      acc += (double)(a.x * a.x + a.y * a.y);
+    }
+  }
+  partials[v * bps + slice] = acc;
+}
+
+__global__ void k_probs_wide_sum(const double *__restrict__ partials, int bps, uint64_t nvalues,
+                                 double *__restrict__ out) {
+  const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvalues) return;
+  double s = 0.0;
+  for (int b = 0; b < bps; ++b) s += partials[v * bps + b];
+  out[v] = s;
+}
+
 template <typename T>
 __global__ void k_probs_all(const T *__restrict__ psi, uint64_t count, uint64_t diag_stride, double *__restrict__ out) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -1127,9 +1203,47 @@ void reduce_dm_trace(Device &dev) {
   finish(dev, 2);
 }
 
+// Marginals over k > 10 qubits into dev.results (2^k doubles).
+void reduce_probabilities_wide(Device &dev, const reg_t &qubits) {
+  const int k = (int)qubits.size();
+  const int nbits = sample_bits(dev);
+  ProbWide w{};
+  w.k = k;
+  uint64_t used = 0;
+  for (int j = 0; j < k; ++j) {
+    w.q[j] = (uint8_t)qubits[j];
+    used |= 1ULL << qubits[j];
+  }
+  w.nfree = 0;
+  for (int b = 0; b < nbits; ++b)
+    if (!(used >> b & 1)) w.free[w.nfree++] = (uint8_t)b;
+  w.diag_stride = diag_stride(dev);
+  const uint64_t D = 1ULL << k, chunks = (D + 255) / 256;
+  // slices: split the groups while the launch has fewer than ~8 CTAs per SM
+  const uint64_t want = std::max<uint64_t>(1, (uint64_t)sm_count() * 8 / chunks);
+  const int bps = (int)std::min<uint64_t>(std::min<uint64_t>(want, 1ULL << w.nfree), 64);
+  if (chunks * bps > 0x7fffffffULL) throw Error(1, "marginal probabilities: too many outcomes");
+  grow(reinterpret_cast<void *&>(dev.results), dev.results_cap, sizeof(double) * D);
+  double *dst = dev.results;
+  if (bps > 1) {
+    grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * D * bps);
+    dst = dev.partials;
+  }
+  if (dev.dbl)
+    k_probs_wide<double2><<<(unsigned)(chunks * bps), 256, 0, dev.stream>>>(st<double2>(dev), w, bps, dst);
+  else
+    k_probs_wide<float2><<<(unsigned)(chunks * bps), 256, 0, dev.stream>>>(st<float2>(dev), w, bps, dst);
+  check_launch("probabilities kernel");
+  if (bps > 1) {
+    k_probs_wide_sum<<<(unsigned)chunks, 256, 0, dev.stream>>>(dev.partials, bps, D, dev.results);
+    check_launch("probabilities sum");
+  }
+}
+
 void reduce_probabilities(Device &dev, const reg_t &qubits) {
   const int k = (int)qubits.size();
-  if (k < 1 || k > 10) throw Error(1, "marginal probabilities support 1..10 qubits");
+  if (k > 10) return reduce_probabilities_wide(dev, qubits);
+  if (k < 1) throw Error(1, "marginal probabilities over no qubits: use the full distribution");
   const int D = 1 << k;
   ensure_partials(dev, D);
   auto p = std::make_unique<ProbParams>();

@@ -204,7 +204,10 @@ class QubitVector:
         return out
 
     def probability(self, outcome: int) -> float:
-        return float(self.probabilities()[outcome])
+        """QubitVector::probability (qubitvector.hpp:302): the one entry read back."""
+        v = C.c_double()
+        self._c(self._L.gbqv_probability(self._h, int(outcome), C.byref(v)))
+        return v.value
 
     def sample_measure(self, rnds) -> np.ndarray:
         r = np.ascontiguousarray(np.asarray(rnds, dtype=np.float64).reshape(-1))
