@@ -195,8 +195,16 @@ int gbqv_probabilities(gbqv_handle h, const uint64_t *qubits, int k, double *out
  * reads the one entry back. */
 int gbqv_probability(gbqv_handle h, uint64_t outcome, double *out);
 /* QubitVector::sample_measure (qubitvector.hpp:2148-2228): for each uniform
- * r in [0,1) the first basis index whose cumulative probability exceeds r. */
+ * r in [0,1) the first basis index whose cumulative probability exceeds r,
+ * with the cumulative sums formed in the reference's order (sequential sums
+ * over 2^index_size blocks, then a sequential walk inside the block), so
+ * that a uniform on a boundary resolves as in the reference.  A uniform at
+ * or above the total of all block sums gives 2^n, as the reference's walk. */
 int gbqv_sample_measure(gbqv_handle h, const double *rnds, uint64_t shots, uint64_t *out);
+/* QubitVector::set_sample_measure_index_size (qubitvector.hpp:457): the
+ * block count 2^index_size of the sampling walk (default 10, the
+ * statevector_sample_measure_opt option). */
+int gbqv_set_sample_measure_index_size(gbqv_handle h, int index_size);
 /* QubitVector::expval_pauli (qubitvector.hpp:2299-2347) and
  * DensityMatrix::expval_pauli (densitymatrix.hpp:445-496). */
 int gbqv_expval_pauli(gbqv_handle h, const uint64_t *qubits, int nq, const char *label,

@@ -231,7 +231,10 @@ class QubitVector {
   uint_t get_omp_threshold() { return omp_threshold_; }
   void set_json_chop_threshold(double t) { json_chop_threshold_ = t; }
   double get_json_chop_threshold() { return json_chop_threshold_; }
-  void set_sample_measure_index_size(int n) { sample_index_size_ = n; }
+  void set_sample_measure_index_size(int n) {
+    check(gbqv_set_sample_measure_index_size(h_, n), h_);
+    sample_index_size_ = n;
+  }
   int get_sample_measure_index_size() { return sample_index_size_; }
   void set_max_matrix_bits(int64_t bits) { max_matrix_bits_ = bits; }
   void set_max_sampling_shots(int64_t shots) { max_sampling_shots_ = shots; }

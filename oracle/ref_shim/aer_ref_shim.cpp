@@ -84,6 +84,12 @@ void ref_qv_sample_measure(void *h, const double *rnds, uint64_t shots, uint64_t
   reg_t s = qv->sample_measure(std::vector<double>(rnds, rnds + shots));
   for (uint64_t i = 0; i < shots; ++i) out[i] = s[i];
 }
+void ref_qv_set_sample_index_size(void *h, int n) {
+  static_cast<QV::QubitVector<double> *>(h)->set_sample_measure_index_size(n);
+}
+void ref_dm_set_sample_index_size(void *h, int n) {
+  static_cast<QV::DensityMatrix<double> *>(h)->set_sample_measure_index_size(n);
+}
 void ref_qv_checkpoint(void *h) { static_cast<QV::QubitVector<double> *>(h)->checkpoint(); }
 void ref_qv_inner_product(void *h, double *re, double *im) {
   cd z = static_cast<QV::QubitVector<double> *>(h)->inner_product();

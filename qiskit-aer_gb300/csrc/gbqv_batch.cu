@@ -299,77 +299,60 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
     // ---------------- runs: forward (dir = 0) and backward (dir = 1) ----------------
     for (int dir = 0; dir < 2; ++dir) {
       if (dir == 1) {
-        // sampling on the final state, before the sweep uncomputes it
-        const int bb = min(I.n, kSampleBits);
-        const uint64_t nb = N >> bb;
-        double *cdf = reinterpret_cast<double *>(lam);  // lam is free until H psi
-        const uint64_t wbase = (uint64_t)member * (blockDim.x >> 5) + (threadIdx.x >> 5);
-        const uint64_t wstride = (uint64_t)(blockDim.x >> 5) * TM;  // warp stride over the team
-        for (uint64_t b = wbase; b < nb; b += wstride) {
-          double sacc = 0.0;
-          for (uint64_t j = threadIdx.x & 31; j < (1ULL << bb); j += 32) {
-            const T a = psi[(b << bb) + j];
-            if constexpr (sizeof(T) == 8)
-              sacc += (double)(a.x * a.x + a.y * a.y);
-            else
-              sacc += (double)a.x * a.x + (double)a.y * a.y;
+        // sampling on the final state, before the sweep uncomputes it, in
+        // the reference's order of operations (QubitVector::sample_measure,
+        // qubitvector.hpp:2148-2228): sequential block totals over 2^10
+        // blocks, their running prefix P, then per shot the block with
+        // r < P[j + 1] and the walk p = P[j] + prob(k) ... until r < p; the
+        // probabilities as std::real(z * conj(z)), no contraction
+        auto prob = [&](uint64_t k) -> double {
+          const T a = psi[k];
+          if constexpr (sizeof(T) == 8)
+            return (double)__fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y));
+          else
+            return __dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y));
+        };
+        const bool blocks = I.n >= kSampleBits;
+        const uint64_t nb = blocks ? 1ULL << kSampleBits : 0, L = blocks ? N >> kSampleBits : 0;
+        double *cdf = reinterpret_cast<double *>(lam);  // P[j + 1] at cdf[j]; lam is free until H psi
+        if (blocks) {
+          for (uint64_t j = tbase; j < nb; j += tstride) {
+            double sacc = 0.0;
+            for (uint64_t t = 0; t < L; ++t) sacc = __dadd_rn(sacc, prob(j * L + t));
+            cdf[j] = sacc;
           }
-          for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
-          if ((threadIdx.x & 31) == 0) cdf[b] = sacc;
-        }
-        if (!team_sync()) return;
-        if (threadIdx.x == 0 && member == 0)
-          for (uint64_t b = 1; b < nb; ++b) cdf[b] += cdf[b - 1];
-        if (!team_sync()) return;
-        const int lane = threadIdx.x & 31;
-        for (uint64_t sh = wbase; sh < I.shots; sh += wstride) {
-          const double r = rnds[I.rnd_off + sh];
-          uint64_t lo = 0, hi = nb;
-          while (lo < hi) {
-            const uint64_t mid = (lo + hi) >> 1;
-            if (r < cdf[mid]) hi = mid; else lo = mid + 1;
-          }
-          uint64_t res = N - 1;
-          if (lo < nb) {
-            double p = lo ? cdf[lo - 1] : 0.0;
-            float rem = (float)(r - p);  // complex64: the block's remaining mass, walked in float
-            const uint64_t b0 = lo << bb;
-            bool found = false;
-            for (uint64_t j0 = 0; j0 < (1ULL << bb) && !found; j0 += 32) {
-              unsigned msk;
-              if constexpr (sizeof(T) == 8) {
-                // complex64: the 32 probabilities and their prefix sums in
-                // float, compared with the block's remaining mass (converted
-                // once per shot; the FP64 pipe is narrow)
-                float v = 0.0f;
-                if (j0 + lane < (1ULL << bb)) {
-                  const T a = psi[b0 + j0 + lane];
-                  v = a.x * a.x + a.y * a.y;
-                }
-                for (int o = 1; o < 32; o <<= 1) {
-                  const float u = __shfl_up_sync(0xffffffffu, v, o);
-                  if (lane >= o) v += u;
-                }
-                msk = __ballot_sync(0xffffffffu, (j0 + lane < (1ULL << bb)) && (rem < v));
-                rem -= __shfl_sync(0xffffffffu, v, 31);
-              } else {
-                double v = 0.0;
-                if (j0 + lane < (1ULL << bb)) {
-                  const T a = psi[b0 + j0 + lane];
-                  v = (double)a.x * a.x + (double)a.y * a.y;
-                }
-                for (int o = 1; o < 32; o <<= 1) {
-                  const double u = __shfl_up_sync(0xffffffffu, v, o);
-                  if (lane >= o) v += u;
-                }
-                msk = __ballot_sync(0xffffffffu, (j0 + lane < (1ULL << bb)) && (r < p + v));
-                p += __shfl_sync(0xffffffffu, v, 31);
-              }
-              if (msk) { res = b0 + j0 + (__ffs(msk) - 1); found = true; }
+          if (!team_sync()) return;
+          if (threadIdx.x == 0 && member == 0) {
+            double run = 0.0;
+            for (uint64_t j = 0; j < nb; ++j) {
+              run = __dadd_rn(run, cdf[j]);
+              cdf[j] = run;
             }
-            if (!found) res = b0 + (1ULL << bb) - 1;
           }
-          if (lane == 0) samples[I.smp_off + sh] = res;
+          if (!team_sync()) return;
+        }
+        for (uint64_t sh = tbase; sh < I.shots; sh += tstride) {
+          const double r = rnds[I.rnd_off + sh];
+          double p = 0.0;
+          uint64_t k = 0;
+          if (blocks) {
+            uint64_t lo = 0, hi = nb;
+            while (lo < hi) {
+              const uint64_t mid = (lo + hi) >> 1;
+              if (r < cdf[mid]) hi = mid; else lo = mid + 1;
+            }
+            if (lo == nb) {  // at or above the total: the reference's walk ends at 2^n
+              samples[I.smp_off + sh] = N;
+              continue;
+            }
+            p = lo ? cdf[lo - 1] : 0.0;
+            k = lo * L;
+          }
+          for (; k < N - 1; ++k) {
+            p = __dadd_rn(p, prob(k));
+            if (r < p) break;
+          }
+          samples[I.smp_off + sh] = k;
         }
         if (!team_sync()) return;  // the CDF (in lambda's space) is read until here
         // lambda = H psi and <H> = Re <psi|lambda>: lambda in the data

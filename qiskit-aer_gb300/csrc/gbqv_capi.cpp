@@ -709,6 +709,14 @@ extern "C" int gbqv_probability(gbqv_handle h, uint64_t outcome, double *out) {
   });
 }
 
+extern "C" int gbqv_set_sample_measure_index_size(gbqv_handle h, int index_size) {
+  return guard(h, [&] {
+    need_handle(h);
+    REQUIRE(index_size >= 1 && index_size <= 24, GBQV_ERR_ARG, "sample_measure index size must be 1..24");
+    h->dev.sample_index_size = index_size;
+  });
+}
+
 extern "C" int gbqv_sample_measure(gbqv_handle h, const double *rnds, uint64_t shots, uint64_t *out) {
   return guard(h, [&] {
     need_handle(h);

@@ -36,7 +36,6 @@ constexpr int kMaxDiagK = 10;          // diagonal entries passed as kernel para
 constexpr int kMaxPermPairs = 1024;
 constexpr int kReduceBlocks = 152 * 4; // 4 CTAs per SM on a GB300
 constexpr int kReduceThreads = 256;
-constexpr int kSampleBlockBits = 10;   // sub-block of the sampling prefix sums
 constexpr int kMaxTerms = 4096;        // Pauli terms per reduction launch
 
 // Per-handle device state.  Scratch buffers grow on demand and live until
@@ -49,6 +48,7 @@ struct Device {
   bool unitary = false;     // UnitaryMatrix: 2 nq vector qubits, identity at initialisation
   int blocking = 1;         // 0 one kernel per op, 1 register-tile runs, 2 shared-memory runs
   int tensor_c128 = 1;      // complex128 dense k = 4, 5: 0 FP64 cores, 1 tensor (tcgen05 for k = 4), 2 mma.sync only
+  int sample_index_size = 10;  // QubitVector::sample_measure_index_size_ (2^this blocks)
   int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up
   // tcgen05 kernel: 128-byte-swizzled TMA descriptors of the state viewed as
   // rows of 8 amplitudes, box height 2^(L-3) for run length L = 7..11; built

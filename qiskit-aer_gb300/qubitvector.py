@@ -209,6 +209,10 @@ class QubitVector:
         self._c(self._L.gbqv_probability(self._h, int(outcome), C.byref(v)))
         return v.value
 
+    def set_sample_measure_index_size(self, index_size: int) -> None:
+        """QubitVector::set_sample_measure_index_size (qubitvector.hpp:457)."""
+        self._c(self._L.gbqv_set_sample_measure_index_size(self._h, int(index_size)))
+
     def sample_measure(self, rnds) -> np.ndarray:
         r = np.ascontiguousarray(np.asarray(rnds, dtype=np.float64).reshape(-1))
         out = np.empty(r.size, dtype=np.uint64)

@@ -62,3 +62,25 @@ def test_sampling_golden_bit_exact():
     with P.DensityMatrix(4) as dm:
         dm.initialize_from_vector(a["dm_rho"])
         np.testing.assert_array_equal(dm.sample_measure(a["dm_rnds"]), a["dm_samples"])
+
+
+def test_sampling_boundaries_bit_exact():
+    """The uniforms of tests/golden/sample_edges.npz (on and one step below
+    the reference's cumulative sums, in the gaps after blocks, above the
+    total): the engine returns the reference's samples, through the
+    statevector and density-matrix handles, with the reference's block
+    count (index size) set where it differs from 10."""
+    import sys
+    sys.path.insert(0, str(GOLDEN))
+    from gen_sample_edges import CASES, state_of
+
+    P = pkg()
+    a = np.load(GOLDEN / "sample_edges.npz")
+    for idx, (kind, n, isz, seed) in enumerate(CASES):
+        data = state_of(kind, n, seed)
+        st = P.QubitVector(n) if kind == "sv" else P.DensityMatrix(n)
+        with st:
+            st.initialize_from_vector(data)
+            st.set_sample_measure_index_size(isz)
+            got = st.sample_measure(a[f"rnds{idx}"])
+        np.testing.assert_array_equal(got, a[f"samples{idx}"], err_msg=f"{kind} {n} {isz}")

@@ -76,6 +76,27 @@ def test_sample_measure_bit_exact():
     np.testing.assert_array_equal(d.sample_measure(a["dm_rnds"]), a["dm_samples"])
 
 
+def _edge_cases():
+    import sys
+    sys.path.insert(0, str(GOLDEN))
+    from gen_sample_edges import CASES, state_of
+
+    a = np.load(GOLDEN / "sample_edges.npz")
+    for idx, (kind, n, isz, seed) in enumerate(CASES):
+        assert list(a[f"case{idx}"]) == [0 if kind == "sv" else 1, n, isz, seed]
+        yield kind, n, isz, state_of(kind, n, seed), a[f"rnds{idx}"], a[f"samples{idx}"]
+
+
+def test_sample_measure_on_boundaries_bit_exact():
+    """Uniforms exactly on the reference's cumulative sums, one step below
+    them, in the rounding gaps after blocks and above the total
+    (tests/golden/gen_sample_edges.py): the oracle returns the reference's
+    samples, the walk's end (2^n) included."""
+    for kind, n, isz, data, r, want in _edge_cases():
+        o = O.OracleQV(n, data) if kind == "sv" else O.OracleDM(n, data)
+        np.testing.assert_array_equal(o.sample_measure(r, index_size=isz), want, err_msg=f"{kind} {n} {isz}")
+
+
 def test_rng_streams_bit_exact():
     a = np.load(GOLDEN / "rng_cases.npz")
     for key in a.files:
