@@ -625,10 +625,27 @@ def bench_sample(args, torch, P):
     t1 = time.perf_counter()
     pm = st.probabilities(list(range(10)))
     t_p = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    pall = st.probabilities()
+    t_all = time.perf_counter() - t2
+    del pall
+    # the first shots against the oracle (the reference's walk, all host cores) on the same state
+    check = None
+    if not args.no_checks:
+        from oracle import oracle as O
+
+        O.build()
+        O.set_threads(os.cpu_count() or 1, 14)
+        o = O.OracleQV(args.qubits, st.copy_to_vector())
+        m = min(args.sample_check, rnds.size)
+        want = o.sample_measure(rnds[:m])
+        check = {"shots_compared": int(m), "identical": bool(np.array_equal(want, s[:m]))}
+        del o
     st.close()
     return {"metric": "shots/s", "value": round(1e5 / t_s, 1), "unit": "shots/s", "higher_is_better": True,
             "n_gpus": 1, "dtype": "c128" if args.precision == "double" else "c64", "data": "synthetic",
             "sample_100k_ms": round(t_s * 1e3, 2), "marginal_10q_ms": round(t_p * 1e3, 2),
+            "probabilities_all_ms": round(t_all * 1e3, 2), "vs_oracle": check,
             "config": {"workload": f"QV {args.qubits}q state, 100k shots", "qubits": args.qubits}}
 
 
@@ -930,6 +947,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the complex64, adjoint and density-matrix runs of the default workload")
     ap.add_argument("--no-checks", action="store_true", help="skip the parity checks of the default workload")
+    ap.add_argument("--sample-check", type=int, default=2000,
+                    help="sample workload: shots compared with the oracle's walk on the same state")
     ap.add_argument("--oracle-qubits", type=int, default=26,
                     help="state size of the default workload's comparison with the oracle")
     ap.add_argument("--ref-ops-per-step", type=int, default=2,
