@@ -486,6 +486,54 @@ def bench_qv(args, torch, P):
             "parity": checks, "variants": variants}
 
 
+def bench_dense5(args, torch, P):
+    """5-qubit dense gates: per layer a seeded permutation of the qubits into
+    groups of five, a Haar-random 32 x 32 unitary on each (the width Aer's
+    Fusion reaches with max_fusion_qubits = 5), applied one op per launch to
+    the 2^qubits state in HBM."""
+    rng = np.random.default_rng(args.seed)
+    n = args.qubits
+    ops = []
+    for _ in range(args.dense5_layers):
+        perm = rng.permutation(n)
+        for g in range(n // 5):
+            z = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
+            q, r = np.linalg.qr(z)
+            ops.append(([int(x) for x in perm[5 * g:5 * g + 5]], q * (np.diag(r) / np.abs(np.diag(r)))))
+    st = P.QubitVector(n, args.precision)
+    st.initialize()
+    stream = torch.cuda.ExternalStream(st.stream())
+    for q, m in ops[:args.warmup]:
+        st.apply_matrix(q, m)
+    st.synchronize()
+    L = P.lib()
+    n0 = L.gbqv_launch_count()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(ops) + 1)]
+    evs[0].record(stream)
+    for i, (q, m) in enumerate(ops):
+        st.apply_matrix(q, m)
+        evs[i + 1].record(stream)
+    evs[-1].synchronize()
+    launches = L.gbqv_launch_count() - n0
+    per = [evs[i].elapsed_time(evs[i + 1]) for i in range(len(ops))]
+    norm = st.norm()
+    st.close()
+    amp = 16 if args.precision == "double" else 8
+    pass_bytes = 2 * (1 << n) * amp
+    ms = float(np.mean(per))
+    peak, kind = hbm_peak()
+    flops = 8 * 32 * (1 << n)
+    return {"metric": "5-qubit dense gate GB/s", "value": round(pass_bytes / ms / 1e6, 1), "unit": "GB/s",
+            "higher_is_better": True, "n_gpus": 1, "dtype": "c128" if args.precision == "double" else "c64",
+            "data": "synthetic", "ms_per_gate": round(ms, 4), "min_ms": round(min(per), 4),
+            "gates": len(ops), "gpu_launches": int(launches), "norm_after": norm,
+            "roofline": {"bound": "hbm", "achieved": round(pass_bytes / ms / 1e6, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(pass_bytes / ms / 1e6 / peak, 4), "peak_kind": kind,
+                         "flops_per_gate": flops, "tflops": round(flops / ms / 1e9, 1)},
+            "config": {"workload": f"{n}q, {args.dense5_layers} layers of {n // 5} Haar SU(32) on disjoint 5-qubit groups",
+                       "qubits": n}}
+
+
 def A_check(L, rc, st):
     if rc != 0:
         raise RuntimeError(L.gbqv_last_error(st.handle).decode())
@@ -920,7 +968,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="qv",
-                    choices=["qv", "adjoint", "dm", "sample", "batch", "estimator", "shots"])
+                    choices=["qv", "adjoint", "dm", "sample", "batch", "estimator", "shots", "dense5"])
+    ap.add_argument("--dense5-layers", type=int, default=4)
     ap.add_argument("--shots-qubits", type=int, default=16)
     ap.add_argument("--shots-rounds", type=int, default=8)
     ap.add_argument("--shots", type=int, default=4096)
@@ -966,7 +1015,8 @@ def main():
     P = entry.load_package()
     P.build()
     fn = {"qv": bench_qv, "adjoint": bench_adjoint, "dm": bench_dm, "sample": bench_sample,
-          "batch": bench_batch, "estimator": bench_estimator, "shots": bench_shots}[args.workload]
+          "batch": bench_batch, "estimator": bench_estimator, "shots": bench_shots,
+          "dense5": bench_dense5}[args.workload]
     line = fn(args, torch, P)
     if int(os.environ.get("RANK", "0")) == 0:
         print(json.dumps(line))

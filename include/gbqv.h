@@ -456,6 +456,16 @@ int gbqv_batch_run(gbqv_batch_t b, int want_grad, double *elapsed_ms);
 int gbqv_batch_result(gbqv_batch_t b, int i, double *energy, double *grad, int nparams, uint64_t *samples,
                       uint64_t shots, double *latency_ms);
 
+/* Test hook of the failure path (no reference counterpart).  enable = 1:
+ * later complex128 dense gates on the tcgen05 kernel withhold the commit of
+ * each CTA's first accumulator, so that tile's epilogue waits on an mbarrier
+ * that nothing completes; its bounded wait gives up after 2 s, the CTA
+ * drains its copies and MMAs, frees its tensor memory and returns, and the
+ * next synchronising call fails with GBQV_ERR_TIMEOUT (the state's contents
+ * are then invalid).  enable = 0 restores normal operation.  No GPU fault is
+ * involved: it exercises the same bounded waits that guard a real stall. */
+int gbqv_test_stall_tensor_pipeline(gbqv_handle h, int enable);
+
 /* Execution policy for gbqv_execute (no reference counterpart: Aer applies
  * one op per pass).  blocking = 0 applies one kernel per op; 1 (default)
  * schedules runs of small ops into cache-blocked passes whose tile is held

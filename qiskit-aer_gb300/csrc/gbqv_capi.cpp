@@ -1075,6 +1075,13 @@ extern "C" int gbqv_set_tensor_c128(gbqv_handle h, int enable) {
   });
 }
 
+extern "C" int gbqv_test_stall_tensor_pipeline(gbqv_handle h, int enable) {
+  return guard(h, [&] {
+    need_handle(h);
+    h->dev.tc_test_stall = enable ? 1 : 0;
+  });
+}
+
 extern "C" int gbqv_set_blocking(gbqv_handle h, int blocking) {
   return guard(h, [&] {
     need_handle(h);

@@ -50,12 +50,13 @@ struct Device {
   int tensor_c128 = 1;      // complex128 dense k = 4, 5: 0 FP64 cores, 1 tensor (tcgen05 for k = 4), 2 mma.sync only
   int sample_index_size = 10;  // QubitVector::sample_measure_index_size_ (2^this blocks)
   int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up
+  int tc_test_stall = 0;    // test hook: the tcgen05 complex128 kernel withholds its first tile's commit
   // tcgen05 kernel: 128-byte-swizzled TMA descriptors of the state viewed as
-  // rows of 8 amplitudes, box height 2^(L-3) for run length L = 7..11; built
+  // rows of 8 amplitudes, box height 2^(L-3) for run length L = 7..12; built
   // on first use, dropped when the state buffer changes
   const void *tmap_state = nullptr;
   unsigned tmap_ok = 0;  // bit L-7: tmap[L-7] is valid
-  alignas(128) unsigned char tmap[5][128];  // CUtensorMap storage (128-byte aligned)
+  alignas(128) unsigned char tmap[6][128];  // CUtensorMap storage (128-byte aligned)
   void *state = nullptr;
   void *ckpt = nullptr;
   cudaStream_t stream = nullptr;
@@ -150,7 +151,7 @@ void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint1
                       uint32_t &runbytes, uint32_t amp_bytes);
 bool tc_tensor_map(Device &dev, uint32_t L, void *out);
 bool tc_runs_map(Device &dev, const reg_t &qubits, uint32_t L, void *out, uint32_t &rank, uint32_t &nreq,
-                 uint32_t &row_step);
+                 uint32_t *row_off);
 int sm_count();
 // complex64 dense 4-qubit gates on tcgen05 (3xTF32, gbqv_tc64.cu)
 bool tc64_dense_available(const Device &dev, int k);

@@ -92,6 +92,7 @@ struct TcParams {
   uint64_t ntiles;
   uint32_t roff[16];      // byte offset in the raw stage of local amplitude j of group 0
   uint32_t nruns, runbytes;
+  uint32_t stall;         // test hook: no accumulator commit for the CTA's first tile
   uint16_t zl[kTcGroups]; // amplitude index of group m within its run (zeros at targets < L)
   int rowbase[kTcReals];  // row key - 1017 per output real (see combine)
 };
@@ -371,7 +372,9 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
         for (int kk = 0; kk < 2; ++kk)
           tc::mma_f16(d0 + 32u * s, tc::smem_desc(a0 + s * kPlaneBytes + kk * 256, 128, 512),
                       tc::smem_desc(mat + kk * 256, 128, 512), tc::idesc_f16_f32(128, 32 * (6 - s)), 1);
-      tc::mma_commit(accf(b));
+      // the test hook leaves the first tile's accumulator uncommitted: its
+      // epilogue's bounded wait runs out and the CTA takes the abort path
+      if (!(p.stall && i == 0)) tc::mma_commit(accf(b));
     }
     // every MMA issued above has completed once `done` flips (bounded wait,
     // independent of the abort flag so TMEM is never freed under a live MMA)
@@ -398,12 +401,13 @@ uint16_t half_bits(int32_t d) {
 
 }  // namespace
 
-// Run geometry of a 128-group tile of a 4-qubit gate on targets `qubits`:
-// run offsets hoff[r] (amplitudes), byte offsets roff[j] of local amplitude j
-// of group 0 in the raw stage, zl[m] = amplitude index of group m inside its
-// run; amp_bytes = 16 (complex128) or 8 (complex64).
+// Run geometry of a 128-group tile of a k-qubit gate (k = 4, 5) on targets
+// `qubits`: run offsets hoff[r] (amplitudes), byte offsets roff[j] of local
+// amplitude j of group 0 in the raw stage, zl[m] = amplitude index of group m
+// inside its run; amp_bytes = 16 (complex128) or 8 (complex64).
 void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint16_t *zl, uint32_t &nruns,
                       uint32_t &runbytes, uint32_t amp_bytes) {
+  const int k = (int)qubits.size();
   reg_t sq = qubits;
   std::sort(sq.begin(), sq.end());
   uint32_t L = 7;
@@ -420,10 +424,10 @@ void tc_tile_geometry(const reg_t &qubits, uint64_t *hoff, uint32_t *roff, uint1
       if (r >> t & 1) off |= 1ULL << high[t];
     hoff[r] = off;
   }
-  for (uint32_t j = 0; j < 16; ++j) {
+  for (uint32_t j = 0; j < (1u << k); ++j) {
     uint64_t lowpart = 0;
     uint32_t r = 0;
-    for (int t = 0; t < 4; ++t) {
+    for (int t = 0; t < k; ++t) {
       if (!(j >> t & 1)) continue;
       const uint64_t q = qubits[t];
       if (q < L) {
@@ -468,7 +472,7 @@ static EncodeTiled encode_tiled() {
 // for int32 row coordinates or encoding fails.
 bool tc_tensor_map(Device &dev, uint32_t L, void *out) {
   const uint32_t amp_log2 = dev.dbl ? 4 : 3, row_amps_log2 = 7 - amp_log2;
-  if ((uint32_t)dev.n - row_amps_log2 >= 31 || L < 7 || L > 11) return false;
+  if ((uint32_t)dev.n - row_amps_log2 >= 31 || L < 7 || L > 12) return false;
   if (dev.tmap_state != dev.state) {
     dev.tmap_ok = 0;
     dev.tmap_state = dev.state;
@@ -494,24 +498,33 @@ bool tc_tensor_map(Device &dev, uint32_t L, void *out) {
 // A descriptor that fetches several runs of a tile in one request: the state
 // as rows of 128 bytes (dims 0, 1) plus one dimension of size 2 and stride
 // 2^q amplitudes for each of the first (up to three) targets q >= L, box
-// height = the run.  Up to three high targets take one request per tile; a
-// fourth takes a second request, `row_step` rows further and 8 runs further
-// in shared memory.  Same shared-memory layout as one request per run (run r
-// = bits of r over the high targets, ascending).  False: use the per-run path.
+// height = the run.  Up to three high targets take one request per tile; each
+// further high target doubles the requests: request q starts row_off[q] rows
+// further (bits of q over the fourth and fifth high targets) and 8 runs
+// further in shared memory.  Same shared-memory layout as one request per run
+// (run r = bits of r over the high targets, ascending).  False: use the
+// per-run path.
 bool tc_runs_map(Device &dev, const reg_t &qubits, uint32_t L, void *out, uint32_t &rank, uint32_t &nreq,
-                 uint32_t &row_step) {
+                 uint32_t *row_off) {
   const uint32_t amp_log2 = dev.dbl ? 4 : 3, row_amps_log2 = 7 - amp_log2;
-  if ((uint32_t)dev.n - row_amps_log2 >= 31 || L < 7 || L > 11) return false;
+  if ((uint32_t)dev.n - row_amps_log2 >= 31 || L < 7 || L > 12) return false;
   const EncodeTiled fn = encode_tiled();
   if (!fn) return false;
   reg_t high;
   for (uint64_t q : qubits)
     if (q >= L) high.push_back(q);
   std::sort(high.begin(), high.end());
+  if (high.size() > 5) return false;
   const uint32_t nd = (uint32_t)std::min<size_t>(high.size(), 3);
   rank = 2 + nd;
-  nreq = high.size() == 4 ? 2 : 1;
-  row_step = high.size() == 4 ? (uint32_t)(1ULL << (high[3] - row_amps_log2)) : 0;
+  nreq = high.size() > 3 ? 1u << (high.size() - 3) : 1u;
+  for (uint32_t q = 0; q < nreq; ++q) {
+    uint64_t rows = 0;
+    for (size_t t = 3; t < high.size(); ++t)
+      if (q >> (t - 3) & 1) rows += 1ULL << (high[t] - row_amps_log2);
+    if (rows > 0x7fffffffULL) return false;
+    row_off[q] = (uint32_t)rows;
+  }
   cuuint64_t dims[5] = {16, (cuuint64_t)1 << (dev.n - row_amps_log2), 2, 2, 2};
   cuuint64_t strides[4] = {128, 0, 0, 0};
   cuuint32_t box[5] = {16, 1u << (L - row_amps_log2), 2, 2, 2};
@@ -577,6 +590,7 @@ void launch_dense_tc(Device &dev, const reg_t &qubits, const cd *mat) {
   int rowkey[kTcReals];
   tc_matrix4(mat, planes.data(), rowkey);
   for (int r = 0; r < kTcReals; ++r) p.rowbase[r] = rowkey[r] - 1017;
+  p.stall = dev.tc_test_stall ? 1u : 0u;
   grow(dev.mat, dev.mat_cap, kMatBytes);
   cuda_check(cudaMemcpyAsync(dev.mat, planes.data(), kMatBytes, cudaMemcpyHostToDevice, dev.stream), "matrix upload");
   int *status = tc_status_word(dev);

@@ -1,7 +1,8 @@
-// gbqv_tc64.cu — complex64 dense 4-qubit gates on the 5th-generation tensor
-// cores in split precision (3xTF32): QubitVector<float>::apply_matrix
+// gbqv_tc64.cu — complex64 dense 4- and 5-qubit gates on the 5th-generation
+// tensor cores in split precision (3xTF32): QubitVector<float>::apply_matrix
 // (src/simulators/statevector/qubitvector.hpp:1298-1303, apply_lambda over
-// 2^4-amplitude groups) for the fused ops of the 30-qubit complex64 workload.
+// 2^k-amplitude groups) for the fused ops of the complex64 workloads (Aer's
+// Fusion emits dense ops of up to 5 qubits).
 //
 // Every real x of a group and every entry a of the real form of the matrix
 // [[Re U, -Im U], [Im U, Re U]] is split as x = x_hi + x_lo with x_hi = x
@@ -13,24 +14,24 @@
 // kernel, the SIMT side is light.
 //
 // One persistent CTA per SM, 18 warps, the same pipeline as the complex128
-// kernel (gbqv_tc.cu):
+// kernel (gbqv_tc.cu); R = 2^(k+1) reals per group (32 or 64):
 //   warps 0-7       producers: two threads per group split each tile of 128
 //                    groups from the raw ring into two tf32 planes (hi, lo)
 //                    in the smem stage of the tile's parity;
-//   warps 8-15      epilogues: one warpgroup per pipeline lane reads the 32
+//   warps 8-15      epilogues: one warpgroup per pipeline lane reads the R
 //                    fp32 outputs of its group from TMEM and stores them;
-//   warp 16 lane 0  issues 12 tcgen05.mma.kind::tf32 per tile (4 K = 8 steps
-//                    x {hi*hi, hi*lo, lo*hi}, M = 128, N = 32) into the lane's
-//                    32 TMEM columns, commits to accf (epilogue) and sfree
-//                    (producers);
+//   warp 16 lane 0  issues 3 R / 8 tcgen05.mma.kind::tf32 per tile (R / 8
+//                    K = 8 steps x {hi*hi, hi*lo, lo*hi}, M = 128, N = R)
+//                    into the lane's R TMEM columns, commits to accf
+//                    (epilogue) and sfree (producers);
 //   warp 17 lane 0  loader: tiled TMA loads (rows of 16 amplitudes, 128-byte
-//                    swizzle) of each tile's <= 16 contiguous runs into a
-//                    4-stage raw ring, one or two requests per tile (a
-//                    descriptor with the high targets as extra dimensions;
-//                    runs of 1 KB fetched one by one ran at 0.45 of HBM).
+//                    swizzle) of each tile's <= 2^k contiguous runs into the
+//                    raw ring (4 stages of 16 KB for k = 4, 2 of 32 KB for
+//                    k = 5), 1 to 4 requests per tile (a descriptor with up
+//                    to three high targets as extra dimensions; runs of 1 KB
+//                    fetched one by one ran at 0.45 of HBM).
 // Shared-memory operands: K-major, no swizzle, 8-row x 16-byte core matrices
-// (4 tf32), 128 bytes apart along K, 1024 bytes apart per 8 rows (a tf32 row
-// of 32 reals is 128 bytes).
+// (4 tf32), 128 bytes apart along K, 4 R bytes apart per 8 rows.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -44,53 +45,66 @@
 namespace gbqv {
 namespace {
 
-constexpr int kG = 128;                     // groups per tile (MMA M)
-constexpr int kR = 32;                      // reals per group (MMA K, matrix rows)
-constexpr int kPlane = kG * kR * 4;         // 16 KB: one tf32 plane of a tile
-constexpr int kStage = 2 * kPlane;          // hi, lo
-constexpr int kMatBytes = 2 * kR * kR * 4;  // 8 KB: matrix hi, lo
-constexpr int kRawStage = kG * 16 * 8;      // 16 KB: a tile's raw amplitudes, run order
-constexpr int kRawStages = 4;
-constexpr int kOffStage = kMatBytes;
-constexpr int kOffRaw = kOffStage + 2 * kStage;
-constexpr int kOffBar = kOffRaw + kRawStages * kRawStage;
-constexpr int kOffMisc = kOffBar + 24 * 8;
-constexpr int kSmem = kOffMisc + 64 + 1024;  // + 1024-byte alignment slack
+constexpr int kG = 128;  // groups per tile (MMA M)
+
+// Sizes of the k-qubit kernel (k = 4, 5).
+template <int KQ>
+struct Tc64Shape {
+  static constexpr int kAmps = 1 << KQ;                 // amplitudes per group
+  static constexpr int kR = 2 * kAmps;                  // reals per group (MMA K, matrix rows, N)
+  static constexpr int kHalf = kAmps / 2;               // amplitudes per producer thread
+  static constexpr int kPlane = kG * kR * 4;            // one tf32 plane of a tile (16 / 32 KB)
+  static constexpr int kStage = 2 * kPlane;             // hi, lo
+  static constexpr int kMatBytes = 2 * kR * kR * 4;     // matrix hi, lo (8 / 32 KB)
+  static constexpr int kRawStage = kG * kAmps * 8;      // a tile's raw amplitudes (16 / 32 KB)
+  static constexpr int kRawStages = KQ == 4 ? 4 : 2;    // 64 KB in flight either way
+  static constexpr int kSbo = kR * 32;                  // bytes between 8-row groups of an operand
+  static constexpr int kOffStage = kMatBytes;
+  static constexpr int kOffRaw = kOffStage + 2 * kStage;
+  static constexpr int kOffBar = kOffRaw + kRawStages * kRawStage;
+  static constexpr int kOffMisc = kOffBar + 24 * 8;
+  static constexpr int kSmem = kOffMisc + 64 + 1024;   // + 1024-byte alignment slack
+  static constexpr uint32_t kTmemCols = 2 * kR;         // two R-column accumulators
+  static_assert(kSmem <= 232448, "shared memory per CTA");
+};
 constexpr int kThreads = 18 * 32;
 constexpr int kMmaWarp = 16, kLoadWarp = 17;
-constexpr uint32_t kTmemCols = 64;          // two 32-column accumulators
 
+template <int KQ>
 struct Tc64Params {
   CUtensorMap tmap;   // 128-byte aligned type; the state as rows of 16 amplitudes
-  // loads of a tile's runs into the 128-byte swizzle layout: 2 = one request
-  // per tile (two with four targets >= L) of a descriptor whose extra
-  // dimensions are the high targets (rank, row_step: see tc_runs_map);
-  // 1 = one 2D request per run; 0 = 1D bulk copies, plain layout (35 qubits)
-  uint32_t swz, rank, nreq, row_step;
+  // loads of a tile's runs into the 128-byte swizzle layout: 2 = 1..4
+  // requests per tile of a descriptor whose extra dimensions are the high
+  // targets (rank, row_off: see tc_runs_map); 1 = one 2D request per run;
+  // 0 = 1D bulk copies, plain layout (35 qubits)
+  uint32_t swz, rank, nreq;
+  uint32_t row_off[4];
   // targets are sorted ascending (the matrix permuted to match); pair0 = 1
   // when qubit 0 is a target: amplitudes j, j + 1 (j even) are then adjacent
   // in memory and move as one 16-byte access
   uint32_t pair0;
-  uint64_t offs[16];
-  uint64_t lowmask[4];
-  uint64_t hoff[16];
+  uint64_t offs[1 << KQ];
+  uint64_t lowmask[KQ];
+  uint64_t hoff[1 << KQ];
   uint64_t ngroups;
   uint64_t ntiles;
-  uint32_t roff[16];
+  uint32_t roff[1 << KQ];
   uint32_t nruns, runbytes;
   uint16_t zl[kG];
 };
 
-__device__ __forceinline__ uint64_t insert_zeros4(uint64_t g, const uint64_t *lowmask) {
+template <int KQ>
+__device__ __forceinline__ uint64_t insert_zeros_k(uint64_t g, const uint64_t *lowmask) {
 #pragma unroll
-  for (int j = 0; j < 4; ++j) g = ((g & ~lowmask[j]) << 1) | (g & lowmask[j]);
+  for (int j = 0; j < KQ; ++j) g = ((g & ~lowmask[j]) << 1) | (g & lowmask[j]);
   return g;
 }
 
 // byte offset of tf32 element (row, k) in a K-major no-swizzle operand whose
-// rows hold 32 reals
-__host__ __device__ constexpr uint32_t off32(uint32_t row, uint32_t k) {
-  return (row >> 3) * 1024 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4;
+// rows hold R reals
+template <int R>
+__host__ __device__ constexpr uint32_t off_r(uint32_t row, uint32_t k) {
+  return (row >> 3) * (R * 32) + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4;
 }
 
 // TF32 rounding (nearest, ties away from zero) of an fp32 bit pattern.
@@ -110,8 +124,14 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint6
       : "memory");
 }
 
+template <int KQ>
 __global__ void __launch_bounds__(kThreads, 1)
-    k_dense_tc4_c64(float2 *psi, const __grid_constant__ Tc64Params p, const uint4 *__restrict__ gmat, int *status) {
+    k_dense_tc_c64(float2 *psi, const __grid_constant__ Tc64Params<KQ> p, const uint4 *__restrict__ gmat, int *status) {
+  using S = Tc64Shape<KQ>;
+  constexpr int kR = S::kR, kHalf = S::kHalf, kPlane = S::kPlane, kStage = S::kStage, kMatBytes = S::kMatBytes;
+  constexpr int kRawStage = S::kRawStage, kRawStages = S::kRawStages, kOffStage = S::kOffStage;
+  constexpr int kOffRaw = S::kOffRaw, kOffBar = S::kOffBar, kOffMisc = S::kOffMisc;
+  constexpr uint32_t kTmemCols = S::kTmemCols;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   // 1024-byte alignment: the swizzle pattern is taken from address bits 4-9
   unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
@@ -167,12 +187,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp < 8) {
     // ---------------- producers ----------------
     // two threads per group, in the two half-warps: half h owns amplitudes
-    // 8h..8h+7, i.e. K chunks 4h..4h+3 (4 reals each) of the group's row
+    // kHalf h .. kHalf (h + 1) - 1, i.e. K chunks of 4 reals from kHalf h / 2
     const int m = 16 * warp + (lane & 15), h = lane >> 4;
-    uint32_t ro[8];
+    uint32_t ro[kHalf];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const uint32_t off = p.roff[8 * h + j] + 8u * p.zl[m];
+    for (int j = 0; j < kHalf; ++j) {
+      const uint32_t off = p.roff[kHalf * h + j] + 8u * p.zl[m];
       ro[j] = p.swz != 0 ? off ^ (((off >> 7) & 7u) << 4) : off;
     }
     uint64_t tile = blockIdx.x;
@@ -183,17 +203,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool landed = tc::mbar_wait(raw_full(slot), (i / kRawStages) & 1, abort_flag);
       if (!__all_sync(0xffffffffu, landed)) break;
       const unsigned char *raw = smem + kOffRaw + slot * kRawStage;
-      float2 v[8];
+      float2 v[kHalf];
       if (p.pair0) {
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {
+        for (int j = 0; j < kHalf; j += 2) {
           const float4 w = *reinterpret_cast<const float4 *>(raw + ro[j]);
           v[j] = make_float2(w.x, w.y);
           v[j + 1] = make_float2(w.z, w.w);
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = *reinterpret_cast<const float2 *>(raw + ro[j]);
+        for (int j = 0; j < kHalf; ++j) v[j] = *reinterpret_cast<const float2 *>(raw + ro[j]);
       }
       // in registers: the raw slot goes back to the loader (the proxy fence
       // orders these reads before its next async-proxy write)
@@ -203,7 +223,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!__all_sync(0xffffffffu, ok)) break;
       unsigned char *stage = smem + kOffStage + b * kStage;
 #pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
+      for (int cc = 0; cc < kHalf / 2; ++cc) {
         const float x[4] = {v[2 * cc].x, v[2 * cc].y, v[2 * cc + 1].x, v[2 * cc + 1].y};
         uint32_t hi[4], lo[4];
 #pragma unroll
@@ -211,7 +231,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           hi[e] = tf32_bits(__float_as_uint(x[e]));
           lo[e] = __float_as_uint(x[e] - __uint_as_float(hi[e]));  // exact
         }
-        const uint32_t o = off32((uint32_t)m, 4u * (4 * h + cc));
+        const uint32_t o = off_r<kR>((uint32_t)m, 4u * ((kHalf / 2) * h + cc));
         *reinterpret_cast<uint4 *>(stage + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
         *reinterpret_cast<uint4 *>(stage + kPlane + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
       }
@@ -221,32 +241,32 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp < kMmaWarp) {
     // ---------------- epilogues: warpgroup b serves pipeline lane b ----------------
     const int b = (warp - 8) >> 2, quarter = warp & 3, m = 32 * quarter + lane;
-    const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * 32u;
+    const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * (uint32_t)kR;
     uint64_t tile = blockIdx.x + (uint64_t)b * gridDim.x;
     for (uint32_t c = 0; tile < ntiles; tile += 2ULL * gridDim.x, ++c) {
       const bool ok = tc::mbar_wait(accf(b), c & 1, abort_flag);
       if (!__all_sync(0xffffffffu, ok)) break;
       tc::fence_after_sync();
-      uint32_t T[4][8];
+      uint32_t T[kR / 8][8];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tc::tmem_ld8(tbase + 8u * q, T[q]);
+      for (int q = 0; q < kR / 8; ++q) tc::tmem_ld8(tbase + 8u * q, T[q]);
       tc::tmem_wait_ld();
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tc::pin(T[q]);
+      for (int q = 0; q < kR / 8; ++q) tc::pin(T[q]);
       tc::fence_before_sync();
       tc::mbar_arrive(acce(b));
       // n >= 11: every tile is full, so the whole warp takes this branch
       // (the lane-pair exchange below needs all 32 lanes)
       const uint64_t grp = tile * kG + m;
       if (grp < p.ngroups) {
-        const uint64_t base = insert_zeros4(grp, p.lowmask);
+        const uint64_t base = insert_zeros_k<KQ>(grp, p.lowmask);
         // output reals 2j, 2j + 1 (columns) are amplitude j (re, im)
         auto out = [&](int j) {
           return make_float2(__uint_as_float(T[j >> 2][(2 * j) & 7]), __uint_as_float(T[j >> 2][(2 * j + 1) & 7]));
         };
         if (p.pair0) {
 #pragma unroll
-          for (int j = 0; j < 16; j += 2) {
+          for (int j = 0; j < S::kAmps; j += 2) {
             const float2 a = out(j), c = out(j + 1);
             *reinterpret_cast<float4 *>(psi + base + p.offs[j]) = make_float4(a.x, a.y, c.x, c.y);
           }
@@ -256,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           // 2jj of both groups, the odd lane amplitude 2jj + 1 of both
           const bool odd = lane & 1;
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
+          for (int jj = 0; jj < S::kAmps / 2; ++jj) {
             const float2 e = out(2 * jj), o = out(2 * jj + 1);
             const float2 give = odd ? e : o;
             const float2 got = make_float2(__shfl_xor_sync(0xffffffffu, give.x, 1), __shfl_xor_sync(0xffffffffu, give.y, 1));
@@ -271,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == kMmaWarp && lane == 0) {
     // ---------------- MMA issuer ----------------
     const uint32_t mat = tc::smem_u32(smem);
-    const uint32_t idesc = idesc_tf32_f32(128, 32);
+    const uint32_t idesc = idesc_tf32_f32(128, kR);
     uint64_t tile = blockIdx.x;
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = (int)(i & 1);
@@ -280,13 +300,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (c >= 1 && !tc::mbar_wait(acce(b), (c - 1) & 1, abort_flag, 32)) break;
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(smem + kOffStage + b * kStage);
-      const uint32_t d = tmem + (uint32_t)b * 32u;
+      const uint32_t d = tmem + (uint32_t)b * (uint32_t)kR;
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        const uint64_t ahi = tc::smem_desc(a0 + kk * 256, 128, 1024);
-        const uint64_t alo = tc::smem_desc(a0 + kPlane + kk * 256, 128, 1024);
-        const uint64_t bhi = tc::smem_desc(mat + kk * 256, 128, 1024);
-        const uint64_t blo = tc::smem_desc(mat + kR * 128 + kk * 256, 128, 1024);
+      for (int kk = 0; kk < kR / 8; ++kk) {
+        const uint64_t ahi = tc::smem_desc(a0 + kk * 256, 128, S::kSbo);
+        const uint64_t alo = tc::smem_desc(a0 + kPlane + kk * 256, 128, S::kSbo);
+        const uint64_t bhi = tc::smem_desc(mat + kk * 256, 128, S::kSbo);
+        const uint64_t blo = tc::smem_desc(mat + kR * kR * 4 + kk * 256, 128, S::kSbo);
         // the two cross terms (small) first, then hi * hi
         mma_tf32(d, ahi, blo, idesc, kk != 0);
         mma_tf32(d, alo, bhi, idesc, 1);
@@ -307,13 +327,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     int slot = 0;
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i, slot = slot == kRawStages - 1 ? 0 : slot + 1) {
       if (i >= kRawStages && !tc::mbar_wait(raw_empty(slot), (i / kRawStages - 1) & 1, abort_flag, 64)) break;
-      const uint64_t first = insert_zeros4(tile * kG, p.lowmask);
+      const uint64_t first = insert_zeros_k<KQ>(tile * kG, p.lowmask);
       const uint32_t dst = tc::smem_u32(smem + kOffRaw + slot * kRawStage);
       tc::mbar_arrive_expect_tx(raw_full(slot), kRawStage);
       if (p.swz == 2) {
         for (uint32_t q = 0; q < p.nreq; ++q) {
           const uint32_t d = dst + q * 8u * p.runbytes;
-          const int y = (int)(first >> 4) + (int)(q * p.row_step);
+          const int y = (int)(first >> 4) + (int)p.row_off[q];
           if (p.rank == 2)
             tc::tma_load_2d(d, &p.tmap, 0, y, raw_full(slot));
           else if (p.rank == 3)
@@ -346,13 +366,14 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 }  // namespace
 
-// Host: the hi / lo tf32 planes of the real form of a 16x16 column-major
-// complex matrix (rows and columns ordered (amplitude j, re/im) -> 2j + c),
-// in the core-matrix layout of the B operand: hi = entry rounded to TF32,
-// lo = fp32 of the remainder (the tensor core reads its TF32 part).
+// Host: the hi / lo tf32 planes of the real form of a D x D column-major
+// complex matrix (D = 2^KQ; rows and columns ordered (amplitude j, re/im) ->
+// 2j + c), in the core-matrix layout of the B operand: hi = entry rounded to
+// TF32, lo = fp32 of the remainder (the tensor core reads its TF32 part).
+template <int KQ>
 void tc64_matrix(const cd *mat, uint32_t *planes) {
-  constexpr int D = 16;
-  std::memset(planes, 0, kMatBytes);
+  constexpr int D = 1 << KQ, R = 2 * D;
+  std::memset(planes, 0, Tc64Shape<KQ>::kMatBytes);
   auto put = [&](int r, int k, double x) {
     const float xf = (float)x;
     uint32_t fb;
@@ -363,8 +384,8 @@ void tc64_matrix(const cd *mat, uint32_t *planes) {
     const float lf = (float)(x - (double)hf);
     uint32_t lb;
     std::memcpy(&lb, &lf, 4);
-    planes[off32((uint32_t)r, (uint32_t)k) / 4] = hb;
-    planes[(kR * 128 + off32((uint32_t)r, (uint32_t)k)) / 4] = lb;
+    planes[off_r<R>((uint32_t)r, (uint32_t)k) / 4] = hb;
+    planes[(R * R * 4 + off_r<R>((uint32_t)r, (uint32_t)k)) / 4] = lb;
   };
   for (int j = 0; j < D; ++j)
     for (int jp = 0; jp < D; ++jp) {
@@ -376,58 +397,68 @@ void tc64_matrix(const cd *mat, uint32_t *planes) {
     }
 }
 
-bool tc64_dense_available(const Device &dev, int k) {
-  return !dev.dbl && dev.tensor_c128 == 1 && k == 4 && dev.n >= 11;
-}
-
-void launch_dense_tc64(Device &dev, const reg_t &qubits_in, const cd *mat_in) {
+template <int KQ>
+void launch_tc64(Device &dev, const reg_t &qubits_in, const cd *mat_in) {
+  using S = Tc64Shape<KQ>;
+  constexpr int D = 1 << KQ;
   // sort the targets; local index bit b' of the sorted order is bit o[b'] of
   // the caller's order
   reg_t qubits = qubits_in;
   std::sort(qubits.begin(), qubits.end());
-  int o[4];
-  for (int b = 0; b < 4; ++b)
+  int o[KQ];
+  for (int b = 0; b < KQ; ++b)
     o[b] = (int)(std::find(qubits_in.begin(), qubits_in.end(), qubits[b]) - qubits_in.begin());
   auto perm = [&](int x) {
     int y = 0;
-    for (int b = 0; b < 4; ++b) y |= ((x >> b) & 1) << o[b];
+    for (int b = 0; b < KQ; ++b) y |= ((x >> b) & 1) << o[b];
     return y;
   };
-  std::vector<cd> matv(256);
-  for (int r = 0; r < 16; ++r)
-    for (int c = 0; c < 16; ++c) matv[r + 16 * c] = mat_in[perm(r) + 16 * perm(c)];
-  const cd *mat = matv.data();
-  Tc64Params p;
+  std::vector<cd> matv((size_t)D * D);
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) matv[r + D * c] = mat_in[perm(r) + D * perm(c)];
+  Tc64Params<KQ> p;
   p.pair0 = qubits[0] == 0 ? 1u : 0u;
   local_offsets(qubits, p.offs);
   sorted_masks(qubits, p.lowmask);
-  p.ngroups = dev.amps() >> 4;
+  p.ngroups = dev.amps() >> KQ;
   p.ntiles = (p.ngroups + kG - 1) / kG;
   tc_tile_geometry(qubits, p.hoff, p.roff, p.zl, p.nruns, p.runbytes, 8);
   uint32_t L = 0;
   while ((8u << L) < p.runbytes) ++L;
   p.rank = 2;
   p.nreq = 1;
-  p.row_step = 0;
-  if (tc_runs_map(dev, qubits, L, &p.tmap, p.rank, p.nreq, p.row_step))
+  for (uint32_t &r : p.row_off) r = 0;
+  if (tc_runs_map(dev, qubits, L, &p.tmap, p.rank, p.nreq, p.row_off))
     p.swz = 2;
   else
     p.swz = tc_tensor_map(dev, L, &p.tmap) ? 1u : 0u;
-  std::vector<uint32_t> planes(kMatBytes / 4);
-  tc64_matrix(mat, planes.data());
-  grow(dev.mat, dev.mat_cap, kMatBytes);
-  cuda_check(cudaMemcpyAsync(dev.mat, planes.data(), kMatBytes, cudaMemcpyHostToDevice, dev.stream), "matrix upload");
+  std::vector<uint32_t> planes(S::kMatBytes / 4);
+  tc64_matrix<KQ>(matv.data(), planes.data());
+  grow(dev.mat, dev.mat_cap, S::kMatBytes);
+  cuda_check(cudaMemcpyAsync(dev.mat, planes.data(), S::kMatBytes, cudaMemcpyHostToDevice, dev.stream),
+             "matrix upload");
   int *status = tc_status_word(dev);
   static bool attr = false;
   if (!attr) {
-    cuda_check(cudaFuncSetAttribute(k_dense_tc4_c64, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem),
+    cuda_check(cudaFuncSetAttribute(k_dense_tc_c64<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem),
                "tcgen05 complex64 kernel attribute");
     attr = true;
   }
   const uint64_t grid = std::min<uint64_t>(p.ntiles, (uint64_t)sm_count());
-  k_dense_tc4_c64<<<(unsigned)grid, kThreads, kSmem, dev.stream>>>(reinterpret_cast<float2 *>(dev.state), p,
-                                                                   reinterpret_cast<const uint4 *>(dev.mat), status);
+  k_dense_tc_c64<KQ><<<(unsigned)grid, kThreads, S::kSmem, dev.stream>>>(
+      reinterpret_cast<float2 *>(dev.state), p, reinterpret_cast<const uint4 *>(dev.mat), status);
   check_launch("tcgen05 complex64 dense kernel");
+}
+
+bool tc64_dense_available(const Device &dev, int k) {
+  return !dev.dbl && dev.tensor_c128 == 1 && (k == 4 || k == 5) && dev.n >= 7 + k;
+}
+
+void launch_dense_tc64(Device &dev, const reg_t &qubits, const cd *mat) {
+  if (qubits.size() == 5)
+    launch_tc64<5>(dev, qubits, mat);
+  else
+    launch_tc64<4>(dev, qubits, mat);
 }
 
 }  // namespace gbqv

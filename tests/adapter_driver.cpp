@@ -69,7 +69,12 @@ int run(QV &qv, std::istream &in, bool density) {
   qv.chunk_setup((int)qv.num_qubits(), (int)qv.num_qubits(), 0, 1);
   qv.initialize();
   std::string op;
-  while (in >> op && op != "end") {
+  bool ended = false;
+  while (in >> op) {
+    if (op == "end") {
+      ended = true;
+      break;
+    }
     if (op == "matrix") {
       reg_t q = read_qubits(in);
       const size_t D = 1ULL << q.size();
@@ -153,6 +158,14 @@ int run(QV &qv, std::istream &in, bool density) {
       std::cerr << "unknown record " << op << '\n';
       return 2;
     }
+    if (!in) {
+      std::cerr << "malformed record " << op << '\n';
+      return 2;
+    }
+  }
+  if (!ended) {
+    std::cerr << "input ended without \"end\"\n";
+    return 2;
   }
   qv.synchronize();
   return 0;

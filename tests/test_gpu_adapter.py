@@ -20,7 +20,8 @@ def driver(tmp_path_factory):
 
 
 def _fmt_c(values):
-    return " ".join(f"{z.real!r} {z.imag!r}" for z in np.asarray(values, dtype=np.complex128).reshape(-1))
+    return " ".join(f"{float(z.real):.17g} {float(z.imag):.17g}"
+                    for z in np.asarray(values, dtype=np.complex128).reshape(-1))
 
 
 def _unitary(rng, k):

@@ -87,3 +87,45 @@ def test_tc64_basis_state_through_permutation_is_exact():
     perm = np.eye(16)[:, np.random.default_rng(3).permutation(16)].astype(complex)
     ops = [([0, 4, 8, 12], np.eye(16, dtype=complex)), ([1, 2, 3, 13], perm)]
     np.testing.assert_array_equal(run(P, n, psi, ops, 1), oracle(n, psi, ops))
+
+
+@pytest.mark.parametrize("n", [12, 13, 16, 20])
+def test_tc64_five_qubit_gates_against_oracle_and_fma(n):
+    """5-qubit gates (K = 64 reals, N = 64 TMEM columns per lane, 2-stage raw
+    ring of 32 KB tiles): every placement kind — all targets low, all high
+    (the loader's 4-request descriptor), qubit 0 a target or not — against
+    the oracle and the fp32-FMA kernel."""
+    P = pkg()
+    rng = np.random.default_rng(5100 + n)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    placements = [[0, 1, 2, 3, 4], [4, 3, 2, 1, 0], [n - 1, n - 2, n - 3, n - 4, n - 5], [0, n - 1, 5, 2, 9],
+                  [7, 8, 9, 10, 11], [1, 3, n - 2, 6, 8]]
+    placements += [[int(x) for x in rng.choice(n, 5, replace=False)] for _ in range(6)]
+    ops = [(q, haar(rng, 32)) for q in placements]
+    got = run(P, n, psi, ops, 1)
+    scale = np.max(np.abs(psi))
+    np.testing.assert_allclose(got, oracle(n, psi, ops), atol=2e-6 * scale * 12, rtol=0)
+    fma = run(P, n, psi, ops, 0)
+    np.testing.assert_allclose(got, fma, atol=2e-6 * scale * 12, rtol=0)
+
+
+def test_tc64_five_qubit_many_tiles_and_permutation_exact():
+    """23 qubits (many tiles per CTA) against the FMA kernel, and a basis
+    state through a 5-qubit permutation stays exact (hi * hi carries the 1s,
+    the cross terms are zero)."""
+    P = pkg()
+    rng = np.random.default_rng(23)
+    n = 23
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    ops = [([int(x) for x in rng.choice(n, 5, replace=False)], haar(rng, 32)) for _ in range(4)]
+    a = run(P, n, psi, ops, 1)
+    b = run(P, n, psi, ops, 0)
+    assert np.max(np.abs(a - b)) < 1e-5 * np.max(np.abs(psi))
+    perm = np.eye(32)[rng.permutation(32)]
+    basis = np.zeros(1 << 14, dtype=complex)
+    basis[12345] = 1.0
+    q = [13, 2, 0, 7, 9]
+    got = run(P, 14, basis, [(q, perm)], 1)
+    np.testing.assert_array_equal(got, oracle(14, basis, [(q, perm)]))
