@@ -88,10 +88,10 @@ def uniforms(seed: int, count: int) -> np.ndarray:
     return out
 
 
-def _narrow(qubits) -> None:
-    """The C restatement keeps per-group index tables of 2^10 entries."""
-    if len(qubits) > 10:
-        raise ValueError("the oracle applies matrices of at most 10 qubits")
+def _narrow(qubits, limit: int = 10) -> None:
+    """The C restatement keeps per-group index tables of 2^limit entries."""
+    if len(qubits) > limit:
+        raise ValueError(f"the oracle applies matrices of at most {limit} qubits")
 
 
 class OracleQV:
@@ -112,7 +112,7 @@ class OracleQV:
         return self.data.ctypes.data_as(_vp)
 
     def apply_matrix(self, qubits, mat):
-        _narrow(qubits)
+        _narrow(qubits, 13)
         q, qp = _u64(qubits)
         m, mp = _c128(np.asarray(mat).reshape(-1, order="F") if np.ndim(mat) == 2 else mat)
         self.lib.orc_apply_matrix(self._p, C.c_int(self.n), qp, C.c_int(len(q)), mp)

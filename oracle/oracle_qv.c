@@ -131,14 +131,20 @@ void orc_apply_matrix(cplx *sv, int n, const uint64_t *qubits, int k, const cplx
     }
     return;
   }
-#pragma omp parallel for OMP_IF(n)
-  for (int64_t i = 0; i < END; ++i) {
-    uint64_t inds[1024];
-    cplx cache[1024];
-    indexes(qubits, qs, k, i, inds);
-    for (uint64_t a = 0; a < DIM; ++a) { cache[a] = sv[inds[a]]; sv[inds[a]] = 0.0; }
-    for (uint64_t a = 0; a < DIM; ++a)
-      for (uint64_t b = 0; b < DIM; ++b) sv[inds[a]] += mat[a + DIM * b] * cache[b];
+  /* per-thread index and cache tables of DIM entries (k <= 13) */
+#pragma omp parallel OMP_IF(n)
+  {
+    uint64_t *inds = (uint64_t *)malloc(sizeof(uint64_t) * DIM);
+    cplx *cache = (cplx *)malloc(sizeof(cplx) * DIM);
+#pragma omp for
+    for (int64_t i = 0; i < END; ++i) {
+      indexes(qubits, qs, k, i, inds);
+      for (uint64_t a = 0; a < DIM; ++a) { cache[a] = sv[inds[a]]; sv[inds[a]] = 0.0; }
+      for (uint64_t a = 0; a < DIM; ++a)
+        for (uint64_t b = 0; b < DIM; ++b) sv[inds[a]] += mat[a + DIM * b] * cache[b];
+    }
+    free(cache);
+    free(inds);
   }
 }
 

@@ -205,6 +205,24 @@ __host__ __device__ __forceinline__ uint64_t split_word_abs(double x, uint32_t e
   return (shr64(m, E3 - ex) + kSplitK) >> 1;
 }
 
+// The same word with two 32-bit funnel shifts, for the common case of a
+// non-zero x whose shift E3 - ex is at most 31 (x within 2^-27 of its
+// group's largest entry): xhi, xlo are the two words of x's bits.  Bit for
+// bit equal to split_word_abs there (checked on the host for every shift).
+__host__ __device__ __forceinline__ uint32_t funnel_r(uint32_t lo, uint32_t hi, uint32_t s) {  // s in [0, 31]
+#ifdef __CUDA_ARCH__
+  return __funnelshift_r(lo, hi, s);
+#else
+  return s == 0 ? lo : (lo >> s) | (hi << (32 - s));
+#endif
+}
+
+__host__ __device__ __forceinline__ uint64_t split_word_abs_near(uint32_t xhi, uint32_t xlo, uint32_t s) {
+  const uint32_t mh = (xhi & 0xFFFFFu) | 0x100000u;
+  const uint64_t t = ((uint64_t)(mh >> s) << 32) | funnel_r(xlo, mh, s);
+  return (t + kSplitK) >> 1;
+}
+
 // Signed digits of x from its word (host side of the kernel's fp16 planes).
 __host__ __device__ __forceinline__ void word_digits(uint64_t w, bool negative, int32_t *d) {
   d[0] = (int32_t)((w >> 40) & 0xFFFF) - 0x6600;

@@ -206,13 +206,14 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       // all-zero group, which is never stored); the fields are kept
       double2 v[8];
       uint32_t ex[16];
-      uint32_t mx = 0;
+      uint32_t mx = 0, mn = 0x7ff;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         v[j] = amp(j);
         ex[2 * j] = ((uint32_t)__double2hiint(v[j].x) >> 20) & 0x7ff;
         ex[2 * j + 1] = ((uint32_t)__double2hiint(v[j].y) >> 20) & 0x7ff;
         mx = max(mx, max(ex[2 * j], ex[2 * j + 1]));
+        mn = min(mn, min(ex[2 * j], ex[2 * j + 1]));
       }
       // the amplitudes are in registers now: the raw slot goes back to the
       // loader before the split.  The proxy fence orders these generic-proxy
@@ -222,29 +223,53 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
       const int key = mx ? (int)mx + 1 : 0;
       const uint32_t E3 = (uint32_t)key + 3;
+      // every real of the warp non-zero and within 2^-27 of its group's
+      // largest: the split takes two 32-bit funnel shifts (the usual case
+      // for a dense state); otherwise the general 64-bit shift
+      const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E3);
+      // digit words of the 16 magnitudes and the sign pairs, before waiting
+      // for the stage: bit 15 <- sign of re, bit 31 <- sign of im (byte sign
+      // replication)
+      uint32_t lo[16], hi[16], sb[8];
+      if (near) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const uint32_t xh = (uint32_t)__double2hiint(v[j].x), yh = (uint32_t)__double2hiint(v[j].y);
+          const uint64_t rw = oz::split_word_abs_near(xh, (uint32_t)__double2loint(v[j].x), E3 - ex[2 * j]);
+          const uint64_t iw = oz::split_word_abs_near(yh, (uint32_t)__double2loint(v[j].y), E3 - ex[2 * j + 1]);
+          lo[2 * j] = (uint32_t)rw;
+          hi[2 * j] = (uint32_t)(rw >> 32);
+          lo[2 * j + 1] = (uint32_t)iw;
+          hi[2 * j + 1] = (uint32_t)(iw >> 32);
+          sb[j] = tc::prmt(xh, yh, 0xF0B0);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const uint64_t rw = oz::split_word_abs(v[j].x, ex[2 * j], E3);
+          const uint64_t iw = oz::split_word_abs(v[j].y, ex[2 * j + 1], E3);
+          lo[2 * j] = (uint32_t)rw;
+          hi[2 * j] = (uint32_t)(rw >> 32);
+          lo[2 * j + 1] = (uint32_t)iw;
+          hi[2 * j + 1] = (uint32_t)(iw >> 32);
+          sb[j] = tc::prmt((uint32_t)__double2hiint(v[j].x), (uint32_t)__double2hiint(v[j].y), 0xF0B0);
+        }
+      }
       const bool ok = c == 0 || tc::mbar_wait(sempty(b), (c - 1) & 1, abort_flag);
       if (!__all_sync(0xffffffffu, ok)) break;
       unsigned char *stage = smem + kOffStage + b * kStageBytes;
       const uint32_t K64 = 0x64646464u;
 #pragma unroll
       for (int q2 = 0; q2 < 2; ++q2) {
-        // the chunk's 8 reals (amplitudes 4q..4q+3, re/im): digit words of
-        // their magnitudes, and per amplitude the (re, im) sign pair as half2
-        // (+-1, +-1) with the bias constants times it, so that one HFMA2 per
-        // plane word both removes the fp16 bias and applies the signs
-        uint32_t lo[8], hi[8], sg[4], c1[4], c0[4];
+        // the chunk's 8 reals (amplitudes 4q..4q+3, re/im): per amplitude the
+        // (re, im) sign pair as half2 (+-1, +-1) with the bias constants
+        // times it, so that one HFMA2 per plane word both removes the fp16
+        // bias and applies the signs
+        uint32_t sg[4], c1[4], c0[4];
+        const uint32_t *lo8 = lo + 8 * q2, *hi8 = hi + 8 * q2;
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const int j = 4 * q2 + jj;
-          const uint64_t rw = oz::split_word_abs(v[j].x, ex[2 * j], E3);
-          const uint64_t iw = oz::split_word_abs(v[j].y, ex[2 * j + 1], E3);
-          lo[2 * jj] = (uint32_t)rw;
-          hi[2 * jj] = (uint32_t)(rw >> 32);
-          lo[2 * jj + 1] = (uint32_t)iw;
-          hi[2 * jj + 1] = (uint32_t)(iw >> 32);
-          // bit 15 <- sign of re, bit 31 <- sign of im (byte sign replication)
-          const uint32_t sb = tc::prmt((uint32_t)__double2hiint(v[j].x), (uint32_t)__double2hiint(v[j].y), 0xF0B0);
-          sg[jj] = (sb & 0x80008000u) | 0x3C003C00u;
+          sg[jj] = (sb[4 * q2 + jj] & 0x80008000u) | 0x3C003C00u;
           c1[jj] = tc::hmul2(sg[jj], 0xE480E480u);  // -1152 * sign
           c0[jj] = tc::hmul2(sg[jj], 0xE600E600u);  // -1536 * sign
         }
@@ -254,38 +279,38 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
         uint32_t w[4];
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x5140);
+          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x5140);
           w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 5 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x5140);
+          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x5140);
           w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 4 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x7362);
+          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x7362);
           w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 3 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo[2 * jj], lo[2 * jj + 1], 0x7362);
+          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x7362);
           w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 2 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(hi[2 * jj], hi[2 * jj + 1], 0x0040);
+          const uint32_t g = tc::prmt(hi8[2 * jj], hi8[2 * jj + 1], 0x0040);
           w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
         }
         *reinterpret_cast<uint4 *>(row + 1 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
         // digit 0: bytes 5-6 of the word are the fp16 bits of 1536 + |d_0|
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj)
-          w[jj] = tc::hfma2(tc::prmt(hi[2 * jj], hi[2 * jj + 1], 0x6521), sg[jj], c0[jj]);
+          w[jj] = tc::hfma2(tc::prmt(hi8[2 * jj], hi8[2 * jj + 1], 0x6521), sg[jj], c0[jj]);
         *reinterpret_cast<uint4 *>(row) = make_uint4(w[0], w[1], w[2], w[3]);
       }
       if (h == 0) colkey[b * kTcGroups + m] = key;

@@ -18,7 +18,27 @@
 
 using namespace gbqv::oz;
 
+// Mode "near": split_word_abs_near against split_word_abs, bit for bit, for
+// every shift 4..31 and random magnitudes and signs.
+static int check_near(int trials) {
+  std::mt19937_64 rng(777);
+  std::uniform_int_distribution<int> sd(4, 31);
+  std::uniform_int_distribution<uint64_t> bits;
+  long bad = 0;
+  for (int t = 0; t < trials; ++t) {
+    uint64_t b = bits(rng);
+    uint32_t ex = (uint32_t)((b >> 52) & 0x7ff);
+    if (ex == 0 || ex == 0x7ff) continue;  // zeros and non-finite values take the generic path
+    const uint32_t s = (uint32_t)sd(rng), E3 = ex + s;
+    const double x = bitsd(b);
+    if (split_word_abs_near((uint32_t)(b >> 32), (uint32_t)b, s) != split_word_abs(x, ex, E3)) ++bad;
+  }
+  printf("%ld 0\n", bad);
+  return 0;
+}
+
 int main(int argc, char **argv) {
+  if (argc > 3 && std::string(argv[3]) == "near") return check_near(argc > 2 ? atoi(argv[2]) : 100000);
   const int K = argc > 1 ? atoi(argv[1]) : 32;   // reals per column
   const int trials = argc > 2 ? atoi(argv[2]) : 2000;
   const bool sgn = argc > 3 && std::string(argv[3]) == "signed";

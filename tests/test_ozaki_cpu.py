@@ -25,3 +25,15 @@ def test_digit_slices_against_quad(tmp_path, reals, trials, mode):
                          check=True).stdout
     rel, absolute = map(float, out.split())
     assert rel < 1e-13, out
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_fast_split_equals_generic_split(tmp_path):
+    """The tcgen05 kernel's fast split (two 32-bit funnel shifts, used when
+    every shift of a warp's reals is <= 31) gives the generic split's word bit
+    for bit."""
+    exe = tmp_path / "ozk"
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "qiskit-aer_gb300" / "csrc"),
+                           str(ROOT / "tests" / "ozaki_check.cpp"), "-o", str(exe), "-lquadmath"])
+    out = subprocess.run([str(exe), "32", "400000", "near"], capture_output=True, text=True, check=True).stdout
+    assert out.split()[0] == "0", out
