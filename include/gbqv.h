@@ -474,6 +474,14 @@ int gbqv_test_stall_tensor_pipeline(gbqv_handle h, int enable);
  * the shared-memory form there too. */
 int gbqv_set_blocking(gbqv_handle h, int blocking);
 
+/* Tile of the cache-blocked runs (no reference counterpart; Aer's nearest
+ * knob is its configured cache-blocking qubit count, cacheblocking.hpp:
+ * 130-131): a run's ops act inside tiles of 2^tile_qubits amplitudes, one
+ * read and write of the state per run.  0 (default) = 12 qubits at
+ * complex128, 13 at complex64; otherwise 10..12 / 10..13.  Smaller tiles
+ * hold fewer ops per run; the autotuner picks it per workload by timing. */
+int gbqv_set_run_tile_qubits(gbqv_handle h, int tile_qubits);
+
 /* Arithmetic of complex128 dense gates on 4 or 5 qubits (no reference
  * counterpart).  1 (default): exact digit slices on the tensor cores, error
  * <= ~1e-13 of (row max x group max) per gate (4-qubit gates on tcgen05 with

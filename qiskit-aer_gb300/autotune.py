@@ -12,6 +12,11 @@ This module picks, per workload shape:
   one of: one kernel per op (0); cache-blocked runs with the tile held in
   registers (1, the default); or cache-blocked runs with the tile swept in
   shared memory (2).
+* the tile of those cache-blocked runs (``gbqv_set_run_tile_qubits``): a
+  run's ops act inside tiles of 2^m amplitudes, one state pass per run;
+  larger tiles hold more ops per run, smaller ones fewer registers and
+  shared memory per CTA.  Candidates: the default m (12 at complex128, 13
+  at complex64) and one and two qubits less.
 * ``gbqv_batch_run``: how the costliest instances of a batch of uneven
   circuits are split over two-CTA teams.  A setting is (at most
   ``max_team_instances`` teams, for instances costing at least
@@ -41,6 +46,8 @@ from . import _capi as A
 
 # statevector execution forms, the default first (gbqv_set_blocking)
 EXECUTE_CANDIDATES = (1, 2, 0)
+# run tile qubits (gbqv_set_run_tile_qubits), the default (0) first
+TILE_CANDIDATES = {"double": (0, 11, 10), "single": (0, 12, 11)}
 # (max_team_instances, min_cost_fraction) for gbqv_batch_set_teams, the default first
 TEAM_CANDIDATES = ((64, 0.5), (0, 0.5), (16, 0.5), (64, 0.25), (64, 0.75))
 
@@ -215,6 +222,38 @@ def tune_execute(state, circuits, tuner: Autotuner | None = None, candidates=EXE
 
     choice = tuner.select(key, candidates, measure)
     A.check(L.gbqv_set_blocking(h, int(choice)), h)
+    state.initialize()
+    return int(choice)
+
+
+def tune_tile(state, circuits, tuner: Autotuner | None = None, candidates=None,
+              timer: Callable[[int, Callable[[], None]], float] | None = None) -> int:
+    """Picks the tile qubits of the cache-blocked runs (gbqv_set_run_tile_qubits,
+    0 = the engine's default) for the op lists `circuits` on the statevector
+    `state`, under the execution form already set on it, by timing each
+    candidate.  On return the state is back in |0...0> with the chosen tile
+    set."""
+    if getattr(state, "_kind", A.STATEVECTOR) != A.STATEVECTOR:
+        raise ValueError("tune_tile tunes statevector handles only")
+    tuner = tuner if tuner is not None else default_tuner()
+    timer = timer if timer is not None else device_timer
+    candidates = candidates if candidates is not None else TILE_CANDIDATES[state.precision]
+    candidates = [c for c in candidates if c == 0 or c <= state.num_qubits()]
+    circuits = list(circuits)
+    L, h = state._L, state.handle
+    key = ("tile", device_tag(), state.precision, state.num_qubits(), circuit_signature(circuits))
+
+    def run_all():
+        for nc in circuits:
+            A.check(L.gbqv_execute(h, nc.handle), h)
+
+    def measure(m):
+        A.check(L.gbqv_set_run_tile_qubits(h, int(m)), h)
+        state.initialize()
+        return timer(state.stream(), run_all)
+
+    choice = tuner.select(key, candidates, measure)
+    A.check(L.gbqv_set_run_tile_qubits(h, int(choice)), h)
     state.initialize()
     return int(choice)
 

@@ -1082,6 +1082,16 @@ extern "C" int gbqv_test_stall_tensor_pipeline(gbqv_handle h, int enable) {
   });
 }
 
+extern "C" int gbqv_set_run_tile_qubits(gbqv_handle h, int tile_qubits) {
+  return guard(h, [&] {
+    need_handle(h);
+    const int hi = h->dev.dbl ? 12 : 13;
+    REQUIRE(tile_qubits == 0 || (tile_qubits >= 10 && tile_qubits <= hi), GBQV_ERR_ARG,
+            "run tile qubits must be 0 (default) or 10.." + std::to_string(hi));
+    h->dev.run_tile_bits = tile_qubits;
+  });
+}
+
 extern "C" int gbqv_set_blocking(gbqv_handle h, int blocking) {
   return guard(h, [&] {
     need_handle(h);

@@ -47,6 +47,7 @@ struct Device {
   bool density = false;
   bool unitary = false;     // UnitaryMatrix: 2 nq vector qubits, identity at initialisation
   int blocking = 1;         // 0 one kernel per op, 1 register-tile runs, 2 shared-memory runs
+  int run_tile_bits = 0;    // tile qubits of the cache-blocked runs (0: 12 at complex128, 13 at complex64)
   int tensor_c128 = 1;      // complex128 dense k = 4, 5: 0 FP64 cores, 1 tensor (tcgen05 for k = 4), 2 mma.sync only
   int sample_index_size = 10;  // QubitVector::sample_measure_index_size_ (2^this blocks)
   int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up

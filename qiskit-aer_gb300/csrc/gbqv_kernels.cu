@@ -1907,7 +1907,7 @@ __global__ void __launch_bounds__(256, 2) k_run(T *__restrict__ psi, const RunPa
   }
 }
 
-int run_tile_bits(const Device &dev) { return dev.dbl ? 12 : 13; }
+int run_tile_bits(const Device &dev) { return dev.run_tile_bits ? dev.run_tile_bits : dev.dbl ? 12 : 13; }
 constexpr int kRunLowBits = 4;
 constexpr int kRunPoolBytes = 32 * 1024;
 

@@ -22,7 +22,7 @@ import warnings
 import numpy as np
 
 from . import _capi as A
-from .autotune import Autotuner, default_tuner, tune_execute
+from .autotune import Autotuner, default_tuner, tune_execute, tune_tile
 from .circuit import Instruction, NativeCircuit, QuantumCircuit, expval_params
 from .noise import apply_readout
 from .qubitvector import DensityMatrix, QubitVector, UnitaryMatrix
@@ -446,7 +446,11 @@ class AerSimulator:
             if not self.options["blocking_enable"]:
                 A.check(st._L.gbqv_set_blocking(st.handle, 0))
             elif self.options["autotune"] and self.method == "statevector":
-                meta["autotune"] = {"blocking": tune_execute(st, [nc for _, nc in segments], self.tuner())}
+                ncs = [nc for _, nc in segments]
+                mode = tune_execute(st, ncs, self.tuner())
+                meta["autotune"] = {"blocking": mode}
+                if mode != 0:  # the cache-blocked forms: their tile as well
+                    meta["autotune"]["tile_qubits"] = tune_tile(st, ncs, self.tuner())
             save_iter = iter(saves)
             pending = next(save_iter, None)
             for bound, nc in segments:

@@ -139,18 +139,24 @@ class FakeLib:
         self.calls.append(("execute", self.mode, c))
         return 0
 
+    def gbqv_set_run_tile_qubits(self, h, m):
+        self.tile = m
+        self.calls.append(("tile", m))
+        return 0
+
 
 class FakeState:
-    def __init__(self, kind=None):
+    def __init__(self, kind=None, n=4):
         P = pkg()
         self._L = FakeLib()
+        self.n = n
         self.handle = object()
         self.precision = "double"
         self._kind = P._capi.STATEVECTOR if kind is None else kind
         self.inits = 0
 
     def num_qubits(self):
-        return 4
+        return self.n
 
     def initialize(self):
         self.inits += 1
@@ -197,6 +203,38 @@ def test_tune_execute_times_every_form_and_leaves_the_choice_set():
     assert st2._L.mode == 2
     with pytest.raises(ValueError):
         T.tune_execute(FakeState(kind=P._capi.DENSITY_MATRIX), circuits, t, timer=timer)
+
+
+def test_tune_tile_times_each_tile_and_caches_the_choice():
+    P = pkg()
+    T = P.autotune
+    st = FakeState(n=20)
+    circuits = [FakeCircuit("seg0", [(1, "unitary", [0, 1])])]
+    cost = {0: 4.0, 11: 3.5, 10: 6.0}
+    st._L.tile = 0
+
+    def timer(stream, fn):
+        fn()
+        return cost[st._L.tile]
+
+    t = T.Autotuner(warmup=1, repeats=2)
+    assert T.tune_tile(st, circuits, t, timer=timer) == 11
+    assert st._L.calls[-2:] == [("tile", 11), ("init",)]
+    assert {c[1] for c in st._L.calls if c[0] == "tile"} == {0, 11, 10}
+    # cached: a second state of the same structure is not timed
+    st2 = FakeState(n=20)
+    assert T.tune_tile(st2, circuits, t, timer=lambda s, fn: pytest.fail("timed")) == 11
+    # tiles above the state size are not candidates
+    small = FakeState(n=10)
+    small._L.tile = 0
+    seen = []
+
+    def timer2(stream, fn):
+        seen.append(small._L.tile)
+        return 1.0
+
+    T.tune_tile(small, [FakeCircuit("x", [(0, "h", [0])])], T.Autotuner(warmup=0, repeats=1), timer=timer2)
+    assert set(seen) == {0, 10}
 
 
 class FakeBatch:

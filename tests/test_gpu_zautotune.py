@@ -29,11 +29,13 @@ def test_autotuned_statevector_run(tmp_path):
     res = sim.run(qc, shots=256, seed_simulator=5)
     mode = res.metadata()["autotune"]["blocking"]
     assert mode in (0, 1, 2)
+    if mode != 0:
+        assert res.metadata()["autotune"]["tile_qubits"] in (0, 11, 10)
     np.testing.assert_allclose(res.get_statevector(), want, atol=1e-12)
     assert sum(res.get_counts().values()) == 256
     entries = json.loads(path.read_text())["entries"]
-    assert len(entries) == 1
-    entry = next(iter(entries.values()))
+    assert len(entries) == (1 if mode == 0 else 2)
+    entry = next(v for k, v in entries.items() if k.startswith("execute"))
     assert entry["choice"] == str(mode)
     assert set(entry["ms"]) == {"0", "1", "2"} and all(v > 0 for v in entry["ms"].values())
     timed = sim.tuner().measurements
@@ -65,3 +67,21 @@ def test_tuned_batch_team_setting(tmp_path):
         assert abs(e0 - e1) < 1e-12 * max(1.0, abs(e0))
         np.testing.assert_allclose(g0, g1, atol=1e-11)
         np.testing.assert_array_equal(s0, s1)
+
+
+@pytest.mark.parametrize("precision,tiles,tol", [("double", (0, 11, 10), 1e-12), ("single", (0, 12, 11), 2e-5)])
+def test_every_run_tile_gives_the_oracle_state(precision, tiles, tol):
+    """The tile sizes the tuner chooses between (gbqv_set_run_tile_qubits)
+    change only the schedule: each gives the oracle's state."""
+    P = pkg()
+    n = 15
+    rng = np.random.default_rng(31)
+    qc = random_small_ops(P, n, 200, rng)
+    want = oracle_of(qc)
+    nc = P.NativeCircuit(n, qc.data)
+    for m in tiles:
+        with P.QubitVector(n, precision) as st:
+            assert st._L.gbqv_set_run_tile_qubits(st.handle, m) == 0
+            st.initialize()
+            assert st._L.gbqv_execute(st.handle, nc.handle) == 0
+            np.testing.assert_allclose(st.copy_to_vector(), want, atol=tol, err_msg=f"tile {m}")
