@@ -319,7 +319,7 @@ extern "C" int gbqv_destroy(gbqv_handle h) {
   if (!h) return GBQV_OK;
   Device &d = h->dev;
   cudaStreamSynchronize(d.stream);
-  for (void *p : {d.state, d.ckpt, (void *)d.partials, (void *)d.results, d.mat, d.aux, d.aux2, (void *)h->io,
+  for (void *p : {d.state, d.ckpt, (void *)d.partials, (void *)d.results, d.mat, d.aux, d.aux2, d.probs, (void *)h->io,
                   (void *)d.tc_status})
     if (p) cudaFree(p);
   if (d.h_results) cudaFreeHost(d.h_results);

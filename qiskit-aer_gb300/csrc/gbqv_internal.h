@@ -68,6 +68,7 @@ struct Device {
   void *mat = nullptr; size_t mat_cap = 0;               // large matrices
   void *aux = nullptr; size_t aux_cap = 0;               // sampling / probabilities
   void *aux2 = nullptr; size_t aux2_cap = 0;
+  void *probs = nullptr; size_t probs_cap = 0;           // sampling: every outcome's probability
   uint64_t amps() const { return 1ULL << n; }
   size_t amp_bytes() const { return dbl ? 16 : 8; }
 };

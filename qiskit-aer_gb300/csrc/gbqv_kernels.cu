@@ -881,134 +881,6 @@ __global__ void k_probs_all(const T *__restrict__ psi, uint64_t count, uint64_t 
   }
 }
 
-// -------------------------------------------------------------------------
-// Sampling (QubitVector::sample_measure, qubitvector.hpp:2148-2228), in the
-// reference's own order of floating-point operations, so that every shot is
-// the reference's for the same uniform, boundaries included:
-//   prob(k)  = fl(fl(re*re) + fl(im*im)) (std::real(z * conj(z)) without
-//              contraction; complex64 in float, then widened), or Re rho_kk;
-//   idxs[j]  = sequential sum of prob over block j (2^isz blocks of L);
-//   P[j+1]   = fl(P[j] + idxs[j]), the values the block walk compares with;
-//   shot r   : block j = first j with r < P[j+1] (none: the walk ends at
-//              END, as the reference's does); then p = P[j] plus prob(k), one
-//              index at a time, until r < p, stopping at END - 1.
-// The in-block walk is the same sequence for every shot of a block: for
-// blocks longer than 1024 amplitudes one thread per block runs it once and
-// keeps every 1024th partial sum, and a shot restarts from the checkpoint
-// before its hit, so no shot walks more than 1024 indices (plus the rare
-// continuation past a block end that the reference's walk also makes).
-// Below 2^isz amplitudes the reference walks from index 0.
-// -------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ double prob_exact(const T *psi, uint64_t i, uint64_t diag_stride);
-
-template <>
-__device__ __forceinline__ double prob_exact<double2>(const double2 *psi, uint64_t i, uint64_t diag_stride) {
-  if (diag_stride) return psi[i * diag_stride].x;
-  const double2 a = psi[i];
-  return __dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y));
-}
-
-template <>
-__device__ __forceinline__ double prob_exact<float2>(const float2 *psi, uint64_t i, uint64_t diag_stride) {
-  if (diag_stride) return (double)psi[i * diag_stride].x;
-  const float2 a = psi[i];
-  return (double)__fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y));
-}
-
-// One thread per block j: the sequential sum of the block (start = 0), or
-// the walk from P[j] with every `ck`-th partial sum stored (start = P).
-template <typename T, bool CHECKPOINTS>
-__global__ void __launch_bounds__(32) k_seq_blocks(const T *__restrict__ psi, uint64_t nblocks, uint64_t L,
-                                                   uint64_t diag_stride, const double *__restrict__ P,
-                                                   double *__restrict__ out, uint64_t ck) {
-  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nblocks) return;
-  const uint64_t base = j * L;
-  double s = CHECKPOINTS ? P[j] : 0.0;
-  uint64_t t = 0;
-  // eight loads ahead of the dependent adds
-  for (; t + 8 <= L; t += 8) {
-    double v[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) v[u] = prob_exact<T>(psi, base + t + u, diag_stride);
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      s = __dadd_rn(s, v[u]);
-      if (CHECKPOINTS && ((t + u + 1) & (ck - 1)) == 0) out[(base + t + u) / ck] = s;
-    }
-  }
-  for (; t < L; ++t) {
-    s = __dadd_rn(s, prob_exact<T>(psi, base + t, diag_stride));
-    if (CHECKPOINTS && ((t + 1) & (ck - 1)) == 0) out[(base + t) / ck] = s;
-  }
-  if (!CHECKPOINTS) out[j] = s;
-}
-
-// P[0] = 0, P[j + 1] = fl(P[j] + idxs[j]): the reference's running sum.
-__global__ void k_seq_prefix(const double *__restrict__ idxs, uint64_t nblocks, double *__restrict__ P) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double p = 0.0;
-  P[0] = 0.0;
-  for (uint64_t j = 0; j < nblocks; ++j) {
-    p = __dadd_rn(p, idxs[j]);
-    P[j + 1] = p;
-  }
-}
-
-// One thread per shot.  n >= isz: the block from P, the checkpoint within
-// the block, then the walk; n < isz: the walk from index 0.
-template <typename T>
-__global__ void __launch_bounds__(256) k_sample_exact(const T *__restrict__ psi, uint64_t END, uint64_t nblocks,
-                                                      uint64_t L, uint64_t diag_stride, const double *__restrict__ P,
-                                                      const double *__restrict__ cps, uint64_t ck,
-                                                      const double *__restrict__ rnds, uint64_t shots,
-                                                      uint64_t *__restrict__ out) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < shots; s += stride) {
-    const double r = rnds[s];
-    double p = 0.0;
-    uint64_t k = 0;
-    if (nblocks) {
-      // first block j with r < P[j + 1] (P is non-decreasing)
-      uint64_t lo = 0, hi = nblocks;
-      while (lo < hi) {
-        const uint64_t mid = (lo + hi) >> 1;
-        if (r < P[mid + 1]) hi = mid; else lo = mid + 1;
-      }
-      if (lo == nblocks) {  // past the last block: the reference's walk ends at END
-        out[s] = END;
-        continue;
-      }
-      const uint64_t j = lo;
-      p = P[j];
-      k = j * L;
-      if (cps) {
-        const uint64_t ncp = L / ck;
-        const double *c = cps + j * ncp;
-        // first checkpoint of the block with r < c[m]
-        uint64_t a = 0, b = ncp;
-        while (a < b) {
-          const uint64_t mid = (a + b) >> 1;
-          if (r < c[mid]) b = mid; else a = mid + 1;
-        }
-        if (a == ncp) {  // r falls in the rounding gap after the block: walk on
-          p = c[ncp - 1];
-          k = (j + 1) * L;
-        } else if (a) {
-          p = c[a - 1];
-          k = j * L + a * ck;
-        }
-      }
-    }
-    for (; k < END - 1; ++k) {
-      p = __dadd_rn(p, prob_exact<T>(psi, k, diag_stride));
-      if (r < p) break;
-    }
-    out[s] = k;
-  }
-}
-
 template <typename T>
 T *st(Device &dev) { return reinterpret_cast<T *>(dev.state); }
 
@@ -1297,55 +1169,6 @@ void probabilities_all(Device &dev, double *d_out) {
   check_launch("probabilities kernel");
 }
 
-void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out, uint64_t amp_offset,
-                    int nbits) {
-  const int n = nbits >= 0 ? nbits : sample_bits(dev);
-  const int isz = dev.sample_index_size;
-  const uint64_t END = 1ULL << n;
-  const uint64_t ds = diag_stride(dev);
-  const uint64_t nblocks = n >= isz ? 1ULL << isz : 0;
-  const uint64_t L = nblocks ? END >> isz : 0;
-  // blocks of up to 1024 amplitudes are walked from P[j] by each shot; longer
-  // blocks keep every 1024th partial sum of the walk
-  const uint64_t ck = 1024;
-  const bool use_cps = L > ck;
-  const uint64_t ncps = use_cps ? END / ck : 0;
-  // idxs[nblocks], P[nblocks + 1], checkpoints[END / ck]
-  grow(dev.aux, dev.aux_cap, sizeof(double) * (2 * nblocks + 1 + ncps + 1));
-  double *idxs = reinterpret_cast<double *>(dev.aux);
-  double *P = idxs + nblocks;
-  double *cps = use_cps ? P + nblocks + 1 : nullptr;
-  if (nblocks) {
-    const unsigned g = (unsigned)((nblocks + 31) / 32);
-    if (dev.dbl) {
-      k_seq_blocks<double2, false><<<g, 32, 0, dev.stream>>>(st<double2>(dev) + amp_offset, nblocks, L, ds, nullptr,
-                                                              idxs, ck);
-    } else {
-      k_seq_blocks<float2, false><<<g, 32, 0, dev.stream>>>(st<float2>(dev) + amp_offset, nblocks, L, ds, nullptr,
-                                                             idxs, ck);
-    }
-    check_launch("sampling block sums");
-    k_seq_prefix<<<1, 32, 0, dev.stream>>>(idxs, nblocks, P);
-    check_launch("sampling block prefix");
-    if (use_cps) {
-      if (dev.dbl)
-        k_seq_blocks<double2, true><<<g, 32, 0, dev.stream>>>(st<double2>(dev) + amp_offset, nblocks, L, ds, P, cps,
-                                                               ck);
-      else
-        k_seq_blocks<float2, true><<<g, 32, 0, dev.stream>>>(st<float2>(dev) + amp_offset, nblocks, L, ds, P, cps,
-                                                              ck);
-      check_launch("sampling block walk");
-    }
-  }
-  const int g2 = grid_for(shots, 256, 16);
-  if (dev.dbl)
-    k_sample_exact<double2><<<g2, 256, 0, dev.stream>>>(st<double2>(dev) + amp_offset, END, nblocks, L, ds, P, cps,
-                                                        ck, d_rnds, shots, d_out);
-  else
-    k_sample_exact<float2><<<g2, 256, 0, dev.stream>>>(st<float2>(dev) + amp_offset, END, nblocks, L, ds, P, cps,
-                                                       ck, d_rnds, shots, d_out);
-  check_launch("sampling search");
-}
 
 // ============================ complex128 on tensor cores ============================
 // Dense k-qubit gates (k = 4, 5) on a complex128 state with FP64 emulated by

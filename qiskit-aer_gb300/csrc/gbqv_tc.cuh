@@ -5,7 +5,9 @@
 // Every wait on an mbarrier is bounded: after kWaitNs of wall time (or when
 // another thread of the CTA has already given up) it returns false, and the
 // caller records the failure and leaves its loop, so a broken pipeline ends
-// the kernel with an error status instead of hanging the GPU.
+// the kernel with an error status instead of hanging the GPU.  Waiting warps
+// are parked by the hardware (try_wait with a suspend-time hint) rather than
+// spinning, which kept the issue slots and integer pipe busy with polling.
 #pragma once
 
 #include <cstdint>
@@ -42,6 +44,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// The same with a suspend-time hint: the warp is parked until the phase
+// completes or about `hint_ns` pass, instead of spinning on issue slots.
+__device__ __forceinline__ bool mbar_try_wait_parked(uint32_t bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, "
+      "p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
 // Waits for the completion of the phase with the given parity.  Returns false
 // (and raises *abort) after kWaitNs, or returns false at once when *abort is
 // already raised by another thread.  sleep_ns > 0 backs off between polls
@@ -53,11 +67,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 1; it < (1u << 26); ++it) {
     if (sleep_ns) __nanosleep(sleep_ns);
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 31) == 0) {
-      if (*abort) return false;
-      if (globaltimer() - t0 > kWaitNs) break;
-    }
+    // parked for up to 20 us per try: the hardware wakes the warp when the
+    // phase completes, so a waiting warp takes no issue slots
+    if (mbar_try_wait_parked(bar, parity, 20000u)) return true;
+    if (*abort) return false;
+    if ((it & 7) == 0 && globaltimer() - t0 > kWaitNs) break;
   }
   *abort = 1;
   return false;
