@@ -253,29 +253,48 @@ __host__ __device__ __forceinline__ uint32_t funnel_l(uint32_t lo, uint32_t hi, 
 #endif
 }
 
-__host__ __device__ __forceinline__ double words_to_double(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3,
-                                                           uint32_t u4, uint32_t u5, int ebase) {
+// The two steps separately (the tcgen05 epilogue checks the fast path's
+// condition for a whole chunk of outputs at once): words -> the ones'
+// complement magnitude (ah, al) of v and its sign mask sg, then the double.
+__host__ __device__ __forceinline__ void words_to_mag(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3, uint32_t u4,
+                                                      uint32_t u5, uint32_t &ah, uint32_t &al, uint32_t &sg) {
   constexpr uint32_t kPair = 257u * 0x4B400000u;
   constexpr uint64_t kBias = (uint64_t)kPair * 0x100010001ULL;  // kPair * (2^32 + 2^16 + 1) mod 2^64
   const uint32_t p01 = u0 * 256u + u1, p23 = u2 * 256u + u3, p45 = u4 * 256u + u5;
-  const uint64_t v = ((uint64_t)p01 << 32) + ((uint64_t)p23 << 16) + (uint64_t)p45 - kBias;
-  const uint32_t sg = (uint32_t)((int32_t)(uint32_t)(v >> 32) >> 31);
-  const uint32_t ah = (uint32_t)(v >> 32) ^ sg, al = (uint32_t)v ^ sg;
-  if (ah != 0 && ebase >= 32) {
-    const uint32_t lz = (uint32_t)clz64((uint64_t)ah << 32);
-    const uint32_t nh = funnel_l(al, ah, lz), nl = al << lz;
-    // mantissa bits 52..0 = n >> 11; the implicit bit adds one to the
-    // exponent field, hence e1 = biased exponent - 1
-    const uint32_t mhi = nh >> 11, mlo = (nh << 21) | (nl >> 11);
-    const uint32_t e1 = (uint32_t)(ebase - (int)lz);
-    return bitsd(((uint64_t)(mhi + (e1 << 20) + (sg << 31)) << 32) | mlo);
-  }
+  // v = p01 2^32 + p23 2^16 + p45 - kBias: the register pair (p01, p45) plus one wide multiply-add
+  const uint64_t v = ((((uint64_t)p01 << 32) | p45) + (uint64_t)p23 * 0x10000u) - kBias;
+  sg = (uint32_t)((int32_t)(uint32_t)(v >> 32) >> 31);
+  ah = (uint32_t)(v >> 32) ^ sg;
+  al = (uint32_t)v ^ sg;
+}
+
+// The double from (ah, al, sg) when ah != 0 and ebase >= 32: normalisation
+// by two 32-bit funnel shifts, no range check.
+__host__ __device__ __forceinline__ double mag_to_double_fast(uint32_t ah, uint32_t al, uint32_t sg, int ebase) {
+  const uint32_t lz = (uint32_t)clz64((uint64_t)ah << 32);
+  const uint32_t nh = funnel_l(al, ah, lz), nl = al << lz;
+  const uint32_t mhi = nh >> 11, mlo = (nh << 21) | (nl >> 11);
+  const uint32_t e1 = (uint32_t)(ebase - (int)lz);
+  return bitsd(((uint64_t)(mhi + (e1 << 20) + (sg << 31)) << 32) | mlo);
+}
+
+// Any (ah, al, sg): the fast form when it applies, else the general 64-bit
+// normalisation (zero and results below 2^-1022 give 0).
+__host__ __device__ __forceinline__ double mag_to_double(uint32_t ah, uint32_t al, uint32_t sg, int ebase) {
+  if (ah != 0 && ebase >= 32) return mag_to_double_fast(ah, al, sg, ebase);
   const uint64_t a = ((uint64_t)ah << 32) | al;
   const int lz = clz64(a);
   const uint64_t n = shl64(a, (uint32_t)lz);
   const int e1 = ebase - lz;
   const uint64_t bits = (n >> 11) + ((uint64_t)(((uint32_t)e1 << 20) | (sg & 0x80000000u)) << 32);
   return (a == 0 || e1 < 0) ? 0.0 : bitsd(bits);
+}
+
+__host__ __device__ __forceinline__ double words_to_double(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3,
+                                                           uint32_t u4, uint32_t u5, int ebase) {
+  uint32_t ah, al, sg;
+  words_to_mag(u0, u1, u2, u3, u4, u5, ah, al, sg);
+  return mag_to_double(ah, al, sg, ebase);
 }
 
 // The same from fp32 level sums (the magic add done here).

@@ -109,13 +109,6 @@ __host__ __device__ constexpr uint32_t core_off(uint32_t row, uint32_t k) {
   return (row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
-// output real i of the loaded chunk (TMEM words 0x4B400000 + T_l); ebase =
-// row key + column key - 1017 (the biased exponent - 1 of a value whose
-// leading bit is bit 63 of v)
-__device__ __forceinline__ double combine(const uint32_t (&T)[6][8], int i, int ebase) {
-  return oz::words_to_double(T[0][i], T[1][i], T[2][i], T[3][i], T[4][i], T[5][i], ebase);
-}
-
 template <int EH>
 __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     k_dense_tc4(double2 *psi, const __grid_constant__ TcParams p, const uint4 *__restrict__ gmat, int *status) {
@@ -341,13 +334,32 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
         tc::tmem_wait_ld();
 #pragma unroll
         for (int l = 0; l < 6; ++l) tc::pin(T[l]);
-        if (live) {
+        // the chunk's 8 outputs as magnitude words; one vote picks the
+        // branch-free conversion for the whole warp (every output at least
+        // 2^-23 of row max x group max: the usual case)
+        uint32_t ah[8], al[8], sg[8];
+        int eb[8];
+        bool fast = true;
 #pragma unroll
-          for (int jj = 0; jj < 4; ++jj) {
-            const double re = combine(T, 2 * jj, p.rowbase[8 * q + 2 * jj] + ck);
-            const double im = combine(T, 2 * jj + 1, p.rowbase[8 * q + 2 * jj + 1] + ck);
-            psi[base + p.offs[4 * q + jj]] = make_double2(re, im);
+        for (int i = 0; i < 8; ++i) {
+          oz::words_to_mag(T[0][i], T[1][i], T[2][i], T[3][i], T[4][i], T[5][i], ah[i], al[i], sg[i]);
+          eb[i] = p.rowbase[8 * q + i] + ck;
+          fast = fast && ah[i] != 0 && eb[i] >= 32;
+        }
+        if (__all_sync(0xffffffffu, fast || !live)) {
+          if (live) {
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj)
+              psi[base + p.offs[4 * q + jj]] =
+                  make_double2(oz::mag_to_double_fast(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
+                               oz::mag_to_double_fast(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
           }
+        } else if (live) {
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj)
+            psi[base + p.offs[4 * q + jj]] =
+                make_double2(oz::mag_to_double(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
+                             oz::mag_to_double(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
         }
       }
       tc::fence_before_sync();
