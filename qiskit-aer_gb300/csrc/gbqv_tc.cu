@@ -316,8 +316,8 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * 256u;
     uint64_t tile = blockIdx.x + (uint64_t)b * gridDim.x;
     for (uint32_t c = 0; tile < ntiles; tile += stride2, ++c) {
-      bool ok = tc::mbar_wait(accf(b), c & 1, abort_flag);
-      ok = ok && tc::mbar_wait(full(b), c & 1, abort_flag);  // producer's colkey write
+      bool ok = tc::mbar_wait(accf(b), c & 1, abort_flag, 64);
+      ok = ok && tc::mbar_wait(full(b), c & 1, abort_flag, 64);  // producer's colkey write
       if (!__all_sync(0xffffffffu, ok)) break;
       tc::fence_after_sync();
       const int ck = colkey[b * kTcGroups + m];
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     uint32_t issued = 0;
     int slot = 0;
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i, slot = slot == kRawStages - 1 ? 0 : slot + 1) {
-      if (i >= kRawStages && !tc::mbar_wait(raw_empty(slot), (i / kRawStages - 1) & 1, abort_flag, 64)) break;
+      if (i >= kRawStages && !tc::mbar_wait(raw_empty(slot), (i / kRawStages - 1) & 1, abort_flag, 256)) break;
       const uint64_t first = insert_zeros_k4(tile * kTcGroups, p.lowmask);
       const uint32_t dst = tc::smem_u32(smem + kOffRaw + slot * kRawStage);
       tc::mbar_arrive_expect_tx(raw_full(slot), kRawStage);
@@ -395,8 +395,8 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = (int)(i & 1);
       const uint32_t c = i >> 1;
-      if (!tc::mbar_wait(full(b), c & 1, abort_flag, 32)) break;
-      if (c >= 1 && !tc::mbar_wait(acce(b), (c - 1) & 1, abort_flag, 32)) break;
+      if (!tc::mbar_wait(full(b), c & 1, abort_flag, 64)) break;
+      if (c >= 1 && !tc::mbar_wait(acce(b), (c - 1) & 1, abort_flag, 64)) break;
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(smem + kOffStage + b * kStageBytes);
       const uint32_t d0 = tmem + (uint32_t)b * 256u;

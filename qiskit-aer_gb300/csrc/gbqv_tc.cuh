@@ -66,12 +66,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 1; it < (1u << 26); ++it) {
+    // a back-off (roles that are not on the critical path) and a try that
+    // may park the warp in hardware keep polling off the issue slots; the
+    // abort flag and the clock are read every 16th try
     if (sleep_ns) __nanosleep(sleep_ns);
-    // parked for up to 20 us per try: the hardware wakes the warp when the
-    // phase completes, so a waiting warp takes no issue slots
     if (mbar_try_wait_parked(bar, parity, 20000u)) return true;
-    if (*abort) return false;
-    if ((it & 7) == 0 && globaltimer() - t0 > kWaitNs) break;
+    if ((it & 15) == 0) {
+      if (*abort) return false;
+      if (globaltimer() - t0 > kWaitNs) break;
+    }
   }
   *abort = 1;
   return false;
