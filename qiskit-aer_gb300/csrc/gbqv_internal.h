@@ -155,6 +155,10 @@ bool tc_tensor_map(Device &dev, uint32_t L, void *out);
 bool tc_runs_map(Device &dev, const reg_t &qubits, uint32_t L, void *out, uint32_t &rank, uint32_t &nreq,
                  uint32_t *row_off);
 int sm_count();
+// complex128 dense 5-qubit gates on tcgen05 (gbqv_tc.cu): usable when the
+// highest target lies above the tile's run bits
+bool tc5_usable(const Device &dev, const reg_t &qubits);
+void launch_dense_tc5(Device &dev, const reg_t &qubits, const cd *mat);
 // complex64 dense 4-qubit gates on tcgen05 (3xTF32, gbqv_tc64.cu)
 bool tc64_dense_available(const Device &dev, int k);
 void launch_dense_tc64(Device &dev, const reg_t &qubits, const cd *mat);

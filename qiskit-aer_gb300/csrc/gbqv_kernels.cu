@@ -1461,6 +1461,8 @@ void launch_dense_tensor(Device &dev, const reg_t &qubits, const cd *mat) {
     launch_dense_tc(dev, qubits, mat);
   else if (qubits.size() == 4)
     dense_oz<4>(dev, qubits, mat);
+  else if (tc5_usable(dev, qubits))
+    launch_dense_tc5(dev, qubits, mat);
   else
     dense_oz<5>(dev, qubits, mat);
 }

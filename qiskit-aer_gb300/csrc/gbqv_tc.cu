@@ -109,6 +109,99 @@ __host__ __device__ constexpr uint32_t core_off(uint32_t row, uint32_t k) {
   return (row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
+// A producer thread's share of a group row: the digit words (lo, hi) of its
+// 8 amplitudes' 16 magnitudes and the (re, im) sign pairs (bit 15 <- sign of
+// re, bit 31 <- sign of im, byte sign replication).  near: every shift of
+// the warp below 32 (the two-funnel-shift split).
+__device__ __forceinline__ void split_words8(const double2 (&v)[8], const uint32_t (&ex)[16], uint32_t E3, bool near,
+                                             uint32_t (&lo)[16], uint32_t (&hi)[16], uint32_t (&sb)[8]) {
+  if (near) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t xh = (uint32_t)__double2hiint(v[j].x), yh = (uint32_t)__double2hiint(v[j].y);
+      const uint64_t rw = oz::split_word_abs_near(xh, (uint32_t)__double2loint(v[j].x), E3 - ex[2 * j]);
+      const uint64_t iw = oz::split_word_abs_near(yh, (uint32_t)__double2loint(v[j].y), E3 - ex[2 * j + 1]);
+      lo[2 * j] = (uint32_t)rw;
+      hi[2 * j] = (uint32_t)(rw >> 32);
+      lo[2 * j + 1] = (uint32_t)iw;
+      hi[2 * j + 1] = (uint32_t)(iw >> 32);
+      sb[j] = tc::prmt(xh, yh, 0xF0B0);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint64_t rw = oz::split_word_abs(v[j].x, ex[2 * j], E3);
+      const uint64_t iw = oz::split_word_abs(v[j].y, ex[2 * j + 1], E3);
+      lo[2 * j] = (uint32_t)rw;
+      hi[2 * j] = (uint32_t)(rw >> 32);
+      lo[2 * j + 1] = (uint32_t)iw;
+      hi[2 * j + 1] = (uint32_t)(iw >> 32);
+      sb[j] = tc::prmt((uint32_t)__double2hiint(v[j].x), (uint32_t)__double2hiint(v[j].y), 0xF0B0);
+    }
+  }
+}
+
+// The six fp16 digit planes of those 16 reals: K chunks 2h, 2h + 1 of group
+// row m in the K-major core-matrix layout of a stage (32 reals per row).
+__device__ __forceinline__ void store_planes8(unsigned char *stage, int m, int h, const uint32_t (&lo)[16],
+                                              const uint32_t (&hi)[16], const uint32_t (&sb)[8]) {
+  const uint32_t K64 = 0x64646464u;
+#pragma unroll
+  for (int q2 = 0; q2 < 2; ++q2) {
+    // the chunk's 8 reals (amplitudes 4q..4q+3, re/im): per amplitude the
+    // (re, im) sign pair as half2 (+-1, +-1) with the bias constants
+    // times it, so that one HFMA2 per plane word both removes the fp16
+    // bias and applies the signs
+    uint32_t sg[4], c1[4], c0[4];
+    const uint32_t *lo8 = lo + 8 * q2, *hi8 = hi + 8 * q2;
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      sg[jj] = (sb[4 * q2 + jj] & 0x80008000u) | 0x3C003C00u;
+      c1[jj] = tc::hmul2(sg[jj], 0xE480E480u);  // -1152 * sign
+      c0[jj] = tc::hmul2(sg[jj], 0xE600E600u);  // -1536 * sign
+    }
+    unsigned char *row = stage + core_off(m, 8 * (2 * h + q2));
+    // digits 1..5 are byte (5 - s) of the word plus 128: fp16 0x64xx =
+    // 1152 + |d| after a byte permute
+    uint32_t w[4];
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x5140);
+      w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
+    }
+    *reinterpret_cast<uint4 *>(row + 5 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x5140);
+      w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
+    }
+    *reinterpret_cast<uint4 *>(row + 4 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x7362);
+      w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
+    }
+    *reinterpret_cast<uint4 *>(row + 3 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x7362);
+      w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
+    }
+    *reinterpret_cast<uint4 *>(row + 2 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const uint32_t g = tc::prmt(hi8[2 * jj], hi8[2 * jj + 1], 0x0040);
+      w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
+    }
+    *reinterpret_cast<uint4 *>(row + 1 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
+    // digit 0: bytes 5-6 of the word are the fp16 bits of 1536 + |d_0|
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj)
+      w[jj] = tc::hfma2(tc::prmt(hi8[2 * jj], hi8[2 * jj + 1], 0x6521), sg[jj], c0[jj]);
+    *reinterpret_cast<uint4 *>(row) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
 template <int EH>
 __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     k_dense_tc4(double2 *psi, const __grid_constant__ TcParams p, const uint4 *__restrict__ gmat, int *status) {
@@ -221,91 +314,12 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       // for a dense state); otherwise the general 64-bit shift
       const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E3);
       // digit words of the 16 magnitudes and the sign pairs, before waiting
-      // for the stage: bit 15 <- sign of re, bit 31 <- sign of im (byte sign
-      // replication)
+      // for the stage
       uint32_t lo[16], hi[16], sb[8];
-      if (near) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const uint32_t xh = (uint32_t)__double2hiint(v[j].x), yh = (uint32_t)__double2hiint(v[j].y);
-          const uint64_t rw = oz::split_word_abs_near(xh, (uint32_t)__double2loint(v[j].x), E3 - ex[2 * j]);
-          const uint64_t iw = oz::split_word_abs_near(yh, (uint32_t)__double2loint(v[j].y), E3 - ex[2 * j + 1]);
-          lo[2 * j] = (uint32_t)rw;
-          hi[2 * j] = (uint32_t)(rw >> 32);
-          lo[2 * j + 1] = (uint32_t)iw;
-          hi[2 * j + 1] = (uint32_t)(iw >> 32);
-          sb[j] = tc::prmt(xh, yh, 0xF0B0);
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const uint64_t rw = oz::split_word_abs(v[j].x, ex[2 * j], E3);
-          const uint64_t iw = oz::split_word_abs(v[j].y, ex[2 * j + 1], E3);
-          lo[2 * j] = (uint32_t)rw;
-          hi[2 * j] = (uint32_t)(rw >> 32);
-          lo[2 * j + 1] = (uint32_t)iw;
-          hi[2 * j + 1] = (uint32_t)(iw >> 32);
-          sb[j] = tc::prmt((uint32_t)__double2hiint(v[j].x), (uint32_t)__double2hiint(v[j].y), 0xF0B0);
-        }
-      }
+      split_words8(v, ex, E3, near, lo, hi, sb);
       const bool ok = c == 0 || tc::mbar_wait(sempty(b), (c - 1) & 1, abort_flag);
       if (!__all_sync(0xffffffffu, ok)) break;
-      unsigned char *stage = smem + kOffStage + b * kStageBytes;
-      const uint32_t K64 = 0x64646464u;
-#pragma unroll
-      for (int q2 = 0; q2 < 2; ++q2) {
-        // the chunk's 8 reals (amplitudes 4q..4q+3, re/im): per amplitude the
-        // (re, im) sign pair as half2 (+-1, +-1) with the bias constants
-        // times it, so that one HFMA2 per plane word both removes the fp16
-        // bias and applies the signs
-        uint32_t sg[4], c1[4], c0[4];
-        const uint32_t *lo8 = lo + 8 * q2, *hi8 = hi + 8 * q2;
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          sg[jj] = (sb[4 * q2 + jj] & 0x80008000u) | 0x3C003C00u;
-          c1[jj] = tc::hmul2(sg[jj], 0xE480E480u);  // -1152 * sign
-          c0[jj] = tc::hmul2(sg[jj], 0xE600E600u);  // -1536 * sign
-        }
-        unsigned char *row = stage + core_off(m, 8 * (2 * h + q2));
-        // digits 1..5 are byte (5 - s) of the word plus 128: fp16 0x64xx =
-        // 1152 + |d| after a byte permute
-        uint32_t w[4];
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x5140);
-          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
-        }
-        *reinterpret_cast<uint4 *>(row + 5 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x5140);
-          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
-        }
-        *reinterpret_cast<uint4 *>(row + 4 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x7362);
-          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
-        }
-        *reinterpret_cast<uint4 *>(row + 3 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(lo8[2 * jj], lo8[2 * jj + 1], 0x7362);
-          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4342), sg[jj], c1[jj]);
-        }
-        *reinterpret_cast<uint4 *>(row + 2 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const uint32_t g = tc::prmt(hi8[2 * jj], hi8[2 * jj + 1], 0x0040);
-          w[jj] = tc::hfma2(tc::prmt(g, K64, 0x4140), sg[jj], c1[jj]);
-        }
-        *reinterpret_cast<uint4 *>(row + 1 * kPlaneBytes) = make_uint4(w[0], w[1], w[2], w[3]);
-        // digit 0: bytes 5-6 of the word are the fp16 bits of 1536 + |d_0|
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj)
-          w[jj] = tc::hfma2(tc::prmt(hi8[2 * jj], hi8[2 * jj + 1], 0x6521), sg[jj], c0[jj]);
-        *reinterpret_cast<uint4 *>(row) = make_uint4(w[0], w[1], w[2], w[3]);
-      }
+      store_planes8(smem + kOffStage + b * kStageBytes, m, h, lo, hi, sb);
       if (h == 0) colkey[b * kTcGroups + m] = key;
       tc::fence_async_smem();
       tc::mbar_arrive(full(b));
@@ -316,8 +330,8 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * 256u;
     uint64_t tile = blockIdx.x + (uint64_t)b * gridDim.x;
     for (uint32_t c = 0; tile < ntiles; tile += stride2, ++c) {
-      bool ok = tc::mbar_wait(accf(b), c & 1, abort_flag, 64);
-      ok = ok && tc::mbar_wait(full(b), c & 1, abort_flag, 64);  // producer's colkey write
+      bool ok = tc::mbar_wait(accf(b), c & 1, abort_flag);
+      ok = ok && tc::mbar_wait(full(b), c & 1, abort_flag);  // producer's colkey write
       if (!__all_sync(0xffffffffu, ok)) break;
       tc::fence_after_sync();
       const int ck = colkey[b * kTcGroups + m];
@@ -371,7 +385,7 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     uint32_t issued = 0;
     int slot = 0;
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i, slot = slot == kRawStages - 1 ? 0 : slot + 1) {
-      if (i >= kRawStages && !tc::mbar_wait(raw_empty(slot), (i / kRawStages - 1) & 1, abort_flag, 256)) break;
+      if (i >= kRawStages && !tc::mbar_wait(raw_empty(slot), (i / kRawStages - 1) & 1, abort_flag, 64)) break;
       const uint64_t first = insert_zeros_k4(tile * kTcGroups, p.lowmask);
       const uint32_t dst = tc::smem_u32(smem + kOffRaw + slot * kRawStage);
       tc::mbar_arrive_expect_tx(raw_full(slot), kRawStage);
@@ -395,8 +409,8 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = (int)(i & 1);
       const uint32_t c = i >> 1;
-      if (!tc::mbar_wait(full(b), c & 1, abort_flag, 64)) break;
-      if (c >= 1 && !tc::mbar_wait(acce(b), (c - 1) & 1, abort_flag, 64)) break;
+      if (!tc::mbar_wait(full(b), c & 1, abort_flag, 32)) break;
+      if (c >= 1 && !tc::mbar_wait(acce(b), (c - 1) & 1, abort_flag, 32)) break;
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(smem + kOffStage + b * kStageBytes);
       const uint32_t d0 = tmem + (uint32_t)b * 256u;
@@ -415,6 +429,313 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     }
     // every MMA issued above has completed once `done` flips (bounded wait,
     // independent of the abort flag so TMEM is never freed under a live MMA)
+    tc::mma_commit(done);
+    int never = 0;
+    tc::mbar_wait(done, 0, &never);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == kMmaWarp) tc::tmem_dealloc(tmem, kTmemCols);
+  if (tid == 0 && *abort_flag) atomicExch(status, 1);
+}
+
+// ---------------------------------------------------------------------------
+// 5-qubit gates (k_dense_tc5): a group is 32 amplitudes (64 reals).  The
+// tile's 128 groups are taken in two K-halves, split by the highest target:
+// half kh holds local amplitudes 16 kh .. 16 kh + 15 of every group, which is
+// a 4-qubit tile (32 KB raw, 32 reals per row) on the four lower targets.
+// Both halves of a tile share one group key (the exponent pass reads both
+// raw halves first).  The two output halves (output reals 0-31, 32-63) take
+// the two TMEM accumulators (columns 0 and 256) the 4-qubit kernel gives its
+// pipeline lanes, so epilogue warpgroups 0-1 drain output half 0 and 2-3
+// output half 1 of the same tile.  Per tile the MMA thread issues, for each
+// output half o and K-half kh, the 12 digit-plane MMAs of the 4-qubit kernel
+// with B = the matrix planes of rows 32 o .. 32 o + 31, columns 32 kh ..
+// 32 kh + 31: 48 MMAs and two accumulator preloads.  Shared memory: matrix
+// planes 48 KB (6 planes x 64 rows x 64 reals, rows of an output half
+// contiguous across planes), two K-half plane stages of 48 KB, two raw
+// K-half slots of 32 KB.
+constexpr int k5MatBytes = 6 * 64 * 64 * 2;  // 48 KB
+constexpr int k5OffInit = k5MatBytes;
+constexpr int k5OffStage = k5OffInit + kInitABytes + kInitBBytes;
+constexpr int k5OffRaw = k5OffStage + 2 * kStageBytes;
+constexpr int k5OffKey = k5OffRaw + 2 * kRawStage;
+constexpr int k5OffBar = k5OffKey + 2 * kTcGroups * 4;
+constexpr int k5OffMisc = k5OffBar + 16 * 8;
+constexpr int k5Smem = k5OffMisc + 64 + 1024;
+static_assert(k5Smem <= 232448, "shared memory per CTA");
+static_assert(k5OffRaw % 1024 == 0, "raw slots on the swizzle period");
+
+struct Tc5Params {
+  CUtensorMap tmap;  // 2D, rows of 8 amplitudes, box = a run (swz = 1)
+  uint32_t swz;
+  uint64_t offs[32];      // amplitude offset of local amplitude j (targets sorted ascending)
+  uint64_t lowmask[5];
+  uint64_t hoff[32];      // amplitude offset of run r from the tile's first amplitude
+  uint64_t ngroups;
+  uint64_t ntiles;
+  uint32_t roff[16];      // byte offset in a raw K-half slot of local amplitude j (< 16) of group 0
+  uint32_t nhalf, runbytes;  // runs per K-half (runs [kh nhalf, (kh + 1) nhalf) form half kh)
+  uint16_t zl[kTcGroups];
+  int rowbase[64];        // row key - 1017 per output real
+};
+
+// byte offset of element (row, k) in the matrix operand: rows of 64 reals
+__host__ __device__ constexpr uint32_t core_off64(uint32_t row, uint32_t k) {
+  return (row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint64_t insert_zeros_k5(uint64_t g, const uint64_t *lowmask) {
+#pragma unroll
+  for (int j = 0; j < 5; ++j) g = ((g & ~lowmask[j]) << 1) | (g & lowmask[j]);
+  return g;
+}
+
+__global__ void __launch_bounds__(tc_threads<2>(), 1)
+    k_dense_tc5(double2 *psi, const __grid_constant__ Tc5Params p, const uint4 *__restrict__ gmat, int *status) {
+  constexpr int kThreads = tc_threads<2>(), kMmaWarp = 24;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+  int *colkey = reinterpret_cast<int *>(smem + k5OffKey);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + k5OffBar);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + k5OffMisc);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + k5OffMisc + 4);
+  // barriers, each with one ordered waiter sequence:
+  //   full[kh]  256 producer arrivals: K-half kh's planes written (MMA waits)
+  //   sfree[kh] MMA commit: stage kh read (producers wait)
+  //   accf[o]   MMA commit: output half o ready (its epilogue waits)
+  //   acce[o]   256 epilogue arrivals: output half o read (MMA waits)
+  //   keyf[p]   256 producer arrivals: colkey[p] written (epilogues wait)
+  //   raw_full[kh] loader + bytes (producers wait), raw_empty[kh] 256
+  //   producer arrivals (loader waits), done: final commit
+  const uint32_t bar0 = tc::smem_u32(bars);
+  auto full = [&](int x) { return bar0 + 8u * x; };
+  auto sfree = [&](int x) { return bar0 + 8u * (2 + x); };
+  auto accf = [&](int x) { return bar0 + 8u * (4 + x); };
+  auto acce = [&](int x) { return bar0 + 8u * (6 + x); };
+  auto keyf = [&](int x) { return bar0 + 8u * (8 + x); };
+  auto raw_full = [&](int x) { return bar0 + 8u * (10 + x); };
+  auto raw_empty = [&](int x) { return bar0 + 8u * (12 + x); };
+  const uint32_t done = bar0 + 8u * 14;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int x = 0; x < 2; ++x) {
+      tc::mbar_init(full(x), 2 * kTcGroups);
+      tc::mbar_init(sfree(x), 1);
+      tc::mbar_init(accf(x), 1);
+      tc::mbar_init(acce(x), 2 * kTcGroups);
+      tc::mbar_init(keyf(x), 2 * kTcGroups);
+      tc::mbar_init(raw_full(x), 1);
+      tc::mbar_init(raw_empty(x), 2 * kTcGroups);
+    }
+    tc::mbar_init(done, 1);
+    *abort_flag = 0;
+    tc::mbar_init_fence();
+  }
+  if (warp == kMmaWarp) {
+    tc::tmem_alloc(tc::smem_u32(tmem_slot), kTmemCols);
+    tc::tmem_relinquish();
+  }
+  {
+    uint4 *dst = reinterpret_cast<uint4 *>(smem);
+    for (int i = tid; i < k5MatBytes / 16; i += kThreads) dst[i] = gmat[i];
+    uint16_t *ia = reinterpret_cast<uint16_t *>(smem + k5OffInit);
+    for (int i = tid; i < (kInitABytes + kInitBBytes) / 2; i += kThreads) ia[i] = 0;
+    __syncthreads();
+    if (tid < kTcGroups) ia[(tid >> 3) * 128 + (tid & 7) * 8] = 0x3F80;  // bf16 1.0
+    if (tid < 6 * kTcReals) ia[kInitABytes / 2 + (tid >> 3) * 128 + (tid & 7) * 8] = 0x4B40;  // bf16 1.5 * 2^23
+  }
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint64_t ntiles = p.ntiles;
+
+  if (warp < 8) {
+    // ---------------- producers: two threads per group, 8 amplitudes of each K-half ----------------
+    const int m = 16 * warp + (lane & 15), h = lane >> 4;
+    uint32_t ro[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t off = p.roff[8 * h + j] + 16u * p.zl[m];
+      ro[j] = p.swz ? off ^ (((off >> 7) & 7u) << 4) : off;
+    }
+    uint64_t tile = blockIdx.x;
+    for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i) {
+      bool ok = tc::mbar_wait(raw_full(0), i & 1, abort_flag);
+      ok = ok && tc::mbar_wait(raw_full(1), i & 1, abort_flag);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      // the group key over both K-halves (exponent fields of the 32 reals)
+      uint32_t mx = 0, mn = 0x7ff;
+#pragma unroll
+      for (int kh = 0; kh < 2; ++kh) {
+        const unsigned char *raw = smem + k5OffRaw + kh * kRawStage;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const uint32_t xh = *reinterpret_cast<const uint32_t *>(raw + ro[j] + 4);
+          const uint32_t yh = *reinterpret_cast<const uint32_t *>(raw + ro[j] + 12);
+          const uint32_t ea = (xh >> 20) & 0x7ff, eb = (yh >> 20) & 0x7ff;
+          mx = max(mx, max(ea, eb));
+          mn = min(mn, min(ea, eb));
+        }
+      }
+      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+      const int key = mx ? (int)mx + 1 : 0;
+      const uint32_t E3 = (uint32_t)key + 3;
+      const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E3);
+      bool stop = false;
+#pragma unroll 1
+      for (int kh = 0; kh < 2; ++kh) {
+        const unsigned char *raw = smem + k5OffRaw + kh * kRawStage;
+        double2 v[8];
+        uint32_t ex[16];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          v[j] = *reinterpret_cast<const double2 *>(raw + ro[j]);
+          ex[2 * j] = ((uint32_t)__double2hiint(v[j].x) >> 20) & 0x7ff;
+          ex[2 * j + 1] = ((uint32_t)__double2hiint(v[j].y) >> 20) & 0x7ff;
+        }
+        tc::fence_async_smem();
+        tc::mbar_arrive(raw_empty(kh));
+        uint32_t lo[16], hi[16], sb[8];
+        split_words8(v, ex, E3, near, lo, hi, sb);
+        const bool freed = i == 0 || tc::mbar_wait(sfree(kh), (i - 1) & 1, abort_flag);
+        if (!__all_sync(0xffffffffu, freed)) {
+          stop = true;
+          break;
+        }
+        store_planes8(smem + k5OffStage + kh * kStageBytes, m, h, lo, hi, sb);
+        if (kh == 0) {
+          if (h == 0) colkey[(i & 1) * kTcGroups + m] = key;
+          tc::mbar_arrive(keyf(i & 1));
+        }
+        tc::fence_async_smem();
+        tc::mbar_arrive(full(kh));
+      }
+      if (stop) break;
+    }
+  } else if (warp < kMmaWarp) {
+    // ---------------- epilogues: warpgroups 0-1 output half 0, 2-3 output half 1 ----------------
+    const int e = warp - 8, o = (e >> 3) & 1, half = (e >> 2) & 1, quarter = warp & 3, m = 32 * quarter + lane;
+    const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)o * 256u;
+    uint64_t tile = blockIdx.x;
+    for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i) {
+      bool ok = tc::mbar_wait(accf(o), i & 1, abort_flag);
+      ok = ok && tc::mbar_wait(keyf(i & 1), (i >> 1) & 1, abort_flag);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      tc::fence_after_sync();
+      const int ck = colkey[(i & 1) * kTcGroups + m];
+      const uint64_t grp = tile * kTcGroups + m;
+      const bool live = grp < p.ngroups && ck != 0;
+      const uint64_t base = live ? insert_zeros_k5(grp, p.lowmask) : 0;
+#pragma unroll
+      for (int qq = 0; qq < 2; ++qq) {
+        const int q = half * 2 + qq;  // chunk of 8 output reals within the output half
+        uint32_t T[6][8];
+#pragma unroll
+        for (int l = 0; l < 6; ++l) tc::tmem_ld8(tbase + 32u * l + 8u * q, T[l]);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int l = 0; l < 6; ++l) tc::pin(T[l]);
+        uint32_t ah[8], al[8], sg[8];
+        int eb[8];
+        bool fast = true;
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+          oz::words_to_mag(T[0][x], T[1][x], T[2][x], T[3][x], T[4][x], T[5][x], ah[x], al[x], sg[x]);
+          eb[x] = p.rowbase[32 * o + 8 * q + x] + ck;
+          fast = fast && ah[x] != 0 && eb[x] >= 32;
+        }
+        const int a0 = 16 * o + 4 * q;  // first local amplitude of the chunk
+        if (__all_sync(0xffffffffu, fast || !live)) {
+          if (live) {
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj)
+              psi[base + p.offs[a0 + jj]] =
+                  make_double2(oz::mag_to_double_fast(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
+                               oz::mag_to_double_fast(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
+          }
+        } else if (live) {
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj)
+            psi[base + p.offs[a0 + jj]] =
+                make_double2(oz::mag_to_double(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
+                             oz::mag_to_double(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
+        }
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive(acce(o));
+    }
+  } else if (warp == kMmaWarp + 1 && lane == 0) {
+    // ---------------- loader: K-half kh of each tile into raw slot kh ----------------
+    uint64_t tile = blockIdx.x;
+    uint32_t issued = 0;
+    for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i) {
+      const uint64_t first = insert_zeros_k5(tile * kTcGroups, p.lowmask);
+      bool ok = true;
+      for (int kh = 0; kh < 2 && ok; ++kh) {
+        if (i >= 1 && !tc::mbar_wait(raw_empty(kh), (i - 1) & 1, abort_flag, 64)) {
+          ok = false;
+          break;
+        }
+        const uint32_t dst = tc::smem_u32(smem + k5OffRaw + kh * kRawStage);
+        tc::mbar_arrive_expect_tx(raw_full(kh), kRawStage);
+        for (uint32_t r = 0; r < p.nhalf; ++r) {
+          const uint64_t off = first + p.hoff[kh * p.nhalf + r];
+          if (p.swz)
+            tc::tma_load_2d(dst + r * p.runbytes, &p.tmap, 0, (int)(off >> 3), raw_full(kh));
+          else
+            tc::bulk_g2s(dst + r * p.runbytes, psi + off, p.runbytes, raw_full(kh));
+        }
+        issued = 2 * i + kh + 1;
+      }
+      if (!ok) break;
+    }
+    // copies in flight after an abort land before the CTA exits
+    int never = 0;
+    for (uint32_t x = issued > 2 ? issued - 2 : 0; x < issued; ++x)
+      tc::mbar_wait(raw_full((int)(x & 1)), (x >> 1) & 1, &never);
+  } else if (warp == kMmaWarp && lane == 0) {
+    // ---------------- MMA issuer ----------------
+    const uint32_t mat = tc::smem_u32(smem);
+    const uint32_t ini = tc::smem_u32(smem + k5OffInit);
+    uint64_t tile = blockIdx.x;
+    bool ok = true;
+    for (uint32_t i = 0; tile < ntiles && ok; tile += gridDim.x, ++i) {
+      for (int kh = 0; kh < 2 && ok; ++kh) {
+        if (!tc::mbar_wait(full(kh), i & 1, abort_flag, 32)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t a0 = tc::smem_u32(smem + k5OffStage + kh * kStageBytes);
+        for (int o = 0; o < 2; ++o) {
+          const uint32_t d0 = tmem + (uint32_t)o * 256u;
+          if (kh == 0) {
+            // output half o of the previous tile has been read: preload its accumulators
+            if (i >= 1 && !tc::mbar_wait(acce(o), (i - 1) & 1, abort_flag, 32)) {
+              ok = false;
+              break;
+            }
+            tc::fence_after_sync();
+            tc::mma_f16(d0, tc::smem_desc(ini, 128, 256), tc::smem_desc(ini + kInitABytes, 128, 256),
+                        tc::idesc_bf16_f32(128, 6 * kTcReals), 0);
+          }
+#pragma unroll
+          for (int s = 0; s < 6; ++s)
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk)
+              tc::mma_f16(d0 + 32u * s, tc::smem_desc(a0 + s * kPlaneBytes + kk * 256, 128, 512),
+                          tc::smem_desc(mat + (uint32_t)o * 24576u + (uint32_t)(4 * kh + 2 * kk) * 128u, 128, 1024),
+                          tc::idesc_f16_f32(128, 32 * (6 - s)), 1);
+          if (kh == 1) tc::mma_commit(accf(o));
+        }
+        if (ok) tc::mma_commit(sfree(kh));
+      }
+    }
     tc::mma_commit(done);
     int never = 0;
     tc::mbar_wait(done, 0, &never);
@@ -607,6 +928,99 @@ void tc_matrix4(const cd *mat, uint16_t *planes, int *rowkey) {
       for (int t = 0; t < 6; ++t) planes[core_off(32 * t + r, k) / 2] = half_bits(d[t]);
     }
   }
+}
+
+// Host: six fp16 digit planes of the real form of a 32x32 column-major
+// complex matrix (targets sorted), rows = output reals (2j + c), K = input
+// reals; matrix row r = 32 o + r' of plane t at operand row (6 o + t) 32 + r'.
+void tc_matrix5(const cd *mat, uint16_t *planes, int *rowkey) {
+  constexpr int D = 32, R = 64;
+  std::vector<double> A((size_t)R * R);
+  for (int j = 0; j < D; ++j)
+    for (int jp = 0; jp < D; ++jp) {
+      const cd z = mat[j + (size_t)D * jp];
+      A[(size_t)(2 * j) * R + 2 * jp] = z.real();
+      A[(size_t)(2 * j) * R + 2 * jp + 1] = -z.imag();
+      A[(size_t)(2 * j + 1) * R + 2 * jp] = z.imag();
+      A[(size_t)(2 * j + 1) * R + 2 * jp + 1] = z.real();
+    }
+  std::memset(planes, 0, k5MatBytes);
+  for (int r = 0; r < R; ++r) {
+    int key = 0;
+    for (int k = 0; k < R; ++k) key = std::max(key, oz::exp_key(A[(size_t)r * R + k]));
+    rowkey[r] = key;
+    const int o = r / 32, rr = r % 32;
+    for (int k = 0; k < R; ++k) {
+      int32_t d[6];
+      oz::bsum_digits(oz::split_bsum(A[(size_t)r * R + k], key), d);
+      for (int t = 0; t < 6; ++t) planes[core_off64((uint32_t)((6 * o + t) * 32 + rr), (uint32_t)k) / 2] = half_bits(d[t]);
+    }
+  }
+}
+
+// The 5-qubit tcgen05 kernel takes a gate whose highest target lies above
+// the tile's run bits (so that the two K-halves are two sets of runs) on a
+// state of at least 12 qubits; 4 targets below L at most keep a run within
+// the 2D descriptor's 256-row box.
+bool tc5_usable(const Device &dev, const reg_t &qubits) {
+  if (!dev.dbl || dev.tensor_c128 != 1 || qubits.size() != 5 || dev.n < 12) return false;
+  reg_t sq = qubits;
+  std::sort(sq.begin(), sq.end());
+  uint32_t L = 7;
+  for (uint64_t q : sq)
+    if (q < L) ++L;
+  return sq[4] >= L;
+}
+
+void launch_dense_tc5(Device &dev, const reg_t &qubits_in, const cd *mat_in) {
+  // targets sorted ascending, the matrix permuted to match
+  reg_t qubits = qubits_in;
+  std::sort(qubits.begin(), qubits.end());
+  int ob[5];
+  for (int b = 0; b < 5; ++b)
+    ob[b] = (int)(std::find(qubits_in.begin(), qubits_in.end(), qubits[b]) - qubits_in.begin());
+  auto perm = [&](int x) {
+    int y = 0;
+    for (int b = 0; b < 5; ++b) y |= ((x >> b) & 1) << ob[b];
+    return y;
+  };
+  std::vector<cd> matv(32 * 32);
+  for (int r = 0; r < 32; ++r)
+    for (int c = 0; c < 32; ++c) matv[r + 32 * c] = mat_in[perm(r) + 32 * perm(c)];
+  Tc5Params p;
+  local_offsets(qubits, p.offs);
+  sorted_masks(qubits, p.lowmask);
+  p.ngroups = dev.amps() >> 5;
+  p.ntiles = (p.ngroups + kTcGroups - 1) / kTcGroups;
+  uint64_t hoff[32];
+  uint32_t roff[32], nruns = 0, runbytes = 0;
+  tc_tile_geometry(qubits, hoff, roff, p.zl, nruns, runbytes, 16);
+  if (nruns < 2) throw Error(1, "5-qubit tensor kernel: the highest target must lie above the tile's runs");
+  for (uint32_t r = 0; r < nruns; ++r) p.hoff[r] = hoff[r];
+  for (int j = 0; j < 16; ++j) p.roff[j] = roff[j];
+  p.nhalf = nruns / 2;
+  p.runbytes = runbytes;
+  uint32_t L = 0;
+  while ((16u << L) < runbytes) ++L;
+  p.swz = tc_tensor_map(dev, L, &p.tmap) ? 1u : 0u;
+  std::vector<uint16_t> planes(k5MatBytes / 2);
+  int rowkey[64];
+  tc_matrix5(matv.data(), planes.data(), rowkey);
+  for (int r = 0; r < 64; ++r) p.rowbase[r] = rowkey[r] - 1017;
+  grow(dev.mat, dev.mat_cap, k5MatBytes);
+  cuda_check(cudaMemcpyAsync(dev.mat, planes.data(), k5MatBytes, cudaMemcpyHostToDevice, dev.stream),
+             "matrix upload");
+  int *status = tc_status_word(dev);
+  static bool attr = false;
+  if (!attr) {
+    cuda_check(cudaFuncSetAttribute(k_dense_tc5, cudaFuncAttributeMaxDynamicSharedMemorySize, k5Smem),
+               "tcgen05 5-qubit kernel attribute");
+    attr = true;
+  }
+  const uint64_t grid = std::min<uint64_t>(p.ntiles, (uint64_t)sm_count());
+  k_dense_tc5<<<(unsigned)grid, tc_threads<2>(), k5Smem, dev.stream>>>(reinterpret_cast<double2 *>(dev.state), p,
+                                                                      reinterpret_cast<const uint4 *>(dev.mat), status);
+  check_launch("tcgen05 complex128 5-qubit dense kernel");
 }
 
 bool tc_dense_available(const Device &dev, int k) {
