@@ -91,7 +91,7 @@ def test_five_qubit_tcgen05_against_oracle_and_fp64(n):
     psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
     psi /= np.linalg.norm(psi)
     placements = [[0, 1, 2, 3, n - 1], [n - 1, n - 2, n - 3, n - 4, n - 5], [n - 1, 0, 5, 2, 9],
-                  [11, 3, 7, 1, n - 1], [0, 1, 2, 3, 4]]
+                  [n - 2, 3, 7, 1, n - 1], [0, 1, 2, 3, 4]]
     placements += [[int(x) for x in rng.choice(n, 5, replace=False)] for _ in range(6)]
     ops = [(q, haar(rng, 32)) for q in placements]
     o = O.OracleQV(n, psi)
