@@ -313,12 +313,11 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       // largest: the split takes two 32-bit funnel shifts (the usual case
       // for a dense state); otherwise the general 64-bit shift
       const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E3);
-      // digit words of the 16 magnitudes and the sign pairs, before waiting
-      // for the stage
-      uint32_t lo[16], hi[16], sb[8];
-      split_words8(v, ex, E3, near, lo, hi, sb);
       const bool ok = c == 0 || tc::mbar_wait(sempty(b), (c - 1) & 1, abort_flag);
       if (!__all_sync(0xffffffffu, ok)) break;
+      // digit words of the 16 magnitudes and the sign pairs, then the planes
+      uint32_t lo[16], hi[16], sb[8];
+      split_words8(v, ex, E3, near, lo, hi, sb);
       store_planes8(smem + kOffStage + b * kStageBytes, m, h, lo, hi, sb);
       if (h == 0) colkey[b * kTcGroups + m] = key;
       tc::fence_async_smem();
