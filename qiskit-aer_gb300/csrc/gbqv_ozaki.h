@@ -9,7 +9,7 @@
 //     x ~= sum_{s=0..5} d_s * 2^(40 - 8 s) * 2^(E - 1071)
 // with balanced digits d_0 in [0, 256], d_1..5 in [-128, 127] (times the
 // sign of x): its significand aligned to the column maximum, rounded to 48
-// bits.
+// bits (truncated to 48 bits in the tcgen05 kernels' state split).
 // Matrix rows get the same treatment with their own row exponent R.  Every
 // product of two digits is <= 2^16, a dot product over K reals is
 // <= K * 2^16 (level 0) or <= K * 2^15 (levels >= 1, one digit is
@@ -187,26 +187,26 @@ __host__ __device__ __forceinline__ uint64_t shl64(uint64_t x, uint32_t s) {
 #endif
 }
 
-// Digit word of |x| against the column key E (E3 = E + 3), given x's biased
-// exponent field ex: the aligned significand rounded half up to 48 bits
-// (a <= 2^48, x ~= sign * a * 2^(E - 1071); symmetric in the sign, so no
-// drift of the norm, and exact values stay exact) plus 0x8080808080 +
-// 0x6600 * 2^40, so that bytes 0..3 and 4 are digits 5..2 and 1 plus 128 and
-// bits 40..55 are the fp16 bits of 1536 + d_0 (d_0 in [0, 256]); the digits
-// of x are these times the sign of x (balanced digits negate digit by
-// digit).  Rounding and the constant come from one add before the halving
-// shift.  Zeros (ex = 0) give digit 0 whenever E >= 50; groups whose
-// largest entry is below 2^-973 are the only ones where a zero turns into a
-// value of order 2^-1022.
-constexpr uint64_t kSplitK = 1ULL + 2ULL * 0x8080808080ULL + (0x6600ULL << 41);
+// Digit word of |x| against the column key E (E4 = E + 4), given x's biased
+// exponent field ex: the aligned significand truncated to 48 bits (a <
+// 2^48, x ~= sign * a * 2^(E - 1071); truncation toward zero is symmetric
+// in the sign, so the state's phases carry no bias, and exact values stay
+// exact) plus 0x8080808080 + 0x6600 * 2^40, so that bytes 0..3 and 4 are
+// digits 5..2 and 1 plus 128 and bits 40..55 are the fp16 bits of 1536 +
+// d_0 (d_0 in [0, 256]); the digits of x are these times the sign of x
+// (balanced digits negate digit by digit).  One 64-bit add of a constant
+// makes the balanced digits.  Zeros (ex = 0) give digit 0 whenever E >= 49;
+// groups whose largest entry is below 2^-974 are the only ones where a zero
+// turns into a value of order 2^-1022.
+constexpr uint64_t kSplitK = 0x8080808080ULL + (0x6600ULL << 40);
 
-__host__ __device__ __forceinline__ uint64_t split_word_abs(double x, uint32_t ex, uint32_t E3) {
+__host__ __device__ __forceinline__ uint64_t split_word_abs(double x, uint32_t ex, uint32_t E4) {
   const uint64_t m = (dbits(x) & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
-  return (shr64(m, E3 - ex) + kSplitK) >> 1;
+  return shr64(m, E4 - ex) + kSplitK;
 }
 
 // The same word with two 32-bit funnel shifts, for the common case of a
-// non-zero x whose shift E3 - ex is at most 31 (x within 2^-27 of its
+// non-zero x whose shift E4 - ex is at most 31 (x within 2^-26 of its
 // group's largest entry): xhi, xlo are the two words of x's bits.  Bit for
 // bit equal to split_word_abs there (checked on the host for every shift).
 __host__ __device__ __forceinline__ uint32_t funnel_r(uint32_t lo, uint32_t hi, uint32_t s) {  // s in [0, 31]
@@ -220,7 +220,7 @@ __host__ __device__ __forceinline__ uint32_t funnel_r(uint32_t lo, uint32_t hi, 
 __host__ __device__ __forceinline__ uint64_t split_word_abs_near(uint32_t xhi, uint32_t xlo, uint32_t s) {
   const uint32_t mh = (xhi & 0xFFFFFu) | 0x100000u;
   const uint64_t t = ((uint64_t)(mh >> s) << 32) | funnel_r(xlo, mh, s);
-  return (t + kSplitK) >> 1;
+  return t + kSplitK;
 }
 
 // Signed digits of x from its word (host side of the kernel's fp16 planes).

@@ -113,14 +113,14 @@ __host__ __device__ constexpr uint32_t core_off(uint32_t row, uint32_t k) {
 // 8 amplitudes' 16 magnitudes and the (re, im) sign pairs (bit 15 <- sign of
 // re, bit 31 <- sign of im, byte sign replication).  near: every shift of
 // the warp below 32 (the two-funnel-shift split).
-__device__ __forceinline__ void split_words8(const double2 (&v)[8], const uint32_t (&ex)[16], uint32_t E3, bool near,
+__device__ __forceinline__ void split_words8(const double2 (&v)[8], const uint32_t (&ex)[16], uint32_t E4, bool near,
                                              uint32_t (&lo)[16], uint32_t (&hi)[16], uint32_t (&sb)[8]) {
   if (near) {
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const uint32_t xh = (uint32_t)__double2hiint(v[j].x), yh = (uint32_t)__double2hiint(v[j].y);
-      const uint64_t rw = oz::split_word_abs_near(xh, (uint32_t)__double2loint(v[j].x), E3 - ex[2 * j]);
-      const uint64_t iw = oz::split_word_abs_near(yh, (uint32_t)__double2loint(v[j].y), E3 - ex[2 * j + 1]);
+      const uint64_t rw = oz::split_word_abs_near(xh, (uint32_t)__double2loint(v[j].x), E4 - ex[2 * j]);
+      const uint64_t iw = oz::split_word_abs_near(yh, (uint32_t)__double2loint(v[j].y), E4 - ex[2 * j + 1]);
       lo[2 * j] = (uint32_t)rw;
       hi[2 * j] = (uint32_t)(rw >> 32);
       lo[2 * j + 1] = (uint32_t)iw;
@@ -130,8 +130,8 @@ __device__ __forceinline__ void split_words8(const double2 (&v)[8], const uint32
   } else {
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const uint64_t rw = oz::split_word_abs(v[j].x, ex[2 * j], E3);
-      const uint64_t iw = oz::split_word_abs(v[j].y, ex[2 * j + 1], E3);
+      const uint64_t rw = oz::split_word_abs(v[j].x, ex[2 * j], E4);
+      const uint64_t iw = oz::split_word_abs(v[j].y, ex[2 * j + 1], E4);
       lo[2 * j] = (uint32_t)rw;
       hi[2 * j] = (uint32_t)(rw >> 32);
       lo[2 * j + 1] = (uint32_t)iw;
@@ -308,16 +308,16 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       tc::mbar_arrive(raw_empty(slot));
       mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
       const int key = mx ? (int)mx + 1 : 0;
-      const uint32_t E3 = (uint32_t)key + 3;
-      // every real of the warp non-zero and within 2^-27 of its group's
+      const uint32_t E4 = (uint32_t)key + 4;
+      // every real of the warp non-zero and within 2^-26 of its group's
       // largest: the split takes two 32-bit funnel shifts (the usual case
       // for a dense state); otherwise the general 64-bit shift
-      const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E3);
+      const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E4);
       const bool ok = c == 0 || tc::mbar_wait(sempty(b), (c - 1) & 1, abort_flag);
       if (!__all_sync(0xffffffffu, ok)) break;
       // digit words of the 16 magnitudes and the sign pairs, then the planes
       uint32_t lo[16], hi[16], sb[8];
-      split_words8(v, ex, E3, near, lo, hi, sb);
+      split_words8(v, ex, E4, near, lo, hi, sb);
       store_planes8(smem + kOffStage + b * kStageBytes, m, h, lo, hi, sb);
       if (h == 0) colkey[b * kTcGroups + m] = key;
       tc::fence_async_smem();
@@ -329,9 +329,15 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
     const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * 256u;
     uint64_t tile = blockIdx.x + (uint64_t)b * gridDim.x;
     for (uint32_t c = 0; tile < ntiles; tile += stride2, ++c) {
-      bool ok = tc::mbar_wait(accf(b), c & 1, abort_flag);
-      ok = ok && tc::mbar_wait(full(b), c & 1, abort_flag);  // producer's colkey write
-      if (!__all_sync(0xffffffffu, ok)) break;
+      // the first warp of the warpgroup polls; the other three sleep in the
+      // named barrier (ids 1..2 EH), which keeps the issue slots for the
+      // producers while the accumulator is not ready
+      bool ok = true;
+      if (quarter == 0) {
+        ok = tc::mbar_wait(accf(b), c & 1, abort_flag);
+        ok = ok && tc::mbar_wait(full(b), c & 1, abort_flag);  // producer's colkey write
+      }
+      if (!tc::bar_and(1 + (e >> 2), 128, ok)) break;
       tc::fence_after_sync();
       const int ck = colkey[b * kTcGroups + m];
       tc::mbar_arrive(sempty(b));
@@ -583,8 +589,8 @@ __global__ void __launch_bounds__(tc_threads<2>(), 1)
       }
       mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
       const int key = mx ? (int)mx + 1 : 0;
-      const uint32_t E3 = (uint32_t)key + 3;
-      const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E3);
+      const uint32_t E4 = (uint32_t)key + 4;
+      const bool near = __all_sync(0xffffffffu, mn != 0 && mn + 31 >= E4);
       bool stop = false;
 #pragma unroll 1
       for (int kh = 0; kh < 2; ++kh) {
@@ -600,7 +606,7 @@ __global__ void __launch_bounds__(tc_threads<2>(), 1)
         tc::fence_async_smem();
         tc::mbar_arrive(raw_empty(kh));
         uint32_t lo[16], hi[16], sb[8];
-        split_words8(v, ex, E3, near, lo, hi, sb);
+        split_words8(v, ex, E4, near, lo, hi, sb);
         const bool freed = i == 0 || tc::mbar_wait(sfree(kh), (i - 1) & 1, abort_flag);
         if (!__all_sync(0xffffffffu, freed)) {
           stop = true;
@@ -622,9 +628,14 @@ __global__ void __launch_bounds__(tc_threads<2>(), 1)
     const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)o * 256u;
     uint64_t tile = blockIdx.x;
     for (uint32_t i = 0; tile < ntiles; tile += gridDim.x, ++i) {
-      bool ok = tc::mbar_wait(accf(o), i & 1, abort_flag);
-      ok = ok && tc::mbar_wait(keyf(i & 1), (i >> 1) & 1, abort_flag);
-      if (!__all_sync(0xffffffffu, ok)) break;
+      // one polling warp per warpgroup, the others wait in named barrier
+      // 1 + warpgroup
+      bool ok = true;
+      if (quarter == 0) {
+        ok = tc::mbar_wait(accf(o), i & 1, abort_flag);
+        ok = ok && tc::mbar_wait(keyf(i & 1), (i >> 1) & 1, abort_flag);
+      }
+      if (!tc::bar_and(1 + (e >> 2), 128, ok)) break;
       tc::fence_after_sync();
       const int ck = colkey[(i & 1) * kTcGroups + m];
       const uint64_t grp = tile * kTcGroups + m;

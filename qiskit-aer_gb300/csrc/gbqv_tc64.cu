@@ -244,8 +244,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * (uint32_t)kR;
     uint64_t tile = blockIdx.x + (uint64_t)b * gridDim.x;
     for (uint32_t c = 0; tile < ntiles; tile += 2ULL * gridDim.x, ++c) {
-      const bool ok = tc::mbar_wait(accf(b), c & 1, abort_flag);
-      if (!__all_sync(0xffffffffu, ok)) break;
+      // one polling warp per warpgroup, the others wait in named barrier 1 + b
+      const bool ok = quarter != 0 || tc::mbar_wait(accf(b), c & 1, abort_flag);
+      if (!tc::bar_and(1 + b, 128, ok)) break;
       tc::fence_after_sync();
       uint32_t T[kR / 8][8];
 #pragma unroll

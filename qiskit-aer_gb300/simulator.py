@@ -15,6 +15,7 @@ they sit.  Result metadata carries the reference's fusion keys
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import time
 import warnings
@@ -284,19 +285,19 @@ class AerSimulator:
         if unknown:
             warnings.warn(f"run options not used by this engine: {', '.join(unknown)}", stacklevel=2)
         run_options = {k: v for k, v in run_options.items() if k in self._DEFAULTS}
-        if not run_options:
-            return self._run(circuits, shots, seed_simulator, parameter_binds, memory)
-        saved = {"method": self.method, "precision": self.precision, "noise_model": self.noise_model,
-                 "options": dict(self.options), "tuner": self._tuner}
-        try:
-            self.set_options(**run_options)
-            return self._run(circuits, shots, seed_simulator, parameter_binds, memory)
-        finally:
-            self.method, self.precision, self.noise_model = saved["method"], saved["precision"], saved["noise_model"]
-            self.options, self._tuner = saved["options"], saved["tuner"]
+        call = self
+        if run_options or bool(memory) != self._want_memory:
+            # the overrides and the memory flag go to a per-call copy, as the
+            # reference builds a per-call config (aerbackend.py
+            # generate_aer_config); the simulator itself is left unchanged, so
+            # concurrent run() calls do not see each other's options
+            call = copy.copy(self)
+            call.options = dict(self.options)
+            call._want_memory = bool(memory)
+            call.set_options(**run_options)
+        return call._run(circuits, shots, seed_simulator, parameter_binds, memory)
 
     def _run(self, circuits, shots, seed_simulator, parameter_binds, memory):
-        self._want_memory = bool(memory)
         single = isinstance(circuits, QuantumCircuit)
         if single:
             circuits = [circuits]

@@ -4,7 +4,7 @@
 // is compared against a __float128 matrix-vector product.  Prints the worst
 // error relative to (row max * column max) and the worst absolute error.
 // Mode "signed" (third argument) checks the tcgen05 kernel's arithmetic: the
-// state's digits from split_word_abs (rounded, sign applied per digit),
+// state's digits from split_word_abs (truncated, sign applied per digit),
 // the matrix's from split_bsum, level sums held as fp32 (|T| <= 2^22) and
 // turned into the double by levels_to_double.
 #include <cmath>
@@ -19,19 +19,19 @@
 using namespace gbqv::oz;
 
 // Mode "near": split_word_abs_near against split_word_abs, bit for bit, for
-// every shift 4..31 and random magnitudes and signs.
+// every shift 5..31 and random magnitudes and signs.
 static int check_near(int trials) {
   std::mt19937_64 rng(777);
-  std::uniform_int_distribution<int> sd(4, 31);
+  std::uniform_int_distribution<int> sd(5, 31);
   std::uniform_int_distribution<uint64_t> bits;
   long bad = 0;
   for (int t = 0; t < trials; ++t) {
     uint64_t b = bits(rng);
     uint32_t ex = (uint32_t)((b >> 52) & 0x7ff);
     if (ex == 0 || ex == 0x7ff) continue;  // zeros and non-finite values take the generic path
-    const uint32_t s = (uint32_t)sd(rng), E3 = ex + s;
+    const uint32_t s = (uint32_t)sd(rng), E4 = ex + s;
     const double x = bitsd(b);
-    if (split_word_abs_near((uint32_t)(b >> 32), (uint32_t)b, s) != split_word_abs(x, ex, E3)) ++bad;
+    if (split_word_abs_near((uint32_t)(b >> 32), (uint32_t)b, s) != split_word_abs(x, ex, E4)) ++bad;
   }
   printf("%ld 0\n", bad);
   return 0;
@@ -64,7 +64,7 @@ int main(int argc, char **argv) {
       int32_t d[6];
       if (sgn) {
         const uint32_t ex = (uint32_t)((dbits(x[j]) >> 52) & 0x7ff);
-        word_digits(split_word_abs(x[j], ex, (uint32_t)E + 3), std::signbit(x[j]), d);
+        word_digits(split_word_abs(x[j], ex, (uint32_t)E + 4), std::signbit(x[j]), d);
       } else
         split6(x[j], E, d);
       for (int s = 0; s < 6; ++s) dx[j * 6 + s] = d[s];

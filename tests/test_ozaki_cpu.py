@@ -16,7 +16,7 @@ ROOT = Path(__file__).resolve().parents[1]
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
 @pytest.mark.parametrize("reals,trials,mode", [(32, 3000, "rounded"), (64, 1500, "rounded"),
-                                               (32, 3000, "signed")])
+                                               (32, 3000, "signed"), (64, 1500, "signed")])
 def test_digit_slices_against_quad(tmp_path, reals, trials, mode):
     exe = tmp_path / "ozk"
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "qiskit-aer_gb300" / "csrc"),

@@ -53,25 +53,32 @@ def test_autotune_cache_option_replaces_the_tuner(tmp_path):
 
 def test_run_options_apply_to_one_call_only():
     """Keyword options of run() override the simulator's options for that
-    call (AerBackend.run's run_options, aerbackend.py:146-185) and are
-    restored afterwards, also when the run fails; unknown ones are ignored
+    call (AerBackend.run's run_options, aerbackend.py:146-185) on a per-call
+    copy: the simulator itself never changes, also when the run fails or
+    while another thread runs with other options; unknown ones are ignored
     with a warning."""
+    import threading
+
     P = pkg()
-    sim = P.AerSimulator()
     nm = P.NoiseModel()
     seen = []
+    gate = threading.Barrier(2, timeout=10)
 
-    def fake_run(circuits, shots, seed, binds, memory):
-        seen.append((sim.method, sim.precision, sim.noise_model, sim.options["fusion_threshold"], shots))
-        if shots == 13:
-            raise RuntimeError("boom")
-        return "result"
+    class Sim(P.AerSimulator):
+        def _run(self, circuits, shots, seed, binds, memory):
+            if shots in (21, 22):  # two concurrent calls meet here
+                gate.wait()
+            seen.append((self.method, self.precision, self.noise_model, self.options["fusion_threshold"], shots,
+                         self._want_memory))
+            if shots == 13:
+                raise RuntimeError("boom")
+            return "result"
 
-    sim._run = fake_run
+    sim = Sim()
     qc = P.QuantumCircuit(1)
     assert sim.run(qc, shots=7, method="density_matrix", precision="single", noise_model=nm,
                    fusion_threshold=2) == "result"
-    assert seen[-1] == ("density_matrix", "single", nm, 2, 7)
+    assert seen[-1][:5] == ("density_matrix", "single", nm, 2, 7)
     assert (sim.method, sim.precision, sim.noise_model, sim.options["fusion_threshold"]) == (
         "statevector", "double", None, None)
     with pytest.raises(RuntimeError):
@@ -83,3 +90,12 @@ def test_run_options_apply_to_one_call_only():
     with pytest.raises(ValueError, match="Invalid simulation method"):
         sim.run(qc, method="mps")
     assert sim.method == "statevector"
+    # two threads on one simulator, each with its own overrides and memory flag
+    t = threading.Thread(target=lambda: sim.run(qc, shots=21, method="density_matrix", memory=True))
+    t.start()
+    sim.run(qc, shots=22, precision="single")
+    t.join()
+    got = {r[4]: r for r in seen[-2:]}
+    assert got[21][:2] == ("density_matrix", "double") and got[21][5] is True
+    assert got[22][:2] == ("statevector", "single") and got[22][5] is False
+    assert (sim.method, sim.precision, sim._want_memory) == ("statevector", "double", False)
