@@ -256,16 +256,43 @@ __host__ __device__ __forceinline__ uint32_t funnel_l(uint32_t lo, uint32_t hi, 
 // The two steps separately (the tcgen05 epilogue checks the fast path's
 // condition for a whole chunk of outputs at once): words -> the ones'
 // complement magnitude (ah, al) of v and its sign mask sg, then the double.
-__host__ __device__ __forceinline__ void words_to_mag(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3, uint32_t u4,
-                                                      uint32_t u5, uint32_t &ah, uint32_t &al, uint32_t &sg) {
+// v itself (two's complement, as its two words)
+__host__ __device__ __forceinline__ void words_to_v(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3, uint32_t u4,
+                                                    uint32_t u5, uint32_t &vh, uint32_t &vl) {
   constexpr uint32_t kPair = 257u * 0x4B400000u;
   constexpr uint64_t kBias = (uint64_t)kPair * 0x100010001ULL;  // kPair * (2^32 + 2^16 + 1) mod 2^64
   const uint32_t p01 = u0 * 256u + u1, p23 = u2 * 256u + u3, p45 = u4 * 256u + u5;
   // v = p01 2^32 + p23 2^16 + p45 - kBias: the register pair (p01, p45) plus one wide multiply-add
   const uint64_t v = ((((uint64_t)p01 << 32) | p45) + (uint64_t)p23 * 0x10000u) - kBias;
-  sg = (uint32_t)((int32_t)(uint32_t)(v >> 32) >> 31);
-  ah = (uint32_t)(v >> 32) ^ sg;
-  al = (uint32_t)v ^ sg;
+  vh = (uint32_t)(v >> 32);
+  vl = (uint32_t)v;
+}
+
+__host__ __device__ __forceinline__ void words_to_mag(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3, uint32_t u4,
+                                                      uint32_t u5, uint32_t &ah, uint32_t &al, uint32_t &sg) {
+  uint32_t vh, vl;
+  words_to_v(u0, u1, u2, u3, u4, u5, vh, vl);
+  sg = (uint32_t)((int32_t)vh >> 31);
+  ah = vh ^ sg;
+  al = vl ^ sg;
+}
+
+// The double v * 2^(ebase - 1085) through the int64 -> double conversion
+// (rounded to nearest) and an add to its exponent field, escale = (ebase -
+// 1085) * 2^20: for |v| >= 2^32 (the high word of v neither 0 nor -1) and
+// ebase >= 32, where the scaled exponent stays in the normal range.  The
+// conversion runs on the FP64 pipe, the integer path (mag_to_double_fast)
+// on the integer pipe; the two agree to the last bit but one (rounding vs
+// truncation).
+__host__ __device__ __forceinline__ double v_to_double_cvt(uint32_t vh, uint32_t vl, int escale) {
+  const int64_t v = (int64_t)(((uint64_t)vh << 32) | vl);
+#ifdef __CUDA_ARCH__
+  const double d = __ll2double_rn((long long)v);
+  return __hiloint2double(__double2hiint(d) + escale, __double2loint(d));
+#else
+  const uint64_t b = dbits((double)v);
+  return bitsd(b + ((uint64_t)(uint32_t)escale << 32));
+#endif
 }
 
 // The double from (ah, al, sg) when ah != 0 and ebase >= 32: normalisation

@@ -9,7 +9,9 @@
 // split into six signed 8-bit digits against the group's exponent, the real
 // form of the matrix into six digits against each row's exponent (host), and
 // the 21 digit-plane products with s + t <= 5 accumulate per level l = s + t
-// in fp32 TMEM, exactly.  Levels are recombined in int64 and rounded once.
+// in fp32 TMEM, exactly.  Levels are recombined in int64 and rounded once
+// (the int64 -> double conversion runs on the FP64 pipe, which is otherwise
+// idle here, so that the integer pipe serves the digit split).
 //
 // One persistent CTA per SM, 17 warps, warp-specialised:
 //   warps 0-7       producers: split each tile of 128 groups (two threads
@@ -95,6 +97,8 @@ struct TcParams {
   uint32_t stall;         // test hook: no accumulator commit for the CTA's first tile
   uint16_t zl[kTcGroups]; // amplitude index of group m within its run (zeros at targets < L)
   int rowbase[kTcReals];  // row key - 1017 per output real (see combine)
+  int rowscale[kTcReals]; // (rowbase - 1085) * 2^20: the exponent-field add of the converting path
+  int rowbase_min;        // min over rowbase: rowbase_min + group key >= 32 lets every row take a fast path
 };
 
 // amplitude index of group g: a zero bit inserted at each (sorted) target
@@ -199,6 +203,43 @@ __device__ __forceinline__ void store_planes8(unsigned char *stage, int m, int h
     for (int jj = 0; jj < 4; ++jj)
       w[jj] = tc::hfma2(tc::prmt(hi8[2 * jj], hi8[2 * jj + 1], 0x6521), sg[jj], c0[jj]);
     *reinterpret_cast<uint4 *>(row) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// The 8 output reals of one chunk (4 amplitudes at psi[base + offs[0..3]],
+// re/im) from their six TMEM level words, for rows with row key - 1017 =
+// rowbase[i] and rowscale[i] = (rowbase[i] - 1085) * 2^20, group key ck.
+// One vote picks the branch-free path for the whole warp (every output at
+// least 2^-23 of row max x group max, and every scale in range: the usual
+// case): the int64 -> double conversion on the otherwise idle FP64 pipe
+// (about 2 per clock per SM) instead of ~11 integer operations per output
+// on the integer pipe that the producers' split needs.  Otherwise the
+// general integer normalisation.
+__device__ __forceinline__ void store_outputs8(double2 *psi, uint64_t base, const uint64_t *offs,
+                                               const uint32_t (&T)[6][8], const int *rowbase, const int *rowscale,
+                                               int ck, bool scale_ok, bool live) {
+  uint32_t vh[8], vl[8];
+  bool fast = scale_ok;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    oz::words_to_v(T[0][i], T[1][i], T[2][i], T[3][i], T[4][i], T[5][i], vh[i], vl[i]);
+    fast = fast && vh[i] + 1u > 1u;
+  }
+  const int ck20 = ck << 20;
+  if (__all_sync(0xffffffffu, fast || !live)) {
+    if (live) {
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj)
+        psi[base + offs[jj]] = make_double2(oz::v_to_double_cvt(vh[2 * jj], vl[2 * jj], rowscale[2 * jj] + ck20),
+                                            oz::v_to_double_cvt(vh[2 * jj + 1], vl[2 * jj + 1], rowscale[2 * jj + 1] + ck20));
+    }
+  } else if (live) {
+    auto out_any = [&](int i) {
+      const uint32_t sg = (uint32_t)((int32_t)vh[i] >> 31);
+      return oz::mag_to_double(vh[i] ^ sg, vl[i] ^ sg, sg, rowbase[i] + ck);
+    };
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) psi[base + offs[jj]] = make_double2(out_any(2 * jj), out_any(2 * jj + 1));
   }
 }
 
@@ -344,6 +385,7 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
       const uint64_t grp = tile * kTcGroups + m;
       const bool live = grp < p.ngroups && ck != 0;
       const uint64_t base = live ? insert_zeros_k4(grp, p.lowmask) : 0;
+      const bool scale_ok = p.rowbase_min + ck >= 32;
 #pragma unroll
       for (int qq = 0; qq < kChunks; ++qq) {
         const int q = half * kChunks + qq;
@@ -353,33 +395,7 @@ __global__ void __launch_bounds__(tc_threads<EH>(), 1)
         tc::tmem_wait_ld();
 #pragma unroll
         for (int l = 0; l < 6; ++l) tc::pin(T[l]);
-        // the chunk's 8 outputs as magnitude words; one vote picks the
-        // branch-free conversion for the whole warp (every output at least
-        // 2^-23 of row max x group max: the usual case)
-        uint32_t ah[8], al[8], sg[8];
-        int eb[8];
-        bool fast = true;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          oz::words_to_mag(T[0][i], T[1][i], T[2][i], T[3][i], T[4][i], T[5][i], ah[i], al[i], sg[i]);
-          eb[i] = p.rowbase[8 * q + i] + ck;
-          fast = fast && ah[i] != 0 && eb[i] >= 32;
-        }
-        if (__all_sync(0xffffffffu, fast || !live)) {
-          if (live) {
-#pragma unroll
-            for (int jj = 0; jj < 4; ++jj)
-              psi[base + p.offs[4 * q + jj]] =
-                  make_double2(oz::mag_to_double_fast(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
-                               oz::mag_to_double_fast(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
-          }
-        } else if (live) {
-#pragma unroll
-          for (int jj = 0; jj < 4; ++jj)
-            psi[base + p.offs[4 * q + jj]] =
-                make_double2(oz::mag_to_double(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
-                             oz::mag_to_double(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
-        }
+        store_outputs8(psi, base, p.offs + 4 * q, T, p.rowbase + 8 * q, p.rowscale + 8 * q, ck, scale_ok, live);
       }
       tc::fence_before_sync();
       tc::mbar_arrive(acce(b));
@@ -484,6 +500,8 @@ struct Tc5Params {
   uint32_t nhalf, runbytes;  // runs per K-half (runs [kh nhalf, (kh + 1) nhalf) form half kh)
   uint16_t zl[kTcGroups];
   int rowbase[64];        // row key - 1017 per output real
+  int rowscale[64];       // (rowbase - 1085) * 2^20
+  int rowbase_min;
 };
 
 // byte offset of element (row, k) in the matrix operand: rows of 64 reals
@@ -641,6 +659,7 @@ __global__ void __launch_bounds__(tc_threads<2>(), 1)
       const uint64_t grp = tile * kTcGroups + m;
       const bool live = grp < p.ngroups && ck != 0;
       const uint64_t base = live ? insert_zeros_k5(grp, p.lowmask) : 0;
+      const bool scale_ok = p.rowbase_min + ck >= 32;
 #pragma unroll
       for (int qq = 0; qq < 2; ++qq) {
         const int q = half * 2 + qq;  // chunk of 8 output reals within the output half
@@ -650,31 +669,9 @@ __global__ void __launch_bounds__(tc_threads<2>(), 1)
         tc::tmem_wait_ld();
 #pragma unroll
         for (int l = 0; l < 6; ++l) tc::pin(T[l]);
-        uint32_t ah[8], al[8], sg[8];
-        int eb[8];
-        bool fast = true;
-#pragma unroll
-        for (int x = 0; x < 8; ++x) {
-          oz::words_to_mag(T[0][x], T[1][x], T[2][x], T[3][x], T[4][x], T[5][x], ah[x], al[x], sg[x]);
-          eb[x] = p.rowbase[32 * o + 8 * q + x] + ck;
-          fast = fast && ah[x] != 0 && eb[x] >= 32;
-        }
         const int a0 = 16 * o + 4 * q;  // first local amplitude of the chunk
-        if (__all_sync(0xffffffffu, fast || !live)) {
-          if (live) {
-#pragma unroll
-            for (int jj = 0; jj < 4; ++jj)
-              psi[base + p.offs[a0 + jj]] =
-                  make_double2(oz::mag_to_double_fast(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
-                               oz::mag_to_double_fast(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
-          }
-        } else if (live) {
-#pragma unroll
-          for (int jj = 0; jj < 4; ++jj)
-            psi[base + p.offs[a0 + jj]] =
-                make_double2(oz::mag_to_double(ah[2 * jj], al[2 * jj], sg[2 * jj], eb[2 * jj]),
-                             oz::mag_to_double(ah[2 * jj + 1], al[2 * jj + 1], sg[2 * jj + 1], eb[2 * jj + 1]));
-        }
+        store_outputs8(psi, base, p.offs + a0, T, p.rowbase + 32 * o + 8 * q, p.rowscale + 32 * o + 8 * q, ck,
+                       scale_ok, live);
       }
       tc::fence_before_sync();
       tc::mbar_arrive(acce(o));
@@ -1016,7 +1013,12 @@ void launch_dense_tc5(Device &dev, const reg_t &qubits_in, const cd *mat_in) {
   std::vector<uint16_t> planes(k5MatBytes / 2);
   int rowkey[64];
   tc_matrix5(matv.data(), planes.data(), rowkey);
-  for (int r = 0; r < 64; ++r) p.rowbase[r] = rowkey[r] - 1017;
+  p.rowbase_min = 1 << 30;
+  for (int r = 0; r < 64; ++r) {
+    p.rowbase[r] = rowkey[r] - 1017;
+    p.rowscale[r] = (int)((uint32_t)(p.rowbase[r] - 1085) << 20);
+    p.rowbase_min = std::min(p.rowbase_min, p.rowbase[r]);
+  }
   grow(dev.mat, dev.mat_cap, k5MatBytes);
   cuda_check(cudaMemcpyAsync(dev.mat, planes.data(), k5MatBytes, cudaMemcpyHostToDevice, dev.stream),
              "matrix upload");
@@ -1050,7 +1052,12 @@ void launch_dense_tc(Device &dev, const reg_t &qubits, const cd *mat) {
   std::vector<uint16_t> planes(kMatBytes / 2);
   int rowkey[kTcReals];
   tc_matrix4(mat, planes.data(), rowkey);
-  for (int r = 0; r < kTcReals; ++r) p.rowbase[r] = rowkey[r] - 1017;
+  p.rowbase_min = 1 << 30;
+  for (int r = 0; r < kTcReals; ++r) {
+    p.rowbase[r] = rowkey[r] - 1017;
+    p.rowscale[r] = (int)((uint32_t)(p.rowbase[r] - 1085) << 20);
+    p.rowbase_min = std::min(p.rowbase_min, p.rowbase[r]);
+  }
   p.stall = dev.tc_test_stall ? 1u : 0u;
   grow(dev.mat, dev.mat_cap, kMatBytes);
   cuda_check(cudaMemcpyAsync(dev.mat, planes.data(), kMatBytes, cudaMemcpyHostToDevice, dev.stream), "matrix upload");

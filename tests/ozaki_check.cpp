@@ -37,8 +37,40 @@ static int check_near(int trials) {
   return 0;
 }
 
+// Mode "cvt": the converting output path (int64 -> double, round to
+// nearest, exponent-field add) against the integer normalisation
+// (truncating) for random level words whose v has |v| >= 2^32 and scales
+// ebase in [32, 1100]: at most one unit in the last place plus one unit of v
+// apart.  Prints the
+// count of larger differences and the count of cases checked.
+static int check_cvt(int trials) {
+  std::mt19937_64 rng(4242);
+  std::uniform_int_distribution<int32_t> td(-(1 << 22), 1 << 22);
+  std::uniform_int_distribution<int> ed(32, 1100);
+  long bad = 0, seen = 0;
+  for (int t = 0; t < trials; ++t) {
+    uint32_t u[6];
+    for (auto &x : u) x = 0x4B400000u + (uint32_t)td(rng);
+    uint32_t vh, vl, ah, al, sg;
+    words_to_v(u[0], u[1], u[2], u[3], u[4], u[5], vh, vl);
+    if (vh + 1u <= 1u) continue;
+    words_to_mag(u[0], u[1], u[2], u[3], u[4], u[5], ah, al, sg);
+    const int eb = ed(rng);
+    const double a = v_to_double_cvt(vh, vl, (int)((uint32_t)(eb - 1085) << 20));
+    const double b = mag_to_double_fast(ah, al, sg, eb);
+    ++seen;
+    // the integer path takes |v| - 1 for negative v (ones' complement): one
+    // unit of v, 2^(ebase - 1085), besides its truncation
+    const double unit = std::ldexp(1.0, eb - 1085);
+    if (std::signbit(a) != std::signbit(b) || std::fabs(a - b) > std::ldexp(std::fabs(b), -51) + unit) ++bad;
+  }
+  printf("%ld %ld\n", bad, seen);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc > 3 && std::string(argv[3]) == "near") return check_near(argc > 2 ? atoi(argv[2]) : 100000);
+  if (argc > 3 && std::string(argv[3]) == "cvt") return check_cvt(argc > 2 ? atoi(argv[2]) : 100000);
   const int K = argc > 1 ? atoi(argv[1]) : 32;   // reals per column
   const int trials = argc > 2 ? atoi(argv[2]) : 2000;
   const bool sgn = argc > 3 && std::string(argv[3]) == "signed";

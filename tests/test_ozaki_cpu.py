@@ -37,3 +37,17 @@ def test_fast_split_equals_generic_split(tmp_path):
                            str(ROOT / "tests" / "ozaki_check.cpp"), "-o", str(exe), "-lquadmath"])
     out = subprocess.run([str(exe), "32", "400000", "near"], capture_output=True, text=True, check=True).stdout
     assert out.split()[0] == "0", out
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_converting_output_path_matches_integer_path(tmp_path):
+    """The tcgen05 epilogue's converting output path (int64 -> double, then
+    an exponent-field add) gives the integer normalisation's double to within
+    one unit in the last place (plus one unit of v, which the integer path
+    drops for negative v), for every sign and scale of the fast path."""
+    exe = tmp_path / "ozk"
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "qiskit-aer_gb300" / "csrc"),
+                           str(ROOT / "tests" / "ozaki_check.cpp"), "-o", str(exe), "-lquadmath"])
+    out = subprocess.run([str(exe), "32", "400000", "cvt"], capture_output=True, text=True, check=True).stdout
+    bad, seen = map(int, out.split())
+    assert bad == 0 and seen > 300000, out
