@@ -7,9 +7,13 @@
 // Every real x of a group and every entry a of the real form of the matrix
 // [[Re U, -Im U], [Im U, Re U]] is split as x = x_hi + x_lo with x_hi = x
 // rounded to TF32 (10-bit mantissa) and x_lo = x - x_hi exact in fp32; the
-// tensor core computes a_hi x_hi + a_lo x_hi + a_hi x_lo (the a_lo x_lo term
-// is below fp32 resolution) with fp32 accumulation in TMEM, which is the
-// fp32-FMA result up to accumulation order.  The split costs two SIMT ops per
+// tensor core computes a_hi x_hi and a_lo x_hi + a_hi x_lo (the a_lo x_lo
+// term is below fp32 resolution) with fp32 accumulation in TMEM: the hi x hi
+// products of the R / 8 K steps in 4 (k = 4) or 3 (k = 5) accumulators and
+// the cross terms in one more, added in fp32 in the epilogue.  The tensor
+// core's accumulation truncates; with one accumulator the 3 R / 8 - 1
+// accumulating MMAs biased every output towards zero and the norm drifted
+// (2e-5 after 24 5-qubit gates, 8e-6 with the cross terms apart).  The split costs two SIMT ops per
 // real and the result is read straight from TMEM, so, unlike the complex128
 // kernel, the SIMT side is light.
 //
@@ -21,8 +25,9 @@
 //   warps 8-15      epilogues: one warpgroup per pipeline lane reads the R
 //                    fp32 outputs of its group from TMEM and stores them;
 //   warp 16 lane 0  issues 3 R / 8 tcgen05.mma.kind::tf32 per tile (R / 8
-//                    K = 8 steps x {hi*hi, hi*lo, lo*hi}, M = 128, N = R)
-//                    into the lane's R TMEM columns, commits to accf
+//                    K = 8 steps x {hi*lo, lo*hi -> cross accumulator,
+//                    hi*hi -> main accumulator kk mod kMain}, M = 128,
+//                    N = R) into the lane's TMEM columns, commits to accf
 //                    (epilogue) and sfree (producers);
 //   warp 17 lane 0  loader: tiled TMA loads (rows of 16 amplitudes, 128-byte
 //                    swizzle) of each tile's <= 2^k contiguous runs into the
@@ -64,7 +69,12 @@ struct Tc64Shape {
   static constexpr int kOffBar = kOffRaw + kRawStages * kRawStage;
   static constexpr int kOffMisc = kOffBar + 24 * 8;
   static constexpr int kSmem = kOffMisc + 64 + 1024;   // + 1024-byte alignment slack
-  static constexpr uint32_t kTmemCols = 2 * kR;         // two R-column accumulators
+  // per pipeline lane b (columns 256 b ..): kMain accumulators of the hi * hi
+  // products (K step kk into accumulator kk mod kMain) at 256 b + j R, then
+  // the cross terms at 256 b + kMain R
+  static constexpr int kMain = KQ == 4 ? 4 : 3;
+  static constexpr uint32_t kTmemCols = 512;
+  static_assert((kMain + 1) * kR <= 256, "accumulators of a pipeline lane");
   static_assert(kSmem <= 232448, "shared memory per CTA");
 };
 constexpr int kThreads = 18 * 32;
@@ -241,7 +251,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp < kMmaWarp) {
     // ---------------- epilogues: warpgroup b serves pipeline lane b ----------------
     const int b = (warp - 8) >> 2, quarter = warp & 3, m = 32 * quarter + lane;
-    const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * (uint32_t)kR;
+    const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)b * 256u;
     uint64_t tile = blockIdx.x + (uint64_t)b * gridDim.x;
     for (uint32_t c = 0; tile < ntiles; tile += 2ULL * gridDim.x, ++c) {
       // one polling warp per warpgroup, the others wait in named barrier 1 + b
@@ -254,6 +264,26 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc::tmem_wait_ld();
 #pragma unroll
       for (int q = 0; q < kR / 8; ++q) tc::pin(T[q]);
+      // output = the kMain hi * hi sums + the cross-term sum, added in fp32
+      // (round to nearest): no full-size partial sum passes through the
+      // tensor core's truncating accumulation
+      constexpr int kC = kR / 8 <= 4 ? kR / 8 : 2;
+#pragma unroll
+      for (int a = 1; a <= S::kMain; ++a)
+#pragma unroll
+      for (int q0 = 0; q0 < kR / 8; q0 += kC) {
+        uint32_t C[kC][8];
+#pragma unroll
+        for (int qq = 0; qq < kC; ++qq) tc::tmem_ld8(tbase + (uint32_t)(a * kR) + 8u * (q0 + qq), C[qq]);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int qq = 0; qq < kC; ++qq) {
+          tc::pin(C[qq]);
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            T[q0 + qq][i] = __float_as_uint(__uint_as_float(T[q0 + qq][i]) + __uint_as_float(C[qq][i]));
+        }
+      }
       tc::fence_before_sync();
       tc::mbar_arrive(acce(b));
       // n >= 11: every tile is full, so the whole warp takes this branch
@@ -301,17 +331,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (c >= 1 && !tc::mbar_wait(acce(b), (c - 1) & 1, abort_flag, 32)) break;
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(smem + kOffStage + b * kStage);
-      const uint32_t d = tmem + (uint32_t)b * (uint32_t)kR;
+      const uint32_t d = tmem + (uint32_t)b * 256u;
 #pragma unroll
       for (int kk = 0; kk < kR / 8; ++kk) {
         const uint64_t ahi = tc::smem_desc(a0 + kk * 256, 128, S::kSbo);
         const uint64_t alo = tc::smem_desc(a0 + kPlane + kk * 256, 128, S::kSbo);
         const uint64_t bhi = tc::smem_desc(mat + kk * 256, 128, S::kSbo);
         const uint64_t blo = tc::smem_desc(mat + kR * kR * 4 + kk * 256, 128, S::kSbo);
-        // the two cross terms (small) first, then hi * hi
-        mma_tf32(d, ahi, blo, idesc, kk != 0);
-        mma_tf32(d, alo, bhi, idesc, 1);
-        mma_tf32(d, ahi, bhi, idesc, 1);
+        // the two cross terms (small) into their own accumulator, hi * hi
+        // into main accumulator kk mod kMain
+        const uint32_t dc = d + (uint32_t)(S::kMain * kR), dm = d + (uint32_t)((kk % S::kMain) * kR);
+        mma_tf32(dc, ahi, blo, idesc, kk != 0);
+        mma_tf32(dc, alo, bhi, idesc, 1);
+        mma_tf32(dm, ahi, bhi, idesc, kk >= S::kMain);
       }
       tc::mma_commit(accf(b));
       tc::mma_commit(sfree(b));
