@@ -123,8 +123,12 @@ __device__ __forceinline__ void split_words8(const double2 (&v)[8], const uint32
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const uint32_t xh = (uint32_t)__double2hiint(v[j].x), yh = (uint32_t)__double2hiint(v[j].y);
+      // dithered truncation: real parts truncated (toward zero), imaginary
+      // parts truncated plus one unit (away from zero), so that the two
+      // biases cancel in the norm; the fast path only ever sees non-zero
+      // reals, and the +1 folds into the split's constant
       const uint64_t rw = oz::split_word_abs_near(xh, (uint32_t)__double2loint(v[j].x), E4 - ex[2 * j]);
-      const uint64_t iw = oz::split_word_abs_near(yh, (uint32_t)__double2loint(v[j].y), E4 - ex[2 * j + 1]);
+      const uint64_t iw = oz::split_word_abs_near(yh, (uint32_t)__double2loint(v[j].y), E4 - ex[2 * j + 1]) + 1;
       lo[2 * j] = (uint32_t)rw;
       hi[2 * j] = (uint32_t)(rw >> 32);
       lo[2 * j + 1] = (uint32_t)iw;

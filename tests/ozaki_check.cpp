@@ -4,7 +4,8 @@
 // is compared against a __float128 matrix-vector product.  Prints the worst
 // error relative to (row max * column max) and the worst absolute error.
 // Mode "signed" (third argument) checks the tcgen05 kernel's arithmetic: the
-// state's digits from split_word_abs (truncated, sign applied per digit),
+// state's digits from split_word_abs (truncated, one unit added to the
+// imaginary parts as in the kernel's fast path, sign applied per digit),
 // the matrix's from split_bsum, level sums held as fp32 (|T| <= 2^22) and
 // turned into the double by levels_to_double.
 #include <cmath>
@@ -96,7 +97,10 @@ int main(int argc, char **argv) {
       int32_t d[6];
       if (sgn) {
         const uint32_t ex = (uint32_t)((dbits(x[j]) >> 52) & 0x7ff);
-        word_digits(split_word_abs(x[j], ex, (uint32_t)E + 4), std::signbit(x[j]), d);
+        // the kernel's fast path adds one unit to the imaginary parts
+        // (odd j) of non-zero reals
+        const uint64_t w = split_word_abs(x[j], ex, (uint32_t)E + 4) + ((j & 1) && x[j] != 0.0 ? 1 : 0);
+        word_digits(w, std::signbit(x[j]), d);
       } else
         split6(x[j], E, d);
       for (int s = 0; s < 6; ++s) dx[j * 6 + s] = d[s];
