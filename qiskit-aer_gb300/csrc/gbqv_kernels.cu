@@ -640,7 +640,28 @@ __global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n
 // The same per state of a stack of 2^sb-amplitude states (one state per
 // parameter binding): blockIdx.y = state, blockIdx.x = term * bps + slice,
 // so that every term of a state runs back to back while the state is in L2;
-// the terms act on qubits below sb.
+// the terms act on qubits below sb (sb <= 31: 32-bit indices).  Per pair the
+// kernel sums zr (s0 + s1) and zi (s1 - s0) with s = the Z-parity signs and
+// applies the phase once at the end: Re(ph z) s0 + Re(ph conj z) s1 = pr zr
+// (s0 + s1) + pi zi (s1 - s0).  complex64 keeps each thread's two sums in
+// float with compensated (Kahan) addition and converts once, so that no FP64
+// operation runs per amplitude (with a double add per 8 amplitudes the FP64
+// pipe was 86 % busy and bounded the kernel); complex128 adds in double.
+template <typename R>
+struct SegSum {
+  R s = 0, c = 0;
+  __device__ __forceinline__ void add(R v) {
+    if constexpr (sizeof(R) == 4) {
+      const R y = v - c, t = s + y;
+      c = (t - s) - y;
+      s = t;
+    } else {
+      s += v;
+    }
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, int sb, int bps, uint64_t nseg,
                                                     uint64_t seg0, const TermDev *__restrict__ terms,
@@ -649,44 +670,36 @@ __global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, i
   const uint64_t seg = seg0 + blockIdx.y;
   const TermDev t = terms[term];
   using R = decltype(T::x);
-  const R pr = (R)t.ph_re, pi = (R)t.ph_im;
   const T *ps = psi + (seg << sb);
-  // complex64: short sums in float, then into the double accumulator (the
-  // FP64 add per amplitude would otherwise bound the kernel); complex128:
-  // every value goes into the double accumulator
-  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
-  double acc = 0.0;
-  R part = 0;
-  int cnt = 0;
-  const uint64_t stride = (uint64_t)bps * blockDim.x;
+  const uint32_t z = (uint32_t)t.z_mask, stride = (uint32_t)bps * blockDim.x;
+  SegSum<R> A, B;
+  double acc;
   if (!t.x_mask) {
-    const uint64_t count = 1ULL << sb;
-    for (uint64_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint32_t count = 1u << sb;
+    for (uint32_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
       const T a = ps[i];
-      R v = pr * (a.x * a.x + a.y * a.y);
-      if (t.z_mask && (__popcll(i & t.z_mask) & 1)) v = -v;
-      part += v;
-      if (++cnt == kChunk) { acc += (double)part; part = 0; cnt = 0; }
+      const R v = a.x * a.x + a.y * a.y;
+      A.add((__popc(i & z) & 1) ? -v : v);
     }
+    acc = t.ph_re * A.value();
   } else {
-    const uint64_t count = 1ULL << (sb - 1);
-    const uint64_t mask_l = (1ULL << t.x_max) - 1;
-    const uint64_t mask_u = ~((1ULL << (t.x_max + 1)) - 1);
-    for (uint64_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
-      const uint64_t i0 = ((i << 1) & mask_u) | (i & mask_l);
-      const uint64_t i1 = i0 ^ t.x_mask;
+    const uint32_t count = 1u << (sb - 1), x = (uint32_t)t.x_mask;
+    const uint32_t mask_l = (1u << t.x_max) - 1;
+    for (uint32_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
+      const uint32_t i0 = ((i & ~mask_l) << 1) | (i & mask_l), i1 = i0 ^ x;
       const T a0 = ps[i0], a1 = ps[i1];
+      // z = a1 * conj(a0)
       const R zr = a1.x * a0.x + a1.y * a0.y;
       const R zi = a1.y * a0.x - a1.x * a0.y;
-      R v0 = pr * zr - pi * zi;
-      R v1 = pr * zr + pi * zi;
-      if (t.z_mask && (__popcll(i0 & t.z_mask) & 1)) v0 = -v0;
-      if (t.z_mask && (__popcll(i1 & t.z_mask) & 1)) v1 = -v1;
-      part += v0 + v1;
-      if (++cnt == kChunk) { acc += (double)part; part = 0; cnt = 0; }
+      const bool n0 = __popc(i0 & z) & 1, n1 = __popc(i1 & z) & 1;
+      if (n0 == n1) {
+        A.add(n0 ? -2 * zr : 2 * zr);
+      } else {
+        B.add(n0 ? 2 * zi : -2 * zi);
+      }
     }
+    acc = t.ph_re * A.value() + t.ph_im * B.value();
   }
-  acc += (double)part;
   acc = block_sum(acc);
   if (threadIdx.x == 0) partials[((size_t)term * nseg + seg) * bps + slice] = acc;
 }
@@ -1017,6 +1030,7 @@ void reduce_expval(Device &dev, const std::vector<PauliTerm> &terms) {
 void reduce_expval_segments(Device &dev, const std::vector<PauliTerm> &terms, int state_bits, uint64_t nseg) {
   if (terms.empty() || nseg == 0) return;
   if (terms.size() > (size_t)kMaxTerms) throw Error(1, "too many Pauli terms in one call");
+  if (state_bits > 31) throw Error(1, "stacked expectation values take states of at most 31 qubits");
   // blocks per state: about 8 blocks of 256 threads per SM over the whole launch
   const uint64_t want = std::max<uint64_t>(1, (uint64_t)kReduceBlocks / 4 / std::max<uint64_t>(nseg, 1));
   const uint64_t cap = std::max<uint64_t>(1, (1ULL << state_bits) / (2 * 256));

@@ -254,3 +254,28 @@ def test_estimator_v2_precision_and_no_parameters():
     assert not np.allclose(noisy.data.evs, exact)
     with pytest.raises(ValueError, match="precision less than 0"):
         est.run([(qc, "ZZ", None, -1.0)])
+
+
+@pytest.mark.parametrize("precision,tol", [("double", 1e-12), ("single", 2e-6)])
+def test_stacked_expvals_against_oracle(precision, tol):
+    """expval_pauli_segments on a stack of 8 random 16-qubit states (the
+    EstimatorV2 reduction: complex64 sums in float with compensation, one
+    conversion per thread) against the oracle's expval_pauli per state, for
+    Z-only terms and terms with X/Y on low and high qubits."""
+    P = pkg()
+    n, nseg = 16, 8
+    rng = np.random.default_rng(61)
+    states = []
+    for _ in range(nseg):
+        v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        states.append(v / np.linalg.norm(v))
+    st = P.QubitVector(n + 3, precision)
+    st.initialize_from_vector(np.concatenate(states))
+    labels = ["Z" * n, "I" * (n - 1) + "X", "Y" + "I" * (n - 1), "XZ" + "I" * (n - 4) + "YZ",
+              "I" * 5 + "ZZ" + "I" * (n - 8) + "X", "Y" * n, "I" * (n - 3) + "XXX", "Z" + "I" * (n - 2) + "Z"]
+    terms = [(list(range(n)), lab) for lab in labels]
+    got = st.expval_pauli_segments(n, nseg, terms)
+    for j, v in enumerate(states):
+        o = O.OracleQV(n, v.astype(np.complex64) if precision == "single" else v)
+        for t, lab in enumerate(labels):
+            assert abs(got[t, j] - o.expval_pauli(list(range(n)), lab)) < tol, (lab, j)
