@@ -482,6 +482,27 @@ int gbqv_set_blocking(gbqv_handle h, int blocking);
  * hold fewer ops per run; the autotuner picks it per workload by timing. */
 int gbqv_set_run_tile_qubits(gbqv_handle h, int tile_qubits);
 
+/* Register-tile runs compiled for their op sequence (no reference
+ * counterpart; Aer's GPU path interprets every gate the same way).  A run
+ * whose structure (ops, qubits, matrix offsets) recurs — the same circuit
+ * over new parameter bindings — is compiled once by NVRTC into a kernel with
+ * every op's bits fixed, the matrices staying data; results are those of the
+ * interpreting kernel.  mode 0: never; 1 (default): from a structure's
+ * second execution on (the first runs the interpreting kernel; compiling
+ * takes about a second); 2: from the first.  Without NVRTC the interpreting
+ * kernel runs. */
+int gbqv_set_run_jit(gbqv_handle h, int mode);
+
+/* Host check of the specialised-run source generator: generates the kernel
+ * of a synthetic run using every op kind and compiles it with NVRTC for
+ * sm_103a (no GPU needed).  0 on success; 1 when it did not compile, with
+ * NVRTC's log in `log` (up to cap - 1 bytes, NUL-terminated); GBQV_ERR_ARG
+ * when NVRTC is not available. */
+int gbqv_run_jit_compile_check(int double_precision, char *log, size_t cap);
+
+/* Process-wide counts of specialised run kernels compiled and launched. */
+int gbqv_run_jit_counts(uint64_t *compiled, uint64_t *launched);
+
 /* Arithmetic of complex128 dense gates on 4 or 5 qubits (no reference
  * counterpart).  1 (default): exact digit slices on the tensor cores, error
  * <= ~1e-13 of (row max x group max) per gate (4-qubit gates on tcgen05 with

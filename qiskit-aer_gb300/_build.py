@@ -19,8 +19,9 @@ LIB = PKG / "libgbqv.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+GEN = BUILD / "gen"
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-I", str(INCLUDE), "-I", str(CSRC)]
+              "-I", str(INCLUDE), "-I", str(CSRC), "-I", str(GEN)]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
 
 
@@ -56,16 +57,28 @@ def _compile(src: Path) -> Path:
     return obj
 
 
+def _generate() -> None:
+    """gbqv_runreg_dev_src.inc: the text of csrc/gbqv_runreg_dev.cuh as a C++
+    string, which the specialised register-tile runs hand to NVRTC."""
+    GEN.mkdir(parents=True, exist_ok=True)
+    text = (CSRC / "gbqv_runreg_dev.cuh").read_text()
+    assert ")GBQVDEV\"" not in text
+    (GEN / "gbqv_runreg_dev_src.inc").write_text(
+        "// generated from csrc/gbqv_runreg_dev.cuh by _build.py\n"
+        "static const char kRunRegDevSrc[] = R\"GBQVDEV(" + text + ")GBQVDEV\";\n")
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
     if not force and not _stale():
         return LIB
     BUILD.mkdir(exist_ok=True)
+    _generate()
     srcs = _sources()
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(_compile, srcs))
     cuda = _cuda_home()
     cmd = [str(cuda / "bin" / "nvcc"), *ARCH, "-shared", "-o", str(LIB) + ".tmp", *map(str, objs),
-           "-lcudart", "-L", str(cuda / "lib64")]
+           "-lcudart", "-ldl", "-L", str(cuda / "lib64")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -83,6 +83,9 @@ _SIGS = {
     "gbqv_set_sample_measure_index_size": (C.c_int, [H, C.c_int]),
     "gbqv_test_stall_tensor_pipeline": (C.c_int, [H, C.c_int]),
     "gbqv_set_run_tile_qubits": (C.c_int, [H, C.c_int]),
+    "gbqv_set_run_jit": (C.c_int, [H, C.c_int]),
+    "gbqv_run_jit_compile_check": (C.c_int, [C.c_int, C.c_char_p, C.c_size_t]),
+    "gbqv_run_jit_counts": (C.c_int, [u64p, u64p]),
     "gbqv_sample_measure": (C.c_int, [H, dp, C.c_uint64, u64p]),
     "gbqv_expval_pauli": (C.c_int, [H, u64p, C.c_int, C.c_char_p, c128, dp]),
     "gbqv_expval_pauli_many": (C.c_int, [H, C.c_int, u64p, C.POINTER(C.c_int), C.POINTER(C.c_char_p), dp, dp, dp]),

@@ -1092,6 +1092,36 @@ extern "C" int gbqv_set_run_tile_qubits(gbqv_handle h, int tile_qubits) {
   });
 }
 
+extern "C" int gbqv_set_run_jit(gbqv_handle h, int mode) {
+  return guard(h, [&] {
+    need_handle(h);
+    REQUIRE(mode >= 0 && mode <= 2, GBQV_ERR_ARG, "run compile mode must be 0, 1 or 2");
+    h->dev.run_jit = mode;
+  });
+}
+
+extern "C" int gbqv_run_jit_counts(uint64_t *compiled, uint64_t *launched) {
+  return guard(nullptr, [&] {
+    REQUIRE(compiled && launched, GBQV_ERR_ARG, "null output");
+    run_jit_counts(*compiled, *launched);
+  });
+}
+
+extern "C" int gbqv_run_jit_compile_check(int double_precision, char *log, size_t cap) {
+  std::string l = "NVRTC is not available";
+  int rc = 0;
+  const int g = guard(nullptr, [&] {
+    REQUIRE(run_jit_available(), GBQV_ERR_ARG, l);
+    rc = run_jit_compile_check(double_precision != 0, l);
+  });
+  if (log && cap) {
+    const size_t k = std::min(cap - 1, l.size());
+    std::memcpy(log, l.data(), k);
+    log[k] = '\0';
+  }
+  return g ? g : rc;
+}
+
 extern "C" int gbqv_set_blocking(gbqv_handle h, int blocking) {
   return guard(h, [&] {
     need_handle(h);

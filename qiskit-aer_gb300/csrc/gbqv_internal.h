@@ -52,6 +52,7 @@ struct Device {
   int sample_index_size = 10;  // QubitVector::sample_measure_index_size_ (2^this blocks)
   int *tc_status = nullptr; // device word raised by a tcgen05 kernel whose bounded wait gave up
   int tc_test_stall = 0;    // test hook: the tcgen05 complex128 kernel withholds its first tile's commit
+  int run_jit = 1;          // register-tile runs compiled for their op sequence: 0 never, 1 from a run's second use, 2 always
   // tcgen05 kernel: 128-byte-swizzled TMA descriptors of the state viewed as
   // rows of 8 amplitudes, box height 2^(L-3) for run length L = 7..12; built
   // on first use, dropped when the state buffer changes
@@ -193,6 +194,11 @@ void launch_run(Device &dev, const std::vector<const RunOp *> &ops, const RunBou
 // The register-tile form of a run (gbqv_runreg.cu), given the tile qubits
 // (ascending) and the length c of their contiguous low prefix; false when the
 // run has an op it does not take or the tile is too small.
+// NVRTC found (the specialised runs of gbqv_runreg.cu can be compiled), and
+// the host check of their source generator (0: compiled; log on failure).
+bool run_jit_available();
+void run_jit_counts(uint64_t &compiled, uint64_t &launched);
+int run_jit_compile_check(bool dbl, std::string &log);
 bool launch_run_reg(Device &dev, const std::vector<const RunOp *> &ops, const std::vector<int> &tile_qubits, int c,
                     const RunBound *bound);
 // Bytes of per-binding matrices one bound run may hold per binding.

@@ -14,13 +14,23 @@
 // register bits; the host picks each segment's register bits by next use.
 // Arithmetic per op is that of the shared-memory run kernel (the same
 // products; a lane op sums its two terms in the order own, partner).
+#include <cuda.h>
+#include <dlfcn.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "gbqv_internal.h"
+#include "gbqv_runreg_dev_src.inc"  // kRunRegDevSrc: the text of gbqv_runreg_dev.cuh (written by the build)
 
 namespace gbqv {
 namespace {
@@ -67,106 +77,7 @@ struct RegParams {
   RegSeg segs[kRegMaxSegs];
 };
 
-template <typename T>
-__device__ __forceinline__ T cmul(T a, T b) {
-  T r;
-  r.x = a.x * b.x - a.y * b.y;
-  r.y = a.x * b.y + a.y * b.x;
-  return r;
-}
-template <typename T>
-__device__ __forceinline__ void cfma(T &acc, T a, T b) {
-  acc.x = fma(a.x, b.x, acc.x);
-  acc.x = fma(-a.y, b.y, acc.x);
-  acc.y = fma(a.x, b.y, acc.y);
-  acc.y = fma(a.y, b.x, acc.y);
-}
-template <typename T>
-__device__ __forceinline__ T czero() {
-  T z;
-  z.x = 0;
-  z.y = 0;
-  return z;
-}
-template <typename T>
-__device__ __forceinline__ T shfl_x(T v, int mask) {
-  T r;
-  r.x = __shfl_xor_sync(0xffffffffu, v.x, mask);
-  r.y = __shfl_xor_sync(0xffffffffu, v.y, mask);
-  return r;
-}
-
-// ---- ops on the register-held amplitudes v[0..R) ----
-template <typename T, int R, int J>
-__device__ __forceinline__ void reg_dense1(T (&v)[R], const T *m) {
-  const T m00 = m[0], m10 = m[1], m01 = m[2], m11 = m[3];
-#pragma unroll
-  for (int p = 0; p < R / 2; ++p) {
-    const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
-    const T a0 = v[i0], a1 = v[i1];
-    T r0 = czero<T>(), r1 = czero<T>();
-    cfma(r0, m00, a0);
-    cfma(r0, m01, a1);
-    cfma(r1, m10, a0);
-    cfma(r1, m11, a1);
-    v[i0] = r0;
-    v[i1] = r1;
-  }
-}
-// real matrix: the complex FMAs above with every imaginary matrix term zero
-template <typename T, int R, int J>
-__device__ __forceinline__ void reg_dense1_real(T (&v)[R], const T *m) {
-  const auto m00 = m[0].x, m10 = m[1].x, m01 = m[2].x, m11 = m[3].x;
-#pragma unroll
-  for (int p = 0; p < R / 2; ++p) {
-    const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
-    const T a0 = v[i0], a1 = v[i1];
-    T r0, r1;
-    r0.x = fma(m01, a1.x, m00 * a0.x);
-    r0.y = fma(m01, a1.y, m00 * a0.y);
-    r1.x = fma(m11, a1.x, m10 * a0.x);
-    r1.y = fma(m11, a1.y, m10 * a0.y);
-    v[i0] = r0;
-    v[i1] = r1;
-  }
-}
-template <typename T, int R, int J>
-__device__ __forceinline__ void reg_diag1(T (&v)[R], const T *d) {
-  const T d0 = d[0], d1 = d[1];
-#pragma unroll
-  for (int i = 0; i < R; ++i) v[i] = cmul(v[i], ((i >> J) & 1) ? d1 : d0);
-}
-template <typename T, int R, int J>
-__device__ __forceinline__ void reg_mcx(T (&v)[R], bool tcond, uint32_t crm) {
-#pragma unroll
-  for (int p = 0; p < R / 2; ++p) {
-    const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
-    const bool sw = tcond && (((uint32_t)i0 & crm) == crm);
-    const T a0 = v[i0], a1 = v[i1];
-    v[i0] = sw ? a1 : a0;
-    v[i1] = sw ? a0 : a1;
-  }
-}
-template <typename T, int R, int A, int B>
-__device__ __forceinline__ void reg_dense2(T (&v)[R], const T *m) {
-#pragma unroll
-  for (int q = 0; q < R / 4; ++q) {
-    // insert zeros at A then B (A < B)
-    int i = ((q >> A) << (A + 1)) | (q & ((1 << A) - 1));
-    i = ((i >> B) << (B + 1)) | (i & ((1 << B) - 1));
-    const int idx[4] = {i, i | (1 << A), i | (1 << B), i | (1 << A) | (1 << B)};
-    T x[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) x[c] = v[idx[c]];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      T acc = czero<T>();
-#pragma unroll
-      for (int c = 0; c < 4; ++c) cfma(acc, m[r + 4 * c], x[c]);
-      v[idx[r]] = acc;
-    }
-  }
-}
+#include "gbqv_runreg_dev.cuh"
 
 template <typename T, int R, int A>
 __device__ __forceinline__ void dense2_b(T (&v)[R], const T *m, int b) {
@@ -219,50 +130,21 @@ __device__ __forceinline__ void apply_reg_op(T (&v)[R], const RegOp &op, const T
         default: break;
       }
       return;
-    case RK_DENSE1_LANE: {
-      // this lane holds row `bit` of the pair: new = m[bit][bit] * own + m[bit][1-bit] * partner's
-      const int bit = (lane >> op.a) & 1;
-      const T ms = bit ? mat[3] : mat[0], mo = bit ? mat[1] : mat[2];
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const T o = shfl_x(v[i], 1 << op.a);
-        T r = czero<T>();
-        cfma(r, ms, v[i]);
-        cfma(r, mo, o);
-        v[i] = r;
-      }
+    case RK_DENSE1_LANE:
+      lane_dense1<T, R>(v, mat, op.a, lane);
       return;
-    }
-    case RK_DENSE1_REAL_LANE: {
-      const int bit = (lane >> op.a) & 1;
-      const auto ms = bit ? mat[3].x : mat[0].x, mo = bit ? mat[1].x : mat[2].x;
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const T o = shfl_x(v[i], 1 << op.a);
-        T r;
-        r.x = fma(mo, o.x, ms * v[i].x);
-        r.y = fma(mo, o.y, ms * v[i].y);
-        v[i] = r;
-      }
+    case RK_DENSE1_REAL_LANE:
+      lane_dense1_real<T, R>(v, mat, op.a, lane);
       return;
-    }
     case RK_DIAG_T: {
       uint32_t td = 0;
       for (int j = 0; j < op.k; ++j) td |= (((uint32_t)tid >> op.dtpos[j]) & 1u) << j;
-      const T d = mat[td];
-#pragma unroll
-      for (int i = 0; i < R; ++i) v[i] = cmul(v[i], d);
+      thread_diag<T, R>(v, mat, td);
       return;
     }
-    case RK_MCX_LANE: {
-      const bool tcond = ((uint32_t)tid & op.ctm) == op.ctm;
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const T o = shfl_x(v[i], 1 << op.a);
-        if (tcond && (((uint32_t)i & op.crm) == op.crm)) v[i] = o;
-      }
+    case RK_MCX_LANE:
+      lane_mcx<T, R>(v, op.a, ((uint32_t)tid & op.ctm) == op.ctm, op.crm);
       return;
-    }
     case RK_DIAG: {
       uint32_t td = 0;
       for (int j = 0; j < op.k; ++j)
@@ -273,24 +155,6 @@ __device__ __forceinline__ void apply_reg_op(T (&v)[R], const RegOp &op, const T
     }
     default: return;
   }
-}
-
-// 16-byte asynchronous global -> shared copies (LDGSTS): the next tile
-// streams in while the current one is computed.
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-__device__ __forceinline__ uint64_t tile_base(uint64_t t, const uint64_t *lowmask, int m) {
-  for (int j = 0; j < m; ++j) {
-    const uint64_t msk = lowmask[j];
-    t = ((t & ~msk) << 1) | (t & msk);
-  }
-  return t;
 }
 
 // Two tile buffers: tile t + gridDim.x is fetched with cp.async into one while
@@ -436,6 +300,392 @@ void launch_reg_t(Device &dev, RegParams &P, const std::vector<T> &pool, const s
   check_launch("run kernel");
 }
 
+// ---------------------------------------------------------------------------
+// Runs specialised to their op sequence.  The interpreting kernel above reads
+// each op's kind and bits from shared memory and dispatches through a switch;
+// the register array then has to sit in the same registers after every case,
+// and the moves and dispatch cost more instructions than the arithmetic
+// (MOV was the most frequent opcode of k_run_reg<float2,4>).  A run whose
+// structure (ops, bits, matrix offsets, segments) recurs is compiled once by
+// NVRTC into a kernel where every op is a straight call with its bits as
+// template arguments; the matrices stay data.  Tiered: the interpreting kernel
+// serves a structure's first execution, its second compiles (about a
+// second), later ones reuse the module.  Without NVRTC (or on a compile
+// error) the interpreting kernel keeps serving, on the GPU.
+
+struct Nvrtc {
+  using Prog = void *;
+  int (*create)(Prog *, const char *, const char *, int, const char *const *, const char *const *) = nullptr;
+  int (*compile)(Prog, int, const char *const *) = nullptr;
+  int (*cubin_size)(Prog, size_t *) = nullptr;
+  int (*cubin)(Prog, char *) = nullptr;
+  int (*log_size)(Prog, size_t *) = nullptr;
+  int (*log)(Prog, char *) = nullptr;
+  int (*destroy)(Prog *) = nullptr;
+  bool ok = false;
+};
+
+const Nvrtc &nvrtc() {
+  static Nvrtc n = [] {
+    Nvrtc r;
+    void *h = dlopen("libnvrtc.so.13", RTLD_NOW | RTLD_LOCAL);
+    if (!h) h = dlopen("libnvrtc.so", RTLD_NOW | RTLD_LOCAL);
+    if (!h) return r;
+    auto sym = [&](auto &f, const char *name) { f = reinterpret_cast<std::remove_reference_t<decltype(f)>>(dlsym(h, name)); };
+    sym(r.create, "nvrtcCreateProgram");
+    sym(r.compile, "nvrtcCompileProgram");
+    sym(r.cubin_size, "nvrtcGetCUBINSize");
+    sym(r.cubin, "nvrtcGetCUBIN");
+    sym(r.log_size, "nvrtcGetProgramLogSize");
+    sym(r.log, "nvrtcGetProgramLog");
+    sym(r.destroy, "nvrtcDestroyProgram");
+    r.ok = r.create && r.compile && r.cubin_size && r.cubin && r.log_size && r.log && r.destroy;
+    return r;
+  }();
+  return n;
+}
+
+struct DriverModule {
+  CUresult (*load)(CUmodule *, const void *) = nullptr;
+  CUresult (*get)(CUfunction *, CUmodule, const char *) = nullptr;
+  CUresult (*attr)(CUfunction, CUfunction_attribute, int) = nullptr;
+  CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, CUstream,
+                     void **, void **) = nullptr;
+  bool ok = false;
+};
+
+const DriverModule &driver_module() {
+  static DriverModule d = [] {
+    DriverModule r;
+    auto entry = [](const char *name) -> void * {
+      void *ptr = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPointByVersion(name, &ptr, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+          q != cudaDriverEntryPointSuccess)
+        ptr = nullptr;
+      cudaGetLastError();
+      return ptr;
+    };
+    r.load = reinterpret_cast<decltype(r.load)>(entry("cuModuleLoadData"));
+    r.get = reinterpret_cast<decltype(r.get)>(entry("cuModuleGetFunction"));
+    r.attr = reinterpret_cast<decltype(r.attr)>(entry("cuFuncSetAttribute"));
+    r.launch = reinterpret_cast<decltype(r.launch)>(entry("cuLaunchKernel"));
+    r.ok = r.load && r.get && r.attr && r.launch;
+    return r;
+  }();
+  return d;
+}
+
+// Kernel arguments of a specialised run (by value).
+struct JitArgs {
+  uint64_t ntiles, nbind;
+  uint64_t lowmask[24];
+  int T[24];
+  int state_bits;
+};
+
+const char *kJitKernel = R"GBQV(
+struct JitArgs {
+  uint64_t ntiles, nbind;
+  uint64_t lowmask[24];
+  int T[24];
+  int state_bits;
+};
+extern "C" __global__ void __launch_bounds__(512, 1)
+    k_run_jit(TT *__restrict__ psi, const TT *__restrict__ pool, const TT *__restrict__ bpool, const JitArgs A) {
+  constexpr uint32_t L = 1u << M, cmask = (1u << C) - 1, kPer = 16 / sizeof(TT);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x, lane = tid & 31;
+  TT *buf0 = reinterpret_cast<TT *>(smem_raw);
+  TT *buf1 = buf0 + L;
+  TT *mats = buf1 + L;
+  TT *bmats = mats + POOL;
+  uint64_t *hi = reinterpret_cast<uint64_t *>(smem_raw + HIOFF);
+  for (int i = tid; i < POOL; i += 512) mats[i] = pool[i];
+  for (uint32_t h = tid; h < (1u << (M - C)); h += 512) {
+    uint64_t a = 0;
+    for (int j = C; j < M; ++j)
+      if ((h >> (j - C)) & 1) a |= 1ULL << A.T[j];
+    hi[h] = a;
+  }
+  __syncthreads();
+  auto skip = [&](uint64_t gb) { return BOUND > 0 && (gb >> A.state_bits) >= A.nbind; };
+  auto fetch = [&](uint64_t t, TT *buf) {
+    const uint64_t gb = tile_base(t, A.lowmask, M);
+    if (skip(gb)) return;
+    for (uint32_t ch = tid; ch < L / kPer; ch += 512) {
+      const uint32_t l = ch * kPer;
+      cp_async16(buf + l, psi + (gb | hi[l >> C] | (l & cmask)));
+    }
+  };
+  uint64_t t = blockIdx.x;
+  if (t < A.ntiles) fetch(t, buf0);
+  cp_async_commit();
+  for (int k = 0; t < A.ntiles; t += gridDim.x, ++k) {
+    TT *tile = (k & 1) ? buf1 : buf0;
+    if (t + gridDim.x < A.ntiles) fetch(t + gridDim.x, (k & 1) ? buf0 : buf1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const uint64_t gbase = tile_base(t, A.lowmask, M);
+    if (skip(gbase)) continue;
+    if (BOUND > 0) {
+      const TT *src = bpool + (gbase >> A.state_bits) * (uint64_t)BOUND;
+      for (int i = tid; i < BOUND; i += 512) bmats[i] = src[i];
+      __syncthreads();
+    }
+    TT v[R];
+    uint32_t tpart;
+SEGMENTS
+    __syncthreads();
+    for (uint32_t l = tid; l < L; l += 512) psi[gbase | hi[l >> C] | (l & cmask)] = tile[l];
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+}
+)GBQV";
+
+// The CUDA source of a run's specialised kernel.
+std::string jit_source(bool dbl, const RegParams &P) {
+  const int R = 1 << P.rb;
+  std::ostringstream o;
+  o << "typedef unsigned int uint32_t;\ntypedef unsigned long long uint64_t;\ntypedef unsigned short uint16_t;\n"
+       "typedef unsigned char uint8_t;\ntypedef signed char int8_t;\ntypedef int int32_t;\n"
+    << kRunRegDevSrc << "\n";
+  const size_t tsz = dbl ? 16 : 8;
+  const size_t hioff = (tsz * (2 * (1u << P.m) + (size_t)P.pool_elems + (size_t)P.bound_elems) + 7) & ~size_t(7);
+  o << "typedef " << (dbl ? "double2" : "float2") << " TT;\n"
+    << "constexpr int R = " << R << ", M = " << P.m << ", C = " << P.c << ", POOL = " << P.pool_elems
+    << ", BOUND = " << P.bound_elems << ";\nconstexpr uint32_t HIOFF = " << hioff << ";\n";
+  std::ostringstream seg;
+  auto tpart_expr = [&](const RegSeg &S) {
+    std::ostringstream e;
+    for (int q = 0; q < kThreadBits; ++q) e << (q ? " | " : "") << "((((uint32_t)tid >> " << q << ") & 1u) << " << (int)S.tb[q] << ")";
+    return e.str();
+  };
+  for (int si = 0; si < P.nsegs; ++si) {
+    const RegSeg &S = P.segs[si];
+    seg << "    {\n";
+    if (si > 0) {
+      const RegSeg &Sp = P.segs[si - 1];
+      seg << "      __syncthreads();\n";
+      for (int i = 0; i < R; ++i) seg << "      tile[tpart | " << Sp.rp[i] << "u] = v[" << i << "];\n";
+      seg << "      __syncthreads();\n";
+    }
+    seg << "      tpart = " << tpart_expr(S) << ";\n";
+    for (int i = 0; i < R; ++i) seg << "      v[" << i << "] = tile[tpart | " << S.rp[i] << "u];\n";
+    for (int oi = S.first; oi < S.first + S.count; ++oi) {
+      const RegOp &op = P.ops[oi];
+      const std::string mat = std::string(op.bound ? "bmats" : "mats") + " + " + std::to_string(op.mat_off);
+      const std::string tcond = "((((uint32_t)tid) & " + std::to_string(op.ctm) + "u) == " + std::to_string(op.ctm) + "u)";
+      switch (op.kind) {
+        case RK_DENSE1: seg << "      reg_dense1<TT, R, " << op.a << ">(v, " << mat << ");\n"; break;
+        case RK_DENSE1_REAL: seg << "      reg_dense1_real<TT, R, " << op.a << ">(v, " << mat << ");\n"; break;
+        case RK_DIAG1: seg << "      reg_diag1<TT, R, " << op.a << ">(v, " << mat << ");\n"; break;
+        case RK_MCX: seg << "      reg_mcx<TT, R, " << op.a << ">(v, " << tcond << ", " << op.crm << "u);\n"; break;
+        case RK_DENSE2: seg << "      reg_dense2<TT, R, " << op.a << ", " << op.b << ">(v, " << mat << ");\n"; break;
+        case RK_DENSE1_LANE: seg << "      lane_dense1<TT, R>(v, " << mat << ", " << op.a << ", lane);\n"; break;
+        case RK_DENSE1_REAL_LANE: seg << "      lane_dense1_real<TT, R>(v, " << mat << ", " << op.a << ", lane);\n"; break;
+        case RK_MCX_LANE: seg << "      lane_mcx<TT, R>(v, " << op.a << ", " << tcond << ", " << op.crm << "u);\n"; break;
+        case RK_DIAG_T:
+        case RK_DIAG: {
+          std::ostringstream td;
+          td << "0u";
+          for (int j = 0; j < op.k; ++j)
+            if (op.dtpos[j] >= 0) td << " | ((((uint32_t)tid >> " << (int)op.dtpos[j] << ") & 1u) << " << j << ")";
+          if (op.kind == RK_DIAG_T) {
+            seg << "      thread_diag<TT, R>(v, " << mat << ", " << td.str() << ");\n";
+          } else {
+            seg << "      {\n        const uint32_t td = " << td.str() << ";\n        const TT *dm = " << mat << ";\n";
+            for (int i = 0; i < R; ++i) seg << "        v[" << i << "] = cmul(v[" << i << "], dm[td | " << (int)op.div[i] << "u]);\n";
+            seg << "      }\n";
+          }
+          break;
+        }
+        default: throw Error(1, "run op kind without a specialised form");
+      }
+    }
+    seg << "    }\n";
+  }
+  const RegSeg &Sl = P.segs[P.nsegs - 1];
+  seg << "    __syncthreads();\n";
+  for (int i = 0; i < R; ++i) seg << "    tile[tpart | " << Sl.rp[i] << "u] = v[" << i << "];\n";
+  std::string k = kJitKernel;
+  const size_t at = k.find("SEGMENTS\n");
+  k.replace(at, 9, seg.str());
+  o << k;
+  return o.str();
+}
+
+// process-wide counts: specialised kernels compiled, and launched
+std::atomic<uint64_t> g_jit_compiled{0}, g_jit_launched{0};
+
+struct JitEntry {
+  int uses = 0;
+  bool failed = false;
+  CUfunction fn = nullptr;
+  size_t smem_attr = 0;
+};
+
+std::mutex &jit_mutex() {
+  static std::mutex m;
+  return m;
+}
+std::unordered_map<std::string, JitEntry> &jit_cache() {
+  static std::unordered_map<std::string, JitEntry> c;
+  return c;
+}
+
+// NVRTC: the source to a cubin for sm_103a; false (with the compiler's log)
+// on failure.
+bool jit_cubin(const std::string &src, std::vector<char> &cubin, std::string &log) {
+  const Nvrtc &n = nvrtc();
+  if (!n.ok) {
+    log = "NVRTC is not available";
+    return false;
+  }
+  Nvrtc::Prog prog = nullptr;
+  if (n.create(&prog, src.c_str(), "gbqv_run_jit.cu", 0, nullptr, nullptr) != 0) {
+    log = "nvrtcCreateProgram failed";
+    return false;
+  }
+  const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17"};
+  const int rc = n.compile(prog, 2, opts);
+  size_t ls = 0;
+  n.log_size(prog, &ls);
+  log.assign(ls, '\0');
+  if (ls) n.log(prog, &log[0]);
+  if (rc == 0) {
+    size_t cs = 0;
+    n.cubin_size(prog, &cs);
+    cubin.resize(cs);
+    n.cubin(prog, cubin.data());
+  }
+  n.destroy(&prog);
+  return rc == 0 && !cubin.empty();
+}
+
+// Compile and load: the kernel, or null (log says why).
+CUfunction jit_compile(const std::string &src, std::string &log) {
+  const DriverModule &d = driver_module();
+  if (!d.ok) {
+    log = "the driver's module entry points are not available";
+    return nullptr;
+  }
+  std::vector<char> cubin;
+  if (!jit_cubin(src, cubin, log)) return nullptr;
+  CUmodule mod = nullptr;  // kept loaded for the life of the process (the cache holds its function)
+  CUfunction fn = nullptr;
+  if (d.load(&mod, cubin.data()) != CUDA_SUCCESS || d.get(&fn, mod, "k_run_jit") != CUDA_SUCCESS) {
+    log += "\nmodule load failed";
+    return nullptr;
+  }
+  return fn;
+}
+
+// The specialised kernel for P, or null (interpreting kernel) under the
+// tiering rule or when compiling fails.
+CUfunction jit_kernel(const Device &dev, bool dbl, const RegParams &P) {
+  if (dev.run_jit == 0) return nullptr;
+  const std::string src = jit_source(dbl, P);
+  std::lock_guard<std::mutex> g(jit_mutex());
+  JitEntry &e = jit_cache()[src];
+  ++e.uses;
+  if (e.fn || e.failed) return e.fn;
+  if (dev.run_jit == 1 && e.uses < 2) return nullptr;
+  std::string log;
+  e.fn = jit_compile(src, log);
+  e.failed = !e.fn;
+  if (e.fn) ++g_jit_compiled;
+  return e.fn;
+}
+
+// A synthetic run (every op kind, three segments) compiled with NVRTC
+// without loading it: the host-side check of the source generator.
+int jit_compile_check(bool dbl, std::string &log) {
+  auto P = std::make_unique<RegParams>();
+  std::memset(P.get(), 0, sizeof(RegParams));
+  P->rb = dbl ? 3 : 4;
+  P->m = P->rb + kThreadBits;
+  P->c = 4;
+  P->nsegs = 3;
+  const int kinds[] = {RK_DENSE1, RK_DENSE1_REAL, RK_DENSE1_LANE, RK_DENSE2, RK_DIAG1, RK_DIAG,
+                       RK_MCX,    RK_MCX_LANE,    RK_DIAG_T,      RK_DENSE1_REAL_LANE};
+  P->nops = 10;
+  for (int o = 0; o < P->nops; ++o) {
+    RegOp &op = P->ops[o];
+    op.kind = kinds[o];
+    op.k = op.kind == RK_DENSE2 || op.kind == RK_DIAG || op.kind == RK_DIAG_T ? 2 : 1;
+    op.a = op.kind == RK_DENSE2 ? 0 : 1;
+    op.b = 2;
+    op.bound = o & 1;
+    op.mat_off = 4 * o;
+    op.ctm = op.kind == RK_MCX || op.kind == RK_MCX_LANE ? 0x20u : 0u;
+    op.crm = op.kind == RK_MCX ? 0x1u : 0u;
+    op.dtpos[0] = op.kind == RK_DIAG ? -1 : 5;
+    op.dtpos[1] = 6;
+    for (int i = 0; i < 32; ++i) op.div[i] = (uint8_t)(i & 1);
+  }
+  for (int sgi = 0; sgi < 3; ++sgi) {
+    RegSeg &S = P->segs[sgi];
+    S.first = sgi == 0 ? 0 : sgi == 1 ? 4 : 7;
+    S.count = sgi == 0 ? 4 : 3;
+    for (int i = 0; i < (1 << P->rb); ++i) S.rp[i] = (uint16_t)(i << sgi);
+    for (int q = 0; q < kThreadBits; ++q) S.tb[q] = (uint8_t)(q < sgi ? q : q + P->rb);
+  }
+  P->pool_elems = 40;
+  P->bound_elems = 40;
+  std::vector<char> cubin;
+  return jit_cubin(jit_source(dbl, *P), cubin, log) ? 0 : 1;
+}
+
+template <typename T, int RB>
+bool launch_reg_jit(Device &dev, RegParams &P, const std::vector<T> &pool, const std::vector<T> &bpool) {
+  CUfunction fn = jit_kernel(dev, sizeof(T) == 16, P);
+  if (!fn) return false;
+  const size_t poolb = pool.size() * sizeof(T), bpoolb = bpool.size() * sizeof(T);
+  const size_t bpool_off = (poolb + 255) & ~size_t(255);
+  grow(dev.mat, dev.mat_cap, bpool_off + bpoolb + 256);
+  char *base = reinterpret_cast<char *>(dev.mat);
+  if (poolb) cuda_check(cudaMemcpyAsync(base, pool.data(), poolb, cudaMemcpyHostToDevice, dev.stream), "run upload");
+  if (bpoolb)
+    cuda_check(cudaMemcpyAsync(base + bpool_off, bpool.data(), bpoolb, cudaMemcpyHostToDevice, dev.stream),
+               "run upload");
+  size_t smem = (sizeof(T) * (2 * (1u << P.m) + pool.size() + (size_t)P.bound_elems) + 7) & ~size_t(7);
+  smem += sizeof(uint64_t) * (1u << (P.m - P.c));
+  const DriverModule &d = driver_module();
+  {
+    std::lock_guard<std::mutex> g(jit_mutex());
+    // one attribute per function, raised to the largest size it has launched with
+    JitEntry *e = nullptr;
+    for (auto &kv : jit_cache())
+      if (kv.second.fn == fn) e = &kv.second;
+    if (e && e->smem_attr < smem) {
+      if (d.attr(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem) != CUDA_SUCCESS)
+        throw Error(3, "run kernel attribute");
+      e->smem_attr = smem;
+    }
+  }
+  JitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.ntiles = P.ntiles;
+  a.nbind = P.nbind;
+  a.state_bits = P.state_bits;
+  for (int j = 0; j < P.m; ++j) {
+    a.lowmask[j] = P.tile_lowmask[j];
+    a.T[j] = P.T[j];
+  }
+  T *psi = reinterpret_cast<T *>(dev.state);
+  const T *pp = reinterpret_cast<const T *>(base), *bp = reinterpret_cast<const T *>(base + bpool_off);
+  void *args[] = {&psi, &pp, &bp, &a};
+  const uint64_t grid = std::min<uint64_t>(P.ntiles, (uint64_t)sm_count());
+  if (d.launch(fn, (unsigned)grid, 1, 1, kRegThreads, 1, 1, (unsigned)smem, dev.stream, args, nullptr) != CUDA_SUCCESS)
+    throw Error(3, "specialised run kernel launch failed");
+  check_launch("specialised run kernel");
+  ++g_jit_launched;
+  return true;
+}
+
 // Register bits for a new segment: `need` plus the tile bits whose next use
 // as a dense / X-target bit comes soonest (ties: higher bits first, so low
 // bits stay thread bits and shared-memory accesses stay contiguous).
@@ -459,6 +709,13 @@ std::vector<int> choose_regs(const std::vector<int> &need, int rb, int m,
 }
 
 }  // namespace
+
+bool run_jit_available() { return nvrtc().ok; }
+void run_jit_counts(uint64_t &compiled, uint64_t &launched) {
+  compiled = g_jit_compiled.load();
+  launched = g_jit_launched.load();
+}
+int run_jit_compile_check(bool dbl, std::string &log) { return jit_compile_check(dbl, log); }
 
 // A run on the register-tile kernel; false when the run has an op it does
 // not take (a dense op on more than 2 qubits) or the tile is too small.
@@ -643,10 +900,15 @@ bool launch_run_reg(Device &dev, const std::vector<const RunOp *> &ops, const st
         }
     }
     switch (rb) {
-      case 2: launch_reg_t<T, 2>(dev, *P, pool, bpool); break;
-      case 3: launch_reg_t<T, 3>(dev, *P, pool, bpool); break;
+      case 2:
+        if (!launch_reg_jit<T, 2>(dev, *P, pool, bpool)) launch_reg_t<T, 2>(dev, *P, pool, bpool);
+        break;
+      case 3:
+        if (!launch_reg_jit<T, 3>(dev, *P, pool, bpool)) launch_reg_t<T, 3>(dev, *P, pool, bpool);
+        break;
       case 4:
-        if constexpr (sizeof(T) == 8) launch_reg_t<T, 4>(dev, *P, pool, bpool);
+        if constexpr (sizeof(T) == 8)
+          if (!launch_reg_jit<T, 4>(dev, *P, pool, bpool)) launch_reg_t<T, 4>(dev, *P, pool, bpool);
         break;
       default: break;
     }

@@ -111,7 +111,7 @@ class AerSimulator:
                  noise_model=None, fusion_enable: bool = True, fusion_max_qubit: int | None = None,
                  fusion_threshold: int | None = None, fusion_cost_factor: float = 1.8,
                  fusion_avx2_costs: bool = True, blocking_enable: bool = True, seed_simulator: int | None = None,
-                 autotune: bool = False, autotune_cache: str | None = None):
+                 autotune: bool = False, autotune_cache: str | None = None, runtime_compile: int = 1):
         if method not in self.METHODS:
             raise ValueError(f"method must be one of {self.METHODS}")
         if device != "GPU":
@@ -122,7 +122,8 @@ class AerSimulator:
         self.options = dict(fusion_enable=fusion_enable, fusion_max_qubit=fusion_max_qubit,
                             fusion_threshold=fusion_threshold, fusion_cost_factor=fusion_cost_factor,
                             fusion_avx2_costs=fusion_avx2_costs, blocking_enable=blocking_enable,
-                            seed_simulator=seed_simulator, autotune=autotune, autotune_cache=autotune_cache)
+                            seed_simulator=seed_simulator, autotune=autotune, autotune_cache=autotune_cache,
+                            runtime_compile=runtime_compile)
         self._tuner = None
 
     # ---- options (AerBackend.set_option / set_options, aerbackend.py:623-658;
@@ -130,7 +131,8 @@ class AerSimulator:
     # aer_simulator.py:877-935) ----
     _DEFAULTS = dict(method="statevector", device="GPU", precision="double", noise_model=None, fusion_enable=True,
                      fusion_max_qubit=None, fusion_threshold=None, fusion_cost_factor=1.8, fusion_avx2_costs=True,
-                     blocking_enable=True, seed_simulator=None, autotune=False, autotune_cache=None)
+                     blocking_enable=True, seed_simulator=None, autotune=False, autotune_cache=None,
+                     runtime_compile=1)
 
     @property
     def name(self) -> str:
@@ -163,6 +165,10 @@ class AerSimulator:
             self.precision = value
         elif key == "noise_model":
             self.noise_model = value
+        elif key == "runtime_compile":
+            if value not in (0, 1, 2):
+                raise ValueError(f"Invalid runtime_compile {value}: 0 (never), 1 (recurring runs) or 2 (always)")
+            self.options[key] = value
         else:
             self.options[key] = value
             if key == "autotune_cache":
@@ -171,6 +177,13 @@ class AerSimulator:
     def set_options(self, **fields) -> None:
         for key, value in fields.items():
             self.set_option(key, value)
+
+    def _state_options(self, st) -> None:
+        """Per-state engine settings taken from the options: runs compiled
+        for their op sequence (gbqv_set_run_jit) unless runtime_compile is
+        the default."""
+        if self.options["runtime_compile"] != 1:
+            A.check(st._L.gbqv_set_run_jit(st.handle, int(self.options["runtime_compile"])), st.handle)
 
     def tuner(self) -> Autotuner:
         """The schedule autotuner of this simulator: its own cache file when
@@ -397,6 +410,7 @@ class AerSimulator:
                     if st is not None:
                         st.close()
                     st, st_bits = QubitVector(n + b, self.precision), b
+                    self._state_options(st)
                 A.check(L.gbqv_execute_bound(st.handle, nc.handle, first, cnt), st.handle)
                 if meas and shots > 0:
                     # every binding draws from its own RngEngine stream, seed_simulator + 2113 k
@@ -444,6 +458,7 @@ class AerSimulator:
         cls = {"density_matrix": DensityMatrix, "unitary": UnitaryMatrix}.get(self.method, QubitVector)
         data = {}
         with cls(circuit.num_qubits, self.precision) as st:
+            self._state_options(st)
             if not self.options["blocking_enable"]:
                 A.check(st._L.gbqv_set_blocking(st.handle, 0))
             elif self.options["autotune"] and self.method == "statevector":

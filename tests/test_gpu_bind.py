@@ -7,6 +7,8 @@ by one (QubitVector arithmetic): complex128 to 1e-12, complex64 to the
 engine's single-precision tolerance.  Also: chunked stacks (bindings split
 over several launches), zero padding states, the per-binding loop used for
 circuits with measurements, and EstimatorV2 broadcasting."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -279,3 +281,40 @@ def test_stacked_expvals_against_oracle(precision, tol):
         o = O.OracleQV(n, v.astype(np.complex64) if precision == "single" else v)
         for t, lab in enumerate(labels):
             assert abs(got[t, j] - o.expval_pauli(list(range(n)), lab)) < tol, (lab, j)
+
+
+@pytest.mark.parametrize("precision,tol", [("double", 1e-13), ("single", 2e-6)])
+def test_specialised_runs_match_interpreting_runs(precision, tol):
+    """Bound runs compiled for their op sequence (runtime_compile=2) give the
+    interpreting kernel's states (runtime_compile=0) and the oracle's, for a
+    circuit of every gate kind over 9 bindings of a 15-qubit state (runs of
+    the register-tile kernel with register, lane and thread bits); a repeat
+    with the default tiering (1) compiles on the second execution."""
+    P = pkg()
+    rng = np.random.default_rng(812)
+    n, nbind = 15, 9
+    qc, params = random_bound_circuit(P, n, 80, 6, rng)
+    qc.save_statevector()
+    values = {p: rng.uniform(-np.pi, np.pi, nbind) for p in params}
+    binds = [{p: v for p, v in values.items() if p in qc.parameters}]
+    L = P.lib()
+
+    def launched():
+        compiled, launches = ctypes.c_uint64(), ctypes.c_uint64()
+        P._capi.check(L.gbqv_run_jit_counts(ctypes.byref(compiled), ctypes.byref(launches)))
+        return launches.value
+
+    res, used = {}, {}
+    for mode in (0, 2, 1):
+        sim = P.AerSimulator(precision=precision, runtime_compile=mode)
+        before = launched()
+        for _ in range(2 if mode == 1 else 1):
+            res[mode] = sim.run(qc, parameter_binds=binds, seed_simulator=5)
+        used[mode] = launched() - before
+    assert used[0] == 0 and used[2] > 0 and used[1] > 0, used
+    for j in range(nbind):
+        a, b, c = (np.asarray(res[m].get_statevector(j)) for m in (0, 2, 1))
+        assert np.max(np.abs(a - b)) <= tol
+        assert np.max(np.abs(a - c)) <= tol
+        o = oracle_binding(qc, {p: v[j] for p, v in binds[0].items()})
+        np.testing.assert_allclose(b, o.data, rtol=0, atol=1e-12 if precision == "double" else 3e-6 * 80)
