@@ -41,7 +41,10 @@ graph-captured persistent launch, next to one instance per launch),
 ``estimator`` (EstimatorV2 job: a parameterised 20-qubit ansatz with 1,024
 parameter sets run on one stack of states, 50 observables), ``shots``
 (a 16-qubit circuit with mid-circuit measurements, conditioned gates and
-resets: 4,096 shots, each running the circuit, stacked as states).
+resets: 4,096 shots, each running the circuit, stacked as states),
+``dense5`` (5-qubit Haar gates on a dense 30-qubit state: the 5-qubit
+tensor-core kernels), ``tune`` (a 28-qubit unfused ansatz through
+AerSimulator.run with the default schedule and with autotune=True).
 
 ``--impl reference`` times the reference's CPU algorithm on the same
 workload (the oracle port: the reference's own build exists only where its
@@ -830,6 +833,48 @@ def hea_bound_circuit(P, n, layers):
     return qc, params
 
 
+def bench_tune(args, torch, P):
+    """Autotuned against default schedule: the HEA circuit (RY, RZ on every
+    qubit and a CX ladder per layer, fixed angles) without fusion, so that its
+    1-2 qubit gates run as cache-blocked runs, through AerSimulator.run with
+    one Z expectation value saved; the default engine schedule against
+    AerSimulator(autotune=True), whose first call times the execution forms
+    and the run tile (untimed here).  Wall time per run() call, median of
+    --steps calls each."""
+    n, layers = args.tune_qubits, args.tune_layers
+    rng = np.random.default_rng(args.seed)
+    qc = P.QuantumCircuit(n)
+    for _ in range(layers):
+        for kind in ("ry", "rz"):
+            for q in range(n):
+                qc.append_gate(kind, [q], [float(rng.uniform(-np.pi, np.pi))])
+        for q in range(n - 1):
+            qc.cx(q, q + 1)
+    qc.save_expectation_value([(1.0, "Z", [0])], label="z0")
+    sims = {"default": P.AerSimulator(precision=args.precision, fusion_enable=False),
+            "tuned": P.AerSimulator(precision=args.precision, fusion_enable=False, autotune=True)}
+    out, meta, vals = {}, {}, {}
+    for name, sim in sims.items():
+        for _ in range(max(args.warmup, 2)):  # the tuned simulator tunes on its first call
+            res = sim.run(qc)
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = sim.run(qc)
+            ts.append(time.perf_counter() - t0)
+        out[name] = float(np.median(ts))
+        meta[name] = res.metadata(0).get("autotune")
+        vals[name] = float(res.data(0)["z0"])
+    dtype = "c128" if args.precision == "double" else "c64"
+    return {"metric": "circuit time, autotuned vs default schedule", "value": round(out["tuned"] * 1e3, 2),
+            "unit": "ms", "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "dtype": dtype,
+            "data": "synthetic", "default_ms": round(out["default"] * 1e3, 2),
+            "speedup": round(out["default"] / out["tuned"], 3), "choice": meta["tuned"],
+            "max_abs_diff_tuned_vs_default": abs(vals["tuned"] - vals["default"]),
+            "config": {"workload": f"HEA {n}q x {layers} layers (RY, RZ, CX ladder), no fusion, <Z_0> saved",
+                       "qubits": n, "layers": layers}}
+
+
 def bench_estimator(args, torch, P):
     """EstimatorV2-shaped job: the parameterised HEA ansatz (n qubits x L
     layers) with B parameter sets and 50 Pauli observables of weight 1-4 on
@@ -973,7 +1018,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="qv",
-                    choices=["qv", "adjoint", "dm", "sample", "batch", "estimator", "shots", "dense5"])
+                    choices=["qv", "adjoint", "dm", "sample", "batch", "estimator", "shots", "dense5", "tune"])
+    ap.add_argument("--tune-qubits", type=int, default=28)
+    ap.add_argument("--tune-layers", type=int, default=8)
     ap.add_argument("--dense5-layers", type=int, default=4)
     ap.add_argument("--shots-qubits", type=int, default=16)
     ap.add_argument("--shots-rounds", type=int, default=8)
@@ -1021,7 +1068,7 @@ def main():
     P.build()
     fn = {"qv": bench_qv, "adjoint": bench_adjoint, "dm": bench_dm, "sample": bench_sample,
           "batch": bench_batch, "estimator": bench_estimator, "shots": bench_shots,
-          "dense5": bench_dense5}[args.workload]
+          "dense5": bench_dense5, "tune": bench_tune}[args.workload]
     line = fn(args, torch, P)
     if int(os.environ.get("RANK", "0")) == 0:
         print(json.dumps(line))
