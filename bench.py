@@ -29,7 +29,9 @@ same circuit under ``variants``.
            the same 2^30-amplitude complex128 state in host memory
   variants the complex64 run of the same circuit; the adjoint gradient of the
            26-qubit, 624-parameter ansatz (complex128 and complex64) against
-           parameter shift on the same GPU; the 14-qubit noisy density matrix
+           parameter shift on the same GPU; the 14-qubit noisy density matrix;
+           100,000 shots on the 30-qubit state; the EstimatorV2 job and the
+           2,048-instance batch (complex64), each as its own workload below
 
 Other workloads (--workload): ``adjoint`` (26-qubit hardware-efficient
 ansatz, 624 parameters, 200 Pauli terms: adjoint gradient vs parameter
@@ -480,6 +482,21 @@ def bench_qv(args, torch, P):
         r = bench_dm(vd, torch, P)
         variants["dm14_c128"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "fused_ops",
                                                    "expval_50_terms_ms", "config")}
+        # the other BASELINE configs, so that every headline number has a record in this line
+        vs = argparse.Namespace(**{**vars(args), "no_checks": True})
+        r = bench_sample(vs, torch, P)
+        variants["sample_30q_c128"] = {k: r[k] for k in ("value", "unit", "sample_100k_ms", "probabilities_all_ms",
+                                                         "config")}
+        ve = argparse.Namespace(**{**vars(args), "precision": "single", "steps": 3, "warmup": 3,
+                                   "per_binding_sample": 1, "no_cpu_baseline": True})
+        r = bench_estimator(ve, torch, P)
+        variants["estimator_c64"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "execute_bound_ms",
+                                                       "expval_50_terms_ms", "e2e", "config")}
+        vb = argparse.Namespace(**{**vars(args), "precision": "single", "steps": 2, "warmup": 1,
+                                   "no_cpu_baseline": True})
+        r = bench_batch(vb, torch, P)
+        variants["batch_c64"] = {k: r[k] for k in ("value", "unit", "launch_ms", "latency_ms_p50", "latency_ms_p99",
+                                                   "speedup_vs_per_launch", "config")}
     return {"metric": "fused-gate GB/s", "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
