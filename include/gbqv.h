@@ -511,8 +511,10 @@ int gbqv_run_jit_counts(uint64_t *compiled, uint64_t *launched);
  * (the reference's arithmetic, 1.2 TFLOP/s on GB300).  On a complex64 state
  * the same setting selects, for 4-qubit dense gates on >= 11 vector qubits,
  * tcgen05 products in split precision (3xTF32, fp32 accumulation; value 1)
- * or fp32 FMAs (0 or 2).  Other values return
- * GBQV_ERR_ARG.  A tcgen05 kernel whose bounded pipeline wait gave up makes
+ * or fp32 FMAs (0 or 2).  At complex128 a non-zero value also lets the
+ * runs compiled for their op sequence (gbqv_set_run_jit) hold their register
+ * amplitudes as float pairs (~48 significant bits on the FP32 pipe); 0 keeps
+ * them in FP64.  Other values return GBQV_ERR_ARG.  A tcgen05 kernel whose bounded pipeline wait gave up makes
  * the next synchronising call return GBQV_ERR_TIMEOUT. */
 int gbqv_set_tensor_c128(gbqv_handle h, int enable);
 

@@ -392,14 +392,14 @@ struct JitArgs {
   int state_bits;
 };
 extern "C" __global__ void __launch_bounds__(512, 1)
-    k_run_jit(TT *__restrict__ psi, const TT *__restrict__ pool, const TT *__restrict__ bpool, const JitArgs A) {
+    k_run_jit(TT *__restrict__ psi, const TR *__restrict__ pool, const TR *__restrict__ bpool, const JitArgs A) {
   constexpr uint32_t L = 1u << M, cmask = (1u << C) - 1, kPer = 16 / sizeof(TT);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, lane = tid & 31;
   TT *buf0 = reinterpret_cast<TT *>(smem_raw);
   TT *buf1 = buf0 + L;
-  TT *mats = buf1 + L;
-  TT *bmats = mats + POOL;
+  TR *mats = reinterpret_cast<TR *>(buf1 + L);
+  TR *bmats = mats + POOL;
   uint64_t *hi = reinterpret_cast<uint64_t *>(smem_raw + HIOFF);
   for (int i = tid; i < POOL; i += 512) mats[i] = pool[i];
   for (uint32_t h = tid; h < (1u << (M - C)); h += 512) {
@@ -430,11 +430,11 @@ extern "C" __global__ void __launch_bounds__(512, 1)
     const uint64_t gbase = tile_base(t, A.lowmask, M);
     if (skip(gbase)) continue;
     if (BOUND > 0) {
-      const TT *src = bpool + (gbase >> A.state_bits) * (uint64_t)BOUND;
+      const TR *src = bpool + (gbase >> A.state_bits) * (uint64_t)BOUND;
       for (int i = tid; i < BOUND; i += 512) bmats[i] = src[i];
       __syncthreads();
     }
-    TT v[R];
+    TR v[R];
     uint32_t tpart;
 SEGMENTS
     __syncthreads();
@@ -445,8 +445,9 @@ SEGMENTS
 }
 )GBQV";
 
-// The CUDA source of a run's specialised kernel.
-std::string jit_source(bool dbl, const RegParams &P) {
+// The CUDA source of a run's specialised kernel; pairs: complex128 with the
+// register amplitudes as float pairs (fcx), the memory stays double2.
+std::string jit_source(bool dbl, bool pairs, const RegParams &P) {
   const int R = 1 << P.rb;
   std::ostringstream o;
   o << "typedef unsigned int uint32_t;\ntypedef unsigned long long uint64_t;\ntypedef unsigned short uint16_t;\n"
@@ -455,6 +456,7 @@ std::string jit_source(bool dbl, const RegParams &P) {
   const size_t tsz = dbl ? 16 : 8;
   const size_t hioff = (tsz * (2 * (1u << P.m) + (size_t)P.pool_elems + (size_t)P.bound_elems) + 7) & ~size_t(7);
   o << "typedef " << (dbl ? "double2" : "float2") << " TT;\n"
+    << "typedef " << (pairs ? "fcx" : "TT") << " TR;\n"
     << "constexpr int R = " << R << ", M = " << P.m << ", C = " << P.c << ", POOL = " << P.pool_elems
     << ", BOUND = " << P.bound_elems << ";\nconstexpr uint32_t HIOFF = " << hioff << ";\n";
   std::ostringstream seg;
@@ -469,24 +471,25 @@ std::string jit_source(bool dbl, const RegParams &P) {
     if (si > 0) {
       const RegSeg &Sp = P.segs[si - 1];
       seg << "      __syncthreads();\n";
-      for (int i = 0; i < R; ++i) seg << "      tile[tpart | " << Sp.rp[i] << "u] = v[" << i << "];\n";
+      for (int i = 0; i < R; ++i) seg << "      tile[tpart | " << Sp.rp[i] << "u] = from_reg(v[" << i << "], TT());\n";
       seg << "      __syncthreads();\n";
     }
     seg << "      tpart = " << tpart_expr(S) << ";\n";
-    for (int i = 0; i < R; ++i) seg << "      v[" << i << "] = tile[tpart | " << S.rp[i] << "u];\n";
+    for (int i = 0; i < R; ++i)
+      seg << "      v[" << i << "] = " << (pairs ? "to_reg_pair" : "to_reg") << "(tile[tpart | " << S.rp[i] << "u]);\n";
     for (int oi = S.first; oi < S.first + S.count; ++oi) {
       const RegOp &op = P.ops[oi];
       const std::string mat = std::string(op.bound ? "bmats" : "mats") + " + " + std::to_string(op.mat_off);
       const std::string tcond = "((((uint32_t)tid) & " + std::to_string(op.ctm) + "u) == " + std::to_string(op.ctm) + "u)";
       switch (op.kind) {
-        case RK_DENSE1: seg << "      reg_dense1<TT, R, " << op.a << ">(v, " << mat << ");\n"; break;
-        case RK_DENSE1_REAL: seg << "      reg_dense1_real<TT, R, " << op.a << ">(v, " << mat << ");\n"; break;
-        case RK_DIAG1: seg << "      reg_diag1<TT, R, " << op.a << ">(v, " << mat << ");\n"; break;
-        case RK_MCX: seg << "      reg_mcx<TT, R, " << op.a << ">(v, " << tcond << ", " << op.crm << "u);\n"; break;
-        case RK_DENSE2: seg << "      reg_dense2<TT, R, " << op.a << ", " << op.b << ">(v, " << mat << ");\n"; break;
-        case RK_DENSE1_LANE: seg << "      lane_dense1<TT, R>(v, " << mat << ", " << op.a << ", lane);\n"; break;
-        case RK_DENSE1_REAL_LANE: seg << "      lane_dense1_real<TT, R>(v, " << mat << ", " << op.a << ", lane);\n"; break;
-        case RK_MCX_LANE: seg << "      lane_mcx<TT, R>(v, " << op.a << ", " << tcond << ", " << op.crm << "u);\n"; break;
+        case RK_DENSE1: seg << "      reg_dense1<TR, R, " << op.a << ">(v, " << mat << ");\n"; break;
+        case RK_DENSE1_REAL: seg << "      reg_dense1_real<TR, R, " << op.a << ">(v, " << mat << ");\n"; break;
+        case RK_DIAG1: seg << "      reg_diag1<TR, R, " << op.a << ">(v, " << mat << ");\n"; break;
+        case RK_MCX: seg << "      reg_mcx<TR, R, " << op.a << ">(v, " << tcond << ", " << op.crm << "u);\n"; break;
+        case RK_DENSE2: seg << "      reg_dense2<TR, R, " << op.a << ", " << op.b << ">(v, " << mat << ");\n"; break;
+        case RK_DENSE1_LANE: seg << "      lane_dense1<TR, R>(v, " << mat << ", " << op.a << ", lane);\n"; break;
+        case RK_DENSE1_REAL_LANE: seg << "      lane_dense1_real<TR, R>(v, " << mat << ", " << op.a << ", lane);\n"; break;
+        case RK_MCX_LANE: seg << "      lane_mcx<TR, R>(v, " << op.a << ", " << tcond << ", " << op.crm << "u);\n"; break;
         case RK_DIAG_T:
         case RK_DIAG: {
           std::ostringstream td;
@@ -494,9 +497,9 @@ std::string jit_source(bool dbl, const RegParams &P) {
           for (int j = 0; j < op.k; ++j)
             if (op.dtpos[j] >= 0) td << " | ((((uint32_t)tid >> " << (int)op.dtpos[j] << ") & 1u) << " << j << ")";
           if (op.kind == RK_DIAG_T) {
-            seg << "      thread_diag<TT, R>(v, " << mat << ", " << td.str() << ");\n";
+            seg << "      thread_diag<TR, R>(v, " << mat << ", " << td.str() << ");\n";
           } else {
-            seg << "      {\n        const uint32_t td = " << td.str() << ";\n        const TT *dm = " << mat << ";\n";
+            seg << "      {\n        const uint32_t td = " << td.str() << ";\n        const TR *dm = " << mat << ";\n";
             for (int i = 0; i < R; ++i) seg << "        v[" << i << "] = cmul(v[" << i << "], dm[td | " << (int)op.div[i] << "u]);\n";
             seg << "      }\n";
           }
@@ -509,7 +512,7 @@ std::string jit_source(bool dbl, const RegParams &P) {
   }
   const RegSeg &Sl = P.segs[P.nsegs - 1];
   seg << "    __syncthreads();\n";
-  for (int i = 0; i < R; ++i) seg << "    tile[tpart | " << Sl.rp[i] << "u] = v[" << i << "];\n";
+  for (int i = 0; i < R; ++i) seg << "    tile[tpart | " << Sl.rp[i] << "u] = from_reg(v[" << i << "], TT());\n";
   std::string k = kJitKernel;
   const size_t at = k.find("SEGMENTS\n");
   k.replace(at, 9, seg.str());
@@ -585,9 +588,9 @@ CUfunction jit_compile(const std::string &src, std::string &log) {
 
 // The specialised kernel for P, or null (interpreting kernel) under the
 // tiering rule or when compiling fails.
-CUfunction jit_kernel(const Device &dev, bool dbl, const RegParams &P) {
+CUfunction jit_kernel(const Device &dev, bool dbl, bool pairs, const RegParams &P) {
   if (dev.run_jit == 0) return nullptr;
-  const std::string src = jit_source(dbl, P);
+  const std::string src = jit_source(dbl, pairs, P);
   std::lock_guard<std::mutex> g(jit_mutex());
   JitEntry &e = jit_cache()[src];
   ++e.uses;
@@ -636,13 +639,36 @@ int jit_compile_check(bool dbl, std::string &log) {
   P->pool_elems = 40;
   P->bound_elems = 40;
   std::vector<char> cubin;
-  return jit_cubin(jit_source(dbl, *P), cubin, log) ? 0 : 1;
+  return jit_cubin(jit_source(dbl, dbl, *P), cubin, log) ? 0 : 1;
 }
 
 template <typename T, int RB>
-bool launch_reg_jit(Device &dev, RegParams &P, const std::vector<T> &pool, const std::vector<T> &bpool) {
-  CUfunction fn = jit_kernel(dev, sizeof(T) == 16, P);
+bool launch_reg_jit(Device &dev, RegParams &P, const std::vector<T> &pool_in, const std::vector<T> &bpool_in) {
+  // complex128 runs hold their registers as float pairs unless native FP64
+  // arithmetic was asked for (gbqv_set_tensor_c128(h, 0)); their matrices are
+  // uploaded as pairs too (same 16 bytes per entry)
+  const bool pairs = sizeof(T) == 16 && dev.tensor_c128 != 0;
+  CUfunction fn = jit_kernel(dev, sizeof(T) == 16, pairs, P);
   if (!fn) return false;
+  std::vector<T> pool_p, bpool_p;
+  if (pairs) {
+    auto split = [](const std::vector<T> &in, std::vector<T> &out) {
+      out.resize(in.size());
+      for (size_t i = 0; i < in.size(); ++i) {
+        const double2 z = reinterpret_cast<const double2 &>(in[i]);
+        float f[4];
+        const double v[2] = {z.x, z.y};
+        for (int c = 0; c < 2; ++c) {
+          f[2 * c] = (float)v[c];
+          f[2 * c + 1] = (float)(v[c] - (double)f[2 * c]);
+        }
+        std::memcpy(&out[i], f, sizeof(f));
+      }
+    };
+    split(pool_in, pool_p);
+    split(bpool_in, bpool_p);
+  }
+  const std::vector<T> &pool = pairs ? pool_p : pool_in, &bpool = pairs ? bpool_p : bpool_in;
   const size_t poolb = pool.size() * sizeof(T), bpoolb = bpool.size() * sizeof(T);
   const size_t bpool_off = (poolb + 255) & ~size_t(255);
   grow(dev.mat, dev.mat_cap, bpool_off + bpoolb + 256);

@@ -11,6 +11,96 @@
 #ifndef GBQV_RUNREG_DEV_CUH
 #define GBQV_RUNREG_DEV_CUH
 
+// ---- float pairs: ~48-bit real arithmetic on the FP32 pipe ----
+// A complex128 run spends 8 FP64 operations per amplitude and 1-qubit op, and
+// FP64 runs at 1.2 TFLOP/s on GB300.  In its specialised kernel the register
+// amplitudes are held as pairs of floats (hi + lo, non-overlapping) with
+// error-free products (FMA) and sums (two-sum), ~48 significant bits: error
+// about 2^-47 of the operands' magnitude per operation, far inside the 1e-12
+// parity tolerance.  The tile in shared memory and the state in HBM stay
+// complex128.
+struct fpair {
+  float hi, lo;
+  __device__ __forceinline__ fpair() {}
+  __device__ __forceinline__ fpair(float h) : hi(h), lo(0.0f) {}
+  __device__ __forceinline__ fpair(float h, float l) : hi(h), lo(l) {}
+};
+__device__ __forceinline__ fpair fp_fast2sum(float a, float b) {
+  const float s = a + b;
+  return fpair(s, b - (s - a));
+}
+__device__ __forceinline__ fpair operator+(fpair a, fpair b) {
+  const float s = a.hi + b.hi, bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);
+  return fp_fast2sum(s, e + a.lo + b.lo);
+}
+__device__ __forceinline__ fpair operator-(fpair a) { return fpair(-a.hi, -a.lo); }
+__device__ __forceinline__ fpair operator-(fpair a, fpair b) { return a + (-b); }
+__device__ __forceinline__ fpair operator*(fpair a, fpair b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return fp_fast2sum(p, e);
+}
+// a * b + c for every register scalar type (the templates below call rfma)
+__device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ fpair rfma(fpair a, fpair b, fpair c) { return a * b + c; }
+
+// double -> pair: hi = the significand cut to 24 bits, lo = the remaining 29
+// bits rounded to a float (integer code, no FP64 operation); |d| below
+// 2^-126 flushes to 0
+__device__ __forceinline__ fpair fpair_from_double(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
+  const int e = (int)((h >> 20) & 0x7ffu);
+  if (e < 897) return fpair(0.0f, 0.0f);
+  const unsigned sgn = h & 0x80000000u;
+  const float hi = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
+  float lo = __uint2float_rn(l & 0x1fffffffu);  // the remainder r, worth r * 2^(e - 1075)
+  lo = e >= 949 ? lo * __uint_as_float((unsigned)(e - 948) << 23) : 0.0f;
+  return fpair(hi, sgn ? -lo : lo);
+}
+// float -> double, exactly, in integer code (zero and subnormal floats give 0)
+__device__ __forceinline__ double float_to_double_bits(float f) {
+  const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+  if (e == 0) return 0.0;
+  return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
+}
+// pair -> double: one FP64 add, rounded to nearest
+__device__ __forceinline__ double fpair_to_double(fpair p) {
+  return float_to_double_bits(p.hi) + float_to_double_bits(p.lo);
+}
+struct fcx {
+  fpair x, y;
+};
+
+// register form of a memory amplitude and back (the identity except for
+// float-pair registers)
+__device__ __forceinline__ float2 to_reg(float2 a) { return a; }
+__device__ __forceinline__ double2 to_reg(double2 a) { return a; }
+__device__ __forceinline__ float2 from_reg(float2 a, float2) { return a; }
+__device__ __forceinline__ double2 from_reg(double2 a, double2) { return a; }
+__device__ __forceinline__ fcx to_reg_pair(double2 a) {
+  fcx r;
+  r.x = fpair_from_double(a.x);
+  r.y = fpair_from_double(a.y);
+  return r;
+}
+__device__ __forceinline__ double2 from_reg(fcx a, double2) {
+  double2 r;
+  r.x = fpair_to_double(a.x);
+  r.y = fpair_to_double(a.y);
+  return r;
+}
+
+__device__ __forceinline__ float shfl_scalar(float v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
+__device__ __forceinline__ double shfl_scalar(double v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
+__device__ __forceinline__ fpair shfl_scalar(fpair v, int mask) {
+  return fpair(__shfl_xor_sync(0xffffffffu, v.hi, mask), __shfl_xor_sync(0xffffffffu, v.lo, mask));
+}
+
 template <typename T>
 __device__ __forceinline__ T cmul(T a, T b) {
   T r;
@@ -20,10 +110,10 @@ __device__ __forceinline__ T cmul(T a, T b) {
 }
 template <typename T>
 __device__ __forceinline__ void cfma(T &acc, T a, T b) {
-  acc.x = fma(a.x, b.x, acc.x);
-  acc.x = fma(-a.y, b.y, acc.x);
-  acc.y = fma(a.x, b.y, acc.y);
-  acc.y = fma(a.y, b.x, acc.y);
+  acc.x = rfma(a.x, b.x, acc.x);
+  acc.x = rfma(-a.y, b.y, acc.x);
+  acc.y = rfma(a.x, b.y, acc.y);
+  acc.y = rfma(a.y, b.x, acc.y);
 }
 template <typename T>
 __device__ __forceinline__ T czero() {
@@ -35,8 +125,8 @@ __device__ __forceinline__ T czero() {
 template <typename T>
 __device__ __forceinline__ T shfl_x(T v, int mask) {
   T r;
-  r.x = __shfl_xor_sync(0xffffffffu, v.x, mask);
-  r.y = __shfl_xor_sync(0xffffffffu, v.y, mask);
+  r.x = shfl_scalar(v.x, mask);
+  r.y = shfl_scalar(v.y, mask);
   return r;
 }
 
@@ -66,10 +156,10 @@ __device__ __forceinline__ void reg_dense1_real(T (&v)[R], const T *m) {
     const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
     const T a0 = v[i0], a1 = v[i1];
     T r0, r1;
-    r0.x = fma(m01, a1.x, m00 * a0.x);
-    r0.y = fma(m01, a1.y, m00 * a0.y);
-    r1.x = fma(m11, a1.x, m10 * a0.x);
-    r1.y = fma(m11, a1.y, m10 * a0.y);
+    r0.x = rfma(m01, a1.x, m00 * a0.x);
+    r0.y = rfma(m01, a1.y, m00 * a0.y);
+    r1.x = rfma(m11, a1.x, m10 * a0.x);
+    r1.y = rfma(m11, a1.y, m10 * a0.y);
     v[i0] = r0;
     v[i1] = r1;
   }
@@ -136,8 +226,8 @@ __device__ __forceinline__ void lane_dense1_real(T (&v)[R], const T *mat, int a,
   for (int i = 0; i < R; ++i) {
     const T o = shfl_x(v[i], 1 << a);
     T r;
-    r.x = fma(mo, o.x, ms * v[i].x);
-    r.y = fma(mo, o.y, ms * v[i].y);
+    r.x = rfma(mo, o.x, ms * v[i].x);
+    r.y = rfma(mo, o.y, ms * v[i].y);
     v[i] = r;
   }
 }
