@@ -58,14 +58,16 @@ def _compile(src: Path) -> Path:
 
 
 def _generate() -> None:
-    """gbqv_runreg_dev_src.inc: the text of csrc/gbqv_runreg_dev.cuh as a C++
-    string, which the specialised register-tile runs hand to NVRTC."""
+    """gbqv_runreg_dev_src.inc: the texts of csrc/gbqv_fpair.cuh and
+    csrc/gbqv_runreg_dev.cuh as C++ strings, which the specialised
+    register-tile runs hand to NVRTC."""
     GEN.mkdir(parents=True, exist_ok=True)
-    text = (CSRC / "gbqv_runreg_dev.cuh").read_text()
-    assert ")GBQVDEV\"" not in text
-    (GEN / "gbqv_runreg_dev_src.inc").write_text(
-        "// generated from csrc/gbqv_runreg_dev.cuh by _build.py\n"
-        "static const char kRunRegDevSrc[] = R\"GBQVDEV(" + text + ")GBQVDEV\";\n")
+    out = "// generated from csrc/gbqv_fpair.cuh and csrc/gbqv_runreg_dev.cuh by _build.py\n"
+    for name, var in (("gbqv_fpair.cuh", "kFpairSrc"), ("gbqv_runreg_dev.cuh", "kRunRegDevSrc")):
+        text = (CSRC / name).read_text()
+        assert ")GBQVDEV\"" not in text
+        out += "static const char " + var + "[] = R\"GBQVDEV(" + text + ")GBQVDEV\";\n"
+    (GEN / "gbqv_runreg_dev_src.inc").write_text(out)
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:

@@ -1526,6 +1526,30 @@ Prim op_prim(const Op &op) {
   throw Error(GBQV_ERR_ARG, "adjoint gradients need unitary ops (got '" + op.name + "')");
 }
 
+// A 1-qubit prim as a column-major 2x2 matrix (false for anything else).
+bool prim_2x2(const Prim &p, uint64_t &q, cd m[4]) {
+  if (p.q.size() != 1) return false;
+  q = p.q[0];
+  switch (p.k) {
+    case P::MCU:
+    case P::MATRIX:
+      if (p.m.size() != 4) return false;
+      for (int j = 0; j < 4; ++j) m[j] = p.m[j];
+      return true;
+    case P::DIAG:
+      if (p.m.size() != 2) return false;
+      m[0] = p.m[0], m[1] = 0.0, m[2] = 0.0, m[3] = p.m[1];
+      return true;
+    case P::MCPHASE:
+      m[0] = 1.0, m[1] = 0.0, m[2] = 0.0, m[3] = p.m[0];
+      return true;
+    case P::MCX:
+      m[0] = 0.0, m[1] = 1.0, m[2] = 1.0, m[3] = 0.0;
+      return true;
+    default: return false;
+  }
+}
+
 // Pauli generator of a parameterised gate, label read right to left.
 bool generator(const Op &op, PauliMasks &m, cd &phase) {
   static const std::unordered_map<std::string, std::string> gens = {
@@ -1577,9 +1601,12 @@ extern "C" int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const i
           const cd ph = add_y_phase(m.num_y, cd(coeffs ? coeffs[t] : 1.0, 0.0));
           ham.push_back(HamTerm{m.x_mask, m.z_mask, ph.real(), ph.imag()});
         }
-        // forward
+        // forward: the same execution as gbqv_execute (cache-blocked runs)
         launch_set_basis(d, 0, cd(1.0, 0.0));
-        for (auto &op : ops) exec_op(d, op);
+        if (d.blocking)
+          execute_blocked(d, ops);
+        else
+          for (auto &op : ops) exec_op(d, op);
         // lam = H psi
         const size_t bytes = d.amps() * d.amp_bytes();
         grow(d.aux, d.aux_cap, bytes);
@@ -1587,14 +1614,70 @@ extern "C" int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const i
         ham_apply(d, d.state, lam, ham);
         grow(reinterpret_cast<void *&>(d.results), d.results_cap, sizeof(double) * 2 * (nslots + 1));
         reduce_pauli_inner(d, d.state, lam, 0, 0, cd(1.0, 0.0), nslots);  // <psi|H psi>
-        // reverse sweep
-        for (int i = (int)ops.size() - 1; i >= 0; --i) {
-          if (slot[i] >= 0) {
-            PauliMasks gm;
-            cd gph;
-            generator(ops[i], gm, gph);
-            reduce_pauli_inner(d, lam, d.state, gm.x_mask, gm.z_mask, gph, slot[i]);
+        // complex128: the sweep runs on float pairs (FP32 pipe) when every op
+        // is a 1-qubit gate whose generator (if any) sits on its qubit, or a
+        // pure permutation (X-type, swaps), the forms that need no FP64
+        struct Step {
+          int form = -1;  // -1: permutation / other; 0..2 fused 1-qubit step
+          uint64_t q = 0;
+          cd m[4];
+          PauliMasks gm;
+          cd gph;
+        };
+        std::vector<Step> steps(ops.size());
+        bool pairs = d.dbl && d.tensor_c128 != 0;
+        for (size_t i = 0; i < ops.size(); ++i) {
+          Step &st = steps[i];
+          if (slot[i] >= 0) generator(ops[i], st.gm, st.gph);
+          const Prim inv = inverse_prim(op_prim(ops[i]));
+          if (prim_2x2(inv, st.q, st.m) && (slot[i] < 0 || ((st.gm.x_mask | st.gm.z_mask) & ~(1ULL << st.q)) == 0)) {
+            bool real = true;
+            for (auto &z : st.m) real &= z.imag() == 0.0;
+            st.form = st.m[1] == 0.0 && st.m[2] == 0.0 ? 2 : real ? 1 : 0;
+          } else if (slot[i] >= 0 || !(inv.k == P::MCX || inv.k == P::MCSWAP || inv.k == P::NONE)) {
+            pairs = false;
           }
+        }
+        if (pairs) {
+          adjoint_to_pairs(d, d.state);
+          adjoint_to_pairs(d, lam);
+          for (int i = (int)ops.size() - 1; i >= 0; --i) {
+            const Step &st = steps[i];
+            if (st.form >= 0) {
+              if (slot[i] >= 0 || i > 0)
+                adjoint_step_pairs(d, d.state, lam, (int)st.q, st.m, st.form, st.gm.x_mask != 0, st.gm.z_mask != 0,
+                                   st.gph, slot[i], i > 0);
+            } else if (i > 0) {  // a permutation moves 16-byte elements whatever they hold
+              const Prim inv = inverse_prim(op_prim(ops[i]));
+              exec_prim(d, inv);
+              std::swap(d.state, d.aux);
+              exec_prim(d, inv);
+              std::swap(d.state, d.aux);
+              lam = d.aux;
+            }
+          }
+          adjoint_from_pairs(d, d.state);  // the handle's state back in complex128
+        }
+        // reverse sweep
+        for (int i = pairs ? -1 : (int)ops.size() - 1; i >= 0; --i) {
+          PauliMasks gm;
+          cd gph;
+          if (slot[i] >= 0) generator(ops[i], gm, gph);
+          if (i > 0) {
+            // a 1-qubit gate whose generator (if any) sits on its own qubit:
+            // the inner product and both inverse applications in one pass
+            const Prim inv = inverse_prim(op_prim(ops[i]));
+            uint64_t q = 0;
+            cd m[4];
+            if (prim_2x2(inv, q, m) && (slot[i] < 0 || ((gm.x_mask | gm.z_mask) & ~(1ULL << q)) == 0)) {
+              bool real = true;
+              for (auto &z : m) real &= z.imag() == 0.0;
+              const int form = m[1] == 0.0 && m[2] == 0.0 ? 2 : real ? 1 : 0;
+              adjoint_step(d, d.state, lam, (int)q, m, form, gm.x_mask != 0, gm.z_mask != 0, gph, slot[i]);
+              continue;
+            }
+          }
+          if (slot[i] >= 0) reduce_pauli_inner(d, lam, d.state, gm.x_mask, gm.z_mask, gph, slot[i]);
           if (i == 0) break;  // psi_0 and lam_0 are not needed
           const Prim inv = inverse_prim(op_prim(ops[i]));
           exec_prim(d, inv);

@@ -118,6 +118,19 @@ void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t 
 // <lam|P|psi> into dev.results[2*slot .. 2*slot+1] (re, im).
 struct HamTerm { uint64_t x_mask, z_mask; double re, im; };
 void ham_apply(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms);
+// One adjoint-sweep step for a 1-qubit gate on qubit q (m: its inverse,
+// column-major; form 0 general, 1 real, 2 diagonal): with slot >= 0 first
+// results[2 slot..] = <lam| phase X^gx Z^gz |psi> (generator on bit q), then
+// psi <- m psi and lam <- m lam, in one pass over both states.
+void adjoint_step(Device &dev, void *psi, void *lam, int q, const cd *m, int form, bool gx, bool gz, cd phase,
+                  int slot);
+// The same on a complex128 state held as float pairs (16 bytes per
+// amplitude, adjoint_to_pairs converts in place); apply = false: the inner
+// product only.
+void adjoint_to_pairs(Device &dev, void *a);
+void adjoint_from_pairs(Device &dev, void *a);
+void adjoint_step_pairs(Device &dev, void *psi, void *lam, int q, const cd *m, int form, bool gx, bool gz, cd phase,
+                        int slot, bool apply);
 void reduce_pauli_inner(Device &dev, const void *lam, const void *psi, uint64_t x_mask, uint64_t z_mask, cd phase,
                         int slot);
 

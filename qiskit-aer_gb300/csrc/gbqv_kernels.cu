@@ -31,6 +31,8 @@ namespace gbqv {
 
 namespace {
 
+#include "gbqv_fpair.cuh"
+
 template <typename R> struct V2;
 template <> struct V2<double> { using t = double2; };
 template <> struct V2<float> { using t = float2; };
@@ -1562,6 +1564,169 @@ __global__ void __launch_bounds__(256) k_pauli_inner(const T *__restrict__ lam, 
   if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = q;
 }
 
+// One step of the adjoint sweep for a 1-qubit gate on qubit q: the
+// generator's Im <lam|P|psi> contribution (P = phase X^x Z^z with x, z
+// within bit q, the sign taken on lam's index as in k_pauli_inner) from the
+// amplitudes as they are, then psi <- M psi and lam <- M lam with M = the
+// gate's inverse, column-major: one read and one write of each state
+// instead of the inner product's read of both and two gate passes.
+// form: 0 general 2x2, 1 real 2x2 (RY, H), 2 diagonal (RZ, phases).
+struct AdjMat {
+  double re[4], im[4];
+};
+
+template <typename T>
+__device__ __forceinline__ void adj_apply(T &x0, T &x1, const AdjMat &M, int form) {
+  using R = decltype(T::x);
+  if (form == 2) {
+    const R d0r = (R)M.re[0], d0i = (R)M.im[0], d1r = (R)M.re[3], d1i = (R)M.im[3];
+    const T a = x0, b = x1;
+    x0.x = a.x * d0r - a.y * d0i;
+    x0.y = a.x * d0i + a.y * d0r;
+    x1.x = b.x * d1r - b.y * d1i;
+    x1.y = b.x * d1i + b.y * d1r;
+  } else if (form == 1) {
+    const R m00 = (R)M.re[0], m10 = (R)M.re[1], m01 = (R)M.re[2], m11 = (R)M.re[3];
+    const T a = x0, b = x1;
+    x0.x = fma(m01, b.x, m00 * a.x);
+    x0.y = fma(m01, b.y, m00 * a.y);
+    x1.x = fma(m11, b.x, m10 * a.x);
+    x1.y = fma(m11, b.y, m10 * a.y);
+  } else {
+    const T a = x0, b = x1;
+    T r0, r1;
+    r0.x = (R)M.re[0] * a.x - (R)M.im[0] * a.y + (R)M.re[2] * b.x - (R)M.im[2] * b.y;
+    r0.y = (R)M.re[0] * a.y + (R)M.im[0] * a.x + (R)M.re[2] * b.y + (R)M.im[2] * b.x;
+    r1.x = (R)M.re[1] * a.x - (R)M.im[1] * a.y + (R)M.re[3] * b.x - (R)M.im[3] * b.y;
+    r1.y = (R)M.re[1] * a.y + (R)M.im[1] * a.x + (R)M.re[3] * b.y + (R)M.im[3] * b.x;
+    x0 = r0;
+    x1 = r1;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_adj_step(T *__restrict__ psi, T *__restrict__ lam, uint64_t npairs, int q,
+                                                  const AdjMat M, int form, int gx, int gz, int inner, double ph_re,
+                                                  double ph_im, double *__restrict__ partials) {
+  using R = decltype(T::x);
+  // complex64: short sums (8 pairs) in float, then into the double sums
+  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
+  double re = 0.0, im = 0.0;
+  R sr = 0, si = 0;
+  int cnt = 0;
+  const uint64_t bit = 1ULL << q, lowm = bit - 1;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += stride) {
+    const uint64_t i0 = ((i & ~lowm) << 1) | (i & lowm), i1 = i0 | bit;
+    T a0 = psi[i0], a1 = psi[i1], l0 = lam[i0], l1 = lam[i1];
+    if (inner) {
+      const T p0 = gx ? a1 : a0, p1 = gx ? a0 : a1;  // psi[i0 ^ x], psi[i1 ^ x]
+      const R zr = l0.x * p0.x + l0.y * p0.y, zi = l0.x * p0.y - l0.y * p0.x;
+      const R wr = l1.x * p1.x + l1.y * p1.y, wi = l1.x * p1.y - l1.y * p1.x;
+      sr += gz ? zr - wr : zr + wr;
+      si += gz ? zi - wi : zi + wi;
+      if (++cnt == kChunk) {
+        re += (double)sr;
+        im += (double)si;
+        sr = 0;
+        si = 0;
+        cnt = 0;
+      }
+    }
+    adj_apply(a0, a1, M, form);
+    adj_apply(l0, l1, M, form);
+    psi[i0] = a0;
+    psi[i1] = a1;
+    lam[i0] = l0;
+    lam[i1] = l1;
+  }
+  if (!inner) return;
+  re += (double)sr;
+  im += (double)si;
+  const double pr = re * ph_re - im * ph_im, pi = re * ph_im + im * ph_re;
+  const double r = block_sum(pr);
+  if (threadIdx.x == 0) partials[blockIdx.x] = r;
+  const double s = block_sum(pi);
+  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = s;
+}
+
+// The adjoint sweep of a complex128 state with psi and lam held as float
+// pairs (fcx, 16 bytes like a double2) for the whole sweep: converted once,
+// then every step runs on the FP32 pipe without touching FP64; the sweep's
+// final states are not needed, only the inner products.
+__global__ void __launch_bounds__(256) k_to_pairs(double2 *__restrict__ a, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+    reinterpret_cast<fcx *>(a)[i] = to_reg_pair(a[i]);
+}
+
+__global__ void __launch_bounds__(256) k_from_pairs(double2 *__restrict__ a, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+    a[i] = from_reg(reinterpret_cast<const fcx *>(a)[i], double2());
+}
+
+__device__ __forceinline__ void adj_apply_pairs(fcx &x0, fcx &x1, const fcx (&m)[4], int form) {
+  const fcx a = x0, b = x1;
+  if (form == 2) {
+    x0.x = a.x * m[0].x - a.y * m[0].y;
+    x0.y = a.x * m[0].y + a.y * m[0].x;
+    x1.x = b.x * m[3].x - b.y * m[3].y;
+    x1.y = b.x * m[3].y + b.y * m[3].x;
+  } else if (form == 1) {
+    x0.x = rfma(m[2].x, b.x, m[0].x * a.x);
+    x0.y = rfma(m[2].x, b.y, m[0].x * a.y);
+    x1.x = rfma(m[3].x, b.x, m[1].x * a.x);
+    x1.y = rfma(m[3].x, b.y, m[1].x * a.y);
+  } else {
+    x0.x = m[0].x * a.x - m[0].y * a.y + m[2].x * b.x - m[2].y * b.y;
+    x0.y = m[0].x * a.y + m[0].y * a.x + m[2].x * b.y + m[2].y * b.x;
+    x1.x = m[1].x * a.x - m[1].y * a.y + m[3].x * b.x - m[3].y * b.y;
+    x1.y = m[1].x * a.y + m[1].y * a.x + m[3].x * b.y + m[3].y * b.x;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_adj_step_pairs(fcx *__restrict__ psi, fcx *__restrict__ lam, uint64_t npairs,
+                                                        int q, const AdjMat M, int form, int gx, int gz, int inner,
+                                                        int apply, double ph_re, double ph_im,
+                                                        double *__restrict__ partials) {
+  fcx m[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    m[j].x = fpair_from_double(M.re[j]);
+    m[j].y = fpair_from_double(M.im[j]);
+  }
+  fpair sr(0.0f), si(0.0f);
+  const uint64_t bit = 1ULL << q, lowm = bit - 1;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += stride) {
+    const uint64_t i0 = ((i & ~lowm) << 1) | (i & lowm), i1 = i0 | bit;
+    fcx a0 = psi[i0], a1 = psi[i1], l0 = lam[i0], l1 = lam[i1];
+    if (inner) {
+      const fcx p0 = gx ? a1 : a0, p1 = gx ? a0 : a1;
+      const fpair zr = l0.x * p0.x + l0.y * p0.y, zi = l0.x * p0.y - l0.y * p0.x;
+      const fpair wr = l1.x * p1.x + l1.y * p1.y, wi = l1.x * p1.y - l1.y * p1.x;
+      sr = sr + (gz ? zr - wr : zr + wr);
+      si = si + (gz ? zi - wi : zi + wi);
+    }
+    if (apply) {
+      adj_apply_pairs(a0, a1, m, form);
+      adj_apply_pairs(l0, l1, m, form);
+      psi[i0] = a0;
+      psi[i1] = a1;
+      lam[i0] = l0;
+      lam[i1] = l1;
+    }
+  }
+  if (!inner) return;
+  const double re = fpair_to_double(sr), im = fpair_to_double(si);
+  const double pr = re * ph_re - im * ph_im, pi = re * ph_im + im * ph_re;
+  const double r = block_sum(pr);
+  if (threadIdx.x == 0) partials[blockIdx.x] = r;
+  const double s = block_sum(pi);
+  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = s;
+}
+
 }  // namespace
 
 void ham_apply(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms) {
@@ -1596,6 +1761,60 @@ void reduce_pauli_inner(Device &dev, const void *lam, const void *psi, uint64_t 
   check_launch("pauli inner product kernel");
   k_finish<<<2, 256, 0, dev.stream>>>(dev.partials, blocks, 2, dev.results + 2 * slot);
   check_launch("reduction finish");
+}
+
+void adjoint_step(Device &dev, void *psi, void *lam, int q, const cd *m, int form, bool gx, bool gz, cd phase,
+                  int slot) {
+  AdjMat M;
+  for (int j = 0; j < 4; ++j) {
+    M.re[j] = m[j].real();
+    M.im[j] = m[j].imag();
+  }
+  const int blocks = kReduceBlocks;
+  const uint64_t npairs = dev.amps() >> 1;
+  if (slot >= 0) grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * blocks * 2);
+  if (dev.dbl)
+    k_adj_step<double2><<<blocks, kReduceThreads, 0, dev.stream>>>(
+        reinterpret_cast<double2 *>(psi), reinterpret_cast<double2 *>(lam), npairs, q, M, form, gx, gz, slot >= 0,
+        phase.real(), phase.imag(), dev.partials);
+  else
+    k_adj_step<float2><<<blocks, kReduceThreads, 0, dev.stream>>>(
+        reinterpret_cast<float2 *>(psi), reinterpret_cast<float2 *>(lam), npairs, q, M, form, gx, gz, slot >= 0,
+        phase.real(), phase.imag(), dev.partials);
+  check_launch("adjoint step kernel");
+  if (slot >= 0) {
+    k_finish<<<2, 256, 0, dev.stream>>>(dev.partials, blocks, 2, dev.results + 2 * slot);
+    check_launch("reduction finish");
+  }
+}
+
+void adjoint_to_pairs(Device &dev, void *a) {
+  k_to_pairs<<<grid_for(dev.amps(), 256), 256, 0, dev.stream>>>(reinterpret_cast<double2 *>(a), dev.amps());
+  check_launch("float-pair conversion kernel");
+}
+
+void adjoint_from_pairs(Device &dev, void *a) {
+  k_from_pairs<<<grid_for(dev.amps(), 256), 256, 0, dev.stream>>>(reinterpret_cast<double2 *>(a), dev.amps());
+  check_launch("float-pair conversion kernel");
+}
+
+void adjoint_step_pairs(Device &dev, void *psi, void *lam, int q, const cd *m, int form, bool gx, bool gz, cd phase,
+                        int slot, bool apply) {
+  AdjMat M;
+  for (int j = 0; j < 4; ++j) {
+    M.re[j] = m[j].real();
+    M.im[j] = m[j].imag();
+  }
+  const int blocks = kReduceBlocks;
+  if (slot >= 0) grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * blocks * 2);
+  k_adj_step_pairs<<<blocks, kReduceThreads, 0, dev.stream>>>(reinterpret_cast<fcx *>(psi), reinterpret_cast<fcx *>(lam),
+                                                              dev.amps() >> 1, q, M, form, gx, gz, slot >= 0, apply,
+                                                              phase.real(), phase.imag(), dev.partials);
+  check_launch("adjoint float-pair step kernel");
+  if (slot >= 0) {
+    k_finish<<<2, 256, 0, dev.stream>>>(dev.partials, blocks, 2, dev.results + 2 * slot);
+    check_launch("reduction finish");
+  }
 }
 
 // ============================ cache-blocked runs ============================

@@ -30,7 +30,7 @@
 #include <vector>
 
 #include "gbqv_internal.h"
-#include "gbqv_runreg_dev_src.inc"  // kRunRegDevSrc: the text of gbqv_runreg_dev.cuh (written by the build)
+#include "gbqv_runreg_dev_src.inc"  // kFpairSrc, kRunRegDevSrc: texts of gbqv_fpair.cuh, gbqv_runreg_dev.cuh (the build)
 
 namespace gbqv {
 namespace {
@@ -452,7 +452,7 @@ std::string jit_source(bool dbl, bool pairs, const RegParams &P) {
   std::ostringstream o;
   o << "typedef unsigned int uint32_t;\ntypedef unsigned long long uint64_t;\ntypedef unsigned short uint16_t;\n"
        "typedef unsigned char uint8_t;\ntypedef signed char int8_t;\ntypedef int int32_t;\n"
-    << kRunRegDevSrc << "\n";
+    << kFpairSrc << "\n" << kRunRegDevSrc << "\n";
   const size_t tsz = dbl ? 16 : 8;
   const size_t hioff = (tsz * (2 * (1u << P.m) + (size_t)P.pool_elems + (size_t)P.bound_elems) + 7) & ~size_t(7);
   o << "typedef " << (dbl ? "double2" : "float2") << " TT;\n"

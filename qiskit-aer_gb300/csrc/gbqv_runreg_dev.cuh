@@ -6,75 +6,15 @@
 // Shared by two compilers: gbqv_runreg.cu includes it (inside its namespace)
 // for the interpreting kernel k_run_reg, and gbqv_runjit.cpp hands its text to
 // the runtime compiler (NVRTC) for the kernels specialised to one run's op
-// sequence.  It therefore includes nothing and uses only builtin vector types
-// and the fixed-width integer names the includer provides.
+// sequence.  It therefore includes only gbqv_fpair.cuh (which NVRTC receives
+// as text ahead of this one) and uses only builtin vector types and the
+// fixed-width integer names the includer provides.
 #ifndef GBQV_RUNREG_DEV_CUH
 #define GBQV_RUNREG_DEV_CUH
 
-// ---- float pairs: ~48-bit real arithmetic on the FP32 pipe ----
-// A complex128 run spends 8 FP64 operations per amplitude and 1-qubit op, and
-// FP64 runs at 1.2 TFLOP/s on GB300.  In its specialised kernel the register
-// amplitudes are held as pairs of floats (hi + lo, non-overlapping) with
-// error-free products (FMA) and sums (two-sum), ~48 significant bits: error
-// about 2^-47 of the operands' magnitude per operation, far inside the 1e-12
-// parity tolerance.  The tile in shared memory and the state in HBM stay
-// complex128.
-struct fpair {
-  float hi, lo;
-  __device__ __forceinline__ fpair() {}
-  __device__ __forceinline__ fpair(float h) : hi(h), lo(0.0f) {}
-  __device__ __forceinline__ fpair(float h, float l) : hi(h), lo(l) {}
-};
-__device__ __forceinline__ fpair fp_fast2sum(float a, float b) {
-  const float s = a + b;
-  return fpair(s, b - (s - a));
-}
-__device__ __forceinline__ fpair operator+(fpair a, fpair b) {
-  const float s = a.hi + b.hi, bb = s - a.hi;
-  const float e = (a.hi - (s - bb)) + (b.hi - bb);
-  return fp_fast2sum(s, e + a.lo + b.lo);
-}
-__device__ __forceinline__ fpair operator-(fpair a) { return fpair(-a.hi, -a.lo); }
-__device__ __forceinline__ fpair operator-(fpair a, fpair b) { return a + (-b); }
-__device__ __forceinline__ fpair operator*(fpair a, fpair b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  return fp_fast2sum(p, e);
-}
-// a * b + c for every register scalar type (the templates below call rfma)
-__device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
-__device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ fpair rfma(fpair a, fpair b, fpair c) { return a * b + c; }
-
-// double -> pair: hi = the significand cut to 24 bits, lo = the remaining 29
-// bits rounded to a float (integer code, no FP64 operation); |d| below
-// 2^-126 flushes to 0
-__device__ __forceinline__ fpair fpair_from_double(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
-  const int e = (int)((h >> 20) & 0x7ffu);
-  if (e < 897) return fpair(0.0f, 0.0f);
-  const unsigned sgn = h & 0x80000000u;
-  const float hi = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
-  float lo = __uint2float_rn(l & 0x1fffffffu);  // the remainder r, worth r * 2^(e - 1075)
-  lo = e >= 949 ? lo * __uint_as_float((unsigned)(e - 948) << 23) : 0.0f;
-  return fpair(hi, sgn ? -lo : lo);
-}
-// float -> double, exactly, in integer code (zero and subnormal floats give 0)
-__device__ __forceinline__ double float_to_double_bits(float f) {
-  const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
-  if (e == 0) return 0.0;
-  return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
-}
-// pair -> double: one FP64 add, rounded to nearest
-__device__ __forceinline__ double fpair_to_double(fpair p) {
-  return float_to_double_bits(p.hi) + float_to_double_bits(p.lo);
-}
-struct fcx {
-  fpair x, y;
-};
+#ifndef __CUDACC_RTC__
+#include "gbqv_fpair.cuh"
+#endif
 
 // register form of a memory amplitude and back (the identity except for
 // float-pair registers)
@@ -82,19 +22,6 @@ __device__ __forceinline__ float2 to_reg(float2 a) { return a; }
 __device__ __forceinline__ double2 to_reg(double2 a) { return a; }
 __device__ __forceinline__ float2 from_reg(float2 a, float2) { return a; }
 __device__ __forceinline__ double2 from_reg(double2 a, double2) { return a; }
-__device__ __forceinline__ fcx to_reg_pair(double2 a) {
-  fcx r;
-  r.x = fpair_from_double(a.x);
-  r.y = fpair_from_double(a.y);
-  return r;
-}
-__device__ __forceinline__ double2 from_reg(fcx a, double2) {
-  double2 r;
-  r.x = fpair_to_double(a.x);
-  r.y = fpair_to_double(a.y);
-  return r;
-}
-
 __device__ __forceinline__ float shfl_scalar(float v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
 __device__ __forceinline__ double shfl_scalar(double v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
 __device__ __forceinline__ fpair shfl_scalar(fpair v, int mask) {
