@@ -1607,13 +1607,6 @@ extern "C" int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const i
           execute_blocked(d, ops);
         else
           for (auto &op : ops) exec_op(d, op);
-        // lam = H psi
-        const size_t bytes = d.amps() * d.amp_bytes();
-        grow(d.aux, d.aux_cap, bytes);
-        void *lam = d.aux;
-        ham_apply(d, d.state, lam, ham);
-        grow(reinterpret_cast<void *&>(d.results), d.results_cap, sizeof(double) * 2 * (nslots + 1));
-        reduce_pauli_inner(d, d.state, lam, 0, 0, cd(1.0, 0.0), nslots);  // <psi|H psi>
         // complex128: the sweep runs on float pairs (FP32 pipe) when every op
         // is a 1-qubit gate whose generator (if any) sits on its qubit, or a
         // pure permutation (X-type, swaps), the forms that need no FP64
@@ -1638,9 +1631,21 @@ extern "C" int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const i
             pairs = false;
           }
         }
+        // lam = H psi and <psi|H psi>
+        const size_t bytes = d.amps() * d.amp_bytes();
+        grow(d.aux, d.aux_cap, bytes);
+        void *lam = d.aux;
+        grow(reinterpret_cast<void *&>(d.results), d.results_cap, sizeof(double) * 2 * (nslots + 1));
         if (pairs) {
           adjoint_to_pairs(d, d.state);
-          adjoint_to_pairs(d, lam);
+          ham_apply_pairs(d, d.state, lam, ham);
+          const cd one[4] = {1.0, 0.0, 0.0, 1.0};
+          adjoint_step_pairs(d, lam, d.state, 0, one, 2, false, false, cd(1.0, 0.0), nslots, false);
+        } else {
+          ham_apply(d, d.state, lam, ham);
+          reduce_pauli_inner(d, d.state, lam, 0, 0, cd(1.0, 0.0), nslots);  // <psi|H psi>
+        }
+        if (pairs) {
           for (int i = (int)ops.size() - 1; i >= 0; --i) {
             const Step &st = steps[i];
             if (st.form >= 0) {

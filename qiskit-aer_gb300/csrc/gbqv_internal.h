@@ -129,6 +129,8 @@ void adjoint_step(Device &dev, void *psi, void *lam, int q, const cd *m, int for
 // product only.
 void adjoint_to_pairs(Device &dev, void *a);
 void adjoint_from_pairs(Device &dev, void *a);
+// lam = H psi with psi and lam as float pairs (complex128 adjoint sweep).
+void ham_apply_pairs(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms);
 void adjoint_step_pairs(Device &dev, void *psi, void *lam, int q, const cd *m, int form, bool gx, bool gz, cd phase,
                         int slot, bool apply);
 void reduce_pauli_inner(Device &dev, const void *lam, const void *psi, uint64_t x_mask, uint64_t z_mask, cd phase,

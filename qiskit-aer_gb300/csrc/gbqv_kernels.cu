@@ -1660,6 +1660,38 @@ __global__ void __launch_bounds__(256) k_to_pairs(double2 *__restrict__ a, uint6
     reinterpret_cast<fcx *>(a)[i] = to_reg_pair(a[i]);
 }
 
+// lam = H psi on float pairs: psi and lam as fcx, the coefficients c_t =
+// coeff_t (-i)^{num_y} as pairs (split on the host); the sign (-1)^{popc(i &
+// z)} and the gather psi[i ^ x] as in k_ham_apply.
+struct HamTermPair {
+  uint64_t x_mask, z_mask;
+  float re_hi, re_lo, im_hi, im_lo;
+};
+
+__global__ void __launch_bounds__(256) k_ham_apply_pairs(const fcx *__restrict__ psi, fcx *__restrict__ out,
+                                                         uint64_t count, const HamTermPair *__restrict__ terms,
+                                                         int nterms) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    fpair sr(0.0f), si(0.0f);
+    for (int t = 0; t < nterms; ++t) {
+      const HamTermPair h = terms[t];
+      const fcx a = psi[i ^ h.x_mask];
+      fpair cr(h.re_hi, h.re_lo), ci(h.im_hi, h.im_lo);
+      if (__popcll(i & h.z_mask) & 1) {
+        cr = -cr;
+        ci = -ci;
+      }
+      sr = sr + (cr * a.x - ci * a.y);
+      si = si + (cr * a.y + ci * a.x);
+    }
+    fcx o;
+    o.x = sr;
+    o.y = si;
+    out[i] = o;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_from_pairs(double2 *__restrict__ a, uint64_t count) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
@@ -1791,6 +1823,27 @@ void adjoint_step(Device &dev, void *psi, void *lam, int q, const cd *m, int for
 void adjoint_to_pairs(Device &dev, void *a) {
   k_to_pairs<<<grid_for(dev.amps(), 256), 256, 0, dev.stream>>>(reinterpret_cast<double2 *>(a), dev.amps());
   check_launch("float-pair conversion kernel");
+}
+
+void ham_apply_pairs(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms) {
+  const size_t bytes = sizeof(HamTermPair) * terms.size();
+  grow(dev.aux2, dev.aux2_cap, bytes);
+  std::vector<HamTermPair> h(terms.size());
+  auto split = [](double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+  };
+  for (size_t i = 0; i < terms.size(); ++i) {
+    h[i].x_mask = terms[i].x_mask;
+    h[i].z_mask = terms[i].z_mask;
+    split(terms[i].re, h[i].re_hi, h[i].re_lo);
+    split(terms[i].im, h[i].im_hi, h[i].im_lo);
+  }
+  cuda_check(cudaMemcpyAsync(dev.aux2, h.data(), bytes, cudaMemcpyHostToDevice, dev.stream), "hamiltonian upload");
+  k_ham_apply_pairs<<<grid_for(dev.amps(), 256), 256, 0, dev.stream>>>(
+      reinterpret_cast<const fcx *>(src), reinterpret_cast<fcx *>(dst), dev.amps(),
+      reinterpret_cast<const HamTermPair *>(dev.aux2), (int)terms.size());
+  check_launch("hamiltonian float-pair kernel");
 }
 
 void adjoint_from_pairs(Device &dev, void *a) {
