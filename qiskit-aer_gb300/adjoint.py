@@ -113,9 +113,14 @@ class Engine:
         return e.value, g
 
     def energy(self, ansatz: Ansatz, theta, ham: Hamiltonian) -> float:
+        """E(theta) by one forward pass: Aer's Fusion pass (statevector
+        defaults) and the cache-blocked runs, as the adjoint's forward pass."""
         nc = NativeCircuit(ansatz.num_qubits, ansatz.instructions(theta))
-        self.qv.initialize()
         L = self.qv._L
+        cfg = A.FusionConfig()
+        A.check(L.gbqv_fusion_default_config(0, C.byref(cfg)))
+        nc.fuse(cfg)
+        self.qv.initialize()
         A.check(L.gbqv_set_blocking(self.qv.handle, 1), self.qv.handle)
         A.check(L.gbqv_execute(self.qv.handle, nc.handle), self.qv.handle)
         _, total = self.qv.expval_pauli_many(ham.terms, ham.coeffs)

@@ -1601,12 +1601,23 @@ extern "C" int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const i
           const cd ph = add_y_phase(m.num_y, cd(coeffs ? coeffs[t] : 1.0, 0.0));
           ham.push_back(HamTerm{m.x_mask, m.z_mask, ph.real(), ph.imag()});
         }
-        // forward: the same execution as gbqv_execute (cache-blocked runs)
+        // forward: only psi is needed, so the bound ops go through Aer's
+        // Fusion pass (statevector defaults) and the cache-blocked runs, as a
+        // gbqv_execute of the fused circuit would
         launch_set_basis(d, 0, cd(1.0, 0.0));
-        if (d.blocking)
-          execute_blocked(d, ops);
-        else
-          for (auto &op : ops) exec_op(d, op);
+        {
+          gbqv_circuit fwd;
+          fwd.num_qubits = c->num_qubits;
+          fwd.ops = ops;
+          gbqv_fusion_config cfg;
+          REQUIRE(gbqv_fusion_default_config(0, &cfg) == GBQV_OK, GBQV_ERR_ARG, "fusion configuration");
+          REQUIRE(gbqv_circuit_fuse(&fwd, &cfg, nullptr, nullptr, 0) == GBQV_OK, GBQV_ERR_ARG,
+                  "fusion of the forward pass failed");
+          if (d.blocking)
+            execute_blocked(d, fwd.ops);
+          else
+            for (auto &op : fwd.ops) exec_op(d, op);
+        }
         // complex128: the sweep runs on float pairs (FP32 pipe) when every op
         // is a 1-qubit gate whose generator (if any) sits on its qubit, or a
         // pure permutation (X-type, swaps), the forms that need no FP64
