@@ -1656,52 +1656,56 @@ extern "C" int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const i
           ham_apply(d, d.state, lam, ham);
           reduce_pauli_inner(d, d.state, lam, 0, 0, cd(1.0, 0.0), nslots);  // <psi|H psi>
         }
-        if (pairs) {
-          for (int i = (int)ops.size() - 1; i >= 0; --i) {
-            const Step &st = steps[i];
-            if (st.form >= 0) {
-              if (slot[i] >= 0 || i > 0)
-                adjoint_step_pairs(d, d.state, lam, (int)st.q, st.m, st.form, st.gm.x_mask != 0, st.gm.z_mask != 0,
-                                   st.gph, slot[i], i > 0);
-            } else if (i > 0) {  // a permutation moves 16-byte elements whatever they hold
-              const Prim inv = inverse_prim(op_prim(ops[i]));
-              exec_prim(d, inv);
-              std::swap(d.state, d.aux);
-              exec_prim(d, inv);
-              std::swap(d.state, d.aux);
-              lam = d.aux;
+        // reverse sweep.  Consecutive 1-qubit steps on distinct qubits (up to
+        // 3) share one pass over psi and lam; permutations and, off the
+        // float-pair path, any other op keep their own kernels
+        auto host_step = [&](int i) {
+          const Step &st = steps[i];
+          AdjStepHost h;
+          h.q = (int)st.q;
+          h.form = st.form;
+          h.gx = st.gm.x_mask != 0;
+          h.gz = st.gm.z_mask != 0;
+          for (int e = 0; e < 4; ++e) h.m[e] = st.m[e];
+          h.phase = st.gph;
+          h.slot = slot[i];
+          return h;
+        };
+        for (int i = (int)ops.size() - 1; i >= 0;) {
+          const Step &st = steps[i];
+          if (st.form >= 0 && i > 0) {
+            std::vector<AdjStepHost> grp;
+            std::vector<uint64_t> used;
+            int j = i;
+            while (j > 0 && grp.size() < 3 && steps[j].form >= 0 &&
+                   std::find(used.begin(), used.end(), steps[j].q) == used.end()) {
+              grp.push_back(host_step(j));
+              used.push_back(steps[j].q);
+              --j;
+            }
+            adjoint_steps(d, d.state, lam, grp, pairs);
+            i = j;
+            continue;
+          }
+          if (slot[i] >= 0) {  // the inner product without a step after it
+            if (pairs) {
+              adjoint_step_pairs(d, d.state, lam, (int)st.q, st.m, st.form, st.gm.x_mask != 0, st.gm.z_mask != 0,
+                                 st.gph, slot[i], false);
+            } else {
+              reduce_pauli_inner(d, lam, d.state, st.gm.x_mask, st.gm.z_mask, st.gph, slot[i]);
             }
           }
-          adjoint_from_pairs(d, d.state);  // the handle's state back in complex128
-        }
-        // reverse sweep
-        for (int i = pairs ? -1 : (int)ops.size() - 1; i >= 0; --i) {
-          PauliMasks gm;
-          cd gph;
-          if (slot[i] >= 0) generator(ops[i], gm, gph);
           if (i > 0) {
-            // a 1-qubit gate whose generator (if any) sits on its own qubit:
-            // the inner product and both inverse applications in one pass
             const Prim inv = inverse_prim(op_prim(ops[i]));
-            uint64_t q = 0;
-            cd m[4];
-            if (prim_2x2(inv, q, m) && (slot[i] < 0 || ((gm.x_mask | gm.z_mask) & ~(1ULL << q)) == 0)) {
-              bool real = true;
-              for (auto &z : m) real &= z.imag() == 0.0;
-              const int form = m[1] == 0.0 && m[2] == 0.0 ? 2 : real ? 1 : 0;
-              adjoint_step(d, d.state, lam, (int)q, m, form, gm.x_mask != 0, gm.z_mask != 0, gph, slot[i]);
-              continue;
-            }
+            exec_prim(d, inv);
+            std::swap(d.state, d.aux);
+            exec_prim(d, inv);
+            std::swap(d.state, d.aux);
+            lam = d.aux;
           }
-          if (slot[i] >= 0) reduce_pauli_inner(d, lam, d.state, gm.x_mask, gm.z_mask, gph, slot[i]);
-          if (i == 0) break;  // psi_0 and lam_0 are not needed
-          const Prim inv = inverse_prim(op_prim(ops[i]));
-          exec_prim(d, inv);
-          std::swap(d.state, d.aux);
-          exec_prim(d, inv);
-          std::swap(d.state, d.aux);
-          lam = d.aux;
+          --i;
         }
+        if (pairs) adjoint_from_pairs(d, d.state);  // the handle's state back in complex128
         std::vector<double> res(2 * (nslots + 1));
         cuda_check(cudaMemcpyAsync(res.data(), d.results, sizeof(double) * res.size(), cudaMemcpyDeviceToHost, d.stream),
                    "gradient copy");

@@ -118,15 +118,24 @@ void sample_measure(Device &dev, const double *d_rnds, uint64_t shots, uint64_t 
 // <lam|P|psi> into dev.results[2*slot .. 2*slot+1] (re, im).
 struct HamTerm { uint64_t x_mask, z_mask; double re, im; };
 void ham_apply(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms);
-// One adjoint-sweep step for a 1-qubit gate on qubit q (m: its inverse,
-// column-major; form 0 general, 1 real, 2 diagonal): with slot >= 0 first
-// results[2 slot..] = <lam| phase X^gx Z^gz |psi> (generator on bit q), then
-// psi <- m psi and lam <- m lam, in one pass over both states.
-void adjoint_step(Device &dev, void *psi, void *lam, int q, const cd *m, int form, bool gx, bool gz, cd phase,
-                  int slot);
-// The same on a complex128 state held as float pairs (16 bytes per
-// amplitude, adjoint_to_pairs converts in place); apply = false: the inner
-// product only.
+// One 1-qubit sweep step on a complex128 state held as float pairs (16
+// bytes per amplitude; adjoint_to_pairs / adjoint_from_pairs convert in
+// place): with slot >= 0 first results[2 slot..] = <lam| phase X^gx Z^gz
+// |psi> (generator on bit q), then, with apply, psi <- m psi and lam <- m lam
+// (m column-major, form 0 general, 1 real, 2 diagonal).
+// Up to 3 consecutive 1-qubit sweep steps on distinct qubits in one pass
+// (psi, lam as complex64 / complex128, or as float pairs): per step the
+// inverse matrix (column-major, form 0 general, 1 real, 2 diagonal), the
+// generator bits (on the step's qubit) and phase, and the result slot (-1:
+// no inner product).
+struct AdjStepHost {
+  int q = 0, form = 0;
+  bool gx = false, gz = false;
+  cd m[4];
+  cd phase = 1.0;
+  int slot = -1;
+};
+void adjoint_steps(Device &dev, void *psi, void *lam, const std::vector<AdjStepHost> &steps, bool pairs);
 void adjoint_to_pairs(Device &dev, void *a);
 void adjoint_from_pairs(Device &dev, void *a);
 // lam = H psi with psi and lam as float pairs (complex128 adjoint sweep).

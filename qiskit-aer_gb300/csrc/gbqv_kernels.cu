@@ -23,6 +23,7 @@
 #include "gbqv_ozaki.h"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 #include <memory>
 #include <atomic>
@@ -1564,91 +1565,16 @@ __global__ void __launch_bounds__(256) k_pauli_inner(const T *__restrict__ lam, 
   if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = q;
 }
 
-// One step of the adjoint sweep for a 1-qubit gate on qubit q: the
-// generator's Im <lam|P|psi> contribution (P = phase X^x Z^z with x, z
-// within bit q, the sign taken on lam's index as in k_pauli_inner) from the
-// amplitudes as they are, then psi <- M psi and lam <- M lam with M = the
-// gate's inverse, column-major: one read and one write of each state
-// instead of the inner product's read of both and two gate passes.
-// form: 0 general 2x2, 1 real 2x2 (RY, H), 2 diagonal (RZ, phases).
+// Adjoint sweep steps for 1-qubit gates: the generator's Im <lam|P|psi>
+// contribution (P = phase X^x Z^z with x, z within the gate's bit, the sign
+// taken on lam's index as in k_pauli_inner) from the amplitudes as they are,
+// then psi <- M psi and lam <- M lam with M = the gate's inverse,
+// column-major: one read and one write of each state instead of the inner
+// product's read of both and two gate passes.  form: 0 general 2x2, 1 real
+// 2x2 (RY, H), 2 diagonal (RZ, phases).
 struct AdjMat {
   double re[4], im[4];
 };
-
-template <typename T>
-__device__ __forceinline__ void adj_apply(T &x0, T &x1, const AdjMat &M, int form) {
-  using R = decltype(T::x);
-  if (form == 2) {
-    const R d0r = (R)M.re[0], d0i = (R)M.im[0], d1r = (R)M.re[3], d1i = (R)M.im[3];
-    const T a = x0, b = x1;
-    x0.x = a.x * d0r - a.y * d0i;
-    x0.y = a.x * d0i + a.y * d0r;
-    x1.x = b.x * d1r - b.y * d1i;
-    x1.y = b.x * d1i + b.y * d1r;
-  } else if (form == 1) {
-    const R m00 = (R)M.re[0], m10 = (R)M.re[1], m01 = (R)M.re[2], m11 = (R)M.re[3];
-    const T a = x0, b = x1;
-    x0.x = fma(m01, b.x, m00 * a.x);
-    x0.y = fma(m01, b.y, m00 * a.y);
-    x1.x = fma(m11, b.x, m10 * a.x);
-    x1.y = fma(m11, b.y, m10 * a.y);
-  } else {
-    const T a = x0, b = x1;
-    T r0, r1;
-    r0.x = (R)M.re[0] * a.x - (R)M.im[0] * a.y + (R)M.re[2] * b.x - (R)M.im[2] * b.y;
-    r0.y = (R)M.re[0] * a.y + (R)M.im[0] * a.x + (R)M.re[2] * b.y + (R)M.im[2] * b.x;
-    r1.x = (R)M.re[1] * a.x - (R)M.im[1] * a.y + (R)M.re[3] * b.x - (R)M.im[3] * b.y;
-    r1.y = (R)M.re[1] * a.y + (R)M.im[1] * a.x + (R)M.re[3] * b.y + (R)M.im[3] * b.x;
-    x0 = r0;
-    x1 = r1;
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_adj_step(T *__restrict__ psi, T *__restrict__ lam, uint64_t npairs, int q,
-                                                  const AdjMat M, int form, int gx, int gz, int inner, double ph_re,
-                                                  double ph_im, double *__restrict__ partials) {
-  using R = decltype(T::x);
-  // complex64: short sums (8 pairs) in float, then into the double sums
-  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
-  double re = 0.0, im = 0.0;
-  R sr = 0, si = 0;
-  int cnt = 0;
-  const uint64_t bit = 1ULL << q, lowm = bit - 1;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += stride) {
-    const uint64_t i0 = ((i & ~lowm) << 1) | (i & lowm), i1 = i0 | bit;
-    T a0 = psi[i0], a1 = psi[i1], l0 = lam[i0], l1 = lam[i1];
-    if (inner) {
-      const T p0 = gx ? a1 : a0, p1 = gx ? a0 : a1;  // psi[i0 ^ x], psi[i1 ^ x]
-      const R zr = l0.x * p0.x + l0.y * p0.y, zi = l0.x * p0.y - l0.y * p0.x;
-      const R wr = l1.x * p1.x + l1.y * p1.y, wi = l1.x * p1.y - l1.y * p1.x;
-      sr += gz ? zr - wr : zr + wr;
-      si += gz ? zi - wi : zi + wi;
-      if (++cnt == kChunk) {
-        re += (double)sr;
-        im += (double)si;
-        sr = 0;
-        si = 0;
-        cnt = 0;
-      }
-    }
-    adj_apply(a0, a1, M, form);
-    adj_apply(l0, l1, M, form);
-    psi[i0] = a0;
-    psi[i1] = a1;
-    lam[i0] = l0;
-    lam[i1] = l1;
-  }
-  if (!inner) return;
-  re += (double)sr;
-  im += (double)si;
-  const double pr = re * ph_re - im * ph_im, pi = re * ph_im + im * ph_re;
-  const double r = block_sum(pr);
-  if (threadIdx.x == 0) partials[blockIdx.x] = r;
-  const double s = block_sum(pi);
-  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = s;
-}
 
 // The adjoint sweep of a complex128 state with psi and lam held as float
 // pairs (fcx, 16 bytes like a double2) for the whole sweep: converted once,
@@ -1759,6 +1685,159 @@ __global__ void __launch_bounds__(256) k_adj_step_pairs(fcx *__restrict__ psi, f
   if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = s;
 }
 
+// K consecutive 1-qubit steps of the adjoint sweep on K distinct qubits in
+// one pass: each thread holds a group of 2^K amplitudes of psi and lam
+// (local bit j <-> the qubit of step j) and runs the steps in sweep order,
+// each step's inner product from the values its predecessors left.  HBM
+// traffic per step falls by K.  E: float2 / double2 (plain arithmetic) or
+// fcx (complex128 as float pairs).
+struct AdjStepDev {
+  int q, form, gx, gz, inner;
+  double re[4], im[4];
+  double ph_re, ph_im;
+};
+template <int K>
+struct AdjSteps {
+  AdjStepDev s[K];
+  uint64_t lowmask[K];  // (1 << q) - 1 of the step qubits, ascending
+};
+
+template <typename E>
+struct AdjReal {
+  using type = decltype(E::x);
+};
+template <>
+struct AdjReal<fcx> {
+  using type = fpair;
+};
+
+template <typename E>
+__device__ __forceinline__ E adj_mat(double re, double im) {
+  E z;
+  if constexpr (std::is_same<E, fcx>::value) {
+    z.x = fpair_from_double(re);
+    z.y = fpair_from_double(im);
+  } else {
+    z.x = (decltype(E::x))re;
+    z.y = (decltype(E::x))im;
+  }
+  return z;
+}
+
+template <typename E>
+__device__ __forceinline__ void adj_apply_g(E &x0, E &x1, const E (&m)[4], int form) {
+  const E a = x0, b = x1;
+  if (form == 2) {
+    x0.x = a.x * m[0].x - a.y * m[0].y;
+    x0.y = a.x * m[0].y + a.y * m[0].x;
+    x1.x = b.x * m[3].x - b.y * m[3].y;
+    x1.y = b.x * m[3].y + b.y * m[3].x;
+  } else if (form == 1) {
+    x0.x = rfma(m[2].x, b.x, m[0].x * a.x);
+    x0.y = rfma(m[2].x, b.y, m[0].x * a.y);
+    x1.x = rfma(m[3].x, b.x, m[1].x * a.x);
+    x1.y = rfma(m[3].x, b.y, m[1].x * a.y);
+  } else {
+    x0.x = m[0].x * a.x - m[0].y * a.y + m[2].x * b.x - m[2].y * b.y;
+    x0.y = m[0].x * a.y + m[0].y * a.x + m[2].x * b.y + m[2].y * b.x;
+    x1.x = m[1].x * a.x - m[1].y * a.y + m[3].x * b.x - m[3].y * b.y;
+    x1.y = m[1].x * a.y + m[1].y * a.x + m[3].x * b.y + m[3].y * b.x;
+  }
+}
+
+template <typename E>
+__device__ __forceinline__ double adj_to_double(E) { return 0.0; }
+
+template <typename E, int K>
+__global__ void __launch_bounds__(256) k_adj_steps(E *__restrict__ psi, E *__restrict__ lam, uint64_t ngroups,
+                                                   const AdjSteps<K> S, double *__restrict__ partials) {
+  using R = typename AdjReal<E>::type;
+  constexpr int G = 1 << K;
+  E m[K][4];
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) m[j][e] = adj_mat<E>(S.s[j].re[e], S.s[j].im[e]);
+  double accr[K], acci[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) accr[j] = acci[j] = 0.0;
+  R fr[K], fi[K];  // per-group sums (fcx: carried across groups in pairs)
+#pragma unroll
+  for (int j = 0; j < K; ++j) fr[j] = fi[j] = R(0.0f);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += stride) {
+    uint64_t base = g;
+#pragma unroll
+    for (int j = 0; j < K; ++j) base = ((base & ~S.lowmask[j]) << 1) | (base & S.lowmask[j]);
+    E a[G], l[G];
+#pragma unroll
+    for (int t = 0; t < G; ++t) {
+      uint64_t idx = base;
+#pragma unroll
+      for (int j = 0; j < K; ++j)
+        if (t >> j & 1) idx |= 1ULL << S.s[j].q;
+      a[t] = psi[idx];
+      l[t] = lam[idx];
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const AdjStepDev &st = S.s[j];
+#pragma unroll
+      for (int t = 0; t < G; ++t) {
+        if (t >> j & 1) continue;
+        const int t1 = t | (1 << j);
+        if (st.inner) {
+          const E p0 = st.gx ? a[t1] : a[t], p1 = st.gx ? a[t] : a[t1];
+          const R zr = l[t].x * p0.x + l[t].y * p0.y, zi = l[t].x * p0.y - l[t].y * p0.x;
+          const R wr = l[t1].x * p1.x + l[t1].y * p1.y, wi = l[t1].x * p1.y - l[t1].y * p1.x;
+          fr[j] = fr[j] + (st.gz ? zr - wr : zr + wr);
+          fi[j] = fi[j] + (st.gz ? zi - wi : zi + wi);
+        }
+        adj_apply_g(a[t], a[t1], m[j], st.form);
+        adj_apply_g(l[t], l[t1], m[j], st.form);
+      }
+    }
+    if constexpr (std::is_same<R, float>::value) {
+      // complex64: the group's float sums into the double accumulators
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        accr[j] += (double)fr[j];
+        acci[j] += (double)fi[j];
+        fr[j] = fi[j] = 0.0f;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < G; ++t) {
+      uint64_t idx = base;
+#pragma unroll
+      for (int j = 0; j < K; ++j)
+        if (t >> j & 1) idx |= 1ULL << S.s[j].q;
+      psi[idx] = a[t];
+      lam[idx] = l[t];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    if (!S.s[j].inner) continue;  // the same value in every thread
+    double re, im;
+    if constexpr (std::is_same<R, fpair>::value) {
+      re = fpair_to_double(fr[j]);
+      im = fpair_to_double(fi[j]);
+    } else if constexpr (std::is_same<R, double>::value) {
+      re = fr[j];
+      im = fi[j];
+    } else {
+      re = accr[j];
+      im = acci[j];
+    }
+    const double pr = re * S.s[j].ph_re - im * S.s[j].ph_im, pi = re * S.s[j].ph_im + im * S.s[j].ph_re;
+    const double r = block_sum(pr);
+    if (threadIdx.x == 0) partials[(2 * j) * gridDim.x + blockIdx.x] = r;
+    const double q = block_sum(pi);
+    if (threadIdx.x == 0) partials[(2 * j + 1) * gridDim.x + blockIdx.x] = q;
+  }
+}
+
 }  // namespace
 
 void ham_apply(Device &dev, const void *src, void *dst, const std::vector<HamTerm> &terms) {
@@ -1793,31 +1872,6 @@ void reduce_pauli_inner(Device &dev, const void *lam, const void *psi, uint64_t 
   check_launch("pauli inner product kernel");
   k_finish<<<2, 256, 0, dev.stream>>>(dev.partials, blocks, 2, dev.results + 2 * slot);
   check_launch("reduction finish");
-}
-
-void adjoint_step(Device &dev, void *psi, void *lam, int q, const cd *m, int form, bool gx, bool gz, cd phase,
-                  int slot) {
-  AdjMat M;
-  for (int j = 0; j < 4; ++j) {
-    M.re[j] = m[j].real();
-    M.im[j] = m[j].imag();
-  }
-  const int blocks = kReduceBlocks;
-  const uint64_t npairs = dev.amps() >> 1;
-  if (slot >= 0) grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * blocks * 2);
-  if (dev.dbl)
-    k_adj_step<double2><<<blocks, kReduceThreads, 0, dev.stream>>>(
-        reinterpret_cast<double2 *>(psi), reinterpret_cast<double2 *>(lam), npairs, q, M, form, gx, gz, slot >= 0,
-        phase.real(), phase.imag(), dev.partials);
-  else
-    k_adj_step<float2><<<blocks, kReduceThreads, 0, dev.stream>>>(
-        reinterpret_cast<float2 *>(psi), reinterpret_cast<float2 *>(lam), npairs, q, M, form, gx, gz, slot >= 0,
-        phase.real(), phase.imag(), dev.partials);
-  check_launch("adjoint step kernel");
-  if (slot >= 0) {
-    k_finish<<<2, 256, 0, dev.stream>>>(dev.partials, blocks, 2, dev.results + 2 * slot);
-    check_launch("reduction finish");
-  }
 }
 
 void adjoint_to_pairs(Device &dev, void *a) {
@@ -1868,6 +1922,58 @@ void adjoint_step_pairs(Device &dev, void *psi, void *lam, int q, const cd *m, i
     k_finish<<<2, 256, 0, dev.stream>>>(dev.partials, blocks, 2, dev.results + 2 * slot);
     check_launch("reduction finish");
   }
+}
+
+template <typename E, int K>
+void launch_adj_steps(Device &dev, void *psi, void *lam, const std::vector<AdjStepHost> &steps) {
+  AdjSteps<K> S;
+  std::vector<uint64_t> qs;
+  for (int j = 0; j < K; ++j) {
+    const AdjStepHost &h = steps[j];
+    AdjStepDev &d = S.s[j];
+    d.q = h.q;
+    d.form = h.form;
+    d.gx = h.gx;
+    d.gz = h.gz;
+    d.inner = h.slot >= 0;
+    for (int e = 0; e < 4; ++e) {
+      d.re[e] = h.m[e].real();
+      d.im[e] = h.m[e].imag();
+    }
+    d.ph_re = h.phase.real();
+    d.ph_im = h.phase.imag();
+    qs.push_back((uint64_t)h.q);
+  }
+  std::sort(qs.begin(), qs.end());
+  for (int j = 0; j < K; ++j) S.lowmask[j] = (1ULL << qs[j]) - 1;
+  const int blocks = kReduceBlocks;
+  grow(reinterpret_cast<void *&>(dev.partials), dev.partials_cap, sizeof(double) * blocks * 2 * K);
+  k_adj_steps<E, K><<<blocks, kReduceThreads, 0, dev.stream>>>(reinterpret_cast<E *>(psi), reinterpret_cast<E *>(lam),
+                                                               dev.amps() >> K, S, dev.partials);
+  check_launch("adjoint steps kernel");
+  for (int j = 0; j < K; ++j)
+    if (steps[j].slot >= 0) {
+      k_finish<<<2, 256, 0, dev.stream>>>(dev.partials + (size_t)2 * j * blocks, blocks, 2,
+                                          dev.results + 2 * steps[j].slot);
+      check_launch("reduction finish");
+    }
+}
+
+void adjoint_steps(Device &dev, void *psi, void *lam, const std::vector<AdjStepHost> &steps, bool pairs) {
+  const int K = (int)steps.size();
+  if (K < 1 || K > 3) throw Error(1, "adjoint steps: 1 to 3 per pass");
+  auto run = [&](auto tag) {
+    using E = decltype(tag);
+    if (K == 1) launch_adj_steps<E, 1>(dev, psi, lam, steps);
+    else if (K == 2) launch_adj_steps<E, 2>(dev, psi, lam, steps);
+    else launch_adj_steps<E, 3>(dev, psi, lam, steps);
+  };
+  if (pairs)
+    run(fcx{});
+  else if (dev.dbl)
+    run(double2{});
+  else
+    run(float2{});
 }
 
 // ============================ cache-blocked runs ============================
