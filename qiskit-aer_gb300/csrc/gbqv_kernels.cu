@@ -1500,28 +1500,23 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_ham_apply(const T *__restrict__ psi, T *__restrict__ out, uint64_t count,
                                                    const HamTermDev *__restrict__ terms, int nterms) {
   using R = decltype(T::x);
-  // complex64: the products and short sums (8 terms) in float, then into the
-  // double sums; complex128: everything in double
-  constexpr int kChunk = sizeof(R) == 4 ? 8 : 1;
+  // complex64: the products in float and the sums compensated (Kahan) in
+  // float, so that no FP64 operation runs per term (with a double add per 8
+  // terms the FP64 pipe bounded the kernel); complex128: everything in double
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
-    double ar = 0.0, ai = 0.0;
-    for (int t0 = 0; t0 < nterms; t0 += kChunk) {
-      R sr = 0, si = 0;
-      for (int t = t0; t < min(nterms, t0 + kChunk); ++t) {
-        const HamTermDev h = terms[t];
-        const T a = psi[i ^ h.x_mask];
-        R cr = (R)h.re, ci = (R)h.im;
-        if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
-        sr += cr * a.x - ci * a.y;
-        si += cr * a.y + ci * a.x;
-      }
-      ar += (double)sr;
-      ai += (double)si;
+    SegSum<R> ar, ai;
+    for (int t = 0; t < nterms; ++t) {
+      const HamTermDev h = terms[t];
+      const T a = psi[i ^ h.x_mask];
+      R cr = (R)h.re, ci = (R)h.im;
+      if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
+      ar.add(cr * a.x - ci * a.y);
+      ai.add(cr * a.y + ci * a.x);
     }
     T o;
-    o.x = (R)ar;
-    o.y = (R)ai;
+    o.x = (R)ar.value();
+    o.y = (R)ai.value();
     out[i] = o;
   }
 }
