@@ -16,20 +16,25 @@
 // before its hit and walks at most 1024 indices (plus the rare continuation
 // past a block end that the reference's walk also makes).
 //
-// The sequential sums are 2^isz dependent chains (1024 by default), far too
-// few threads to cover HBM latency with ordinary loads.  So the
-// probabilities are first written out in one parallel pass (8 bytes per
-// outcome), and each CTA then streams the probabilities of 8 chains through
-// a 3-stage shared-memory ring filled by bulk copies (cp.async.bulk, 8 KB
-// per chain per stage), the 8 chain threads adding from shared memory.
-// Every wait is bounded; a stalled ring raises the device status word that
-// the host reports as GBQV_ERR_TIMEOUT.  When the probability buffer cannot
-// be allocated, or the blocks are short, the chains read the state itself.
+// The sequential sums are 2^isz chains (1024 by default) of L terms each.
+// For blocks longer than 1024 terms:
+//   1. the probabilities are written out (8 bytes per outcome) with an
+//      approximate sum per step of 256 outcomes;
+//   2. prefix sums of those predict every chain's running sum at each step;
+//   3. one parallel pass computes, per step and for both chains, the integer
+//      sum of the step's terms on the ulp grid of the predicted running sum
+//      (gbqv_seqsum.h: exact while the sum keeps its binade and no term
+//      rounds on a tie);
+//   4. each chain (one warp) then advances step by step, adding the step's
+//      grid units where its binade was predicted right and the step is
+//      clean, and adding term by term otherwise.
+// When the probability buffer cannot be allocated, or the blocks are short,
+// one thread per chain adds term by term from the state itself.
 #include <algorithm>
 #include <cstdint>
 
 #include "gbqv_internal.h"
-#include "gbqv_tc.cuh"
+#include "gbqv_seqsum.h"
 
 namespace gbqv {
 namespace {
@@ -51,13 +56,98 @@ __device__ __forceinline__ double prob_exact<float2>(const float2 *psi, uint64_t
   return (double)__fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y));
 }
 
-// Every outcome's probability, in the reference's rounding.
+constexpr int kStep = 256;  // terms per grid step (one warp, 8 per lane)
+
+__device__ __forceinline__ uint64_t umin(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+// A float no larger than the double x (truncated significand; 0 below the
+// float range): the step sums only predict the running sums' binades.
+__device__ __forceinline__ float approx_float(double x) {
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
+  if (e <= 0) return 0.0f;
+  const uint32_t f = e >= 255 ? 0x7f7fffffu : ((uint32_t)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  return __uint_as_float(f | (hi & 0x80000000u));
+}
+
+// Every outcome's probability in the reference's rounding, one warp per step
+// of 256 outcomes, and each step's approximate sum.
 template <typename T>
-__global__ void __launch_bounds__(256) k_probs_exact(const T *__restrict__ psi, uint64_t count, uint64_t diag_stride,
-                                                     double *__restrict__ out) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
-    out[i] = prob_exact<T>(psi, i, diag_stride);
+__global__ void __launch_bounds__(256) k_probs_steps(const T *__restrict__ psi, uint64_t nsteps, uint64_t diag_stride,
+                                                     double *__restrict__ out, float *__restrict__ stepsum) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < nsteps; t += warps) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int u = 0; u < kStep / 32; ++u) {
+      const uint64_t i = t * kStep + 32 * u + lane;
+      const double p = prob_exact<T>(psi, i, diag_stride);
+      out[i] = p;
+      acc += approx_float(p);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) stepsum[t] = acc;
+  }
+}
+
+// Per chain (one CTA of 256 threads): the exclusive prefix of its step sums
+// (the predicted running sum at each step's start) and the chain's total.
+__global__ void __launch_bounds__(256) k_step_prefix(const float *__restrict__ stepsum, uint64_t steps_per_chain,
+                                                     double *__restrict__ pred, double *__restrict__ total) {
+  __shared__ double wsum[8];
+  const uint64_t base = (uint64_t)blockIdx.x * steps_per_chain;
+  const uint64_t per = (steps_per_chain + 255) / 256;
+  const uint64_t t0 = umin(threadIdx.x * per, steps_per_chain), t1 = umin(t0 + per, steps_per_chain);
+  double own = 0.0;
+  for (uint64_t t = t0; t < t1; ++t) own += stepsum[base + t];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double incl = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  double before = incl - own;
+  for (int k = 0; k < w; ++k) before += wsum[k];
+  for (uint64_t t = t0; t < t1; ++t) {
+    pred[base + t] = before;
+    before += stepsum[base + t];
+  }
+  if (threadIdx.x == 255) {
+    double all = 0.0;
+    for (int k = 0; k < 8; ++k) all += wsum[k];
+    total[blockIdx.x] = all;
+  }
+}
+
+// Exclusive prefix of the chain totals (one CTA, chains <= 2^24): the
+// predicted start of each block's walk.
+__global__ void __launch_bounds__(1024) k_chain_prefix(const double *__restrict__ total, uint64_t nchains,
+                                                       double *__restrict__ start) {
+  __shared__ double wsum[32];
+  const uint64_t per = (nchains + 1023) / 1024;
+  const uint64_t c0 = umin(threadIdx.x * per, nchains), c1 = umin(c0 + per, nchains);
+  double own = 0.0;
+  for (uint64_t c = c0; c < c1; ++c) own += total[c];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double incl = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  double before = incl - own;
+  for (int k = 0; k < w; ++k) before += wsum[k];
+  for (uint64_t c = c0; c < c1; ++c) {
+    start[c] = before;
+    before += total[c];
+  }
 }
 
 // One thread per block reading the state itself: the block's sequential sum
@@ -89,92 +179,258 @@ __global__ void __launch_bounds__(32) k_seq_blocks(const T *__restrict__ psi, ui
   if (!CHECKPOINTS) out[j] = s;
 }
 
-// The staged form over the probability buffer: CTA = kChains chain threads
-// (warp 0) + one loader thread (warp 1); blocks of L >= kChunk doubles.
-constexpr int kChains = 8;
-constexpr int kChunk = 1024;                     // doubles per chain per stage, one checkpoint each
-constexpr int kStages = 3;
-constexpr int kRowBytes = kChunk * 8 + 16;       // row pitch: chain b's row starts 4 banks after b - 1's
-constexpr int kStageBytes = kChains * kRowBytes;
-constexpr int kSeqSmem = kStages * kStageBytes + 2 * kStages * 8 + 16;
+constexpr unsigned kFull = 0xffffffffu;
 
-template <bool WALK>
-__global__ void __launch_bounds__(64) k_seq_chains(const double *__restrict__ probs, uint64_t nblocks, uint64_t L,
-                                                   const double *__restrict__ P, double *__restrict__ out,
-                                                   int *status) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * kStageBytes);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kStages * kStageBytes + 2 * kStages * 8);
-  const uint32_t bar0 = tc::smem_u32(bars);
-  auto full = [&](int s) { return bar0 + 8u * s; };
-  auto empty = [&](int s) { return bar0 + 8u * (kStages + s); };
-  const uint64_t chain0 = (uint64_t)blockIdx.x * kChains;
-  const int active = (int)std::min<uint64_t>(kChains, nblocks - chain0);
-  const uint64_t nchunks = L / kChunk;
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      tc::mbar_init(full(s), 1);
-      tc::mbar_init(empty(s), (uint32_t)active);
-    }
-    *abort_flag = 0;
-    tc::mbar_init_fence();
-  }
-  __syncthreads();
-  if (tid < active) {
-    const uint64_t j = chain0 + tid;
-    double acc = WALK ? P[j] : 0.0;
-    bool ok = true;
-    for (uint64_t c = 0; c < nchunks; ++c) {
-      const int s = (int)(c % kStages);
-      if (!tc::mbar_wait(full(s), (uint32_t)((c / kStages) & 1), abort_flag)) {
-        ok = false;
-        break;
-      }
-      const double *row = reinterpret_cast<const double *>(smem + s * kStageBytes + tid * kRowBytes);
-      for (int t = 0; t < kChunk; t += 8) {
-        double v[8];
+__device__ __forceinline__ bool parity(uint32_t m) { return __popc(m) & 1; }
+
+// One step's record for binade e (warp-wide; this lane holds terms 32u + lane
+// as words hi[u], lo[u]): M = the grid units with ties rounded down plus the
+// ties after the first, decided by prefix parities (gbqv_seqsum.h); has_tie
+// and fp = whether the step has a tie and the parity of the rounded-down
+// prefix up to and including the first one, which decides it against the
+// running sum's parity.
+struct StepRecord {
+  uint64_t M;
+  bool bad, has_tie, fp;
+};
+
+__device__ __forceinline__ StepRecord step_record(const uint32_t (&hi)[kStep / 32], const uint32_t (&lo)[kStep / 32],
+                                                  int e, bool bad, int lane) {
+  uint64_t m[kStep / 32], sum = 0;
+  uint32_t ties = 0;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = row[t + u];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) acc = __dadd_rn(acc, v[u]);
-      }
-      if (WALK) out[j * nchunks + c] = acc;
-      // these generic-proxy reads come before the loader's next bulk
-      // (async-proxy) write into the stage
-      tc::fence_async_smem();
-      tc::mbar_arrive(empty(s));
-    }
-    if (ok && !WALK) out[j] = acc;
-  } else if (tid == 32) {
-    // loader: chunk c of every active chain into stage c % kStages
-    uint64_t issued = 0;
-    for (uint64_t c = 0; c < nchunks; ++c) {
-      const int s = (int)(c % kStages);
-      if (c >= kStages && !tc::mbar_wait(empty(s), (uint32_t)((c / kStages - 1) & 1), abort_flag, 64)) break;
-      tc::mbar_arrive_expect_tx(full(s), (uint32_t)(active * kChunk * 8));
-      for (int b = 0; b < active; ++b)
-        tc::bulk_g2s(tc::smem_u32(smem + s * kStageBytes + b * kRowBytes), probs + (chain0 + b) * L + c * kChunk,
-                     kChunk * 8, full(s));
-      issued = c + 1;
-    }
-    // copies in flight after an abort land before the CTA exits
-    int never = 0;
-    for (uint64_t c = issued > kStages ? issued - kStages : 0; c < issued; ++c)
-      tc::mbar_wait(full((int)(c % kStages)), (uint32_t)((c / kStages) & 1), &never);
+  for (int u = 0; u < kStep / 32; ++u) {
+    bool tie = false;
+    m[u] = seq::grid_units_fast(hi[u], lo[u], e, bad, tie);
+    ties |= (tie ? 1u : 0u) << u;
+    sum += m[u];
   }
-  __syncthreads();
-  if (tid == 0 && *abort_flag) atomicExch(status, 1);
+  StepRecord r{0, __any_sync(kFull, bad) != 0, false, false};
+  if (__any_sync(kFull, ties != 0)) {  // warp-uniform
+    uint32_t tm[kStep / 32], om[kStep / 32];
+    bool G[kStep / 32 + 1];  // parity of the odd units in the groups before u
+    G[0] = false;
+#pragma unroll
+    for (int u = 0; u < kStep / 32; ++u) {
+      tm[u] = __ballot_sync(kFull, (ties >> u) & 1);
+      om[u] = __ballot_sync(kFull, m[u] & 1);
+      G[u + 1] = G[u] ^ parity(om[u]);
+    }
+    // parity of the rounded-down prefix up to and including term (u, l)
+    auto dpar = [&](int u, int l) { return G[u] ^ parity(om[u] & ((2u << l) - 1)); };
+    r.has_tie = true;
+    bool found = false;
+#pragma unroll
+    for (int u = 0; u < kStep / 32; ++u)
+      if (!found && tm[u]) {
+        r.fp = dpar(u, __ffs(tm[u]) - 1);
+        found = true;
+      }
+#pragma unroll
+    for (int u = 0; u < kStep / 32; ++u) {
+      if (!((ties >> u) & 1)) continue;
+      // the tie before this one in term order: lower lane of this group, or
+      // the last tie of the nearest earlier group with one
+      bool prev = false, prev_par = false;
+      const uint32_t b = tm[u] & ((1u << lane) - 1);
+      if (b) {
+        prev = true;
+        prev_par = dpar(u, 31 - __clz(b));
+      } else {
+#pragma unroll
+        for (int v = u - 1; v >= 0; --v)
+          if (!prev && tm[v]) {
+            prev = true;
+            prev_par = dpar(v, 31 - __clz(tm[v]));
+          }
+      }
+      if (prev && dpar(u, lane) != prev_par) sum += 1;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+  r.M = sum;
+  return r;
 }
 
-// P[0] = 0, P[j + 1] = fl(P[j] + idxs[j]): the reference's running sum.
-__global__ void k_seq_prefix(const double *__restrict__ idxs, uint64_t nblocks, double *__restrict__ P) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double p = 0.0;
-  P[0] = 0.0;
-  for (uint64_t j = 0; j < nblocks; ++j) {
-    p = __dadd_rn(p, idxs[j]);
-    P[j + 1] = p;
+// The records of every step, for both chains of its block: the block sum
+// (running sum predicted by pred[t]) and the walk (start[j] + pred[t]).  One
+// record per step and chain: {M (2 words), e | bad << 16 | nonzero << 17 |
+// has_tie << 18 | fp << 19}.
+__global__ void __launch_bounds__(256) k_grid_units(const double *__restrict__ probs, uint64_t nsteps,
+                                                    int chain_shift, const double *__restrict__ pred,
+                                                    const double *__restrict__ start, uint4 *__restrict__ rec_sum,
+                                                    uint4 *__restrict__ rec_walk) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < nsteps; t += warps) {
+    const double pr = pred[t];
+    const uint64_t b1 = (uint64_t)__double_as_longlong(pr),
+                   b2 = (uint64_t)__double_as_longlong(__dadd_rn(start[t >> chain_shift], pr));
+    uint32_t hi[kStep / 32], lo[kStep / 32];
+    bool nz = false;
+#pragma unroll
+    for (int u = 0; u < kStep / 32; ++u) {
+      const double x = probs[t * kStep + 32 * u + lane];
+      hi[u] = (uint32_t)__double2hiint(x);
+      lo[u] = (uint32_t)__double2loint(x);
+      nz |= ((hi[u] << 1) | lo[u]) != 0;
+    }
+    nz = __any_sync(kFull, nz);
+    const StepRecord r1 = step_record(hi, lo, seq::bexp(b1), !seq::grid_ok(b1), lane);
+    const StepRecord r2 = step_record(hi, lo, seq::bexp(b2), !seq::grid_ok(b2), lane);
+    if (lane == 0) {
+      auto meta = [&](const StepRecord &r, uint64_t b) {
+        return (uint32_t)seq::bexp(b) | (r.bad ? 1u << 16 : 0u) | (nz ? 1u << 17 : 0u) | (r.has_tie ? 1u << 18 : 0u) |
+               (r.fp ? 1u << 19 : 0u);
+      };
+      rec_sum[t] = make_uint4((uint32_t)r1.M, (uint32_t)(r1.M >> 32), meta(r1, b1), 0u);
+      rec_walk[t] = make_uint4((uint32_t)r2.M, (uint32_t)(r2.M >> 32), meta(r2, b2), 0u);
+    }
+  }
+}
+
+
+__device__ __forceinline__ uint64_t warp_incl_u64(uint64_t v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t u = __shfl_up_sync(kFull, v, o);
+    if (lane >= o) v += u;
+  }
+  return v;
+}
+
+// The running sum s (bits, warp-uniform) after the terms held one per lane
+// (x bits, in lane order), equal to sequential double additions: runs of
+// terms on one grid advance by a prefix sum of their grid units; a term that
+// ties, reaches the next binade or crosses it is added on its own.  `mine`
+// receives the sum after this lane's term.
+__device__ uint64_t add_lanes(uint64_t sb, uint64_t xb, int lane, uint64_t &mine) {
+  int from = 0;
+  while (from < 32) {
+    int f;
+    if (sb == 0) {  // 0 + x = x for the first term that is not a zero
+      const unsigned nz = __ballot_sync(kFull, lane >= from && (xb << 1) != 0);
+      f = nz ? __ffs(nz) - 1 : 32;
+      if (lane >= from && lane < f) mine = 0;
+      if (f == 32) return 0;
+      sb = __shfl_sync(kFull, xb, f);
+      if (lane == f) mine = sb;
+      from = f + 1;
+      continue;
+    }
+    if (seq::grid_ok(sb)) {
+      bool bad = false, tie = false;
+      const uint64_t m =
+          lane >= from ? seq::grid_units_fast((uint32_t)(xb >> 32), (uint32_t)xb, seq::bexp(sb), bad, tie) : 0;
+      const uint64_t incl = warp_incl_u64(m, lane), frac = sb & seq::kFrac;
+      const unsigned viol = __ballot_sync(kFull, lane >= from && (bad || tie || frac + incl > seq::kFrac));
+      f = viol ? __ffs(viol) - 1 : 32;
+      if (lane >= from && lane < f) mine = (sb & ~seq::kFrac) | (frac + incl);
+      sb = (sb & ~seq::kFrac) | (frac + (f ? __shfl_sync(kFull, incl, f - 1) : 0));
+      if (f == 32) return sb;
+    } else {
+      f = from;
+    }
+    sb = (uint64_t)__double_as_longlong(
+        __dadd_rn(__longlong_as_double((long long)sb), __longlong_as_double(__shfl_sync(kFull, (long long)xb, f))));
+    if (lane == f) mine = sb;
+    from = f + 1;
+  }
+  return sb;
+}
+
+// The chains over the probability buffer, one warp per chain (block j of
+// nsteps steps of 256 terms).  32 steps at a time, one per lane: the steps
+// whose record holds the running sum's binade and no tie advance together by
+// a prefix sum of their grid units, up to the first step that does not
+// (mispredicted binade, a tie, a term that reaches the next binade, a sum
+// that crosses it), which is added term by term (add_lanes over its 256
+// terms).  A zero sum stays zero over steps of zeros.  WALK starts from P[j]
+// and stores the sum after every 4th step (1024 terms); otherwise the chain
+// starts from 0 and stores its total.
+template <bool WALK>
+__global__ void __launch_bounds__(32) k_grid_chain(const double *__restrict__ probs, uint64_t nsteps,
+                                                   const uint4 *__restrict__ rec, const double *__restrict__ P,
+                                                   double *__restrict__ out) {
+  const uint64_t j = blockIdx.x;
+  const int lane = threadIdx.x;
+  const uint64_t step0 = j * nsteps, ncp = nsteps / 4;
+  uint64_t sb = (uint64_t)__double_as_longlong(WALK ? P[j] : 0.0);
+  uint4 next = lane < nsteps ? rec[step0 + lane] : make_uint4(0, 0, 0, 0);
+  for (uint64_t t0 = 0; t0 < nsteps; t0 += 32) {
+    const uint4 r = next;
+    if (t0 + 32 + lane < nsteps) next = rec[step0 + t0 + 32 + lane];
+    const int cnt = nsteps - t0 < 32 ? (int)(nsteps - t0) : 32;
+    const uint64_t M = (uint64_t)r.x | ((uint64_t)r.y << 32);
+    const int e_rec = (int)(r.z & 0x7ff);
+    const bool bad_rec = (r.z >> 16) & 1, nz_rec = (r.z >> 17) & 1, tie_rec = (r.z >> 18) & 1,
+               fp_rec = (r.z >> 19) & 1;
+    const bool ck_lane = WALK && ((t0 + lane + 1) & 3) == 0;
+    int from = 0;
+    while (from < cnt) {
+      int f;
+      if (sb == 0) {
+        const unsigned nz = __ballot_sync(kFull, lane >= from && lane < cnt && nz_rec);
+        f = nz ? __ffs(nz) - 1 : cnt;
+        if (ck_lane && lane >= from && lane < f) out[j * ncp + ((t0 + lane + 1) >> 2) - 1] = 0.0;
+      } else if (seq::grid_ok(sb)) {
+        // the parity of the sum at this step's start: after the last earlier
+        // step with a tie (whose end parity is its units' parity xor fp),
+        // else from the batch start, flipped by every odd M in between
+        const uint64_t frac = sb & seq::kFrac;
+        const uint32_t range = (cnt == 32 ? kFull : (1u << cnt) - 1) & ~((1u << from) - 1);
+        const bool in = (range >> lane) & 1;
+        const uint32_t T = __ballot_sync(kFull, in && tie_rec), A = __ballot_sync(kFull, in && (M & 1)),
+                       F = __ballot_sync(kFull, in && fp_rec);
+        const uint32_t below = range & ((1u << lane) - 1), tb = T & below;
+        bool pin;
+        if (tb) {
+          const int k = 31 - __clz(tb);
+          pin = (((A ^ F) >> k) & 1) ^ parity(A & below & ~((2u << k) - 1));
+        } else {
+          pin = (frac & 1) ^ parity(A & below);
+        }
+        const bool clean = !bad_rec && e_rec == seq::bexp(sb);
+        const uint64_t units = M + (tie_rec && pin != fp_rec ? 1 : 0);
+        const uint64_t incl = warp_incl_u64(in && clean ? units : 0, lane);
+        const unsigned viol =
+            __ballot_sync(kFull, lane >= from && lane < cnt && (!clean || frac + incl > seq::kFrac));
+        f = viol ? __ffs(viol) - 1 : cnt;
+        if (ck_lane && lane >= from && lane < f)
+          out[j * ncp + ((t0 + lane + 1) >> 2) - 1] =
+              __longlong_as_double((long long)((sb & ~seq::kFrac) | (frac + incl)));
+        sb = (sb & ~seq::kFrac) | (frac + (f ? __shfl_sync(kFull, incl, f - 1) : 0));
+      } else {
+        f = from;
+      }
+      if (f >= cnt) break;
+      // step f, term by term
+      const double *x = probs + (step0 + t0 + f) * kStep;
+      uint64_t xb[kStep / 32], mine;
+#pragma unroll
+      for (int k = 0; k < kStep / 32; ++k) xb[k] = (uint64_t)__double_as_longlong(x[32 * k + lane]);
+#pragma unroll
+      for (int k = 0; k < kStep / 32; ++k) sb = add_lanes(sb, xb[k], lane, mine);
+      if (WALK && lane == 0 && ((t0 + f + 1) & 3) == 0)
+        out[j * ncp + ((t0 + f + 1) >> 2) - 1] = __longlong_as_double((long long)sb);
+      from = f + 1;
+    }
+  }
+  if (!WALK && lane == 0) out[j] = __longlong_as_double((long long)sb);
+}
+
+// P[0] = 0, P[j + 1] = fl(P[j] + idxs[j]): the reference's running sum,
+// 32 block totals at a time (add_lanes).
+__global__ void __launch_bounds__(32) k_seq_prefix(const double *__restrict__ idxs, uint64_t nblocks,
+                                                   double *__restrict__ P) {
+  const int lane = threadIdx.x;
+  uint64_t sb = 0, mine = 0;
+  if (lane == 0) P[0] = 0.0;
+  for (uint64_t j0 = 0; j0 < nblocks; j0 += 32) {
+    const uint64_t xb = j0 + lane < nblocks ? (uint64_t)__double_as_longlong(idxs[j0 + lane]) : 0;
+    sb = add_lanes(sb, xb, lane, mine);
+    if (j0 + lane < nblocks) P[j0 + lane + 1] = __longlong_as_double((long long)mine);
   }
 }
 
@@ -242,7 +498,7 @@ void sample_t(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out
   const uint64_t ds = diag_stride_of(dev);
   const uint64_t nblocks = n >= isz ? 1ULL << isz : 0;
   const uint64_t L = nblocks ? END >> isz : 0;
-  const uint64_t ck = kChunk;
+  const uint64_t ck = 1024;  // checkpoint stride of the block walk
   // blocks of up to 1024 amplitudes are walked from P[j] by each shot;
   // longer blocks keep every 1024th partial sum of the walk
   const bool use_cps = L > ck;
@@ -252,61 +508,66 @@ void sample_t(Device &dev, const double *d_rnds, uint64_t shots, uint64_t *d_out
   double *idxs = reinterpret_cast<double *>(dev.aux);
   double *P = idxs + nblocks;
   double *cps = use_cps ? P + nblocks + 1 : nullptr;
-  // the probability buffer, for the staged chains (long blocks) and the walks
+  // the probability buffer (long blocks), followed by the grid steps' data:
+  // step sums, predicted running sums, chain totals and starts, and one
+  // record per step for each of the two chains
+  const uint64_t NS = use_cps ? END / kStep : 0;
+  const size_t step_bytes = NS * (sizeof(float) + sizeof(double) + 2 * sizeof(uint4)) + 2 * nblocks * sizeof(double);
   double *probs = nullptr;
   if (use_cps) {
     try {
-      probs = static_cast<double *>(grow(dev.probs, dev.probs_cap, sizeof(double) * END));
+      probs = static_cast<double *>(grow(dev.probs, dev.probs_cap, sizeof(double) * END + step_bytes));
     } catch (const Error &) {
       cudaGetLastError();  // no room for 8 bytes per outcome: the chains read the state
       probs = nullptr;
     }
   }
   if (probs) {
-    k_probs_exact<T><<<(unsigned)std::min<uint64_t>((END + 255) / 256, (uint64_t)sm_count() * 16), 256, 0,
-                       dev.stream>>>(psi, END, ds, probs);
+    float *stepsum = reinterpret_cast<float *>(probs + END);
+    double *pred = reinterpret_cast<double *>(stepsum + NS);
+    double *total = pred + NS, *start = total + nblocks;
+    uint4 *rec_sum = reinterpret_cast<uint4 *>(start + nblocks), *rec_walk = rec_sum + NS;
+    const unsigned gs = (unsigned)std::min<uint64_t>((NS + 7) / 8, (uint64_t)sm_count() * 8);
+    k_probs_steps<T><<<gs, 256, 0, dev.stream>>>(psi, NS, ds, probs, stepsum);
     check_launch("sampling probabilities");
-  }
-  if (nblocks) {
-    if (probs) {
-      static bool attr = false;
-      if (!attr) {
-        cuda_check(cudaFuncSetAttribute(k_seq_chains<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSeqSmem),
-                   "sampling chain attribute");
-        cuda_check(cudaFuncSetAttribute(k_seq_chains<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSeqSmem),
-                   "sampling chain attribute");
-        attr = true;
-      }
-      int *status = tc_status_word(dev);
-      const unsigned g = (unsigned)((nblocks + kChains - 1) / kChains);
-      k_seq_chains<false><<<g, 64, kSeqSmem, dev.stream>>>(probs, nblocks, L, nullptr, idxs, status);
-      check_launch("sampling block sums");
-      k_seq_prefix<<<1, 32, 0, dev.stream>>>(idxs, nblocks, P);
-      check_launch("sampling block prefix");
-      k_seq_chains<true><<<g, 64, kSeqSmem, dev.stream>>>(probs, nblocks, L, P, cps, status);
+    k_step_prefix<<<(unsigned)nblocks, 256, 0, dev.stream>>>(stepsum, NS / nblocks, pred, total);
+    check_launch("sampling step prefix");
+    k_chain_prefix<<<1, 1024, 0, dev.stream>>>(total, nblocks, start);
+    check_launch("sampling chain prefix");
+    k_grid_units<<<gs, 256, 0, dev.stream>>>(probs, NS, n - isz - 8, pred, start, rec_sum, rec_walk);
+    check_launch("sampling grid units");
+    k_grid_chain<false><<<(unsigned)nblocks, 32, 0, dev.stream>>>(probs, L / kStep, rec_sum, nullptr, idxs);
+    check_launch("sampling block sums");
+    k_seq_prefix<<<1, 32, 0, dev.stream>>>(idxs, nblocks, P);
+    check_launch("sampling block prefix");
+    k_grid_chain<true><<<(unsigned)nblocks, 32, 0, dev.stream>>>(probs, L / kStep, rec_walk, P, cps);
+    check_launch("sampling block walk");
+  } else if (nblocks) {
+    const unsigned g = (unsigned)((nblocks + 31) / 32);
+    k_seq_blocks<T, false><<<g, 32, 0, dev.stream>>>(psi, nblocks, L, ds, nullptr, idxs, ck);
+    check_launch("sampling block sums");
+    k_seq_prefix<<<1, 32, 0, dev.stream>>>(idxs, nblocks, P);
+    check_launch("sampling block prefix");
+    if (use_cps) {
+      k_seq_blocks<T, true><<<g, 32, 0, dev.stream>>>(psi, nblocks, L, ds, P, cps, ck);
       check_launch("sampling block walk");
-    } else {
-      const unsigned g = (unsigned)((nblocks + 31) / 32);
-      k_seq_blocks<T, false><<<g, 32, 0, dev.stream>>>(psi, nblocks, L, ds, nullptr, idxs, ck);
-      check_launch("sampling block sums");
-      k_seq_prefix<<<1, 32, 0, dev.stream>>>(idxs, nblocks, P);
-      check_launch("sampling block prefix");
-      if (use_cps) {
-        k_seq_blocks<T, true><<<g, 32, 0, dev.stream>>>(psi, nblocks, L, ds, P, cps, ck);
-        check_launch("sampling block walk");
-      }
     }
   }
   const unsigned g2 = (unsigned)std::min<uint64_t>((shots + 255) / 256, (uint64_t)sm_count() * 16);
   k_sample_exact<T><<<std::max(g2, 1u), 256, 0, dev.stream>>>(psi, probs, END, nblocks, L, ds, P, cps, ck, d_rnds,
                                                               shots, d_out);
   check_launch("sampling search");
-  // a large probability buffer is not kept between calls (cudaFree waits
-  // for the kernels above)
+  // the probability buffer is kept for the next call while at least a
+  // quarter of the device's memory stays free, else released (cudaFree
+  // waits for the kernels above)
   if (dev.probs && dev.probs_cap > (1ULL << 30)) {
-    cuda_check(cudaFree(dev.probs), "sampling buffer release");
-    dev.probs = nullptr;
-    dev.probs_cap = 0;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < total_b / 4) {
+      cudaGetLastError();
+      cuda_check(cudaFree(dev.probs), "sampling buffer release");
+      dev.probs = nullptr;
+      dev.probs_cap = 0;
+    }
   }
 }
 

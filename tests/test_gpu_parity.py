@@ -137,6 +137,129 @@ def test_sampling_edges():
         assert qv.sample_measure([]).size == 0
 
 
+def _grid_state(kind, n, rng):
+    if kind == "gauss":
+        return rand_state(rng, n)
+    if kind == "uniform":
+        return np.full(1 << n, 2.0 ** (-n / 2), dtype=complex)
+    if kind == "dyadic":  # probabilities 2^-2k: ties on most grids of the running sums
+        k = rng.integers(n // 2 + 2, n // 2 + 9, size=1 << n)
+        psi = (2.0 ** -k) * rng.choice(np.array([1, -1, 1j, -1j]), size=1 << n)
+        return psi * 2.0 ** np.floor(np.log2(1 / np.sum(np.abs(psi) ** 2)) / 2)  # total in (1/4, 1]
+    psi = rand_state(rng, n) * (rng.random(1 << n) < 0.01)  # sparse
+    return psi / np.linalg.norm(psi)
+
+
+def _edge_uniforms(probs, isz, rng, count):
+    """Uniforms on the reference's running sums (in-order accumulation, the
+    block totals from 0 and the walk from the block prefix), one step below
+    and one above them, plus random ones."""
+    nb = 1 << isz
+    blocks = probs.reshape(nb, -1)
+    idxs = np.add.accumulate(blocks, axis=1)[:, -1]
+    pre = np.concatenate([[0.0], np.add.accumulate(idxs)])[:-1]
+    out = [rng.random(count)]
+    for j in rng.integers(0, nb, size=6):
+        walk = np.add.accumulate(np.concatenate([[pre[j]], blocks[j]]))[1:]
+        v = walk[rng.integers(0, walk.size, size=count // 12)]
+        out += [v, np.nextafter(v, 0.0), np.nextafter(v, 1.0)]
+    r = np.concatenate(out)
+    return r[(r >= 0) & (r < 1)]
+
+
+@pytest.mark.parametrize("kind", ["gauss", "uniform", "dyadic", "sparse"])
+@pytest.mark.parametrize("isz", [10, 3])
+def test_sampling_grid_chains_bit_exact(kind, isz):
+    """Long blocks (2^22 outcomes in 2^isz blocks): the block sums and the
+    checkpointed walk run as grid-step chains; shots on and beside the
+    reference's running sums equal the oracle's."""
+    P = pkg()
+    n = 22
+    rng = np.random.default_rng(["gauss", "uniform", "dyadic", "sparse"].index(kind) * 16 + isz)
+    psi = _grid_state(kind, n, rng)
+    rnds = _edge_uniforms(np.abs(psi) ** 2, isz, rng, 1200)
+    with P.QubitVector(n) as qv:
+        qv.initialize_from_vector(psi)
+        qv.set_sample_measure_index_size(isz)
+        got = qv.sample_measure(rnds)
+    want = O.OracleQV(n, psi).sample_measure(rnds, index_size=isz)
+    np.testing.assert_array_equal(got, want)
+
+
+def _walk_samples(probs, rnds, isz):
+    """QubitVector::sample_measure (qubitvector.hpp:2148-2228) for n >= the
+    index size, restated with numpy's in-order accumulation over given
+    probabilities (here a complex64 state's, products in float)."""
+    END = probs.size
+    L = END >> isz
+    idxs = np.add.accumulate(probs.reshape(-1, L), axis=1)[:, -1]
+    P = np.add.accumulate(np.concatenate([[0.0], idxs]))
+    out = np.empty(rnds.size, dtype=np.uint64)
+    walks = {}
+    for i, r in enumerate(rnds):
+        j = int(np.searchsorted(P[1:], r, side="right"))
+        if j == idxs.size:
+            out[i] = END
+            continue
+        if j not in walks:
+            walks[j] = np.add.accumulate(np.concatenate([[P[j]], probs[j * L:(j + 1) * L]]))[1:]
+        w = walks[j]
+        k = int(np.searchsorted(w, r, side="right"))
+        s = j * L + k
+        if k == L:  # past the block's end: the walk goes on, one index at a time
+            p = w[-1]
+            s = (j + 1) * L
+            while s < END - 1:
+                p = p + probs[s]
+                if r < p:
+                    break
+                s += 1
+        out[i] = min(s, END - 1)
+    return out
+
+
+@pytest.mark.parametrize("kind", ["gauss", "sparse"])
+@pytest.mark.parametrize("isz", [10, 3])
+def test_sampling_grid_chains_complex64(kind, isz):
+    """The same at complex64, whose probabilities (float products, widened)
+    carry 24 bits: the block walk meets a tie on most steps, which the grid
+    steps decide by prefix parities; shots equal the reference's walk over
+    those probabilities."""
+    P = pkg()
+    n = 22
+    rng = np.random.default_rng(["gauss", "sparse"].index(kind) * 16 + isz + 100)
+    psi = _grid_state(kind, n, rng)
+    with P.QubitVector(n, "single") as qv:
+        qv.initialize_from_vector(psi)
+        qv.set_sample_measure_index_size(isz)
+        a = np.asarray(qv.copy_to_vector()).astype(np.complex64)
+        probs = (a.real * a.real + a.imag * a.imag).astype(np.float64)
+        rnds = _edge_uniforms(probs, isz, rng, 1200)
+        got = qv.sample_measure(rnds)
+    np.testing.assert_array_equal(got, _walk_samples(probs, rnds, isz))
+
+
+def test_sampling_grid_chain_density_matrix():
+    """Two chains over the 2^12 diagonal of a 12-qubit density matrix (index
+    size 1), diagonal entries with rounding noise around zero."""
+    P = pkg()
+    n = 12
+    rng = np.random.default_rng(5)
+    a = rng.normal(size=(1 << n, 8)) + 1j * rng.normal(size=(1 << n, 8))
+    rho = a @ a.conj().T
+    rho /= np.trace(rho).real
+    d = np.arange(1 << n)
+    rho[d[::97], d[::97]] = -1e-19  # negative diagonal entries: added term by term
+    vec = rho.reshape(-1, order="F")
+    rnds = rng.random(3000)
+    with P.DensityMatrix(n) as dm:
+        dm.initialize_from_vector(vec)
+        dm.set_sample_measure_index_size(1)
+        got = dm.sample_measure(rnds)
+    want = O.OracleDM(n, vec).sample_measure(rnds, index_size=1)
+    np.testing.assert_array_equal(got, want)
+
+
 def test_checkpoint_inner_product():
     P = pkg()
     rng = np.random.default_rng(2)
