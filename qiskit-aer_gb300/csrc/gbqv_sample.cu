@@ -70,6 +70,24 @@ __device__ __forceinline__ float approx_float(double x) {
   return __uint_as_float(f | (hi & 0x80000000u));
 }
 
+// prob_exact with the final add on the integer pipe (seq::add_nonneg, the
+// hardware add where it declines): the pass that writes every probability
+// is otherwise bound by the FP64 pipe.
+template <typename T>
+__device__ __forceinline__ double prob_split(const T *psi, uint64_t i, uint64_t diag_stride) {
+  return prob_exact<T>(psi, i, diag_stride);
+}
+template <>
+__device__ __forceinline__ double prob_split<double2>(const double2 *psi, uint64_t i, uint64_t diag_stride) {
+  if (diag_stride) return psi[i * diag_stride].x;
+  const double2 a = psi[i];
+  const double x = __dmul_rn(a.x, a.x), y = __dmul_rn(a.y, a.y);
+  uint64_t r;
+  if (seq::add_nonneg((uint64_t)__double_as_longlong(x), (uint64_t)__double_as_longlong(y), r))
+    return __longlong_as_double((long long)r);
+  return __dadd_rn(x, y);
+}
+
 // Every outcome's probability in the reference's rounding, one warp per step
 // of 256 outcomes, and each step's approximate sum.
 template <typename T>
@@ -82,7 +100,7 @@ __global__ void __launch_bounds__(256) k_probs_steps(const T *__restrict__ psi, 
 #pragma unroll
     for (int u = 0; u < kStep / 32; ++u) {
       const uint64_t i = t * kStep + 32 * u + lane;
-      const double p = prob_exact<T>(psi, i, diag_stride);
+      const double p = prob_split<T>(psi, i, diag_stride);
       out[i] = p;
       acc += approx_float(p);
     }

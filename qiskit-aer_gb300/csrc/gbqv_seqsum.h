@@ -146,6 +146,51 @@ __host__ __device__ __forceinline__ uint64_t grid_units_fast(uint32_t hi, uint32
   return grid_units32(hi, lo, e, bad, tie);
 }
 
+// fl(a + b) for doubles a, b >= 0 given as bits, rounded to nearest even, in
+// integer arithmetic (an add on the FP64 pipe, moved to the integer pipe):
+// significands aligned with 10 guard bits and a sticky bit, added,
+// renormalised and rounded.  False where the hardware add is wanted: a
+// subnormal b other than zero, an infinite, NaN or negative operand.
+__host__ __device__ __forceinline__ bool add_nonneg(uint64_t a, uint64_t b, uint64_t &r) {
+  if (a < b) {  // a >= b: bit order is value order for non-negative doubles
+    const uint64_t t = a;
+    a = b;
+    b = t;
+  }
+  const int ea = (int)(a >> 52), eb = (int)(b >> 52);
+  if (ea >= 2047) return false;  // a infinite, NaN or negative (b > a as bits then)
+  if (b == 0) {
+    r = a;
+    return true;
+  }
+  if (eb == 0) return false;
+  const int d = ea - eb;
+  if (d > 60) {  // b below 2^-8 units of a: rounds to a
+    r = a;
+    return true;
+  }
+  const uint64_t ma = ((a & kFrac) | (1ULL << 52)) << 10;  // leading bit 62
+  const uint64_t mb0 = ((b & kFrac) | (1ULL << 52)) << 10;
+  const uint64_t mb = d ? mb0 >> d : mb0;
+  bool sticky = d ? (mb0 << (64 - d)) != 0 : false;
+  uint64_t sum = ma + mb;
+  int e = ea;
+  if (sum >> 63) {
+    sticky |= (sum & 1) != 0;
+    sum >>= 1;
+    ++e;
+  }
+  uint64_t m = sum >> 10;  // 53 bits
+  const uint32_t g = (uint32_t)(sum & 0x3ff);
+  if (g > 0x200 || (g == 0x200 && (sticky || (m & 1)))) ++m;
+  if (m >> 53) {
+    m >>= 1;
+    ++e;
+  }
+  r = e >= 2047 ? 0x7ffULL << 52 : ((uint64_t)e << 52) | (m & kFrac);
+  return true;
+}
+
 // s += g * M when the result stays below 2^(e+1); false (s unchanged) if not
 __host__ __device__ __forceinline__ bool grid_add(uint64_t &sb, uint64_t M) {
   const uint64_t f = (sb & kFrac) + M;

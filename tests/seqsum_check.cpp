@@ -14,6 +14,8 @@
 // mismatches> <32-step batch mismatches>".
 // seqsum_check words <trials>: the 32-bit-word forms of the grid units
 // against the 64-bit one; prints the number of differences.
+// seqsum_check add <trials>: the integer add of non-negative doubles against
+// the host's; prints the number of differences.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -37,6 +39,7 @@ static double dbl(uint64_t b) {
 }
 
 constexpr int kStep = 256;
+static constexpr uint64_t kFracMask() { return (1ULL << 52) - 1; }
 
 // A step's record as the grid-units kernel builds it for binade e (terms in
 // order, ties rounded down): M = units + the ties after the first decided by
@@ -233,7 +236,39 @@ static long check_words(long trials, std::mt19937_64 &rng) {
   return bad_count;
 }
 
+// add_nonneg against the host's double addition (round to nearest even) on
+// squares of random doubles, near-ties, wide exponent gaps, zeros, values at
+// the top of the range and operands it hands back to the hardware
+static long check_add(long trials, std::mt19937_64 &rng) {
+  long bad_count = 0;
+  std::normal_distribution<double> g(0.0, 1.0);
+  for (long i = 0; i < trials; ++i) {
+    double x, y;
+    switch (i % 8) {
+      case 0: { const double a = g(rng), b = g(rng); x = a * a; y = b * b; break; }  // probabilities
+      case 1: { const double a = g(rng); x = a * a; y = std::ldexp(a * a, -(int)(rng() % 64)); break; }
+      case 2: x = std::ldexp(1.0, (int)(rng() % 40) - 20); y = std::ldexp(1.0 + (double)(rng() % 8), (int)(rng() % 120) - 110); break;  // near ties
+      case 3: x = dbl(rng() >> 1); y = dbl(rng() >> 1); break;  // any bits, non-negative (incl. nan, inf, subnormal)
+      case 4: x = std::ldexp(g(rng) * g(rng) + 1.0, 1020); y = std::ldexp(std::abs(g(rng)) + 1.0, 1020 - (int)(rng() % 3)); break;  // overflow
+      case 5: x = std::abs(g(rng)); y = (rng() % 2) ? 0.0 : std::ldexp(1.0, -1074 + (int)(rng() % 60)); break;  // zero, subnormal
+      case 6: { const uint64_t m = (rng() & kFracMask()) | 1; x = dbl((1023ULL << 52) | m); y = dbl(((1023ULL - 53 - (rng() % 3)) << 52) | (rng() & 7)); break; }  // ties at the unit
+      default: { const float a = (float)g(rng), b = (float)g(rng); x = (double)(a * a); y = (double)(b * b); break; }
+    }
+    uint64_t r;
+    if (seq::add_nonneg(bits(x), bits(y), r)) {
+      const double want = x + y;
+      if (r != bits(want) && !(std::isnan(want) && std::isnan(dbl(r)))) ++bad_count;
+    }
+  }
+  return bad_count;
+}
+
 int main(int argc, char **argv) {
+  if (argc > 1 && std::string(argv[1]) == "add") {
+    std::mt19937_64 rng(7);
+    printf("%ld\n", check_add(argc > 2 ? atol(argv[2]) : 1000000, rng));
+    return 0;
+  }
   if (argc > 1 && std::string(argv[1]) == "words") {
     std::mt19937_64 rng(99);
     printf("%ld\n", check_words(argc > 2 ? atol(argv[2]) : 200000, rng));

@@ -39,3 +39,13 @@ def test_word_form_equals_grid_units(tmp_path):
     out = subprocess.run([str(_exe(tmp_path)), "words", "400000"], capture_output=True, text=True,
                          check=True).stdout
     assert out.split() == ["0"], out
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_integer_add_equals_double_add(tmp_path):
+    """The probabilities pass adds fl(re^2) + fl(im^2) in integer arithmetic
+    (seq::add_nonneg): bit for bit the double addition, ties, exponent gaps,
+    zeros and overflow included."""
+    out = subprocess.run([str(_exe(tmp_path)), "add", "2000000"], capture_output=True, text=True,
+                         check=True).stdout
+    assert out.split() == ["0"], out
