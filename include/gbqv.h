@@ -446,6 +446,13 @@ int gbqv_batch_add(gbqv_batch_t b, int num_qubits, int ngates, const int *kinds,
  * a bounded barrier after each run (GBQV_ERR_TIMEOUT if one gives up).  Set
  * before the first gbqv_batch_run; default 64 and 0.5. */
 int gbqv_batch_set_teams(gbqv_batch_t b, int max_team_instances, double min_cost_fraction);
+/* Complex128 batches: on != 0 runs the gates, the Hamiltonian and the
+ * generator sums in FP64; the default holds the states as pairs of floats
+ * (~48-bit arithmetic on the FP32 pipe, 16 bytes per amplitude like
+ * complex128, errors near 1e-14), with energies, gradients and sampling
+ * probabilities accumulated in double.  Set before the first
+ * gbqv_batch_run. */
+int gbqv_batch_set_fp64(gbqv_batch_t b, int on);
 /* Run every instance in one persistent kernel launch (captured once as a CUDA
  * graph and replayed on later calls): forward pass, `shots` samples of the
  * final state, E = <H>, and with want_grad the adjoint gradient dE/dparams.

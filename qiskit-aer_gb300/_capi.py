@@ -141,6 +141,7 @@ _SIGS = {
                                  C.c_uint64, C.POINTER(C.c_int)]),
     "gbqv_batch_run": (C.c_int, [H, C.c_int, dp]),
     "gbqv_batch_set_teams": (C.c_int, [H, C.c_int, C.c_double]),
+    "gbqv_batch_set_fp64": (C.c_int, [H, C.c_int]),
     "gbqv_batch_result": (C.c_int, [H, C.c_int, dp, dp, C.c_int, u64p, C.c_uint64, dp]),
     "gbqv_adjoint_expval_grad": (C.c_int, [H, H, C.POINTER(C.c_int), dp, C.c_int, C.c_int, u64p, C.POINTER(C.c_int),
                                            C.POINTER(C.c_char_p), dp, dp, dp]),

@@ -60,6 +60,11 @@ class Batch:
         call before the first run."""
         A.check(self._L.gbqv_batch_set_teams(self._h, int(max_team_instances), float(min_cost_fraction)))
 
+    def set_fp64(self, on: bool = True) -> None:
+        """Complex128 arithmetic on the FP64 pipe instead of float pairs
+        (gbqv_batch_set_fp64); call before the first run."""
+        A.check(self._L.gbqv_batch_set_fp64(self._h, int(bool(on))))
+
     def run(self, want_grad: bool = True) -> float:
         ms = C.c_double()
         A.check(self._L.gbqv_batch_run(self._h, int(want_grad), C.byref(ms)))

@@ -30,9 +30,12 @@
 namespace gbqv {
 namespace {
 
+#include "gbqv_fpair.cuh"
+
 constexpr int kBatchThreads = 256;
 constexpr int kBatchMaxRunOps = 128;
 constexpr int kSampleBits = 10;
+constexpr int kTermCache = 128;  // Hamiltonian terms staged in shared memory per instance
 
 enum BKind { B_RX = 0, B_RY = 1, B_RZ = 2, B_CX = 3, B_CZ = 4, B_H = 5 };
 
@@ -67,19 +70,45 @@ __device__ __forceinline__ T cmul(T a, T b) {
   return r;
 }
 
+// The register/data real of each instantiation: float (complex64), double
+// (complex128 on the FP64 pipe) or a float pair (complex128 held as pairs of
+// floats, ~48 bits, on the FP32 pipe: gbqv_fpair.cuh).  Conversions from
+// double are explicit: a double would otherwise narrow to a float silently
+// on its way to a pair.
+template <typename R>
+__device__ __forceinline__ R from_d(double d) {
+  return (R)d;
+}
+template <>
+__device__ __forceinline__ fpair from_d<fpair>(double d) {
+  return fpair_from_double(d);
+}
+__device__ __forceinline__ double to_d(float v) { return (double)v; }
+__device__ __forceinline__ double to_d(double v) { return v; }
+__device__ __forceinline__ double to_d(fpair v) { return fpair_to_double(v); }
+__device__ __forceinline__ float shfl_xor_r(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_xor_r(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ fpair shfl_xor_r(fpair v, int o) {
+  return fpair(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+__device__ __forceinline__ fpair &operator+=(fpair &a, fpair b) {
+  a = a + b;
+  return a;
+}
+
 template <typename T>
 __device__ __forceinline__ void cfma(T &acc, T a, T b) {
-  acc.x = fma(a.x, b.x, acc.x);
-  acc.x = fma(-a.y, b.y, acc.x);
-  acc.y = fma(a.x, b.y, acc.y);
-  acc.y = fma(a.y, b.x, acc.y);
+  acc.x = rfma(a.x, b.x, acc.x);
+  acc.x = rfma(-a.y, b.y, acc.x);
+  acc.y = rfma(a.x, b.y, acc.y);
+  acc.y = rfma(a.y, b.x, acc.y);
 }
 
 template <typename T>
 __device__ __forceinline__ T cplx(double re, double im) {
   T r;
-  r.x = (decltype(r.x))re;
-  r.y = (decltype(r.y))im;
+  r.x = from_d<decltype(r.x)>(re);
+  r.y = from_d<decltype(r.y)>(im);
   return r;
 }
 
@@ -155,10 +184,10 @@ __device__ __forceinline__ void tile_gate(T *tile, int m, int kind, decltype(T::
       const uint32_t i0 = ins1(p, a), i1 = i0 | (1u << a);
       const T x0 = tile[i0], x1 = tile[i1];
       T y0, y1;
-      y0.x = fma(s1, x1.y, gc * x0.x);
-      y0.y = fma(-s1, x1.x, gc * x0.y);
-      y1.x = fma(s1, x0.y, gc * x1.x);
-      y1.y = fma(-s1, x0.x, gc * x1.y);
+      y0.x = rfma(s1, x1.y, gc * x0.x);
+      y0.y = rfma(-s1, x1.x, gc * x0.y);
+      y1.x = rfma(s1, x0.y, gc * x1.x);
+      y1.y = rfma(-s1, x0.x, gc * x1.y);
       tile[i0] = y0;
       tile[i1] = y1;
     }
@@ -168,7 +197,7 @@ __device__ __forceinline__ void tile_gate(T *tile, int m, int kind, decltype(T::
   if (kind == B_RY) {
     m00 = gc; m01 = -s1; m10 = s1; m11 = gc;
   } else {
-    const R h = (R)0.70710678118654752440;
+    const R h = from_d<R>(0.70710678118654752440);
     m00 = h; m01 = h; m10 = h; m11 = -h;
   }
 #pragma unroll kU
@@ -176,10 +205,10 @@ __device__ __forceinline__ void tile_gate(T *tile, int m, int kind, decltype(T::
     const uint32_t i0 = ins1(p, a), i1 = i0 | (1u << a);
     const T x0 = tile[i0], x1 = tile[i1];
     T y0, y1;
-    y0.x = fma(m01, x1.x, m00 * x0.x);
-    y0.y = fma(m01, x1.y, m00 * x0.y);
-    y1.x = fma(m11, x1.x, m10 * x0.x);
-    y1.y = fma(m11, x1.y, m10 * x0.y);
+    y0.x = rfma(m01, x1.x, m00 * x0.x);
+    y0.y = rfma(m01, x1.y, m00 * x0.y);
+    y1.x = rfma(m11, x1.x, m10 * x0.x);
+    y1.y = rfma(m11, x1.y, m10 * x0.y);
     tile[i0] = y0;
     tile[i1] = y1;
   }
@@ -194,7 +223,7 @@ __device__ __forceinline__ decltype(T::x) tile_generator(const T *lam, const T *
   using R = decltype(T::x);
   const uint32_t L = MT ? (1u << MT) : (1u << m), bit = 1u << a;
   constexpr int kU = MT ? 16 : 1;
-  R acc = 0;
+  R acc = R(0.0f);
 #pragma unroll kU
   for (uint32_t l = threadIdx.x; l < L; l += kBatchThreads) {
     const T lv = lam[l];
@@ -206,7 +235,7 @@ __device__ __forceinline__ decltype(T::x) tile_generator(const T *lam, const T *
       pv = psi[l ^ bit];
     } else {  // Y = -i X Z in the (x, z) form: phase -i, sign (-1)^{bit of l}
       const T v = psi[l ^ bit];
-      const R sg = (l & bit) ? R(-1) : R(1);
+      const R sg = (l & bit) ? R(-1.0f) : R(1.0f);
       pv.x = sg * v.y;   // -i * v = (v.y, -v.x)
       pv.y = -sg * v.x;
     }
@@ -240,6 +269,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
   __shared__ decltype(T::x) s_c[kBatchMaxRunOps], s_s[kBatchMaxRunOps];
   __shared__ double gacc[kBatchMaxRunOps][kBatchThreads / 32];
   __shared__ decltype(T::x) gaccf[kBatchMaxRunOps][kBatchThreads / 32];  // this tile group's sums, data precision
+  __shared__ uint64_t s_tx[kTermCache], s_tz[kTermCache];
+  __shared__ decltype(T::x) s_tc[kTermCache][2];
   __shared__ int s_idx, s_member, s_abort;
   __shared__ unsigned s_nsync;
   __shared__ int s_T[64];
@@ -307,10 +338,12 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
         // probabilities as std::real(z * conj(z)), no contraction
         auto prob = [&](uint64_t k) -> double {
           const T a = psi[k];
-          if constexpr (sizeof(T) == 8)
+          if constexpr (sizeof(T) == 8) {
             return (double)__fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y));
-          else
-            return __dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y));
+          } else {
+            const double re = to_d(a.x), im = to_d(a.y);
+            return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+          }
         };
         const bool blocks = I.n >= kSampleBits;
         const uint64_t nb = blocks ? 1ULL << kSampleBits : 0, L = blocks ? N >> kSampleBits : 0;
@@ -359,19 +392,43 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
         // precision (complex64 sums its terms in float: the FP64 pipe is
         // far narrower), <H> accumulated in double
         using Rt = decltype(T::x);
+        // the coefficients in the data precision, converted once per
+        // instance (a conversion from double runs on the FP64 pipe)
+        const bool staged = I.nterms <= kTermCache;
+        if (staged)
+          for (int t = threadIdx.x; t < I.nterms; t += blockDim.x) {
+            const TermDevB h = terms[I.term_off + t];
+            s_tx[t] = h.x_mask;
+            s_tz[t] = h.z_mask;
+            s_tc[t][0] = from_d<Rt>(h.re);
+            s_tc[t][1] = from_d<Rt>(h.im);
+          }
+        __syncthreads();
         double e_acc = 0.0;
         for (uint64_t i = tbase; i < N; i += tstride) {
-          Rt ar = 0, ai = 0;
+          Rt ar = Rt(0.0f), ai = Rt(0.0f);
           for (int t = 0; t < I.nterms; ++t) {
-            const TermDevB h = terms[I.term_off + t];
-            const T a = psi[i ^ h.x_mask];
-            Rt cr = (Rt)h.re, ci = (Rt)h.im;
-            if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
+            uint64_t xm, zm;
+            Rt cr, ci;
+            if (staged) {
+              xm = s_tx[t];
+              zm = s_tz[t];
+              cr = s_tc[t][0];
+              ci = s_tc[t][1];
+            } else {
+              const TermDevB h = terms[I.term_off + t];
+              xm = h.x_mask;
+              zm = h.z_mask;
+              cr = from_d<Rt>(h.re);
+              ci = from_d<Rt>(h.im);
+            }
+            const T a = psi[i ^ xm];
+            if (__popcll(i & zm) & 1) { cr = -cr; ci = -ci; }
             ar += cr * a.x - ci * a.y;
             ai += cr * a.y + ci * a.x;
           }
           const T p = psi[i];
-          e_acc += (double)(p.x * ar + p.y * ai);
+          e_acc += to_d(p.x * ar + p.y * ai);
           T l;
           l.x = ar;
           l.y = ai;
@@ -399,7 +456,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
         }
         for (int i = threadIdx.x; i < kBatchMaxRunOps * (kBatchThreads / 32); i += blockDim.x) {
           gacc[i / (kBatchThreads / 32)][i % (kBatchThreads / 32)] = 0.0;
-          gaccf[i / (kBatchThreads / 32)][i % (kBatchThreads / 32)] = 0;
+          gaccf[i / (kBatchThreads / 32)][i % (kBatchThreads / 32)] = decltype(T::x)(0.0f);
         }
         __syncthreads();
         for (int k = threadIdx.x; k < R.count; k += blockDim.x) {
@@ -412,8 +469,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
           s_g[k] = g;
           s_a[k] = (uint8_t)a;
           s_b[k] = (uint8_t)b;
-          s_c[k] = (decltype(T::x))g.c;
-          s_s[k] = (decltype(T::x))g.s;
+          s_c[k] = from_d<decltype(T::x)>(g.c);
+          s_s[k] = from_d<decltype(T::x)>(g.s);
         }
         __syncthreads();
         const int m = __popcll(R.tmask);
@@ -475,14 +532,14 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
               // double accumulator of the warp
               auto part = m == M ? tile_generator<T, M>(tl, tp, m, g.kind, a)
                                  : tile_generator<T, 0>(tl, tp, m, g.kind, a);
-              for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+              for (int o = 16; o > 0; o >>= 1) part += shfl_xor_r(part, o);
               if ((threadIdx.x & 31) == 0) {
                 // 16 tiles' warp sums in the data precision, then into double
                 auto &f = gaccf[oi][threadIdx.x >> 5];
                 f += part;
                 if ((lt & 15) == 15) {
-                  gacc[oi][threadIdx.x >> 5] += (double)f;
-                  f = 0;
+                  gacc[oi][threadIdx.x >> 5] += to_d(f);
+                  f = decltype(T::x)(0.0f);
                 }
               }
             }
@@ -509,7 +566,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const InstDev *__restri
             const GateDev &g = s_g[k];
             if (g.param < 0) continue;
             double sum = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += gacc[k][w] + (double)gaccf[k][w];
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += gacc[k][w] + to_d(gaccf[k][w]);
             if (TM == 1)
               grads[I.grad_off + g.param] += sum;
             else
@@ -543,6 +600,7 @@ struct BatchInstHost {
 
 struct gbqv_batch {
   bool dbl = true;
+  bool fp64 = false;  // complex128 gates on the FP64 pipe instead of float pairs
   std::vector<BatchInstHost> inst;
   // device buffers
   cudaStream_t stream = nullptr;
@@ -661,6 +719,14 @@ extern "C" int gbqv_batch_set_teams(gbqv_batch_t b, int max_team_instances, doub
       throw Error(GBQV_ERR_ARG, "team settings out of range (at most 64 team instances)");
     b->team_max = max_team_instances;
     b->team_frac = min_cost_fraction;
+  });
+}
+
+extern "C" int gbqv_batch_set_fp64(gbqv_batch_t b, int on) {
+  return bguard([&] {
+    if (!b) throw Error(GBQV_ERR_ARG, "null batch");
+    if (b->graph) throw Error(GBQV_ERR_ARG, "the arithmetic is fixed once the batch has run");
+    b->fp64 = on != 0;
   });
 }
 
@@ -906,8 +972,10 @@ extern "C" int gbqv_batch_run(gbqv_batch_t b, int want_grad, double *elapsed_ms)
     // one persistent launch (plus the queue reset), captured once as a CUDA graph
     if (!b->graph) {
       cuda_check(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-      if (b->dbl)
+      if (b->dbl && b->fp64)
         launch_batch<double2, 11>(b, L, want_grad);
+      else if (b->dbl)
+        launch_batch<fcx, 11>(b, L, want_grad);
       else
         launch_batch<float2, 12>(b, L, want_grad);
       cuda_check(cudaStreamEndCapture(b->stream, &b->graph_def), "graph capture");

@@ -36,12 +36,17 @@ def _oracle_state(inst):
     return o
 
 
-@pytest.mark.parametrize("precision,tol,gtol", [("double", 1e-11, 1e-9), ("single", 2e-4, 2e-3)])
-def test_batch_matches_single_instance_engine(precision, tol, gtol):
+@pytest.mark.parametrize("precision,fp64,tol,gtol", [("double", False, 1e-11, 1e-9), ("double", True, 1e-11, 1e-9),
+                                                     ("single", False, 2e-4, 2e-3)])
+def test_batch_matches_single_instance_engine(precision, fp64, tol, gtol):
+    """complex128 as float pairs (the default) and on the FP64 pipe, and
+    complex64."""
     P = pkg()
     B, adj = P.batched, P.adjoint
     insts = B.config5_instances(10, seed=5, qmin=3, qmax=13, dmin=1, dmax=4, tmin=4, tmax=12, shots=300)
     b = B.Batch(precision)
+    if fp64:
+        b.set_fp64(True)
     for inst in insts:
         b.add(inst["n"], inst["gates"], inst["theta"], inst["terms"], inst["coeffs"], inst["shots"], inst["seed"])
     ms = b.run(want_grad=True)
