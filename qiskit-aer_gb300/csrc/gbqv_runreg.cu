@@ -4,9 +4,9 @@
 // X gates whose qubits all lie in one tile of m vector qubits) costs one
 // HBM read and one write of the state.  Inside the tile the ops used to
 // sweep shared memory one by one with a barrier between them; here each of
-// the 512 threads holds 2^(m-9) amplitudes of the tile in registers.  The m
+// the 256 threads holds 2^(m-8) amplitudes of the tile in registers.  The m
 // tile bits are split into register bits (the thread's own amplitudes) and
-// 9 thread bits; an op whose dense qubits are register bits is applied in
+// 8 thread bits; an op whose dense qubits are register bits is applied in
 // registers, a 1-qubit dense op or an X target on one of the 5 lane bits is
 // applied with warp shuffles, diagonals and controls may sit on any bit.
 // When an op needs a bit that is neither, the tile is re-laid out once
@@ -35,8 +35,26 @@
 namespace gbqv {
 namespace {
 
-constexpr int kRegThreads = 512;  // 9 thread bits: one CTA per SM, 128 registers a thread
-constexpr int kThreadBits = 9;
+// Tile shapes.  complex64: 256 threads (8 thread bits), 5 register bits (32
+// amplitudes a thread), two CTAs per SM each with one tile buffer, so that
+// one CTA's loads and barriers overlap the other's arithmetic.  complex128:
+// 512 threads (9 thread bits), 3 register bits, one CTA per SM with two tile
+// buffers (the next tile loads while this one is computed).  The
+// interpreting kernel at 32 register amplitudes needs more than 128
+// registers a thread for its dispatch: one CTA per SM, two buffers.
+int reg_tbits(bool dbl) { return dbl ? 9 : 8; }
+template <typename T, int RB>
+struct RegShape {
+  static constexpr int kThreads = sizeof(T) == 8 ? 256 : 512;
+  static constexpr int kTbits = sizeof(T) == 8 ? 8 : 9;
+  static constexpr int kCtas = (sizeof(T) == 8 && RB <= 4) ? 2 : 1;
+  static constexpr int kBufs = kCtas == 1 ? 2 : 1;
+};
+// the specialised kernel's: 128 registers suffice at complex64
+struct JitShape {
+  int threads, tbits, ctas, bufs;
+};
+JitShape jit_shape(bool dbl) { return dbl ? JitShape{512, 9, 1, 2} : JitShape{256, 8, 2, 1}; }
 constexpr int kRegMaxOps = 24;
 constexpr int kRegMaxSegs = kRegMaxOps + 1;
 
@@ -157,35 +175,39 @@ __device__ __forceinline__ void apply_reg_op(T (&v)[R], const RegOp &op, const T
   }
 }
 
-// Two tile buffers: tile t + gridDim.x is fetched with cp.async into one while
-// tile t is computed in registers (and re-laid out) through the other.
+// One or two tile buffers (RegShape): with two, tile t + gridDim.x is
+// fetched with cp.async into one while tile t is computed in registers (and
+// re-laid out) through the other; with one, tile t is fetched, computed and
+// written back while the SM's other CTA overlaps it.
 template <typename T, int RB>
-__global__ void __launch_bounds__(kRegThreads, 1) k_run_reg(T *__restrict__ psi, const RegParams *__restrict__ P,
-                                                           const T *__restrict__ pool, const T *__restrict__ bpool) {
-  constexpr int R = 1 << RB;
+__global__ void __launch_bounds__(RegShape<T, RB>::kThreads, RegShape<T, RB>::kCtas)
+    k_run_reg(T *__restrict__ psi, const RegParams *__restrict__ P, const T *__restrict__ pool,
+              const T *__restrict__ bpool) {
+  constexpr int R = 1 << RB, NT = RegShape<T, RB>::kThreads, TBITS = RegShape<T, RB>::kTbits,
+                NBUF = RegShape<T, RB>::kBufs;
   constexpr uint32_t kPer = 16 / sizeof(T);  // amplitudes per 16-byte copy
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = P->m, c = P->c, nsegs = P->nsegs, nops = P->nops;
   const int tid = threadIdx.x;
   const uint32_t L = 1u << m, cmask = (1u << c) - 1;
   T *buf0 = reinterpret_cast<T *>(smem_raw);
-  T *buf1 = buf0 + L;
-  T *mats = buf1 + L;
+  T *buf1 = buf0 + (NBUF == 2 ? L : 0);
+  T *mats = buf0 + NBUF * L;
   T *bmats = mats + P->pool_elems;
   RegOp *ops = reinterpret_cast<RegOp *>(bmats + P->bound_elems);
   RegSeg *segs = reinterpret_cast<RegSeg *>(ops + nops);
   uint64_t *hi = reinterpret_cast<uint64_t *>((reinterpret_cast<uintptr_t>(segs + nsegs) + 7) & ~uintptr_t(7));
-  for (int i = tid; i < P->pool_elems; i += kRegThreads) mats[i] = pool[i];
+  for (int i = tid; i < P->pool_elems; i += NT) mats[i] = pool[i];
   {
     const int *src = reinterpret_cast<const int *>(P->ops);
     int *dst = reinterpret_cast<int *>(ops);
-    for (int i = tid; i < nops * (int)(sizeof(RegOp) / 4); i += kRegThreads) dst[i] = src[i];
+    for (int i = tid; i < nops * (int)(sizeof(RegOp) / 4); i += NT) dst[i] = src[i];
     src = reinterpret_cast<const int *>(P->segs);
     dst = reinterpret_cast<int *>(segs);
-    for (int i = tid; i < nsegs * (int)(sizeof(RegSeg) / 4); i += kRegThreads) dst[i] = src[i];
+    for (int i = tid; i < nsegs * (int)(sizeof(RegSeg) / 4); i += NT) dst[i] = src[i];
   }
   const uint32_t nhi = 1u << (m - c);
-  for (uint32_t h = tid; h < nhi; h += kRegThreads) {
+  for (uint32_t h = tid; h < nhi; h += NT) {
     uint64_t a = 0;
     for (int j = c; j < m; ++j)
       if ((h >> (j - c)) & 1) a |= 1ULL << P->T[j];
@@ -198,25 +220,35 @@ __global__ void __launch_bounds__(kRegThreads, 1) k_run_reg(T *__restrict__ psi,
   auto fetch = [&](uint64_t t, T *buf) {
     const uint64_t gb = tile_base(t, P->tile_lowmask, m);
     if (skip(gb)) return;
-    for (uint32_t ch = tid; ch < L / kPer; ch += kRegThreads) {
+    for (uint32_t ch = tid; ch < L / kPer; ch += NT) {
       const uint32_t l = ch * kPer;  // kPer consecutive tile indices: consecutive amplitudes (c >= 4)
       cp_async16(buf + l, psi + (gb | hi[l >> c] | (l & cmask)));
     }
   };
   uint64_t t = blockIdx.x;
-  if (t < P->ntiles) fetch(t, buf0);
-  cp_async_commit();
-  for (int k = 0; t < P->ntiles; t += gridDim.x, ++k) {
-    T *tile = (k & 1) ? buf1 : buf0;
-    if (t + gridDim.x < P->ntiles) fetch(t + gridDim.x, (k & 1) ? buf0 : buf1);
+  if (NBUF == 2) {
+    if (t < P->ntiles) fetch(t, buf0);
     cp_async_commit();
-    cp_async_wait<1>();  // this tile's copies (all but the group just issued)
-    __syncthreads();
+  }
+  for (int k = 0; t < P->ntiles; t += gridDim.x, ++k) {
+    T *tile = (NBUF == 2 && (k & 1)) ? buf1 : buf0;
     const uint64_t gbase = tile_base(t, P->tile_lowmask, m);
-    if (skip(gbase)) continue;  // same value in every thread of the CTA
+    if (NBUF == 2) {
+      if (t + gridDim.x < P->ntiles) fetch(t + gridDim.x, (k & 1) ? buf0 : buf1);
+      cp_async_commit();
+      cp_async_wait<1>();  // this tile's copies (all but the group just issued)
+      __syncthreads();
+      if (skip(gbase)) continue;  // same value in every thread of the CTA
+    } else {
+      if (skip(gbase)) continue;
+      fetch(t, tile);
+      cp_async_commit();
+      cp_async_wait<0>();
+      __syncthreads();
+    }
     if (bound) {
       const T *src = bpool + (gbase >> P->state_bits) * (uint64_t)P->bound_elems;
-      for (int i = tid; i < P->bound_elems; i += kRegThreads) bmats[i] = src[i];
+      for (int i = tid; i < P->bound_elems; i += NT) bmats[i] = src[i];
       __syncthreads();
     }
     T v[R];
@@ -232,7 +264,7 @@ __global__ void __launch_bounds__(kRegThreads, 1) k_run_reg(T *__restrict__ psi,
       }
       tpart = 0;
 #pragma unroll
-      for (int q = 0; q < kThreadBits; ++q) tpart |= (((uint32_t)tid >> q) & 1u) << S.tb[q];
+      for (int q = 0; q < TBITS; ++q) tpart |= (((uint32_t)tid >> q) & 1u) << S.tb[q];
 #pragma unroll
       for (int i = 0; i < R; ++i) v[i] = tile[tpart | S.rp[i]];
       for (int o = S.first; o < S.first + S.count; ++o) {
@@ -247,8 +279,8 @@ __global__ void __launch_bounds__(kRegThreads, 1) k_run_reg(T *__restrict__ psi,
       for (int i = 0; i < R; ++i) tile[tpart | Sl.rp[i]] = v[i];
     }
     __syncthreads();
-    for (uint32_t l = tid; l < L; l += kRegThreads) psi[gbase | hi[l >> c] | (l & cmask)] = tile[l];
-    __syncthreads();  // the buffer is fetched into again two tiles later; bmats are rewritten next tile
+    for (uint32_t l = tid; l < L; l += NT) psi[gbase | hi[l >> c] | (l & cmask)] = tile[l];
+    __syncthreads();  // the buffer is fetched into again; bmats are rewritten next tile
   }
   cp_async_wait<0>();
 }
@@ -279,7 +311,8 @@ void launch_reg_t(Device &dev, RegParams &P, const std::vector<T> &pool, const s
   if (bpoolb)
     cuda_check(cudaMemcpyAsync(base + bpool_off, bpool.data(), bpoolb, cudaMemcpyHostToDevice, dev.stream),
                "run upload");
-  size_t smem = sizeof(T) * (2 * (1u << P.m) + pool.size() + (size_t)P.bound_elems);
+  constexpr int NT = RegShape<T, RB>::kThreads;
+  size_t smem = sizeof(T) * (RegShape<T, RB>::kBufs * (1u << P.m) + pool.size() + (size_t)P.bound_elems);
   smem += sizeof(RegOp) * P.nops + sizeof(RegSeg) * P.nsegs;
   smem = (smem + 7) & ~size_t(7);
   smem += sizeof(uint64_t) * (1u << (P.m - P.c));
@@ -290,11 +323,11 @@ void launch_reg_t(Device &dev, RegParams &P, const std::vector<T> &pool, const s
     attr_set = true;
   }
   int per_sm = 0;
-  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run_reg<T, RB>, kRegThreads, smem),
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run_reg<T, RB>, NT, smem),
              "occupancy");
   per_sm = std::max(per_sm, 1);
   const uint64_t grid = std::min<uint64_t>(P.ntiles, (uint64_t)sm_count() * per_sm);
-  k_run_reg<T, RB><<<(unsigned)grid, kRegThreads, smem, dev.stream>>>(
+  k_run_reg<T, RB><<<(unsigned)grid, NT, smem, dev.stream>>>(
       reinterpret_cast<T *>(dev.state), reinterpret_cast<const RegParams *>(base),
       reinterpret_cast<const T *>(base + pool_off), reinterpret_cast<const T *>(base + bpool_off));
   check_launch("run kernel");
@@ -391,18 +424,18 @@ struct JitArgs {
   int T[24];
   int state_bits;
 };
-extern "C" __global__ void __launch_bounds__(512, 1)
+extern "C" __global__ void __launch_bounds__(NT, NCTA)
     k_run_jit(TT *__restrict__ psi, const TR *__restrict__ pool, const TR *__restrict__ bpool, const JitArgs A) {
   constexpr uint32_t L = 1u << M, cmask = (1u << C) - 1, kPer = 16 / sizeof(TT);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, lane = tid & 31;
   TT *buf0 = reinterpret_cast<TT *>(smem_raw);
-  TT *buf1 = buf0 + L;
-  TR *mats = reinterpret_cast<TR *>(buf1 + L);
+  TT *buf1 = buf0 + (NBUF == 2 ? L : 0);
+  TR *mats = reinterpret_cast<TR *>(buf0 + NBUF * L);
   TR *bmats = mats + POOL;
   uint64_t *hi = reinterpret_cast<uint64_t *>(smem_raw + HIOFF);
-  for (int i = tid; i < POOL; i += 512) mats[i] = pool[i];
-  for (uint32_t h = tid; h < (1u << (M - C)); h += 512) {
+  for (int i = tid; i < POOL; i += NT) mats[i] = pool[i];
+  for (uint32_t h = tid; h < (1u << (M - C)); h += NT) {
     uint64_t a = 0;
     for (int j = C; j < M; ++j)
       if ((h >> (j - C)) & 1) a |= 1ULL << A.T[j];
@@ -413,32 +446,42 @@ extern "C" __global__ void __launch_bounds__(512, 1)
   auto fetch = [&](uint64_t t, TT *buf) {
     const uint64_t gb = tile_base(t, A.lowmask, M);
     if (skip(gb)) return;
-    for (uint32_t ch = tid; ch < L / kPer; ch += 512) {
+    for (uint32_t ch = tid; ch < L / kPer; ch += NT) {
       const uint32_t l = ch * kPer;
       cp_async16(buf + l, psi + (gb | hi[l >> C] | (l & cmask)));
     }
   };
   uint64_t t = blockIdx.x;
-  if (t < A.ntiles) fetch(t, buf0);
-  cp_async_commit();
-  for (int k = 0; t < A.ntiles; t += gridDim.x, ++k) {
-    TT *tile = (k & 1) ? buf1 : buf0;
-    if (t + gridDim.x < A.ntiles) fetch(t + gridDim.x, (k & 1) ? buf0 : buf1);
+  if (NBUF == 2) {
+    if (t < A.ntiles) fetch(t, buf0);
     cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
+  }
+  for (int k = 0; t < A.ntiles; t += gridDim.x, ++k) {
+    TT *tile = (NBUF == 2 && (k & 1)) ? buf1 : buf0;
     const uint64_t gbase = tile_base(t, A.lowmask, M);
-    if (skip(gbase)) continue;
+    if (NBUF == 2) {
+      if (t + gridDim.x < A.ntiles) fetch(t + gridDim.x, (k & 1) ? buf0 : buf1);
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+      if (skip(gbase)) continue;
+    } else {
+      if (skip(gbase)) continue;
+      fetch(t, tile);
+      cp_async_commit();
+      cp_async_wait<0>();
+      __syncthreads();
+    }
     if (BOUND > 0) {
       const TR *src = bpool + (gbase >> A.state_bits) * (uint64_t)BOUND;
-      for (int i = tid; i < BOUND; i += 512) bmats[i] = src[i];
+      for (int i = tid; i < BOUND; i += NT) bmats[i] = src[i];
       __syncthreads();
     }
     TR v[R];
     uint32_t tpart;
 SEGMENTS
     __syncthreads();
-    for (uint32_t l = tid; l < L; l += 512) psi[gbase | hi[l >> C] | (l & cmask)] = tile[l];
+    for (uint32_t l = tid; l < L; l += NT) psi[gbase | hi[l >> C] | (l & cmask)] = tile[l];
     __syncthreads();
   }
   cp_async_wait<0>();
@@ -454,15 +497,18 @@ std::string jit_source(bool dbl, bool pairs, const RegParams &P) {
        "typedef unsigned char uint8_t;\ntypedef signed char int8_t;\ntypedef int int32_t;\n"
     << kFpairSrc << "\n" << kRunRegDevSrc << "\n";
   const size_t tsz = dbl ? 16 : 8;
-  const size_t hioff = (tsz * (2 * (1u << P.m) + (size_t)P.pool_elems + (size_t)P.bound_elems) + 7) & ~size_t(7);
+  const JitShape sh = jit_shape(dbl);
+  const size_t hioff =
+      (tsz * ((size_t)sh.bufs * (1u << P.m) + (size_t)P.pool_elems + (size_t)P.bound_elems) + 7) & ~size_t(7);
   o << "typedef " << (dbl ? "double2" : "float2") << " TT;\n"
     << "typedef " << (pairs ? "fcx" : "TT") << " TR;\n"
+    << "constexpr int NT = " << sh.threads << ", NCTA = " << sh.ctas << ", NBUF = " << sh.bufs << ";\n"
     << "constexpr int R = " << R << ", M = " << P.m << ", C = " << P.c << ", POOL = " << P.pool_elems
     << ", BOUND = " << P.bound_elems << ";\nconstexpr uint32_t HIOFF = " << hioff << ";\n";
   std::ostringstream seg;
   auto tpart_expr = [&](const RegSeg &S) {
     std::ostringstream e;
-    for (int q = 0; q < kThreadBits; ++q) e << (q ? " | " : "") << "((((uint32_t)tid >> " << q << ") & 1u) << " << (int)S.tb[q] << ")";
+    for (int q = 0; q < sh.tbits; ++q) e << (q ? " | " : "") << "((((uint32_t)tid >> " << q << ") & 1u) << " << (int)S.tb[q] << ")";
     return e.str();
   };
   for (int si = 0; si < P.nsegs; ++si) {
@@ -608,8 +654,8 @@ CUfunction jit_kernel(const Device &dev, bool dbl, bool pairs, const RegParams &
 int jit_compile_check(bool dbl, std::string &log) {
   auto P = std::make_unique<RegParams>();
   std::memset(P.get(), 0, sizeof(RegParams));
-  P->rb = dbl ? 3 : 4;
-  P->m = P->rb + kThreadBits;
+  P->rb = dbl ? 3 : 5;
+  P->m = P->rb + reg_tbits(dbl);
   P->c = 4;
   P->nsegs = 3;
   const int kinds[] = {RK_DENSE1, RK_DENSE1_REAL, RK_DENSE1_LANE, RK_DENSE2, RK_DIAG1, RK_DIAG,
@@ -634,7 +680,7 @@ int jit_compile_check(bool dbl, std::string &log) {
     S.first = sgi == 0 ? 0 : sgi == 1 ? 4 : 7;
     S.count = sgi == 0 ? 4 : 3;
     for (int i = 0; i < (1 << P->rb); ++i) S.rp[i] = (uint16_t)(i << sgi);
-    for (int q = 0; q < kThreadBits; ++q) S.tb[q] = (uint8_t)(q < sgi ? q : q + P->rb);
+    for (int q = 0; q < reg_tbits(dbl); ++q) S.tb[q] = (uint8_t)(q < sgi ? q : q + P->rb);
   }
   P->pool_elems = 40;
   P->bound_elems = 40;
@@ -677,7 +723,8 @@ bool launch_reg_jit(Device &dev, RegParams &P, const std::vector<T> &pool_in, co
   if (bpoolb)
     cuda_check(cudaMemcpyAsync(base + bpool_off, bpool.data(), bpoolb, cudaMemcpyHostToDevice, dev.stream),
                "run upload");
-  size_t smem = (sizeof(T) * (2 * (1u << P.m) + pool.size() + (size_t)P.bound_elems) + 7) & ~size_t(7);
+  const JitShape sh = jit_shape(sizeof(T) == 16);
+  size_t smem = (sizeof(T) * ((size_t)sh.bufs * (1u << P.m) + pool.size() + (size_t)P.bound_elems) + 7) & ~size_t(7);
   smem += sizeof(uint64_t) * (1u << (P.m - P.c));
   const DriverModule &d = driver_module();
   {
@@ -704,8 +751,9 @@ bool launch_reg_jit(Device &dev, RegParams &P, const std::vector<T> &pool_in, co
   T *psi = reinterpret_cast<T *>(dev.state);
   const T *pp = reinterpret_cast<const T *>(base), *bp = reinterpret_cast<const T *>(base + bpool_off);
   void *args[] = {&psi, &pp, &bp, &a};
-  const uint64_t grid = std::min<uint64_t>(P.ntiles, (uint64_t)sm_count());
-  if (d.launch(fn, (unsigned)grid, 1, 1, kRegThreads, 1, 1, (unsigned)smem, dev.stream, args, nullptr) != CUDA_SUCCESS)
+  const uint64_t grid = std::min<uint64_t>(P.ntiles, (uint64_t)sm_count() * sh.ctas);
+  if (d.launch(fn, (unsigned)grid, 1, 1, (unsigned)sh.threads, 1, 1, (unsigned)smem, dev.stream, args, nullptr) !=
+      CUDA_SUCCESS)
     throw Error(3, "specialised run kernel launch failed");
   check_launch("specialised run kernel");
   ++g_jit_launched;
@@ -748,8 +796,9 @@ int run_jit_compile_check(bool dbl, std::string &log) { return jit_compile_check
 bool launch_run_reg(Device &dev, const std::vector<const RunOp *> &ops, const std::vector<int> &tile_qubits, int c,
                     const RunBound *bound) {
   const int m = (int)tile_qubits.size();
-  const int rb = m - kThreadBits;
-  const int maxrb = dev.dbl ? 3 : 4;
+  const int tbits = reg_tbits(dev.dbl);
+  const int rb = m - tbits;
+  const int maxrb = dev.dbl ? 3 : 5;
   if (rb < 2 || rb > maxrb || (int)ops.size() > kRegMaxOps || ops.empty()) return false;
   for (const RunOp *op : ops) {
     if (op->kind == 0 && op->qubits.size() > 2) return false;
@@ -821,7 +870,7 @@ bool launch_run_reg(Device &dev, const std::vector<const RunOp *> &ops, const st
         if ((i >> p) & 1) a |= 1u << rg[p];
       S.rp[i] = (uint16_t)a;
     }
-    for (int q = 0; q < kThreadBits; ++q) S.tb[q] = (uint8_t)tb[q];
+    for (int q = 0; q < tbits; ++q) S.tb[q] = (uint8_t)tb[q];
     auto rpos = [&](int b) { return (int)(std::find(rg.begin(), rg.end(), b) - rg.begin()); };
     auto tpos = [&](int b) { return (int)(std::find(tb.begin(), tb.end(), b) - tb.begin()); };
     for (size_t o : seg_ops[s]) {
@@ -935,6 +984,10 @@ bool launch_run_reg(Device &dev, const std::vector<const RunOp *> &ops, const st
       case 4:
         if constexpr (sizeof(T) == 8)
           if (!launch_reg_jit<T, 4>(dev, *P, pool, bpool)) launch_reg_t<T, 4>(dev, *P, pool, bpool);
+        break;
+      case 5:
+        if constexpr (sizeof(T) == 8)
+          if (!launch_reg_jit<T, 5>(dev, *P, pool, bpool)) launch_reg_t<T, 5>(dev, *P, pool, bpool);
         break;
       default: break;
     }
