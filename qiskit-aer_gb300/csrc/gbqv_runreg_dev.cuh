@@ -42,6 +42,28 @@ __device__ __forceinline__ void cfma(T &acc, T a, T b) {
   acc.y = rfma(a.x, b.y, acc.y);
   acc.y = rfma(a.y, b.x, acc.y);
 }
+// m0 * a0 + m1 * a1, and sum_c m[stride c] * x[c]: multiply-add chains at
+// complex64 / complex128 (the order of the shared-memory run kernel), one
+// compensated dot product per real part for float pairs (gbqv_fpair.cuh)
+template <typename T>
+__device__ __forceinline__ T cdot2(T m0, T a0, T m1, T a1) {
+  T r;
+  r.x = 0;
+  r.y = 0;
+  cfma(r, m0, a0);
+  cfma(r, m1, a1);
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ T cdot4(const T *m, int stride, const T (&x)[4]) {
+  T r;
+  r.x = 0;
+  r.y = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) cfma(r, m[stride * c], x[c]);
+  return r;
+}
+
 template <typename T>
 __device__ __forceinline__ T czero() {
   T z;
@@ -65,13 +87,8 @@ __device__ __forceinline__ void reg_dense1(T (&v)[R], const T *m) {
   for (int p = 0; p < R / 2; ++p) {
     const int i0 = ((p >> J) << (J + 1)) | (p & ((1 << J) - 1)), i1 = i0 | (1 << J);
     const T a0 = v[i0], a1 = v[i1];
-    T r0 = czero<T>(), r1 = czero<T>();
-    cfma(r0, m00, a0);
-    cfma(r0, m01, a1);
-    cfma(r1, m10, a0);
-    cfma(r1, m11, a1);
-    v[i0] = r0;
-    v[i1] = r1;
+    v[i0] = cdot2(m00, a0, m01, a1);
+    v[i1] = cdot2(m10, a0, m11, a1);
   }
 }
 // real matrix: the complex FMAs above with every imaginary matrix term zero
@@ -120,12 +137,7 @@ __device__ __forceinline__ void reg_dense2(T (&v)[R], const T *m) {
 #pragma unroll
     for (int c = 0; c < 4; ++c) x[c] = v[idx[c]];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      T acc = czero<T>();
-#pragma unroll
-      for (int c = 0; c < 4; ++c) cfma(acc, m[r + 4 * c], x[c]);
-      v[idx[r]] = acc;
-    }
+    for (int r = 0; r < 4; ++r) v[idx[r]] = cdot4(m + r, 4, x);
   }
 }
 
@@ -139,10 +151,7 @@ __device__ __forceinline__ void lane_dense1(T (&v)[R], const T *mat, int a, int 
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const T o = shfl_x(v[i], 1 << a);
-    T r = czero<T>();
-    cfma(r, ms, v[i]);
-    cfma(r, mo, o);
-    v[i] = r;
+    v[i] = cdot2(ms, v[i], mo, o);
   }
 }
 template <typename T, int R>
