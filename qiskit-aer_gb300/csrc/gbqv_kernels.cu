@@ -649,7 +649,9 @@ __global__ void __launch_bounds__(256) k_expval(const T *__restrict__ psi, int n
 // (s0 + s1) + pi zi (s1 - s0).  complex64 keeps each thread's two sums in
 // float with compensated (Kahan) addition and converts once, so that no FP64
 // operation runs per amplitude (with a double add per 8 amplitudes the FP64
-// pipe was 86 % busy and bounded the kernel); complex128 adds in double.
+// pipe was 86 % busy and bounded the kernel); complex128 forms the products
+// and the thread's sums as float pairs (compensated dot products,
+// gbqv_fpair.cuh), then adds in double.
 template <typename R>
 struct SegSum {
   R s = 0, c = 0;
@@ -677,7 +679,43 @@ __global__ void __launch_bounds__(256) k_expval_seg(const T *__restrict__ psi, i
   const uint32_t z = (uint32_t)t.z_mask, stride = (uint32_t)bps * blockDim.x;
   SegSum<R> A, B;
   double acc;
-  if (!t.x_mask) {
+  if constexpr (sizeof(T) == 16) {
+    // complex128: products and sums as float pairs (~48 bits, FP32 pipe;
+    // conversions on the integer pipe), the thread's sums into double once
+    fpair fa(0.0f), fb(0.0f);
+    auto dbl2 = [](fpair v) { return fpair(2.0f * v.hi, 2.0f * v.lo); };
+    if (!t.x_mask) {
+      const uint32_t count = 1u << sb;
+      for (uint32_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const fcx a = to_reg_pair(ps[i]);
+        fp_dot d = fp_dot_first(a.x, a.x);
+        fp_dot_add(d, a.y, a.y);
+        const fpair v = fp_dot_done(d);
+        fa = fa + ((__popc(i & z) & 1) ? -v : v);
+      }
+      acc = t.ph_re * fpair_to_double(fa);
+    } else {
+      const uint32_t count = 1u << (sb - 1), x = (uint32_t)t.x_mask;
+      const uint32_t mask_l = (1u << t.x_max) - 1;
+      for (uint32_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const uint32_t i0 = ((i & ~mask_l) << 1) | (i & mask_l), i1 = i0 ^ x;
+        const fcx a0 = to_reg_pair(ps[i0]), a1 = to_reg_pair(ps[i1]);
+        const bool n0 = __popc(i0 & z) & 1, n1 = __popc(i1 & z) & 1;
+        if (n0 == n1) {  // 2 Re(a1 conj a0)
+          fp_dot d = fp_dot_first(a1.x, a0.x);
+          fp_dot_add(d, a1.y, a0.y);
+          const fpair zr = dbl2(fp_dot_done(d));
+          fa = fa + (n0 ? -zr : zr);
+        } else {  // 2 Im(a1 conj a0)
+          fp_dot d = fp_dot_first(a1.y, a0.x);
+          fp_dot_add(d, -a1.x, a0.y);
+          const fpair zi = dbl2(fp_dot_done(d));
+          fb = fb + (n0 ? zi : -zi);
+        }
+      }
+      acc = t.ph_re * fpair_to_double(fa) + t.ph_im * fpair_to_double(fb);
+    }
+  } else if (!t.x_mask) {
     const uint32_t count = 1u << sb;
     for (uint32_t i = slice * blockDim.x + threadIdx.x; i < count; i += stride) {
       const T a = ps[i];
