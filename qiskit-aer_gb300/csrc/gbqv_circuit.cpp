@@ -1671,8 +1671,55 @@ extern "C" int gbqv_adjoint_expval_grad(gbqv_handle h, gbqv_circuit_t c, const i
           h.slot = slot[i];
           return h;
         };
+        // CX (one control), X and SWAP without a generator: a run of three or
+        // more of them is uncomputed in one gather per state (their product
+        // is a linear map of the index bits plus a constant), through the
+        // third state buffer
+        auto linear_op = [&](int i) {
+          if (slot[i] >= 0) return false;
+          const Prim inv = inverse_prim(op_prim(ops[i]));
+          return (inv.k == P::MCX && inv.q.size() <= 2) || (inv.k == P::MCSWAP && inv.q.size() == 2);
+        };
         for (int i = (int)ops.size() - 1; i >= 0;) {
           const Step &st = steps[i];
+          if (i > 0 && linear_op(i)) {
+            int j = i;
+            while (j > 0 && linear_op(j)) --j;  // ops j + 1 .. i (op 0 is never uncomputed)
+            if (i - j >= 3) {
+              // src(y) = M y ^ c, M's columns composed in application order
+              // (i first): CX(a -> b) adds column b to column a, X(q) adds
+              // column q to c, SWAP exchanges two columns
+              std::vector<uint64_t> col(d.n);
+              for (int q = 0; q < d.n; ++q) col[q] = 1ULL << q;
+              uint64_t cst = 0;
+              for (int k = i; k > j; --k) {
+                const Prim inv = inverse_prim(op_prim(ops[k]));
+                if (inv.k == P::MCX && inv.q.size() == 1)
+                  cst ^= col[inv.q[0]];
+                else if (inv.k == P::MCX)
+                  col[inv.q[0]] ^= col[inv.q[1]];
+                else
+                  std::swap(col[inv.q[0]], col[inv.q[1]]);
+              }
+              LinearGatherHost g;
+              g.c = cst;
+              for (int q = 0; q < d.n; ++q)
+                if (col[q] != (1ULL << q)) {
+                  g.q.push_back(q);
+                  g.d.push_back(col[q] ^ (1ULL << q));
+                }
+              grow(d.aux2, d.aux2_cap, bytes);
+              gather_linear(d, d.state, d.aux2, g);
+              std::swap(d.state, d.aux2);  // the state buffer (exactly `bytes`) becomes the scratch
+              d.aux2_cap = bytes;
+              gather_linear(d, d.aux, d.aux2, g);
+              std::swap(d.aux, d.aux2);
+              std::swap(d.aux_cap, d.aux2_cap);
+              lam = d.aux;
+              i = j;
+              continue;
+            }
+          }
           if (st.form >= 0 && i > 0) {
             std::vector<AdjStepHost> grp;
             std::vector<uint64_t> used;

@@ -136,6 +136,14 @@ struct AdjStepHost {
   int slot = -1;
 };
 void adjoint_steps(Device &dev, void *psi, void *lam, const std::vector<AdjStepHost> &steps, bool pairs);
+// A product of CX, X and SWAP gates as one gather pass, out[y] = in[src(y)]:
+// src(y) = y ^ c ^ (xor of d[k] over the qubits q[k] whose bit is set in y).
+struct LinearGatherHost {
+  std::vector<int> q;
+  std::vector<uint64_t> d;
+  uint64_t c = 0;
+};
+void gather_linear(Device &dev, const void *in, void *out, const LinearGatherHost &g);
 void adjoint_to_pairs(Device &dev, void *a);
 void adjoint_from_pairs(Device &dev, void *a);
 // lam = H psi with psi and lam as float pairs (complex128 adjoint sweep).

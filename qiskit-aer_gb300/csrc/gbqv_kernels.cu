@@ -1992,6 +1992,51 @@ void launch_adj_steps(Device &dev, void *psi, void *lam, const std::vector<AdjSt
     }
 }
 
+namespace {
+// out[y] = in[src(y)] for a linear (GF(2)) map of the index bits plus a
+// constant: the source index from the map's columns, one pass that reads
+// and writes each element once (a run of CX / X / SWAP gates is otherwise
+// one pass per gate)
+struct LinearGather {
+  int nq;
+  int q[64];
+  uint64_t d[64];
+  uint64_t c;
+};
+template <typename E>
+__global__ void __launch_bounds__(256) k_gather_linear(const E *__restrict__ in, E *__restrict__ out, uint64_t count,
+                                                       const __grid_constant__ LinearGather G) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t y = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; y < count; y += stride) {
+    uint64_t src = y ^ G.c;
+    for (int k = 0; k < G.nq; ++k)
+      if ((y >> G.q[k]) & 1) src ^= G.d[k];
+    out[y] = in[src];
+  }
+}
+}  // namespace
+
+void gather_linear(Device &dev, const void *in, void *out, const LinearGatherHost &g) {
+  LinearGather G;
+  std::memset(&G, 0, sizeof(G));
+  if (g.q.size() > 64 || g.q.size() != g.d.size()) throw Error(1, "linear gather: bad map");
+  G.nq = (int)g.q.size();
+  for (int k = 0; k < G.nq; ++k) {
+    G.q[k] = g.q[k];
+    G.d[k] = g.d[k];
+  }
+  G.c = g.c;
+  const uint64_t count = dev.amps();
+  const unsigned grid = (unsigned)std::min<uint64_t>((count + 255) / 256, (uint64_t)sm_count() * 16);
+  if (dev.amp_bytes() == 16)
+    k_gather_linear<uint4><<<grid, 256, 0, dev.stream>>>(static_cast<const uint4 *>(in), static_cast<uint4 *>(out),
+                                                         count, G);
+  else
+    k_gather_linear<uint2><<<grid, 256, 0, dev.stream>>>(static_cast<const uint2 *>(in), static_cast<uint2 *>(out),
+                                                         count, G);
+  check_launch("linear gather");
+}
+
 void adjoint_steps(Device &dev, void *psi, void *lam, const std::vector<AdjStepHost> &steps, bool pairs) {
   const int K = (int)steps.size();
   if (K < 1 || K > 3) throw Error(1, "adjoint steps: 1 to 3 per pass");

@@ -704,6 +704,19 @@ __global__ void __launch_bounds__(tc_threads<2>(), 1)
         issued = 2 * i + kh + 1;
       }
       if (!ok) break;
+      // the CTA's next tile into L2 now: its K-halves are loaded only as the
+      // producers free this tile's slots, and then arrive from L2
+      const uint64_t next = tile + gridDim.x;
+      if (next < ntiles) {
+        const uint64_t nfirst = insert_zeros_k5(next * kTcGroups, p.lowmask);
+        for (uint32_t r = 0; r < 2 * p.nhalf; ++r) {
+          const uint64_t off = nfirst + p.hoff[r];
+          if (p.swz)
+            tc::tma_prefetch_2d(&p.tmap, 0, (int)(off >> 3));
+          else
+            tc::bulk_prefetch_l2(psi + off, p.runbytes);
+        }
+      }
     }
     // copies in flight after an abort land before the CTA exits
     int never = 0;

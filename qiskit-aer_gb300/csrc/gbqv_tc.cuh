@@ -187,6 +187,16 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const void *tmap, int 
       : "memory");
 }
 
+// L2 prefetches, nothing to wait for: a tile of a 2D tensor map (the
+// coordinates of a load), and a plain 16-byte aligned range (a multiple of
+// 16 bytes).
+__device__ __forceinline__ void tma_prefetch_2d(const void *tmap, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global [%0, {%1, %2}];" ::"l"(tmap), "r"(x), "r"(y) : "memory");
+}
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // The same with 3 to 5 dimensions (coordinates beyond y are 0).
 template <int N>
 __device__ __forceinline__ void tma_load_nd(uint32_t dst, const void *tmap, int y, uint32_t bar) {

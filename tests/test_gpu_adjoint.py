@@ -22,6 +22,10 @@ def oracle_energy(ansatz, theta, ham):
             o.apply_mcx(ins.qubits)
         elif ins.name == "h":
             o.apply_mcu(ins.qubits, O.u4(np.pi / 2, 0, np.pi, 0))
+        elif ins.name == "x":
+            o.apply_mcx(ins.qubits)
+        elif ins.name == "swap":
+            o.apply_mcswap(ins.qubits)
     return sum(c * o.expval_pauli(q, lab) for (q, lab), c in zip(ham.terms, ham.coeffs))
 
 
@@ -49,6 +53,38 @@ def test_adjoint_vs_param_shift_and_oracle(precision):
     fd = eng.finite_diff_grad(ans, theta, ham, [0, 5, 17, ans.num_params - 1], h=1e-5 if precision == "double" else 1e-2)
     for i, v in fd.items():
         assert abs(v - g[i]) < (1e-7 if precision == "double" else 5e-2), (i, v, g[i])
+    eng.close()
+
+
+@pytest.mark.parametrize("precision,atol,etol", [("double", 1e-10, 1e-11), ("single", 2e-3, 1e-4)])
+def test_permutation_runs_in_one_gather(precision, atol, etol):
+    """Runs of CX, X and SWAP gates between the rotations, uncomputed in the
+    sweep as one gather per state (their product is a linear map of the
+    index bits plus a constant): gradients against parameter shift, energy
+    against the oracle."""
+    P = pkg()
+    adj = P.adjoint
+    rng = np.random.default_rng(21)
+    n = 6
+    gates = [("h", [q], None, None) for q in range(n)]
+    p = 0
+    perm_runs = ([("cx", [0, 3]), ("x", [2]), ("swap", [1, 4]), ("cx", [4, 0]), ("cx", [2, 5]), ("x", [5])],
+                 [("swap", [0, 2]), ("cx", [5, 1]), ("cx", [1, 2]), ("cx", [2, 3]), ("swap", [3, 5])],
+                 [("x", [0]), ("x", [4]), ("cx", [3, 4])])
+    for run in perm_runs:
+        for q in range(n):
+            gates.append(("ry" if q % 2 else "rz", [q], p, None))
+            p += 1
+        gates += [(name, q, None, None) for name, q in run]
+    gates.append(("rx", [2], p, None))
+    ans = adj.Ansatz(n, gates)
+    ham = adj.random_hamiltonian(n, 15, rng)
+    theta = rng.uniform(-3, 3, ans.num_params)
+    eng = adj.Engine(n, precision)
+    e, g = eng.energy_and_grad(ans, theta, ham)
+    ps = eng.param_shift_grad(ans, theta, ham)
+    np.testing.assert_allclose(g, [ps[i] for i in range(ans.num_params)], atol=atol)
+    assert abs(e - oracle_energy(ans, theta, ham)) < etol
     eng.close()
 
 
