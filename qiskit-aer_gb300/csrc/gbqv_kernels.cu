@@ -2003,14 +2003,27 @@ struct LinearGather {
   uint64_t d[64];
   uint64_t c;
 };
+// The source index through per-byte tables in shared memory: tab[b][v] = the
+// xor of d[k] over the map's qubits in byte b of the index whose bit is set
+// in v, so that src = y ^ c ^ tab[0][y & 255] ^ tab[1][(y >> 8) & 255] ^ ...
+constexpr int kGatherBytes = 5;  // indices below 2^40
 template <typename E>
 __global__ void __launch_bounds__(256) k_gather_linear(const E *__restrict__ in, E *__restrict__ out, uint64_t count,
                                                        const __grid_constant__ LinearGather G) {
+  __shared__ uint64_t tab[kGatherBytes][256];
+  for (int e = threadIdx.x; e < kGatherBytes * 256; e += blockDim.x) {
+    const int b = e >> 8, v = e & 255;
+    uint64_t x = 0;
+    for (int k = 0; k < G.nq; ++k)
+      if ((G.q[k] >> 3) == b && ((v >> (G.q[k] & 7)) & 1)) x ^= G.d[k];
+    tab[b][v] = x;
+  }
+  __syncthreads();
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t y = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; y < count; y += stride) {
     uint64_t src = y ^ G.c;
-    for (int k = 0; k < G.nq; ++k)
-      if ((y >> G.q[k]) & 1) src ^= G.d[k];
+#pragma unroll
+    for (int b = 0; b < kGatherBytes; ++b) src ^= tab[b][(y >> (8 * b)) & 255];
     out[y] = in[src];
   }
 }
@@ -2020,6 +2033,8 @@ void gather_linear(Device &dev, const void *in, void *out, const LinearGatherHos
   LinearGather G;
   std::memset(&G, 0, sizeof(G));
   if (g.q.size() > 64 || g.q.size() != g.d.size()) throw Error(1, "linear gather: bad map");
+  for (int q : g.q)
+    if (q < 0 || q >= 8 * kGatherBytes) throw Error(1, "linear gather: qubit beyond the tables");
   G.nq = (int)g.q.size();
   for (int k = 0; k < G.nq; ++k) {
     G.q[k] = g.q[k];
