@@ -1532,6 +1532,7 @@ struct HamTermDev {
   uint64_t x_mask, z_mask;
   double re, im;  // coeff * (-i)^{num_y}
 };
+constexpr int kHamCache = 512;  // terms staged in shared memory
 
 // out = sum_t c_t P_t psi  (one pass writing out, gathers from psi per term)
 template <typename T>
@@ -1541,14 +1542,42 @@ __global__ void __launch_bounds__(256) k_ham_apply(const T *__restrict__ psi, T 
   // complex64: the products in float and the sums compensated (Kahan) in
   // float, so that no FP64 operation runs per term (with a double add per 8
   // terms the FP64 pipe bounded the kernel); complex128: everything in double
+  // the terms with their coefficients in the data precision, once per CTA
+  // (a double -> float conversion per amplitude and term ran on the FP64
+  // pipe and bounded the kernel at complex64)
+  __shared__ uint64_t s_x[kHamCache], s_z[kHamCache];
+  __shared__ R s_re[kHamCache], s_im[kHamCache];
+  const bool staged = nterms <= kHamCache;
+  if (staged)
+    for (int t = threadIdx.x; t < nterms; t += blockDim.x) {
+      const HamTermDev h = terms[t];
+      s_x[t] = h.x_mask;
+      s_z[t] = h.z_mask;
+      s_re[t] = (R)h.re;
+      s_im[t] = (R)h.im;
+    }
+  __syncthreads();
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
     SegSum<R> ar, ai;
+#pragma unroll 4
     for (int t = 0; t < nterms; ++t) {
-      const HamTermDev h = terms[t];
-      const T a = psi[i ^ h.x_mask];
-      R cr = (R)h.re, ci = (R)h.im;
-      if (__popcll(i & h.z_mask) & 1) { cr = -cr; ci = -ci; }
+      uint64_t xm, zm;
+      R cr, ci;
+      if (staged) {
+        xm = s_x[t];
+        zm = s_z[t];
+        cr = s_re[t];
+        ci = s_im[t];
+      } else {
+        const HamTermDev h = terms[t];
+        xm = h.x_mask;
+        zm = h.z_mask;
+        cr = (R)h.re;
+        ci = (R)h.im;
+      }
+      const T a = psi[i ^ xm];
+      if (__popcll(i & zm) & 1) { cr = -cr; ci = -ci; }
       ar.add(cr * a.x - ci * a.y);
       ai.add(cr * a.y + ci * a.x);
     }
