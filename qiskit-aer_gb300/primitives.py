@@ -211,15 +211,27 @@ class EstimatorV2:
         for lab in paulis:
             circ.save_expectation_value([(1.0, lab, list(range(n)))], label=lab)
         run_options = dict(self._options.run_options)
-        if params:
+        sim_meta = None
+        if params and self._fast_bound(circ, run_options):
+            # every binding on the bound stack, the expectation values straight
+            # into E (the same kernels as backend.run; no per-binding results)
             flat = values.reshape(-1, len(params))
-            binds = [{p: flat[:, i] for i, p in enumerate(params)}]
-            result = self._backend.run(circ, parameter_binds=binds, **run_options)
+            binds = self._backend._check_binds([circ], [{p: flat[:, i] for i, p in enumerate(params)}], True)[0]
+            nbind = flat.shape[0]
+            arrays, sim_meta = self._backend._run_bound(circ, binds, nbind, [0] * nbind, 0, arrays_only=True)
+            E = np.stack([arrays[lab] for lab in paulis], axis=1) if paulis else np.zeros((nbind, 0))
+            nexp = nbind
         else:
-            result = self._backend.run(circ, **run_options)
-        # E[binding, pauli] and the observables' coefficients C[observable, pauli]
-        nexp = len(result.results) if params else 1
-        E = np.array([[result.data(j)[lab] for lab in paulis] for j in range(nexp)]).reshape(nexp, len(paulis))
+            if params:
+                flat = values.reshape(-1, len(params))
+                binds = [{p: flat[:, i] for i, p in enumerate(params)}]
+                result = self._backend.run(circ, parameter_binds=binds, **run_options)
+            else:
+                result = self._backend.run(circ, **run_options)
+            # E[binding, pauli] and the observables' coefficients C[observable, pauli]
+            nexp = len(result.results) if params else 1
+            E = np.array([[result.data(j)[lab] for lab in paulis] for j in range(nexp)]).reshape(nexp, len(paulis))
+            sim_meta = result.metadata(0) if result.results else {}
         Cm = np.zeros((obs_flat.size, len(paulis)), dtype=complex)
         for i, d in enumerate(obs_flat):
             for lab, coeff in d.items():
@@ -232,7 +244,15 @@ class EstimatorV2:
             evs = rng.normal(evs, precision, evs.shape)
         return PubResult(DataBin(evs=evs, stds=stds, shape=evs.shape),
                          metadata={"target_precision": precision, "circuit_metadata": circuit.metadata,
-                                   "simulator_metadata": result.metadata(0) if result.results else {}})
+                                   "simulator_metadata": sim_meta})
+
+    def _fast_bound(self, circ: QuantumCircuit, run_options: dict) -> bool:
+        """The bound stack serves the pub directly when the backend is this
+        engine's simulator with its own options (no per-call overrides) and
+        the circuit runs bound (unitary body, saves at the end)."""
+        b = self._backend
+        return (not run_options and isinstance(b, AerSimulator) and hasattr(b, "_run_bound")
+                and b._bound_batchable(circ))
 
 
 # ---------------------------------------------------------------------------

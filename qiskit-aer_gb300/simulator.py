@@ -384,13 +384,17 @@ class AerSimulator:
     # largest stack of bound states held at once: 2^31 amplitudes (34 GB at complex128)
     MAX_STACK_QUBITS = 31
 
-    def _run_bound(self, circuit: QuantumCircuit, binds: dict, nbind: int, seeds, shots: int):
+    def _run_bound(self, circuit: QuantumCircuit, binds: dict, nbind: int, seeds, shots: int,
+                   arrays_only: bool = False):
         """Every binding of a parameterised circuit at once
         (BatchShotsExecutor over runtime-bound parameters,
         batch_shots_executor.hpp:152-314): the circuit is assembled once, its
         parameterised gates get per-binding values (gbqv_circuit_bind_param),
         and each chunk of bindings runs on one stack of states
-        (gbqv_execute_bound); expectation values are reduced per state."""
+        (gbqv_execute_bound); expectation values are reduced per state, every
+        saved observable's Paulis in one call.  arrays_only: only the
+        expectation values, as {label: value per binding} with the run's
+        metadata (the EstimatorV2 path, no per-binding result dicts)."""
         n = circuit.num_qubits
         body, meas, saves = circuit.split_final()
         mq = [q for m in meas for q in m.qubits]
@@ -398,7 +402,18 @@ class AerSimulator:
         counts = [None] * nbind
         nc = NativeCircuit(n, body)
         nc.bind(binds, nbind)
-        data = [{} for _ in range(nbind)]
+        data = [{} for _ in range(nbind)] if not arrays_only else None
+        arrays = {}
+        # the expectation-value saves: their Paulis in one list, and per save
+        # the coefficient of each
+        ev_saves = [ins for _, ins in saves if ins.name != "statevector"]
+        ev_terms, ev_coef = [], []
+        for ins in ev_saves:
+            label, terms = ins.data
+            params = expval_params(terms)
+            ev_coef.append((label, len(ev_terms), np.array([c1 for _, c1, _ in params])))
+            ev_terms.extend(ql for ql, _, _ in params)
+            arrays[label] = np.zeros(nbind)
         chunk = 1 << max(0, self.MAX_STACK_QUBITS - n)
         L = A.lib()
         st, st_bits = None, -1
@@ -424,19 +439,20 @@ class AerSimulator:
                         if self._want_memory:
                             data[first + j]["memory"] = self._memory(self._memory_values(sj, mq, mc))
                 for _, ins in saves:
-                    if ins.name == "statevector":
+                    if ins.name == "statevector" and not arrays_only:
                         vec = st.copy_to_vector()
                         for j in range(cnt):
                             data[first + j][ins.data] = vec[j << n:(j + 1) << n].copy()
-                        continue
-                    label, terms = ins.data
-                    params = expval_params(terms)
-                    vals = st.expval_pauli_segments(n, cnt, [ql for ql, _, _ in params])
-                    total = np.zeros(cnt)
-                    for (_, c1, _), v in zip(params, vals):  # in parameter order, per binding
-                        total += c1 * v
-                    for j in range(cnt):
-                        data[first + j][label] = float(total[j])
+                if ev_terms:
+                    vals = st.expval_pauli_segments(n, cnt, ev_terms)  # [term, binding]
+                    for label, off, coef in ev_coef:
+                        total = np.zeros(cnt)
+                        for c1, v in zip(coef, vals[off:off + coef.size]):  # in parameter order, per binding
+                            total += c1 * v
+                        arrays[label][first:first + cnt] = total
+                        if not arrays_only:
+                            for j in range(cnt):
+                                data[first + j][label] = float(total[j])
             if st is not None:
                 st.synchronize()
         finally:
@@ -444,6 +460,8 @@ class AerSimulator:
                 st.close()
         meta = {"fusion": {"enabled": False}, "parameter_binding": {"batched": True, "bindings": nbind,
                                                                    "stack_qubits": n + max(st_bits, 0)}}
+        if arrays_only:
+            return arrays, meta
         return [{"counts": counts[j], "data": data[j], "metadata": dict(meta), "seed_simulator": seeds[j],
                  "shots": shots} for j in range(nbind)]
 
