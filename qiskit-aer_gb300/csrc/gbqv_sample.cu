@@ -203,17 +203,18 @@ __device__ __forceinline__ bool parity(uint32_t m) { return __popc(m) & 1; }
 
 // One step's record for binade e (warp-wide; this lane holds terms 32u + lane
 // as words hi[u], lo[u]): M = the grid units with ties rounded down plus the
-// ties after the first, decided by prefix parities (gbqv_seqsum.h); has_tie
-// and fp = whether the step has a tie and the parity of the rounded-down
-// prefix up to and including the first one, which decides it against the
-// running sum's parity.
+// ties after the first that round up, decided by prefix parities from the
+// warp's tie and odd-unit masks (seq::tie_rounds); has_tie and fp = whether
+// the step has a tie and the parity of the rounded-down prefix up to and
+// including the first one, which decides it against the running sum's
+// parity.
 struct StepRecord {
   uint64_t M;
   bool bad, has_tie, fp;
 };
 
 __device__ __forceinline__ StepRecord step_record(const uint32_t (&hi)[kStep / 32], const uint32_t (&lo)[kStep / 32],
-                                                  int e, bool bad, int lane) {
+                                                  int e, bool bad) {
   uint64_t m[kStep / 32], sum = 0;
   uint32_t ties = 0;
 #pragma unroll
@@ -224,50 +225,19 @@ __device__ __forceinline__ StepRecord step_record(const uint32_t (&hi)[kStep / 3
     sum += m[u];
   }
   StepRecord r{0, __any_sync(kFull, bad) != 0, false, false};
-  if (__any_sync(kFull, ties != 0)) {  // warp-uniform
+  uint32_t extra = 0;
+  if (__any_sync(kFull, ties != 0)) {  // warp-uniform: the ties from the masks (seq::tie_rounds)
     uint32_t tm[kStep / 32], om[kStep / 32];
-    bool G[kStep / 32 + 1];  // parity of the odd units in the groups before u
-    G[0] = false;
 #pragma unroll
     for (int u = 0; u < kStep / 32; ++u) {
       tm[u] = __ballot_sync(kFull, (ties >> u) & 1);
       om[u] = __ballot_sync(kFull, m[u] & 1);
-      G[u + 1] = G[u] ^ parity(om[u]);
     }
-    // parity of the rounded-down prefix up to and including term (u, l)
-    auto dpar = [&](int u, int l) { return G[u] ^ parity(om[u] & ((2u << l) - 1)); };
-    r.has_tie = true;
-    bool found = false;
-#pragma unroll
-    for (int u = 0; u < kStep / 32; ++u)
-      if (!found && tm[u]) {
-        r.fp = dpar(u, __ffs(tm[u]) - 1);
-        found = true;
-      }
-#pragma unroll
-    for (int u = 0; u < kStep / 32; ++u) {
-      if (!((ties >> u) & 1)) continue;
-      // the tie before this one in term order: lower lane of this group, or
-      // the last tie of the nearest earlier group with one
-      bool prev = false, prev_par = false;
-      const uint32_t b = tm[u] & ((1u << lane) - 1);
-      if (b) {
-        prev = true;
-        prev_par = dpar(u, 31 - __clz(b));
-      } else {
-#pragma unroll
-        for (int v = u - 1; v >= 0; --v)
-          if (!prev && tm[v]) {
-            prev = true;
-            prev_par = dpar(v, 31 - __clz(tm[v]));
-          }
-      }
-      if (prev && dpar(u, lane) != prev_par) sum += 1;
-    }
+    extra = seq::tie_rounds(tm, om, r.has_tie, r.fp);
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-  r.M = sum;
+  r.M = sum + extra;
   return r;
 }
 
@@ -295,8 +265,8 @@ __global__ void __launch_bounds__(256) k_grid_units(const double *__restrict__ p
       nz |= ((hi[u] << 1) | lo[u]) != 0;
     }
     nz = __any_sync(kFull, nz);
-    const StepRecord r1 = step_record(hi, lo, seq::bexp(b1), !seq::grid_ok(b1), lane);
-    const StepRecord r2 = step_record(hi, lo, seq::bexp(b2), !seq::grid_ok(b2), lane);
+    const StepRecord r1 = step_record(hi, lo, seq::bexp(b1), !seq::grid_ok(b1));
+    const StepRecord r2 = step_record(hi, lo, seq::bexp(b2), !seq::grid_ok(b2));
     if (lane == 0) {
       auto meta = [&](const StepRecord &r, uint64_t b) {
         return (uint32_t)seq::bexp(b) | (r.bad ? 1u << 16 : 0u) | (nz ? 1u << 17 : 0u) | (r.has_tie ? 1u << 18 : 0u) |

@@ -191,6 +191,72 @@ __host__ __device__ __forceinline__ bool add_nonneg(uint64_t a, uint64_t b, uint
   return true;
 }
 
+// Tie bookkeeping of a step from bit masks, terms in groups of 32 (term
+// 32 u + l is bit l of group u): tm[u] marks the ties, om[u] the odd units
+// (ties rounded down).  Returns the number of ties after the first that
+// round up (each one whose rounded-down prefix parity differs from that of
+// the tie before it), has_tie, and fp = the prefix parity at the first tie.
+// Prefix parities by a prefix xor of om; the parity of the tie before each
+// position by a doubling fill (log2 32 steps) that copies each tie's parity
+// forward over the positions without a tie.
+__host__ __device__ __forceinline__ uint32_t prefix_xor32(uint32_t x) {
+  x ^= x << 1;
+  x ^= x << 2;
+  x ^= x << 4;
+  x ^= x << 8;
+  x ^= x << 16;
+  return x;
+}
+__host__ __device__ __forceinline__ uint32_t popc32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return (uint32_t)__popc(x);
+#else
+  return (uint32_t)__builtin_popcount(x);
+#endif
+}
+template <int G>
+__host__ __device__ __forceinline__ uint32_t tie_rounds(const uint32_t (&tm)[G], const uint32_t (&om)[G], bool &has_tie,
+                                                        bool &fp) {
+  uint32_t extra = 0, odd_before = 0, prev_par = 0;
+  bool have_prev = false;
+  has_tie = false;
+  fp = false;
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+  for (int u = 0; u < G; ++u) {
+    const uint32_t T = tm[u];
+    const uint32_t Px = prefix_xor32(om[u]) ^ (odd_before ? 0xffffffffu : 0u);  // parity at each position
+    if (T) {
+      uint32_t val = Px & T, hv = T;  // the last tie's parity at or below each position
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+      for (int sh = 1; sh < 32; sh <<= 1) {
+        val |= (val << sh) & ~hv;
+        hv |= hv << sh;
+      }
+      const uint32_t carry = have_prev ? 0xffffffffu : 0u;
+      const uint32_t hv_prev = (hv << 1) | carry;  // a tie strictly before the position
+      const uint32_t f_prev = (val << 1) | (~(hv << 1) & (prev_par ? carry : 0u));
+      extra += popc32(T & hv_prev & (Px ^ f_prev));
+#ifdef __CUDA_ARCH__
+      const int low = __ffs(T) - 1, high = 31 - __clz(T);
+#else
+      const int low = __builtin_ctz(T), high = 31 - __builtin_clz(T);
+#endif
+      if (!has_tie) {
+        fp = (Px >> low) & 1;
+        has_tie = true;
+      }
+      prev_par = (Px >> high) & 1;
+      have_prev = true;
+    }
+    odd_before ^= popc32(om[u]) & 1;
+  }
+  return extra;
+}
+
 // s += g * M when the result stays below 2^(e+1); false (s unchanged) if not
 __host__ __device__ __forceinline__ bool grid_add(uint64_t &sb, uint64_t M) {
   const uint64_t f = (sb & kFrac) + M;

@@ -70,6 +70,23 @@ static Record record_of(const double *x, int e) {
   return r;
 }
 
+// the same record from the kernel's masks (terms 32 u + l, seq::tie_rounds)
+static Record record_bits(const double *x, int e) {
+  Record r;
+  uint32_t tm[kStep / 32] = {0}, om[kStep / 32] = {0};
+  for (int p = 0; p < kStep; ++p) {
+    const uint64_t xb = bits(x[p]);
+    bool tie = false;
+    const uint64_t m = seq::grid_units_fast((uint32_t)(xb >> 32), (uint32_t)xb, e, r.bad, tie);
+    r.nz |= (xb << 1) != 0;
+    r.M += m;
+    tm[p / 32] |= (tie ? 1u : 0u) << (p % 32);
+    om[p / 32] |= (uint32_t)(m & 1) << (p % 32);
+  }
+  r.M += seq::tie_rounds(tm, om, r.has_tie, r.fp);
+  return r;
+}
+
 // the step's units for a running sum whose significand has parity `odd`
 static uint64_t step_units(const Record &r, bool odd) { return r.M + (r.has_tie && (odd != r.fp) ? 1 : 0); }
 
@@ -368,7 +385,13 @@ int main(int argc, char **argv) {
           want[st] = bits(ref);
         }
         std::vector<Record> rec(NS);
-        for (int st = 0; st < NS; ++st) rec[st] = record_of(&x[st * kStep], e_rec[st]);
+        for (int st = 0; st < NS; ++st) {
+          rec[st] = record_of(&x[st * kStep], e_rec[st]);
+          const Record rb = record_bits(&x[st * kStep], e_rec[st]);
+          if (rb.M != rec[st].M || rb.has_tie != rec[st].has_tie || (rb.has_tie && rb.fp != rec[st].fp) ||
+              rb.bad != rec[st].bad)
+            ++batch_mismatches;
+        }
         uint64_t sb = bits(s0), vals[32];
         for (int t0 = 0; t0 < NS; t0 += 32) {
           const int cnt = NS - t0 < 32 ? NS - t0 : 32;
