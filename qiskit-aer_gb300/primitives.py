@@ -236,8 +236,11 @@ class EstimatorV2:
         for i, d in enumerate(obs_flat):
             for lab, coeff in d.items():
                 Cm[i, col[lab]] += coeff
-        rows = E[bc_pos.reshape(-1) if params else np.zeros(bc_pos.size, dtype=np.int64)]
-        evs = np.real(np.sum(rows * Cm[bc_oid.reshape(-1)], axis=-1)).reshape(bc_pos.shape).astype(float)
+        # every (binding, observable) pair as one product, then the pub's
+        # broadcast positions gathered from it
+        F = np.real(E.astype(complex) @ Cm.T)  # [binding, observable]
+        pos = bc_pos.reshape(-1) if params else np.zeros(bc_pos.size, dtype=np.int64)
+        evs = F[pos, bc_oid.reshape(-1)].reshape(bc_pos.shape).astype(float)
         stds = np.full(bc_pos.shape, precision)
         if precision > 0:
             rng = np.random.default_rng(self._options.run_options.get("seed_simulator"))
