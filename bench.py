@@ -484,7 +484,8 @@ def bench_qv(args, torch, P):
         r = bench_dm(vd, torch, P)
         variants["dm14_c128"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "fused_ops",
                                                    "expval_50_terms_ms", "config")}
-        # the other BASELINE configs, so that every headline number has a record in this line
+        # the other workloads (sampling, parameter binding, batched instances),
+        # so that every headline number has a record in this line
         vs = argparse.Namespace(**{**vars(args), "no_checks": True})
         r = bench_sample(vs, torch, P)
         variants["sample_30q_c128"] = {k: r[k] for k in ("value", "unit", "sample_100k_ms", "probabilities_all_ms",
