@@ -23,11 +23,12 @@
 //   2. prefix sums of those predict every chain's running sum at each step;
 //   3. one parallel pass computes, per step and for both chains, the integer
 //      sum of the step's terms on the ulp grid of the predicted running sum
-//      (gbqv_seqsum.h: exact while the sum keeps its binade and no term
-//      rounds on a tie);
-//   4. each chain (one warp) then advances step by step, adding the step's
-//      grid units where its binade was predicted right and the step is
-//      clean, and adding term by term otherwise.
+//      (gbqv_seqsum.h: exact while the sum keeps its binade; a term that
+//      rounds on a tie is decided by prefix parities, the first one of a
+//      step by the running sum's parity when the chain reaches it);
+//   4. each chain (one warp) then advances 32 steps per warp scan, adding
+//      the steps' grid units where their binade was predicted right and the
+//      sum stays in it, and adding term by term otherwise.
 // When the probability buffer cannot be allocated, or the blocks are short,
 // one thread per chain adds term by term from the state itself.
 #include <algorithm>
