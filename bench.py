@@ -31,7 +31,8 @@ same circuit under ``variants``.
            26-qubit, 624-parameter ansatz (complex128 and complex64) against
            parameter shift on the same GPU; the 14-qubit noisy density matrix;
            100,000 shots on the 30-qubit state; the EstimatorV2 job and the
-           2,048-instance batch (complex64), each as its own workload below
+           2,048-instance batch (complex64 and complex128), each as its own
+           workload below
 
 Other workloads (--workload): ``adjoint`` (26-qubit hardware-efficient
 ansatz, 624 parameters, 200 Pauli terms: adjoint gradient vs parameter
@@ -500,6 +501,15 @@ def bench_qv(args, torch, P):
         r = bench_batch(vb, torch, P)
         variants["batch_c64"] = {k: r[k] for k in ("value", "unit", "launch_ms", "latency_ms_p50", "latency_ms_p99",
                                                    "speedup_vs_per_launch", "config")}
+        # the same two at complex128 (float-pair arithmetic on the FP32 pipe)
+        ve2 = argparse.Namespace(**{**vars(ve), "precision": "double", "steps": 1, "warmup": 2})
+        r = bench_estimator(ve2, torch, P)
+        variants["estimator_c128"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "execute_bound_ms",
+                                                        "expval_50_terms_ms", "e2e", "config")}
+        vb2 = argparse.Namespace(**{**vars(vb), "precision": "double", "steps": 1})
+        r = bench_batch(vb2, torch, P)
+        variants["batch_c128"] = {k: r[k] for k in ("value", "unit", "launch_ms", "latency_ms_p50", "latency_ms_p99",
+                                                    "speedup_vs_per_launch", "config")}
     return {"metric": "fused-gate GB/s", "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
