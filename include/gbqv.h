@@ -407,6 +407,23 @@ int gbqv_collapse_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const
 int gbqv_apply_matrix_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
                                const gbqv_c128 *mat, const uint8_t *mask);
 
+/* Sampled Kraus noise on a stack of shots (the statevector method's Kraus
+ * noise, State::apply_kraus, src/simulators/statevector/
+ * statevector_state.hpp:1112-1156, one shot per state).
+ *
+ * rdm_segments: out[(s D + a) D + b] = rho_s[a][b] = sum over the other
+ *   qubits of x_a conj(x_b) in state s (D = 2^k, k <= 3, bit j of a on
+ *   qubits[j]): the caller gets every operator's probability
+ *   ||K psi_s||^2 = tr(K^dag K rho_s), the QubitVector::norm(qubits, mat)
+ *   of apply_kraus (qubitvector.hpp:1878-2082), from one pass.
+ * kraus_segments: state s gets mats[branch[s]] (m <= 255 column-major
+ *   matrices) with every entry times scale[s] (1/sqrt(p), as apply_kraus
+ *   scales the chosen matrix); branch[s] = 255 leaves state s untouched. */
+int gbqv_rdm_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                      gbqv_c128 *out);
+int gbqv_kraus_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                        const gbqv_c128 *mats, int m, const uint8_t *branch, const double *scale);
+
 /* Adjoint-method gradient of E(theta) = <psi(theta)|H|psi(theta)>, psi =
  * c applied to |0...0>.  No counterpart in the reference (Aer has no gradient
  * code); it extends the statevector surface for the torch.autograd wrapper.

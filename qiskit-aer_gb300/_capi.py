@@ -132,6 +132,8 @@ _SIGS = {
     "gbqv_draw_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, dp, vp, dp]),
     "gbqv_collapse_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, vp, vp, dp]),
     "gbqv_apply_matrix_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, vp, vp]),
+    "gbqv_rdm_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, vp]),
+    "gbqv_kraus_segments": (C.c_int, [H, C.c_int, C.c_uint64, u64p, C.c_int, vp, C.c_int, vp, dp]),
     "gbqv_set_blocking": (C.c_int, [H, C.c_int]),
     "gbqv_set_tensor_c128": (C.c_int, [H, C.c_int]),
     "gbqv_batch_create": (C.c_int, [C.c_int, C.POINTER(H)]),

@@ -904,6 +904,51 @@ extern "C" int gbqv_apply_matrix_segments(gbqv_handle h, int state_qubits, uint6
   });
 }
 
+extern "C" int gbqv_rdm_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                                 gbqv_c128 *out) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    check_stack(d, state_qubits, nseg, "rdm_segments");
+    reg_t q = check_qubits(qubits, k, state_qubits, "rdm_segments");
+    REQUIRE(k <= seg_max_kraus_qubits() && out, GBQV_ERR_ARG, "rdm_segments: 1..3 qubits, an output");
+    reduce_rdm_segments(d, q, state_qubits, nseg);
+    const size_t D = 1ULL << k, E = D * D;
+    std::vector<double> v(nseg * E);
+    read_results(d, v.data(), v.size());
+    // the packed values (diagonal; real part above, imaginary part below it)
+    // to full Hermitian matrices
+    for (uint64_t s = 0; s < nseg; ++s) {
+      const double *e = v.data() + s * E;
+      gbqv_c128 *r = out + s * E;
+      for (size_t a = 0; a < D; ++a) {
+        r[a * D + a] = gbqv_c128{e[a * D + a], 0.0};
+        for (size_t b = a + 1; b < D; ++b) {
+          r[a * D + b] = gbqv_c128{e[a * D + b], e[b * D + a]};
+          r[b * D + a] = gbqv_c128{e[a * D + b], -e[b * D + a]};
+        }
+      }
+    }
+  });
+}
+
+extern "C" int gbqv_kraus_segments(gbqv_handle h, int state_qubits, uint64_t nseg, const uint64_t *qubits, int k,
+                                   const gbqv_c128 *mats, int m, const uint8_t *branch, const double *scale) {
+  return guard(h, [&] {
+    need_handle(h);
+    Device &d = h->dev;
+    check_stack(d, state_qubits, nseg, "kraus_segments");
+    reg_t q = check_qubits(qubits, k, state_qubits, "kraus_segments");
+    REQUIRE(k <= seg_max_kraus_qubits() && mats && branch && scale, GBQV_ERR_ARG,
+            "kraus_segments: 1..3 qubits, matrices and two per-state arrays");
+    REQUIRE(m >= 1 && m <= 255, GBQV_ERR_ARG, "kraus_segments: 1..255 operators");
+    for (uint64_t s = 0; s < nseg; ++s)
+      REQUIRE(branch[s] == 0xff || branch[s] < m, GBQV_ERR_ARG,
+              "kraus_segments: operator of state " + std::to_string(s) + " out of range");
+    launch_kraus_segments(d, q, state_qubits, nseg, reinterpret_cast<const cd *>(mats), m, branch, scale);
+  });
+}
+
 // ============================== density matrix ==============================
 
 namespace gbqv {

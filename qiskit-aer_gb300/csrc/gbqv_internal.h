@@ -253,5 +253,11 @@ void launch_matrix_segments(Device &dev, const reg_t &qubits, int state_bits, ui
                             const uint8_t *mask);
 void draw_segments(Device &dev, const reg_t &qubits, int state_bits, uint64_t nseg, const double *u,
                    uint32_t *outcome, double *prob);
+// sampled Kraus noise: per-state reduced density matrices of k <= 3 qubits
+// (nseg 4^k values in dev.results) and the chosen operator per state
+int seg_max_kraus_qubits();
+void reduce_rdm_segments(Device &dev, const reg_t &qubits, int state_bits, uint64_t nseg);
+void launch_kraus_segments(Device &dev, const reg_t &qubits, int state_bits, uint64_t nseg, const cd *mats, int m,
+                           const uint8_t *branch, const double *scale);
 
 }  // namespace gbqv

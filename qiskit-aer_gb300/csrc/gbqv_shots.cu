@@ -294,6 +294,94 @@ __global__ void __launch_bounds__(256) k_matrix_seg(T *__restrict__ psi, int sb,
   }
 }
 
+// Reduced density matrix of K qubits per state, rho[a][b] = sum over the
+// other qubits of x_a conj(x_b): every Kraus operator's probability
+// ||K psi||^2 = tr(K^dag K rho) then follows on the host from one pass over
+// the stack, where State::apply_kraus (statevector_state.hpp:1112-1156)
+// takes one QubitVector::norm(qubits, mat) pass (qubitvector.hpp:1878-2082)
+// per operator.  Value e of a state: e = a D + a holds rho[a][a]; for a < b,
+// e = a D + b the real and e = b D + a the imaginary part of rho[a][b].
+// Grid and partials as k_probs_seg, D^2 values per state.
+template <typename T, int K>
+__global__ void __launch_bounds__(256) k_rdm_seg(const T *__restrict__ psi, int sb, int bps, uint64_t seg0, SegQ q,
+                                                 double *__restrict__ partials) {
+  constexpr int D = 1 << K, E = D * D;
+  const uint64_t seg = seg0 + blockIdx.y;
+  const T *ps = psi + (seg << sb);
+  const uint64_t ngroups = 1ULL << (sb - K);
+  double acc[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) acc[e] = 0.0;
+  const uint64_t stride = (uint64_t)bps * blockDim.x;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += stride) {
+    const uint64_t base = spread_zeros<K>(g, q.lowmask);
+    double xr[D], xi[D];
+#pragma unroll
+    for (int v = 0; v < D; ++v) {
+      const T a = ps[base + q.offs[v]];
+      xr[v] = (double)a.x;
+      xi[v] = (double)a.y;
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      acc[a * D + a] += xr[a] * xr[a] + xi[a] * xi[a];
+#pragma unroll
+      for (int b = a + 1; b < D; ++b) {
+        acc[a * D + b] += xr[a] * xr[b] + xi[a] * xi[b];
+        acc[b * D + a] += xi[a] * xr[b] - xr[a] * xi[b];
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const double s = seg_block_sum(acc[e]);
+    if (threadIdx.x == 0) partials[(seg * E + e) * bps + blockIdx.x] = s;
+  }
+}
+
+// The Kraus operator State::apply_kraus chose for each state, normalised:
+// mats[branch[s]] (column-major) with every entry times scale[s] (the
+// reference scales the matrix by 1/sqrt(p) before applying it), on state s;
+// branch 0xff leaves the state untouched.
+template <typename T, int K>
+__global__ void __launch_bounds__(256) k_kraus_seg(T *__restrict__ psi, int sb, uint64_t total, SegQ q,
+                                                   const double2 *__restrict__ mats,
+                                                   const uint8_t *__restrict__ branch,
+                                                   const double *__restrict__ scale) {
+  using R = decltype(T::x);
+  constexpr int D = 1 << K;
+  const int gb = sb - K;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t G = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; G < total; G += stride) {
+    const uint64_t seg = G >> gb;
+    const int br = branch[seg];
+    if (br == 0xff) continue;
+    const double2 *m = mats + (size_t)br * D * D;
+    const double sc = scale[seg];
+    T *ps = psi + (seg << sb);
+    const uint64_t base = spread_zeros<K>(G & ((1ULL << gb) - 1), q.lowmask);
+    T x[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) x[c] = ps[base + q.offs[c]];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      T y;
+      y.x = 0;
+      y.y = 0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const double2 md = __ldg(m + r + D * c);
+        const R wx = (R)(md.x * sc), wy = (R)(md.y * sc);
+        y.x = fma(wx, x[c].x, y.x);
+        y.x = fma(-wy, x[c].y, y.x);
+        y.y = fma(wx, x[c].y, y.y);
+        y.y = fma(wy, x[c].x, y.y);
+      }
+      ps[base + q.offs[r]] = y;
+    }
+  }
+}
+
 SegQ make_segq(const reg_t &qubits) {
   SegQ q{};
   local_offsets(qubits, q.offs);
@@ -350,10 +438,83 @@ void matrix_any(Device &d, int sb, uint64_t nseg, const SegQ &q, int k, const do
   }
 }
 
+template <typename T, int K>
+void rdm_k(Device &d, int sb, uint64_t nseg, const SegQ &q, int bps) {
+  for (uint64_t s0 = 0; s0 < nseg; s0 += 65535) {
+    dim3 grid((unsigned)bps, (unsigned)std::min<uint64_t>(65535, nseg - s0));
+    k_rdm_seg<T, K><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, bps, s0, q, d.partials);
+  }
+}
+
+template <typename T>
+void rdm_any(Device &d, int sb, uint64_t nseg, const SegQ &q, int k, int bps) {
+  switch (k) {
+    case 1: rdm_k<T, 1>(d, sb, nseg, q, bps); break;
+    case 2: rdm_k<T, 2>(d, sb, nseg, q, bps); break;
+    default: rdm_k<T, 3>(d, sb, nseg, q, bps); break;
+  }
+}
+
+template <typename T>
+void kraus_any(Device &d, int sb, uint64_t nseg, const SegQ &q, int k, const double2 *mats, const uint8_t *branch,
+               const double *scale) {
+  const uint64_t total = nseg << (sb - k);
+  const int grid = grid_of(total);
+  switch (k) {
+    case 1: k_kraus_seg<T, 1><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, mats, branch, scale); break;
+    case 2: k_kraus_seg<T, 2><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, mats, branch, scale); break;
+    default: k_kraus_seg<T, 3><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, mats, branch, scale); break;
+  }
+}
+
 }  // namespace
 
 int seg_max_measure_qubits() { return 30; }
 int seg_max_matrix_qubits() { return kMaxSegMatK; }
+int seg_max_kraus_qubits() { return 3; }
+
+void reduce_rdm_segments(Device &d, const reg_t &qubits, int sb, uint64_t nseg) {
+  const int k = (int)qubits.size();
+  if (k < 1 || k > seg_max_kraus_qubits() || k > sb) throw Error(1, "segment density matrices: 1..3 qubits");
+  const uint64_t nvalues = nseg << (2 * k);
+  const SegQ q = make_segq(qubits);
+  // slices per state as for the probabilities: ~8 CTAs per SM, >= 2 groups per thread
+  const uint64_t want = std::max<uint64_t>(1, (uint64_t)sm_count() * 8 / nseg);
+  const uint64_t cap = std::max<uint64_t>(1, (1ULL << (sb - k)) / 512);
+  const int bps = (int)std::min<uint64_t>(std::min(want, cap), 256);
+  grow(reinterpret_cast<void *&>(d.partials), d.partials_cap, sizeof(double) * nvalues * bps);
+  grow(reinterpret_cast<void *&>(d.results), d.results_cap, sizeof(double) * nvalues);
+  if (d.dbl)
+    rdm_any<double2>(d, sb, nseg, q, k, bps);
+  else
+    rdm_any<float2>(d, sb, nseg, q, k, bps);
+  check_launch("segment density matrix kernel");
+  k_sum_slices<<<(unsigned)((nvalues + 255) / 256), 256, 0, d.stream>>>(d.partials, bps, nvalues, d.results);
+  check_launch("segment density matrix sum");
+}
+
+void launch_kraus_segments(Device &d, const reg_t &qubits, int sb, uint64_t nseg, const cd *mats, int m,
+                           const uint8_t *branch, const double *scale) {
+  const int k = (int)qubits.size();
+  if (k < 1 || k > seg_max_kraus_qubits() || k > sb) throw Error(1, "segment Kraus operators: 1..3 qubits");
+  // matrices (16-byte entries), then the per-state scales and branches
+  const size_t D = 1ULL << k, mbytes = (size_t)m * D * D * 16;
+  grow(d.aux2, d.aux2_cap, mbytes + nseg * 9);
+  char *base = reinterpret_cast<char *>(d.aux2);
+  cuda_check(cudaMemcpyAsync(base, mats, mbytes, cudaMemcpyHostToDevice, d.stream), "Kraus upload");
+  cuda_check(cudaMemcpyAsync(base + mbytes, scale, nseg * 8, cudaMemcpyHostToDevice, d.stream), "Kraus upload");
+  cuda_check(cudaMemcpyAsync(base + mbytes + nseg * 8, branch, nseg, cudaMemcpyHostToDevice, d.stream),
+             "Kraus upload");
+  const SegQ q = make_segq(qubits);
+  const double2 *dm = reinterpret_cast<const double2 *>(base);
+  const double *ds = reinterpret_cast<const double *>(base + mbytes);
+  const uint8_t *db = reinterpret_cast<const uint8_t *>(base + mbytes + nseg * 8);
+  if (d.dbl)
+    kraus_any<double2>(d, sb, nseg, q, k, dm, db, ds);
+  else
+    kraus_any<float2>(d, sb, nseg, q, k, dm, db, ds);
+  check_launch("segment Kraus kernel");
+}
 
 void reduce_probabilities_segments(Device &d, const reg_t &qubits, int sb, uint64_t nseg) {
   const int k = (int)qubits.size();

@@ -86,6 +86,55 @@ class QuantumError:
     def to_instruction_args(self):
         return self.superop
 
+    def kraus(self) -> list:
+        """The channel's canonical Kraus operators (QuantumError::kraus,
+        src/noise/quantum_error.hpp:405-430), computed once."""
+        if getattr(self, "_kraus", None) is None:
+            self._kraus = superop_kraus(self.superop, self.num_qubits)
+        return self._kraus
+
+
+def superop_kraus(superop: np.ndarray, num_qubits: int, threshold: float = 1e-10) -> list:
+    """Canonical Kraus operators of a superoperator (Utils::superop2kraus,
+    src/framework/noise_utils.hpp:33-87): the Choi matrix
+    C = sum vec(K) vec(K)^dag (vec column-major) rearranged from S =
+    sum conj(K) (x) K, its eigenvectors largest eigenvalue first, and
+    K = sqrt(lambda) unvec(v) for every eigenvalue above the threshold."""
+    d = 1 << num_qubits
+    s4 = np.asarray(superop, dtype=complex).reshape(d, d, d, d)  # [c', r, c'', r'']: conj(K)[c', c''] K[r, r'']
+    choi = np.einsum("ebca->abce", s4).reshape(d * d, d * d)
+    choi = 0.5 * (choi + choi.conj().T)
+    w, v = np.linalg.eigh(choi)
+    keep = [idx for idx in range(d * d - 1, -1, -1) if w[idx] > threshold]
+    # Within an eigenspace of equal eigenvalues any orthonormal basis gives
+    # canonical operators (the eigensolver returns one of them); where Pauli
+    # matrices span the eigenspace they are taken, so that a Pauli channel's
+    # operators are its Paulis, each a multiple of a unitary.
+    pv = _pauli_vectors(num_qubits)
+    start = 0
+    while start < len(keep):
+        end = start + 1
+        while end < len(keep) and w[keep[start]] - w[keep[end]] <= 1e-12:
+            end += 1
+        if end - start > 1:
+            cols = keep[start:end]
+            weight = np.sum(np.abs(v[:, cols].conj().T @ pv) ** 2, axis=0)
+            sel = np.nonzero(weight > 1 - 1e-9)[0]
+            if sel.size == len(cols):
+                v[:, cols] = pv[:, sel]
+        start = end
+    return [np.sqrt(w[idx]) * v[:, idx].reshape((d, d), order="F") for idx in keep]
+
+
+def _pauli_vectors(num_qubits: int) -> np.ndarray:
+    """Columns: vec (column-major) of every num_qubits-qubit Pauli matrix
+    divided by sqrt(2^num_qubits), orthonormal."""
+    one = [np.eye(2), np.array([[0, 1], [1, 0]]), np.array([[0, -1j], [1j, 0]]), np.diag([1.0, -1.0])]
+    mats = [np.eye(1, dtype=complex)]
+    for _ in range(num_qubits):
+        mats = [np.kron(p, m) for p in one for m in mats]
+    return np.stack([m.reshape(-1, order="F") for m in mats], axis=1) / np.sqrt(1 << num_qubits)
+
 
 def _check_probs(probs) -> None:
     probs = [float(p) for p in probs]

@@ -75,6 +75,52 @@ def uniforms(seed: int, count: int) -> np.ndarray:
     return out
 
 
+def kraus_draws(probs: np.ndarray, u: np.ndarray):
+    """State::apply_kraus's choice for each row (statevector_state.hpp:
+    1112-1156): probs[s, j] = ||K_j psi_s||^2; with r = u[s], the first
+    operator j < m - 1 whose sequential sum of probabilities exceeds r is
+    applied scaled by 1/sqrt(p_j); if none, the last, scaled by
+    1/sqrt(1 - that sum).  Returns (operator index, scale) per row."""
+    p = np.asarray(probs, dtype=np.float64)
+    rows, m = p.shape
+    branch = np.full(rows, m - 1, dtype=np.int64)
+    scale = np.ones(rows, dtype=np.float64)
+    if m > 1 and rows:
+        acc = np.add.accumulate(p[:, :m - 1], axis=1)
+        hit = acc > np.asarray(u, dtype=np.float64)[:, None]
+        got = hit.any(axis=1)
+        first = np.argmax(hit, axis=1)
+        branch[got] = first[got]
+        scale[got] = 1.0 / np.sqrt(p[got, first[got]])
+        scale[~got] = 1.0 / np.sqrt(1.0 - acc[~got, -1])
+    return branch, scale
+
+
+class KrausOp:
+    """A Kraus channel sampled once per shot on a statevector
+    (State::apply_kraus): the operators as given (a circuit's kraus
+    instruction) or a noise model error's canonical ones
+    (Utils::superop2kraus).  `gram` holds K^dag K, from which each shot's
+    probabilities follow from its reduced density matrix; `fixed` the
+    probabilities when every K^dag K is a multiple of the identity (a
+    mixture of unitaries), which then need no pass over the states."""
+
+    def __init__(self, qubits, mats):
+        self.qubits = [int(q) for q in qubits]
+        D = 1 << len(self.qubits)
+        self.mats = np.stack([np.asarray(m, dtype=np.complex128) for m in mats])
+        if self.mats.shape[1:] != (D, D):
+            raise ValueError(f"Kraus operators on {len(self.qubits)} qubits must be {D}x{D}")
+        if not 1 <= len(mats) <= 255:
+            raise ValueError("a Kraus channel takes 1..255 operators")
+        self.gram = np.einsum("jba,jbc->jac", self.mats.conj(), self.mats)
+        # column-major matrices, one after another
+        self.colmajor = np.ascontiguousarray(self.mats.transpose(0, 2, 1)).reshape(-1)
+        c = np.einsum("jaa->j", self.gram).real / D
+        flat = np.max(np.abs(self.gram - c[:, None, None] * np.eye(D)))
+        self.fixed = c if flat <= 1e-13 else None
+
+
 class Result:
     def __init__(self, results, time_taken):
         self.results = results
@@ -235,7 +281,10 @@ class AerSimulator:
         if self.noise_model is None or not self.noise_model.has_quantum_errors():
             return (body, list(positions)) if positions is not None else body
         if self.method != "density_matrix":
-            raise ValueError("noise is supported with method='density_matrix' (superoperator noise)")
+            if any(self._error_kraus(ins) for ins in body):
+                raise ValueError("noise on a statevector is sampled per shot as Kraus channels, in circuits run "
+                                 "shot by shot; use method='density_matrix' for superoperator noise")
+            return (body, list(positions)) if positions is not None else body
         out, new_index = [], []
         for ins in body:
             new_index.append(len(out))
@@ -465,8 +514,40 @@ class AerSimulator:
         return [{"counts": counts[j], "data": data[j], "metadata": dict(meta), "seed_simulator": seeds[j],
                  "shots": shots} for j in range(nbind)]
 
+    def _sampled_noise(self, circuit: QuantumCircuit) -> bool:
+        """A statevector run whose noise model puts an error on some
+        instruction of the circuit: every such error becomes a Kraus channel
+        sampled per shot (the reference's Kraus noise method,
+        circuit_executor.hpp:648-657), so the circuit runs shot by shot."""
+        if self.method != "statevector" or self.noise_model is None or not self.noise_model.has_quantum_errors():
+            return False
+        return any(self._error_kraus(ins) for ins in circuit.data)
+
+    def _error_kraus(self, ins, before: bool | None = None) -> list:
+        """The noise model's errors on one instruction as KrausOps: after a
+        gate or reset, before a measure (noise_model.hpp:1075-1085)."""
+        if self.noise_model is None or not self.noise_model.has_quantum_errors():
+            return []
+        if ins.kind == "measure":
+            name = "measure"
+        elif ins.kind == "reset":
+            name = "reset"
+        elif ins.kind == "gate":
+            name = ins.name
+        else:
+            return []
+        if before is not None and before != (name == "measure"):
+            return []
+        out = []
+        for q, err in self.noise_model.op_errors(name, ins.qubits):
+            if err.num_qubits != len(q):
+                raise ValueError(f"error on '{name}' acts on {err.num_qubits} qubits, the instruction on {len(q)}")
+            if not err.ideal():
+                out.append(KrausOp(q, err.kraus()))
+        return out
+
     def _run_one(self, circuit: QuantumCircuit, shots: int, seed: int):
-        if self.method == "statevector" and circuit.needs_shots("statevector"):
+        if self.method == "statevector" and (circuit.needs_shots("statevector") or self._sampled_noise(circuit)):
             return self._run_shots(circuit, shots, seed)
         if self.method == "density_matrix" and circuit.needs_shots("density_matrix"):
             return self._run_shots_dm(circuit, shots, seed)
@@ -532,10 +613,9 @@ class AerSimulator:
         qubitvector_thrust.hpp:2251-2448): each stretch runs once over the
         whole group, each measurement is one probability pass, a host draw
         per shot from its own stream and one collapse pass."""
-        if self.noise_model is not None and self.noise_model.has_quantum_errors():
-            raise NotImplementedError("noise on a statevector needs per-shot noise sampling; use density_matrix")
         cfg = self.fusion_config()
         items, stretch = [], []
+        noisy = self._sampled_noise(circuit)
 
         def flush():
             if stretch:
@@ -547,19 +627,34 @@ class AerSimulator:
         for ins in circuit.data:
             if ins.kind in ("save", "set"):
                 raise NotImplementedError(f"{ins.kind} instructions in a circuit run shot by shot")
+            if ins.kind == "superop":
+                raise ValueError("superop instructions need method='density_matrix'")
+            # noise ops inherit the instruction's condition (noise_model.hpp:422-431)
+            errs = self._error_kraus(ins) if noisy else []
             if ins.kind == "kraus":
-                raise NotImplementedError("Kraus channels on a statevector need per-shot noise sampling")
-            if ins.kind in ("measure", "reset"):
                 flush()
+                items.append(("kraus", KrausOp(ins.qubits, ins.data), ins.condition))
+            elif ins.kind in ("measure", "reset"):
+                flush()
+                if ins.kind == "measure":
+                    items.extend(("kraus", e, ins.condition) for e in errs)
                 items.append((ins.kind, ins, ins.condition))
+                if ins.kind == "reset":
+                    items.extend(("kraus", e, ins.condition) for e in errs)
             elif ins.condition is not None:
                 flush()
                 cond = Instruction(ins.kind, ins.name, ins.qubits, ins.params, ins.data, ins.clbits)
                 items.append(("ops", NativeCircuit(circuit.num_qubits, [cond]), ins.condition))
+                items.extend(("kraus", e, ins.condition) for e in errs)
             elif ins.kind != "barrier":
                 stretch.append(ins)
+                if errs:
+                    flush()
+                    items.extend(("kraus", e, None) for e in errs)
         flush()
         meta = {"fusion": {"enabled": bool(cfg.enable)}, "shot_branching": False, "measure_sampling": False}
+        if noisy:
+            meta["noise"] = "kraus"
         matrices = self._conditioned_matrices(items)
         if matrices is not None and circuit.num_clbits <= 63:
             memory = self._shots_batched(circuit.num_qubits, items, matrices, shots, seed)
@@ -584,7 +679,7 @@ class AerSimulator:
         path (a conditioned op on more than 4 qubits)."""
         out = {}
         for idx, (kind, obj, cond) in enumerate(items):
-            if kind in ("measure", "reset"):
+            if kind in ("measure", "reset", "kraus"):
                 continue
             if cond is None:
                 continue
@@ -608,15 +703,17 @@ class AerSimulator:
                           22 - k_host, 27 - k_dev))
 
     def _draws_per_shot(self, items) -> int:
-        """Uniforms one shot consumes at most: one per measure / reset, one
-        per readout error after a measurement."""
+        """Uniforms one shot consumes at most: one per measure / reset /
+        Kraus channel, one per readout error after a measurement."""
         return sum(1 + (len(self._readout_ops([obj])) if kind == "measure" else 0)
-                   for kind, obj, _ in items if kind in ("measure", "reset"))
+                   for kind, obj, _ in items if kind in ("measure", "reset", "kraus"))
 
     def _shots_batched(self, n, items, matrices, shots, seed):
         L = A.lib()
         ndraw = self._draws_per_shot(items)
-        ks = [len(obj.qubits) for kind, obj, _ in items if kind in ("measure", "reset")]
+        # a Kraus channel's 4^k complex values per state count as 2k + 1 qubits of probabilities
+        ks = [len(obj.qubits) if kind != "kraus" else 2 * len(obj.qubits) + 1
+              for kind, obj, _ in items if kind in ("measure", "reset", "kraus")]
         b = self._shot_group_bits(n, shots, ks)
         group = 1 << b
         out = np.zeros(shots, dtype=np.uint64)
@@ -654,6 +751,10 @@ class AerSimulator:
                     k = len(qubits)
                     qarr = (C.c_uint64 * k)(*qubits)
                     rows = np.nonzero(active)[0]
+                    if kind == "kraus":
+                        self._kraus_apply(st, n, cnt, obj, rows, u[rows, used[rows]])
+                        used[rows] += 1
+                        continue
                     if k <= self.HOST_DRAW_QUBITS:
                         probs = np.empty((cnt, 1 << k), dtype=np.float64)
                         A.check(L.gbqv_probabilities_segments(h, n, cnt, qarr, k, probs.ctypes.data_as(A.dp)), h)
@@ -697,6 +798,31 @@ class AerSimulator:
             st.synchronize()
         return out
 
+    @staticmethod
+    def _kraus_apply(st, n, cnt, op: KrausOp, rows, u) -> None:
+        """State::apply_kraus on the states `rows` of a stack of cnt states
+        of n qubits, each with its uniform u: the operators' probabilities
+        from each state's reduced density matrix (one pass; none for a
+        mixture of unitaries), the choice per state, then one pass applying
+        each state's normalised operator."""
+        L, h = A.lib(), st.handle
+        k, m = len(op.qubits), op.mats.shape[0]
+        qarr = (C.c_uint64 * k)(*op.qubits)
+        if op.fixed is not None:
+            probs = np.broadcast_to(op.fixed, (rows.size, m))
+        else:
+            D = 1 << k
+            rho = np.empty((cnt, D, D), dtype=np.complex128)
+            A.check(L.gbqv_rdm_segments(h, n, cnt, qarr, k, rho.ctypes.data_as(A.vp)), h)
+            probs = np.einsum("jab,sba->sj", op.gram, rho[rows]).real
+        chosen, sc = kraus_draws(probs, u)
+        branch = np.full(cnt, 255, dtype=np.uint8)
+        branch[rows] = chosen
+        scale = np.zeros(cnt, dtype=np.float64)
+        scale[rows] = sc
+        A.check(L.gbqv_kraus_segments(h, n, cnt, qarr, k, op.colmajor.ctypes.data_as(A.vp), m,
+                                      branch.ctypes.data_as(A.vp), scale.ctypes.data_as(A.dp)), h)
+
     def _shots_serial(self, n, items, shots, seed):
         """One state, one shot at a time (classical memory wider than 63
         bits, or a conditioned op beyond the stacked kernels)."""
@@ -714,6 +840,10 @@ class AerSimulator:
                             continue
                     if kind == "ops":
                         A.check(st._L.gbqv_execute(st.handle, obj.handle), st.handle)
+                        continue
+                    if kind == "kraus":
+                        self._kraus_apply(st, n, 1, obj, np.zeros(1, dtype=np.int64), u[used:used + 1])
+                        used += 1
                         continue
                     qubits = obj.qubits
                     probs = st.probabilities(qubits)
