@@ -339,26 +339,22 @@ __global__ void __launch_bounds__(256) k_rdm_seg(const T *__restrict__ psi, int 
   }
 }
 
-// The Kraus operator State::apply_kraus chose for each state, normalised:
-// mats[branch[s]] (column-major) with every entry times scale[s] (the
-// reference scales the matrix by 1/sqrt(p) before applying it), on state s;
-// branch 0xff leaves the state untouched.
+// The Kraus operator State::apply_kraus chose for each selected state,
+// normalised: state sel[i] gets the column-major matrix smats[i] (the chosen
+// operator with every entry already times 1/sqrt(p), as the reference
+// scales it before applying it), in the state's precision.  Only the
+// selected states are visited.
 template <typename T, int K>
 __global__ void __launch_bounds__(256) k_kraus_seg(T *__restrict__ psi, int sb, uint64_t total, SegQ q,
-                                                   const double2 *__restrict__ mats,
-                                                   const uint8_t *__restrict__ branch,
-                                                   const double *__restrict__ scale) {
-  using R = decltype(T::x);
+                                                   const T *__restrict__ smats,
+                                                   const uint32_t *__restrict__ sel) {
   constexpr int D = 1 << K;
   const int gb = sb - K;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t G = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; G < total; G += stride) {
-    const uint64_t seg = G >> gb;
-    const int br = branch[seg];
-    if (br == 0xff) continue;
-    const double2 *m = mats + (size_t)br * D * D;
-    const double sc = scale[seg];
-    T *ps = psi + (seg << sb);
+    const uint64_t i = G >> gb;
+    const T *m = smats + i * (D * D);
+    T *ps = psi + ((uint64_t)sel[i] << sb);
     const uint64_t base = spread_zeros<K>(G & ((1ULL << gb) - 1), q.lowmask);
     T x[D];
 #pragma unroll
@@ -370,8 +366,8 @@ __global__ void __launch_bounds__(256) k_kraus_seg(T *__restrict__ psi, int sb, 
       y.y = 0;
 #pragma unroll
       for (int c = 0; c < D; ++c) {
-        const double2 md = __ldg(m + r + D * c);
-        const R wx = (R)(md.x * sc), wy = (R)(md.y * sc);
+        const T w = m[r + D * c];
+        const auto wx = w.x, wy = w.y;
         y.x = fma(wx, x[c].x, y.x);
         y.x = fma(-wy, x[c].y, y.x);
         y.y = fma(wx, x[c].y, y.y);
@@ -456,14 +452,13 @@ void rdm_any(Device &d, int sb, uint64_t nseg, const SegQ &q, int k, int bps) {
 }
 
 template <typename T>
-void kraus_any(Device &d, int sb, uint64_t nseg, const SegQ &q, int k, const double2 *mats, const uint8_t *branch,
-               const double *scale) {
-  const uint64_t total = nseg << (sb - k);
+void kraus_any(Device &d, int sb, uint64_t nsel, const SegQ &q, int k, const T *smats, const uint32_t *sel) {
+  const uint64_t total = nsel << (sb - k);
   const int grid = grid_of(total);
   switch (k) {
-    case 1: k_kraus_seg<T, 1><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, mats, branch, scale); break;
-    case 2: k_kraus_seg<T, 2><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, mats, branch, scale); break;
-    default: k_kraus_seg<T, 3><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, mats, branch, scale); break;
+    case 1: k_kraus_seg<T, 1><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, smats, sel); break;
+    case 2: k_kraus_seg<T, 2><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, smats, sel); break;
+    default: k_kraus_seg<T, 3><<<grid, 256, 0, d.stream>>>(st<T>(d), sb, total, q, smats, sel); break;
   }
 }
 
@@ -497,22 +492,39 @@ void launch_kraus_segments(Device &d, const reg_t &qubits, int sb, uint64_t nseg
                            const uint8_t *branch, const double *scale) {
   const int k = (int)qubits.size();
   if (k < 1 || k > seg_max_kraus_qubits() || k > sb) throw Error(1, "segment Kraus operators: 1..3 qubits");
-  // matrices (16-byte entries), then the per-state scales and branches
-  const size_t D = 1ULL << k, mbytes = (size_t)m * D * D * 16;
-  grow(d.aux2, d.aux2_cap, mbytes + nseg * 9);
+  (void)m;
+  // the states that take an operator, each with its scaled matrix
+  // (std::complex times double, entry by entry, as the reference scales it)
+  const size_t D2 = (size_t)1 << (2 * k);
+  std::vector<uint32_t> sel;
+  std::vector<cd> smats;
+  for (uint64_t s = 0; s < nseg; ++s) {
+    if (branch[s] == 0xff) continue;
+    sel.push_back((uint32_t)s);
+    const cd *src = mats + (size_t)branch[s] * D2;
+    for (size_t e = 0; e < D2; ++e) smats.push_back(src[e] * scale[s]);
+  }
+  if (sel.empty()) return;
+  // the matrices in the state's precision (a complex64 entry rounded once)
+  const size_t esize = d.dbl ? sizeof(double2) : sizeof(float2);
+  const size_t mbytes = smats.size() * esize;
+  grow(d.aux2, d.aux2_cap, mbytes + sel.size() * 4);
   char *base = reinterpret_cast<char *>(d.aux2);
-  cuda_check(cudaMemcpyAsync(base, mats, mbytes, cudaMemcpyHostToDevice, d.stream), "Kraus upload");
-  cuda_check(cudaMemcpyAsync(base + mbytes, scale, nseg * 8, cudaMemcpyHostToDevice, d.stream), "Kraus upload");
-  cuda_check(cudaMemcpyAsync(base + mbytes + nseg * 8, branch, nseg, cudaMemcpyHostToDevice, d.stream),
+  if (d.dbl) {
+    cuda_check(cudaMemcpyAsync(base, smats.data(), mbytes, cudaMemcpyHostToDevice, d.stream), "Kraus upload");
+  } else {
+    std::vector<float2> f(smats.size());
+    for (size_t e = 0; e < f.size(); ++e) f[e] = make_float2((float)smats[e].real(), (float)smats[e].imag());
+    cuda_check(cudaMemcpyAsync(base, f.data(), mbytes, cudaMemcpyHostToDevice, d.stream), "Kraus upload");
+  }
+  cuda_check(cudaMemcpyAsync(base + mbytes, sel.data(), sel.size() * 4, cudaMemcpyHostToDevice, d.stream),
              "Kraus upload");
   const SegQ q = make_segq(qubits);
-  const double2 *dm = reinterpret_cast<const double2 *>(base);
-  const double *ds = reinterpret_cast<const double *>(base + mbytes);
-  const uint8_t *db = reinterpret_cast<const uint8_t *>(base + mbytes + nseg * 8);
+  const uint32_t *ds = reinterpret_cast<const uint32_t *>(base + mbytes);
   if (d.dbl)
-    kraus_any<double2>(d, sb, nseg, q, k, dm, db, ds);
+    kraus_any<double2>(d, sb, sel.size(), q, k, reinterpret_cast<const double2 *>(base), ds);
   else
-    kraus_any<float2>(d, sb, nseg, q, k, dm, db, ds);
+    kraus_any<float2>(d, sb, sel.size(), q, k, reinterpret_cast<const float2 *>(base), ds);
   check_launch("segment Kraus kernel");
 }
 

@@ -119,6 +119,11 @@ class KrausOp:
         c = np.einsum("jaa->j", self.gram).real / D
         flat = np.max(np.abs(self.gram - c[:, None, None] * np.eye(D)))
         self.fixed = c if flat <= 1e-13 else None
+        # operators that are multiples of the identity: normalised, they
+        # leave a state as it is (to within one rounding) and are skipped
+        self.corner = self.mats[:, 0, 0].copy()
+        self.ident = np.array([abs(M[0, 0]) > 0 and np.max(np.abs(M - M[0, 0] * np.eye(D))) <= 1e-15
+                               for M in self.mats])
 
 
 class Result:
@@ -804,7 +809,8 @@ class AerSimulator:
         of n qubits, each with its uniform u: the operators' probabilities
         from each state's reduced density matrix (one pass; none for a
         mixture of unitaries), the choice per state, then one pass applying
-        each state's normalised operator."""
+        each state's normalised operator, over the states whose operator
+        is not a multiple of the identity."""
         L, h = A.lib(), st.handle
         k, m = len(op.qubits), op.mats.shape[0]
         qarr = (C.c_uint64 * k)(*op.qubits)
@@ -816,10 +822,13 @@ class AerSimulator:
             A.check(L.gbqv_rdm_segments(h, n, cnt, qarr, k, rho.ctypes.data_as(A.vp)), h)
             probs = np.einsum("jab,sba->sj", op.gram, rho[rows]).real
         chosen, sc = kraus_draws(probs, u)
+        keep = ~(op.ident[chosen] & (np.abs(op.corner[chosen] * sc - 1.0) <= 1e-14))
+        if not keep.any():
+            return
         branch = np.full(cnt, 255, dtype=np.uint8)
-        branch[rows] = chosen
+        branch[rows[keep]] = chosen[keep]
         scale = np.zeros(cnt, dtype=np.float64)
-        scale[rows] = sc
+        scale[rows[keep]] = sc[keep]
         A.check(L.gbqv_kraus_segments(h, n, cnt, qarr, k, op.colmajor.ctypes.data_as(A.vp), m,
                                       branch.ctypes.data_as(A.vp), scale.ctypes.data_as(A.dp)), h)
 
@@ -943,20 +952,17 @@ class AerSimulator:
 
     @staticmethod
     def _collapse(st, qubits, meas_state: int, final_state: int, prob: float):
-        """measure_reset_update: project onto meas_state, renormalise by
-        1/sqrt(p), then move meas_state to final_state (X for one qubit, a
-        transposition for several)."""
-        dim = 1 << len(qubits)
-        diag = np.zeros(dim, dtype=complex)
-        diag[meas_state] = 1.0 / np.sqrt(prob)
-        st.apply_diagonal_matrix(qubits, diag)
-        if final_state != meas_state:
-            if len(qubits) == 1:
-                st.apply_mcx(qubits)
-            else:
-                perm = np.eye(dim, dtype=complex)
-                perm[[final_state, meas_state]] = perm[[meas_state, final_state]]
-                st.apply_matrix(qubits, perm)
+        """measure_reset_update on one state: the amplitude of meas_state
+        times 1/sqrt(p) moves to final_state, the others become 0 (the
+        stacked collapse kernel on a stack of one state, any register
+        width)."""
+        k = len(qubits)
+        qarr = (C.c_uint64 * k)(*qubits)
+        meas = np.array([meas_state], dtype=np.uint32)
+        final = np.array([final_state], dtype=np.uint32)
+        scale = np.array([1.0 / np.sqrt(prob)])
+        A.check(A.lib().gbqv_collapse_segments(st.handle, st.num_qubits(), 1, qarr, k, meas.ctypes.data_as(A.vp),
+                                               final.ctypes.data_as(A.vp), scale.ctypes.data_as(A.dp)), st.handle)
 
     def _readout_ops(self, meas) -> list:
         """Readout errors after the measurements, in order: (clbits, probs)."""
