@@ -630,8 +630,15 @@ class AerSimulator:
                 stretch.clear()
 
         for ins in circuit.data:
-            if ins.kind in ("save", "set"):
-                raise NotImplementedError(f"{ins.kind} instructions in a circuit run shot by shot")
+            if ins.kind == "set":
+                raise NotImplementedError("set instructions in a circuit run shot by shot")
+            if ins.kind == "save" and ins.name not in self.SHOT_SAVES:
+                raise NotImplementedError(f"save instructions other than {', '.join(self.SHOT_SAVES)} in a circuit "
+                                          "run shot by shot")
+            if ins.kind == "save":
+                flush()
+                items.append(("save", ins, None))
+                continue
             if ins.kind == "superop":
                 raise ValueError("superop instructions need method='density_matrix'")
             # noise ops inherit the instruction's condition (noise_model.hpp:422-431)
@@ -661,12 +668,18 @@ class AerSimulator:
         if noisy:
             meta["noise"] = "kraus"
         matrices = self._conditioned_matrices(items)
+        sums = {}
         if matrices is not None and circuit.num_clbits <= 63:
-            memory = self._shots_batched(circuit.num_qubits, items, matrices, shots, seed)
+            memory = self._shots_batched(circuit.num_qubits, items, matrices, shots, seed, sums)
             meta["batched_shots_optimization"] = True  # batch_shots_executor.hpp:373
         else:
-            memory = self._shots_serial(circuit.num_qubits, items, shots, seed)
+            memory = self._shots_serial(circuit.num_qubits, items, shots, seed, sums)
         data = {}
+        names = {(obj.data if obj.name == "probabilities" else obj.data[0]): obj.name
+                 for kind, obj, _ in items if kind == "save"}
+        for label, total in sums.items():  # the average over the shots
+            avg = total / shots
+            data[label] = {"expval": float, "expval_var": lambda a: a.tolist()}.get(names[label], np.asarray)(avg)
         if self._want_memory and circuit.num_clbits:
             data["memory"] = self._memory(memory)
         counts = None
@@ -677,6 +690,39 @@ class AerSimulator:
                 counts[key] = counts.get(key, 0) + 1
         return {"counts": counts, "data": data, "metadata": meta, "seed_simulator": seed, "shots": shots}
 
+    # saves a circuit run shot by shot supports: each averaged over the shots
+    SHOT_SAVES = ("expval", "expval_var", "probabilities")
+
+    @staticmethod
+    def _save_shots(st, n, cnt, ins, sums) -> None:
+        """A save in a circuit run shot by shot.  The reference averages it
+        over the shots (save_data_average, the default `average` subtype of
+        save_expval and save_probabilities: Base::apply_save_expval,
+        state.hpp:416-447, the probabilities in statevector_state.hpp); here
+        each group adds its states' values to a running sum, divided by the
+        number of shots at the end."""
+        L, h = A.lib(), st.handle
+        if ins.name == "probabilities":
+            k = len(ins.qubits)
+            qarr = (C.c_uint64 * k)(*ins.qubits)
+            probs = np.empty((cnt, 1 << k), dtype=np.float64)
+            A.check(L.gbqv_probabilities_segments(h, n, cnt, qarr, k, probs.ctypes.data_as(A.dp)), h)
+            label, val = ins.data, probs.sum(axis=0)
+        else:
+            label, terms = ins.data
+            if not terms:
+                raise ValueError("Invalid save expval instruction (Pauli components are empty).")
+            variance = ins.name == "expval_var"
+            params = expval_params(terms, variance)
+            vals = st.expval_pauli_segments(n, cnt, [ql for ql, _, _ in params])  # [term, state]
+            ev, sq = np.zeros(cnt), np.zeros(cnt)
+            for (_, c1, c2), v in zip(params, vals):
+                ev += c1 * v
+                if variance:
+                    sq += c2 * v
+            val = np.array([ev.sum(), (sq - ev * ev).sum()]) if variance else ev.sum()
+        sums[label] = sums[label] + val if label in sums else val
+
     @staticmethod
     def _conditioned_matrices(items):
         """The matrix of every classically conditioned op, for applying it to
@@ -684,7 +730,7 @@ class AerSimulator:
         path (a conditioned op on more than 4 qubits)."""
         out = {}
         for idx, (kind, obj, cond) in enumerate(items):
-            if kind in ("measure", "reset", "kraus"):
+            if kind in ("measure", "reset", "kraus", "save"):
                 continue
             if cond is None:
                 continue
@@ -713,12 +759,13 @@ class AerSimulator:
         return sum(1 + (len(self._readout_ops([obj])) if kind == "measure" else 0)
                    for kind, obj, _ in items if kind in ("measure", "reset", "kraus"))
 
-    def _shots_batched(self, n, items, matrices, shots, seed):
+    def _shots_batched(self, n, items, matrices, shots, seed, sums):
         L = A.lib()
         ndraw = self._draws_per_shot(items)
         # a Kraus channel's 4^k complex values per state count as 2k + 1 qubits of probabilities
         ks = [len(obj.qubits) if kind != "kraus" else 2 * len(obj.qubits) + 1
-              for kind, obj, _ in items if kind in ("measure", "reset", "kraus")]
+              for kind, obj, _ in items
+              if kind in ("measure", "reset", "kraus") or (kind == "save" and obj.name == "probabilities")]
         b = self._shot_group_bits(n, shots, ks)
         group = 1 << b
         out = np.zeros(shots, dtype=np.uint64)
@@ -742,6 +789,9 @@ class AerSimulator:
                             active &= ((memory >> np.uint64(c)) & np.uint64(1)) == ((value >> i) & 1)
                         if not active.any():
                             continue
+                    if kind == "save":
+                        self._save_shots(st, n, cnt, obj, sums)
+                        continue
                     if kind == "ops":
                         if active.all():
                             A.check(L.gbqv_execute_segments(h, obj.handle), h)
@@ -832,7 +882,7 @@ class AerSimulator:
         A.check(L.gbqv_kraus_segments(h, n, cnt, qarr, k, op.colmajor.ctypes.data_as(A.vp), m,
                                       branch.ctypes.data_as(A.vp), scale.ctypes.data_as(A.dp)), h)
 
-    def _shots_serial(self, n, items, shots, seed):
+    def _shots_serial(self, n, items, shots, seed, sums):
         """One state, one shot at a time (classical memory wider than 63
         bits, or a conditioned op beyond the stacked kernels)."""
         ndraw = self._draws_per_shot(items)
@@ -853,6 +903,9 @@ class AerSimulator:
                     if kind == "kraus":
                         self._kraus_apply(st, n, 1, obj, np.zeros(1, dtype=np.int64), u[used:used + 1])
                         used += 1
+                        continue
+                    if kind == "save":
+                        self._save_shots(st, n, 1, obj, sums)
                         continue
                     qubits = obj.qubits
                     probs = st.probabilities(qubits)

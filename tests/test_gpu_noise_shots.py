@@ -43,9 +43,11 @@ def noisy_ops(sim, ins):
     return (errs, []) if ins.kind == "measure" else ([], errs)
 
 
-def oracle_memory(P, sim, qc, shots, seed):
+def oracle_memory(P, sim, qc, shots, seed, sums=None):
     """The per-shot loop on the oracle: shot i from |0...0> with the stream
-    seed + i, one uniform per Kraus channel and per measure / reset."""
+    seed + i, one uniform per Kraus channel and per measure / reset; saves
+    add each shot's value to `sums` (expectation values of Pauli sums,
+    probabilities)."""
     out = []
     for shot in range(shots):
         o = O.OracleQV(qc.num_qubits)
@@ -56,6 +58,16 @@ def oracle_memory(P, sim, qc, shots, seed):
                 cb, val = ins.condition
                 if any(((mem >> c) & 1) != ((val >> i) & 1) for i, c in enumerate(cb)):
                     continue
+            if ins.kind == "save":
+                if ins.name == "probabilities":
+                    label, val = ins.data, o.probabilities(ins.qubits)
+                else:
+                    label, terms = ins.data
+                    val = sum(c * o.expval_pauli(q, lab) for c, lab, q in terms)
+                    if ins.name == "expval_var":   # a single Pauli: <P^2> = 1
+                        val = np.array([val, 1.0 - val * val])
+                sums[label] = sums.get(label, 0) + val
+                continue
             before, after = noisy_ops(sim, ins)
             for op in before:
                 oracle_apply_kraus(o, op.qubits, list(op.mats), u[used])
@@ -251,3 +263,33 @@ def test_noisy_statevector_counts_follow_the_density_matrix():
         p = probs[v]
         c = counts.get(format(v, "04b"), 0)
         assert abs(c - shots * p) <= 5 * np.sqrt(shots * p * (1 - p)) + 2, (v, c, shots * p)
+
+
+def test_saves_average_over_noisy_shots():
+    """save_expval, save_expval_var and save_probabilities in a circuit run
+    shot by shot: the average over the shots (the reference's default
+    `average` subtype), mid-circuit and at the end, against the oracle loop,
+    stacked and one state at a time."""
+    P = pkg()
+    n = 4
+    qc = feedback_circuit(P, n, np.random.default_rng(61))
+    final = qc.data.pop()                        # the final measurement goes last again below
+    qc.save_expectation_value([(0.7, "ZZ", [0, 2]), (-0.4, "X", [1])], label="mid")
+    qc.u3(0.3, 0.2, 0.1, 3)
+    qc.save_expectation_value_variance([(1.0, "Y", [3])], label="var")
+    qc.save_probabilities([2, 0], label="p")
+    qc.data.append(final)
+    nm = noise_model(P)
+    want = {}
+    sim = P.AerSimulator(noise_model=nm)
+    oracle_memory(P, sim, qc, 24, 5, want)
+    for serial in (False, True):
+        s2 = P.AerSimulator(noise_model=nm)
+        s2.SHOT_GROUP_BITS = 3
+        if serial:
+            s2._conditioned_matrices = lambda items: None
+        got = s2.run(qc, shots=24, seed_simulator=5).data()
+        assert isinstance(got["mid"], float)
+        assert abs(got["mid"] - want["mid"] / 24) < 1e-12
+        np.testing.assert_allclose(got["var"], want["var"] / 24, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(got["p"], want["p"] / 24, rtol=0, atol=1e-12)
