@@ -45,6 +45,8 @@ graph-captured persistent launch, next to one instance per launch),
 parameter sets run on one stack of states, 50 observables), ``shots``
 (a 16-qubit circuit with mid-circuit measurements, conditioned gates and
 resets: 4,096 shots, each running the circuit, stacked as states),
+``noisy`` (a 16-qubit circuit of 188 noisy gates on the statevector method,
+each error a Kraus channel drawn per shot: 4,096 shots stacked as states),
 ``dense5`` (5-qubit Haar gates on a dense 30-qubit state: the 5-qubit
 tensor-core kernels), ``tune`` (a 28-qubit unfused ansatz through
 AerSimulator.run with the default schedule and with autotune=True).
@@ -850,6 +852,70 @@ def bench_shots(args, torch, P):
     return line
 
 
+def noisy_circuit(P, n, layers, seed):
+    """U3 with seeded angles on every qubit and CX on alternate pairs, per
+    layer; every qubit measured at the end."""
+    rng = np.random.default_rng(seed)
+    qc = P.QuantumCircuit(n, n)
+    for r in range(layers):
+        for q in range(n):
+            qc.u3(*rng.uniform(0, 2 * np.pi, 3), q)
+        for q in range(r % 2, n - 1, 2):
+            qc.cx(q, q + 1)
+    qc.measure(list(range(n)), list(range(n)))
+    return qc
+
+
+def noisy_model(P, kind):
+    """depol: depolarizing 1e-3 on U3 and 1e-2 on CX (mixtures of Paulis);
+    damp: depolarizing 1e-3 then amplitude damping 2e-3 on U3, the tensor
+    product of two of those on CX (state-dependent Kraus probabilities)."""
+    nm = P.NoiseModel()
+    if kind == "depol":
+        nm.add_all_qubit_quantum_error(P.depolarizing_error(1e-3, 1), ["u3"])
+        nm.add_all_qubit_quantum_error(P.depolarizing_error(1e-2, 2), ["cx"])
+    else:
+        e1 = P.depolarizing_error(1e-3, 1).compose(P.amplitude_damping_error(2e-3))
+        nm.add_all_qubit_quantum_error(e1, ["u3"])
+        nm.add_all_qubit_quantum_error(e1.tensor(e1), ["cx"])
+    return nm
+
+
+def bench_noisy(args, torch, P):
+    """Noise sampled per shot on the statevector method (the reference's
+    Kraus noise method): every noisy gate is a Kraus channel drawn per shot,
+    shots stacked as states, through AerSimulator.run; next to one shot at a
+    time on one state (a sample of 32 shots)."""
+    qc = noisy_circuit(P, args.shots_qubits, args.noisy_layers, args.seed)
+    nm = noisy_model(P, args.noise)
+    sim = P.AerSimulator(precision=args.precision, noise_model=nm)
+    for _ in range(max(1, args.warmup)):
+        sim.run(qc, shots=min(args.shots, 256), seed_simulator=args.seed)
+    clocks = ClockSampler().start()
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        counts = sim.run(qc, shots=args.shots, seed_simulator=args.seed + i).get_counts()
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    t = float(np.median(times))
+    one = P.AerSimulator(precision=args.precision, noise_model=nm)
+    one._conditioned_matrices = lambda items: None   # the one-state loop
+    t0 = time.perf_counter()
+    one.run(qc, shots=32, seed_simulator=args.seed)
+    t1 = time.perf_counter() - t0
+    channels = sum(1 for ins in qc.data if ins.kind == "gate")
+    return {"metric": "shots/s (noise sampled per shot, statevector)", "value": round(args.shots / t, 1),
+            "unit": "shots/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t * 1e3, 2), "dtype": "c128" if args.precision == "double" else "c64",
+            "data": "synthetic", "outcomes": len(counts),
+            "config": {"workload": f"{args.shots_qubits}q, {args.noisy_layers} layers of U3 + alternate CX, "
+                                   f"{channels} noisy gates ({args.noise}); final measure of every qubit; "
+                                   f"{args.shots} shots", "qubits": args.shots_qubits, "shots": args.shots},
+            "one_shot_at_a_time_shots_per_s": round(32 / t1, 1),
+            "speedup_vs_one_shot_at_a_time": round((args.shots / t) / (32 / t1), 1), "clocks": clk}
+
+
 def hea_bound_circuit(P, n, layers):
     """RY(theta) and RZ(theta) on every qubit, then a CX ladder, per layer;
     one Parameter per rotation (the adjoint workload's ansatz, parameterised)."""
@@ -1051,13 +1117,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="qv",
-                    choices=["qv", "adjoint", "dm", "sample", "batch", "estimator", "shots", "dense5", "tune"])
+                    choices=["qv", "adjoint", "dm", "sample", "batch", "estimator", "shots", "noisy", "dense5",
+                             "tune"])
     ap.add_argument("--tune-qubits", type=int, default=28)
     ap.add_argument("--tune-layers", type=int, default=8)
     ap.add_argument("--dense5-layers", type=int, default=4)
     ap.add_argument("--shots-qubits", type=int, default=16)
     ap.add_argument("--shots-rounds", type=int, default=8)
     ap.add_argument("--shots", type=int, default=4096)
+    ap.add_argument("--noisy-layers", type=int, default=8, help="noisy workload: layers")
+    ap.add_argument("--noise", choices=["depol", "damp"], default="damp", help="noisy workload: noise model")
     ap.add_argument("--est-qubits", type=int, default=20)
     ap.add_argument("--est-layers", type=int, default=8)
     ap.add_argument("--est-bindings", type=int, default=1024)
@@ -1100,7 +1169,7 @@ def main():
     P = entry.load_package()
     P.build()
     fn = {"qv": bench_qv, "adjoint": bench_adjoint, "dm": bench_dm, "sample": bench_sample,
-          "batch": bench_batch, "estimator": bench_estimator, "shots": bench_shots,
+          "batch": bench_batch, "estimator": bench_estimator, "shots": bench_shots, "noisy": bench_noisy,
           "dense5": bench_dense5, "tune": bench_tune}[args.workload]
     line = fn(args, torch, P)
     if int(os.environ.get("RANK", "0")) == 0:
