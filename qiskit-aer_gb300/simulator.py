@@ -6,7 +6,9 @@ and the controller path it drives: per-circuit seeds
 ``seed_simulator + 2113*i`` (src/controllers/controller_execute.hpp:188-210),
 the Fusion pass with the per-method defaults of
 ``Executor::transpile_fusion`` (simulators/circuit_executor.hpp:1228-1287),
-noise inserted as superoperators for the density-matrix method, ops applied
+noise inserted as superoperators for the density-matrix method and sampled
+per shot as Kraus channels for the statevector method
+(circuit_executor.hpp:648-657, State::apply_kraus), ops applied
 in order (State::apply_ops, state.hpp:295-340), final measurements sampled
 from ``shots`` uniforms of one RngEngine stream
 (statevector_state.hpp:1016-1052), and save instructions evaluated where
