@@ -95,6 +95,9 @@ def oracle_memory(P, sim, qc, shots, seed, sums=None):
                 if ins.kind == "measure":
                     for i, c in enumerate(ins.clbits):
                         mem = (mem & ~(1 << c)) | (((k >> i) & 1) << c)
+                    for bits, rp in sim._readout_ops([ins]):   # readout errors draw after the outcome
+                        mem = P.noise.apply_readout(mem, bits, rp, u[used])
+                        used += 1
             for op in after:
                 oracle_apply_kraus(o, op.qubits, list(op.mats), u[used])
                 used += 1
@@ -293,3 +296,19 @@ def test_saves_average_over_noisy_shots():
         assert abs(got["mid"] - want["mid"] / 24) < 1e-12
         np.testing.assert_allclose(got["var"], want["var"] / 24, rtol=0, atol=1e-12)
         np.testing.assert_allclose(got["p"], want["p"] / 24, rtol=0, atol=1e-12)
+
+
+def test_kraus_noise_with_readout_errors():
+    """Kraus channels and readout errors on the same shots: each shot's
+    stream serves the channels, the outcome and then the readout errors in
+    circuit order, stacked as in the oracle loop."""
+    P = pkg()
+    n = 4
+    qc = feedback_circuit(P, n, np.random.default_rng(90))
+    nm = noise_model(P)
+    nm.add_all_qubit_readout_error(P.ReadoutError([[0.9, 0.1], [0.2, 0.8]]))
+    nm.add_readout_error(P.ReadoutError([[0.7, 0.3], [0.05, 0.95]]), [1])
+    sim = P.AerSimulator(noise_model=nm)
+    sim.SHOT_GROUP_BITS = 4
+    got = sim.run(qc, shots=40, seed_simulator=71, memory=True).get_memory()
+    assert got == oracle_memory(P, sim, qc, 40, 71)
